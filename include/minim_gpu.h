@@ -1,0 +1,226 @@
+/*
+ * minim_gpu.h -- C ABI of the GB300-native minimisation engine.
+ *
+ * Plain C types only: pointers, sizes, ints and doubles.  Every function
+ * returns an int status (MINIM_GPU_OK == 0) and records a message that
+ * minim_gpu_last_error() returns.  Kernels never trap: per-instance failures
+ * come back as a result status word.
+ *
+ * What each entry point replaces in the reference C++ library (paths are
+ * relative to the minim source tree):
+ *   minim_gpu_instance_create   State::State(pot, coords)       src/State.cpp:12-26
+ *                               + Potential::init/initLocal     src/potentials/LjNd.cpp:12-26,
+ *                                 src/potentials/PhaseField.cpp:137-235,
+ *                                 src/potentials/BarAndHinge.cpp:16-248
+ *   minim_gpu_energy_gradient   State::energy/gradient/energyGradient
+ *                                                               src/State.cpp:134-192
+ *   minim_gpu_instance_set_coords / get_coords
+ *                               State::coords(in) / coords()    src/State.cpp:282-288
+ *   minim_gpu_instance_set_fixed
+ *                               Potential::setConstraints(iFix) src/Potential.cpp:80-84
+ *   minim_gpu_apply_constraints State::applyConstraints         src/State.cpp:321-323
+ *   minim_gpu_minimise          Minimiser::minimise(state)      src/Minimiser.cpp:27-38
+ *                               with Lbfgs/Fire/GradDescent     src/minimisers/{Lbfgs,Fire,GradDescent}.cpp
+ *   minim_gpu_batch_*           (no counterpart: many States minimised together)
+ *   minim_gpu_server_*          (no counterpart: continuous batching of requests)
+ */
+#ifndef MINIM_GPU_H
+#define MINIM_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MINIM_GPU_ABI_VERSION 1
+
+/* ---- call status ------------------------------------------------------ */
+enum {
+  MINIM_GPU_OK = 0,
+  MINIM_GPU_ERR_INVALID = 1,   /* bad argument (reference: std::invalid_argument) */
+  MINIM_GPU_ERR_RUNTIME = 2,   /* reference: std::runtime_error */
+  MINIM_GPU_ERR_CUDA = 3,      /* a CUDA call failed */
+  MINIM_GPU_ERR_OOM = 4,       /* device allocation failed */
+  MINIM_GPU_ERR_NO_DEVICE = 5, /* no usable sm_103 device */
+  MINIM_GPU_ERR_BUSY = 6       /* request not finished / not known */
+};
+
+/* ---- per-instance result status (device status word) ------------------- */
+enum {
+  MINIM_RES_CONVERGED = 0,  /* checkConvergence() became true */
+  MINIM_RES_MAXITER = 1,    /* loop ran iter = 0..maxIter without converging */
+  MINIM_RES_NAN = 2,        /* a non-finite energy or gradient was produced */
+  MINIM_RES_TIMEOUT = 3,    /* a device wait gave up (bounded barrier) */
+  MINIM_RES_CANCELLED = 4,  /* cancelled by the caller before completion */
+  MINIM_RES_RUNNING = 5,    /* still in progress (serving) */
+  MINIM_RES_REJECTED = 6    /* could not be admitted (does not fit in memory) */
+};
+
+/* ---- potential kinds ---------------------------------------------------- */
+enum { MINIM_GPU_LJ = 0, MINIM_GPU_PF = 1, MINIM_GPU_BAH = 2 };
+
+/* LjNd(nDim, sigma, epsilon): include/potentials/LjNd.h:22-24 */
+typedef struct {
+  int ndim;         /* 2 or 3 */
+  double sigma;     /* default 1 */
+  double epsilon;   /* default 1 */
+} minim_gpu_lj_params;
+
+/* PhaseField (MODEL_BASIC): include/potentials/PhaseField.h:13-69.
+ * Arrays may be NULL with count 0 to take the reference defaults. */
+enum { MINIM_PF_DENSITY_HARD = 0, MINIM_PF_DENSITY_SOFT = 1,
+       MINIM_PF_DENSITY_NONE = 2, MINIM_PF_DENSITY_FIXED = 3 };
+typedef struct {
+  int grid[3];                  /* setGridSize */
+  int nfluid;                   /* setNFluid (default 1) */
+  double resolution;            /* setResolution (default 1) */
+  int n_interface_size;         /* 0 (default = resolution), or nfluid */
+  const double* interface_size;
+  int n_surface_tension;        /* 1, nfluid, or ngrid*nfluid (per node) */
+  const double* surface_tension;
+  int density_constraint;       /* MINIM_PF_DENSITY_* (default hard) */
+  double density_const;         /* default 1 */
+  int volume_fixed;             /* setVolumeFixed / setVolume */
+  double vol_const;             /* default 0.01 (only the energy diagnostic uses it) */
+  const double* volume;         /* nfluid target volumes, or NULL = initial volumes */
+  const double* pressure;       /* nfluid, or NULL (= 0) */
+  const char* solid;            /* ngrid (0/1), or NULL (= no solid) */
+  int n_contact_angle;          /* 0, ngrid, or ngrid*nfluid */
+  const double* contact_angle;  /* degrees */
+  const double* force;          /* nfluid*3, or NULL (setForce) */
+  const char* fix_fluid;        /* nfluid, or NULL (setFixFluid) */
+  const double* confinement;    /* nfluid, or NULL (setConfinement) */
+} minim_gpu_pf_params;
+
+/* BarAndHinge: include/potentials/BarAndHinge.h:10-60.
+ * Topology comes either from a triangulation (setTriangulation) or from
+ * explicit bond/hinge lists (setBondList/setHingeList, with stride >= 2 / 4;
+ * entries after the first 2 / 4 are the adjacent-triangle vertices / bond
+ * index used only by the thickness-based rigidities). */
+typedef struct {
+  int ntri; const int* tris;                     /* 3 per triangle */
+  int nbond; const int* bonds; int bond_stride;  /* optional explicit bonds */
+  int nhinge; const int* hinges; int hinge_stride;
+  double modulus;                                /* default 1 */
+  double poisson_ratio;                          /* default 0.3 */
+  int n_thickness; const double* thickness;      /* 0, 1 or nvert */
+  int n_kbond; const double* kbond;              /* 0, 1 or nbond */
+  int n_khinge; const double* khinge;            /* 0, 1 or nhinge */
+  int n_length0; const double* length0;          /* 0 (from coords), 1 or nbond */
+  int n_theta0; const double* theta0;            /* 0 (from coords), 1 or nhinge */
+  int n_force; const double* force;              /* 0, 3 or 3*nvert */
+  int wall_on, wall_adhesion;
+  double wall_epsilon;                           /* default 1e-12 */
+  double wall_sigma;                             /* default 1e-5 */
+} minim_gpu_bah_params;
+
+/* ---- minimisers ---------------------------------------------------------- */
+enum { MINIM_LBFGS = 0, MINIM_FIRE = 1, MINIM_GD = 2 };
+enum { MINIM_LS_BACKTRACKING = 0, MINIM_LS_NONE = 1 };
+/* Precision of the coordinates while minimising.  MIXED runs FP32
+ * coordinates/gradients with FP64 reductions, then switches to FP64
+ * coordinates for the final polish; FP64 runs FP64 coordinates throughout;
+ * FP32 never switches. */
+enum { MINIM_PREC_MIXED = 0, MINIM_PREC_FP64 = 1, MINIM_PREC_FP32 = 2 };
+
+typedef struct {
+  int method;        /* MINIM_LBFGS / MINIM_FIRE / MINIM_GD */
+  int linesearch;    /* MINIM_LS_*; reference default: backtracking, except Fire(dtMax) */
+  int max_iter;      /* Minimiser::maxIter (default 100000) */
+  double tol;        /* State::convergence; < 0 takes the potential's default */
+  int m;             /* Lbfgs::setM (default 5) */
+  double max_step;   /* Lbfgs::setMaxStep (default 0 = off) */
+  double init_step;  /* Lbfgs::setInitStep (default 1) */
+  double dt_max;     /* Fire dtMax (0 = estimate 0.1/sqrt|g| at start) */
+  double alpha;      /* GradDescent::setAlpha (default 0.1) */
+  int precision;     /* MINIM_PREC_* */
+} minim_gpu_minimiser_params;
+
+typedef struct {
+  int status;           /* MINIM_RES_* */
+  int iter;             /* Minimiser::iter after minimise() (reference meaning) */
+  int fp64_iters;       /* iterations run with FP64 coordinates */
+  int evals;            /* potential evaluations (energy-only and energy+gradient) */
+  double energy;        /* energy at the returned coordinates */
+  double rms;           /* sqrt(g.g/ndof) at the returned coordinates */
+  double dt_max;        /* Fire: the dtMax used (estimated when 0 was passed) */
+  double latency_ms;    /* serving: submit -> completion wall time */
+} minim_gpu_result;
+
+typedef struct minim_gpu_instance_s* minim_gpu_handle;
+typedef struct minim_gpu_batch_s* minim_gpu_batch;
+typedef struct minim_gpu_server_s* minim_gpu_server;
+
+/* ---- library ------------------------------------------------------------ */
+int minim_gpu_abi_version(void);
+int minim_gpu_last_error(char* buf, size_t len);
+/* Fills defaults equal to the reference's constructors and setters. */
+void minim_gpu_default_minimiser(int method, minim_gpu_minimiser_params* out);
+void minim_gpu_default_pf(minim_gpu_pf_params* out);
+void minim_gpu_default_bah(minim_gpu_bah_params* out);
+/* Number of potential/minimiser kernel launches issued by this process. */
+int64_t minim_gpu_launch_count(void);
+
+/* ---- single instances ------------------------------------------------------ */
+/* Copies the host arrays into device-owned buffers; the caller keeps its own.
+ * params points at minim_gpu_{lj,pf,bah}_params according to kind. */
+int minim_gpu_instance_create(int kind, const void* params, const double* x0,
+                              size_t ndof, minim_gpu_handle* out);
+int minim_gpu_instance_destroy(minim_gpu_handle h);
+int minim_gpu_instance_ndof(minim_gpu_handle h, size_t* ndof);
+/* The potential's own default convergence (PhaseField: 1e-8*sigma*res^2). */
+int minim_gpu_instance_default_tol(minim_gpu_handle h, double* tol);
+int minim_gpu_instance_set_coords(minim_gpu_handle h, const double* x);
+int minim_gpu_instance_get_coords(minim_gpu_handle h, double* x);
+/* Fixed degrees of freedom: gradient (and step) components forced to 0. */
+int minim_gpu_instance_set_fixed(minim_gpu_handle h, const int* idof, size_t n);
+/* Energy and constrained gradient at x (x == NULL: the resident coordinates).
+ * e and g may each be NULL, as in the reference. */
+int minim_gpu_energy_gradient(minim_gpu_handle h, const double* x, double* e, double* g);
+/* In-place State::applyConstraints on a host vector of length ndof. */
+int minim_gpu_apply_constraints(minim_gpu_handle h, double* v);
+/* Device-resident minimisation of one instance using the whole GPU; on
+ * return the instance holds the minimised coordinates. */
+int minim_gpu_minimise(minim_gpu_handle h, const minim_gpu_minimiser_params* mp,
+                       minim_gpu_result* res);
+
+/* ---- batches: many instances in one persistent launch --------------------- */
+int minim_gpu_batch_create(minim_gpu_batch* out);
+int minim_gpu_batch_add(minim_gpu_batch b, minim_gpu_handle h,
+                        const minim_gpu_minimiser_params* mp);
+/* threads_per_cta 0 = autotuned; results has one entry per added instance. */
+int minim_gpu_batch_run(minim_gpu_batch b, int threads_per_cta, minim_gpu_result* results);
+int minim_gpu_batch_destroy(minim_gpu_batch b);
+
+/* ---- serving: continuous batching ------------------------------------------ */
+typedef struct {
+  size_t max_bytes;     /* device memory budget for resident instances (0 = 50% free) */
+  int max_slots;        /* maximum concurrently resident instances (0 = 4096) */
+  int slice_iters;      /* iterations each resident instance runs per step (0 = 64) */
+  int threads_per_cta;  /* 0 = autotuned */
+} minim_gpu_server_config;
+
+int minim_gpu_server_create(const minim_gpu_server_config* cfg, minim_gpu_server* out);
+/* Queue a request; it is admitted once slots and memory allow. */
+int minim_gpu_server_submit(minim_gpu_server s, int kind, const void* params,
+                            const double* x0, size_t ndof,
+                            const minim_gpu_minimiser_params* mp, uint64_t* request_id);
+/* One scheduling step: admit queued requests, run one slice on every
+ * resident instance, retire the finished ones.  Reports what is resident
+ * and what is still queued. */
+int minim_gpu_server_step(minim_gpu_server s, int* n_resident, int* n_queued);
+/* Completed requests since the last call (ids and results), at most max. */
+int minim_gpu_server_poll(minim_gpu_server s, uint64_t* ids, minim_gpu_result* res,
+                          int max, int* n_done);
+/* Copy out a completed request's coordinates and release it. */
+int minim_gpu_server_take(minim_gpu_server s, uint64_t id, double* x, size_t ndof);
+int minim_gpu_server_cancel(minim_gpu_server s, uint64_t id);
+int minim_gpu_server_destroy(minim_gpu_server s);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MINIM_GPU_H */
