@@ -1,0 +1,316 @@
+"""Benchmark: converged minimisations per second on one GB300.
+
+Headline workload (the single-GPU plain-method configuration): a binary
+PhaseField on a periodic 192^3 grid (resolution 1, interface width 1,
+surface tension 1), concentration 0 + U[-0.05, 0.05] (seed 0), minimised by
+L-BFGS (m = 10) to gradient RMS < 1e-7 with FP32 fields, FP64 reductions
+and an FP64 polishing stage.  One step = one complete minimisation from the
+initial field.  Inputs are resident in HBM before the timed region; each
+step's working set (x, g, 2 x 11 history vectors: ~0.8 GB) exceeds the
+129 MB L2, so no flush is needed between steps.
+
+Also reported (keys "batched" and "plain"): 4096 Lennard-Jones clusters,
+N ~ U{13..400}, half FIRE (dtMax 0.1, no line search) and half L-BFGS
+(m = 5) to RMS < 1e-6, run by the persistent batch kernels, against the same
+instances minimised one at a time with the whole GPU (a sample).
+
+--impl reference times the CPU restatement of the reference algorithm
+(oracle/, or the reference library itself when it was built on this host)
+on a bounded sample of the same workload.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+GRID = (192, 192, 192)
+TOL = 1e-7
+METRIC = "converged minimisations/s batched vs plain on GB300 at ΔE/E<1e-8; p50/p99 ms"
+
+
+def _peaks():
+    try:
+        with open(os.path.join(HERE, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return d.get("hbm_gbs", 6800.0), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi clock/throttle sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self):
+        self.rows = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def start(self):
+        def run():
+            while not self._stop.is_set():
+                try:
+                    out = subprocess.run(["nvidia-smi", "--query-gpu=" + self.Q, "--format=csv,noheader,nounits",
+                                          "-i", os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0]],
+                                         capture_output=True, text=True, timeout=5).stdout
+                    for line in out.strip().splitlines():
+                        self.rows.append([c.strip() for c in line.split(",")])
+                except Exception:
+                    pass
+                self._stop.wait(0.2)
+        self._t = threading.Thread(target=run, daemon=True)
+        self._t.start()
+
+    def stop(self):
+        self._stop.set()
+        if self._t:
+            self._t.join(timeout=10)
+        sm = [float(r[1]) for r in self.rows if len(r) > 2 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) > 2 and r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in self.rows:
+            for k, nm in enumerate(names):
+                if len(r) > 5 + k and r[5 + k].lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def pf_setup():
+    from minim_gb300 import abi
+    from tests.workloads import pf_noise
+    p = abi.phase_field(GRID, interface_size=1.0, surface_tension=1.0)
+    x0 = pf_noise(GRID, seed=0, amp=0.05)
+    mp = abi.minimiser("lbfgs", m=10, tol=TOL, precision="mixed")
+    return p, x0, mp
+
+
+def lj_batch_setup(count=4096):
+    from minim_gb300 import abi
+    from tests.workloads import Rng, lj_cluster
+    rng = Rng(12345)
+    sizes = 13 + (rng.uniform(count) * (400 - 13 + 1)).astype(int)
+    items = []
+    for i, n in enumerate(sizes):
+        x0 = lj_cluster(int(n), seed=i)
+        if i < count // 2:
+            mp = abi.minimiser("fire", dt_max=0.1, tol=1e-6)  # Fire(0.1): no line search
+        else:
+            mp = abi.minimiser("lbfgs", m=5, tol=1e-6)
+        items.append((x0, mp))
+    return abi.lj(), items
+
+
+def run_gpu(args):
+    import torch  # noqa: F401  (device plumbing only)
+    from minim_gb300 import abi, runtime
+    from oracle.oracle import Oracle
+
+    p, x0, mp = pf_setup()
+    runtime.load()
+    # warm-up (W full minimisations)
+    insts = [runtime.Instance(p, x0) for _ in range(args.steps)]
+    warm = runtime.Instance(p, x0)
+    for _ in range(args.warmup):
+        warm.coords = x0
+        r = warm.minimise(mp)
+    del warm
+
+    clocks = Clocks()
+    clocks.start()
+    launches0 = runtime.launch_count()
+    kernel_ms, abytes, results = 0.0, 0.0, []
+    t0 = time.perf_counter()
+    for inst in insts:
+        r = inst.minimise(mp)
+        st = runtime.last_run_stats()
+        kernel_ms += st["kernel_ms"]
+        abytes += st["abytes"]
+        results.append(r)
+    t1 = time.perf_counter()
+    launches = runtime.launch_count() - launches0
+    clk = clocks.stop()
+    ok = all(r.status == abi.RES_CONVERGED for r in results)
+    value = args.steps / (kernel_ms / 1e3)
+    ms_per_step = kernel_ms / args.steps
+    lat = [runtime.last_run_stats()["kernel_ms"]]
+
+    # parity of the last result under the FP64 checker (energy and RMS at x)
+    xg = insts[-1].coords
+    ora = Oracle(p, x0)
+    e_chk, g_chk = ora.energy_gradient(xg)
+    e_init = ora.energy(x0)
+    rel_err = abs(results[-1].energy - e_chk) / max(abs(e_chk), 1e-300)
+    floor_err = abs(results[-1].energy - e_chk) / max(abs(e_chk), abs(e_init))
+    rms_chk = float(np.sqrt(np.mean(g_chk ** 2)))
+    del insts
+
+    # end to end through the C ABI with host buffers: H2D of x0, minimise,
+    # D2H of the result, every step
+    e2e_times = []
+    for _ in range(args.steps):
+        ta = time.perf_counter()
+        inst = runtime.Instance(p, x0)
+        inst.minimise(mp)
+        _ = inst.coords
+        e2e_times.append(time.perf_counter() - ta)
+        inst.close()
+    e2e_value = args.steps / sum(e2e_times)
+
+    hbm_peak, peak_kind = _peaks()
+    achieved = abytes / (kernel_ms / 1e3) / 1e9
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                "frac": achieved / hbm_peak, "traffic": None, "peak_source": peak_kind,
+                "kernel": "grid_kernel<K_PF1> (fused L-BFGS minimiser)"}
+
+    out = {
+        "metric": METRIC, "value": value, "unit": "minimisations/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32+fp64",
+        "data": "synthetic (seeded noise field)",
+        "config": {"workload": "PhaseField binary 192^3 periodic, Lbfgs m=10, RMS<1e-7, mixed FP32/FP64",
+                   "grid": list(GRID), "ndof": int(np.prod(GRID)), "l2": "working set > L2, no flush"},
+        "iterations": results[-1].iter, "fp64_iters": results[-1].fp64_iters,
+        "converged": ok, "energy": results[-1].energy,
+        "parity": {"energy_rel_err": rel_err, "energy_err_vs_max_E_Einit": floor_err,
+                   "oracle_rms_at_x": rms_chk},
+        "e2e": {"value": e2e_value, "unit": "minimisations/s",
+                "h2d_bytes_per_step": int(x0.size * 8), "d2h_bytes_per_step": int(x0.size * 8)},
+        "gpu_launches": int(launches), "roofline": roofline, "clocks": clk,
+        "wall_s_timed": t1 - t0,
+    }
+    if not args.no_batched:
+        out.update(run_batched(args))
+    if not args.no_cpu:
+        out["cpu_baseline"] = cpu_baseline(results[-1].iter, budget_s=args.cpu_budget)
+    return out
+
+
+def run_batched(args):
+    from minim_gb300 import abi, runtime
+    p, items = lj_batch_setup(args.batch)
+    insts = [runtime.Instance(p, x0) for x0, _ in items]
+    b = runtime.Batch()
+    for inst, (_, mp) in zip(insts, items):
+        b.add(inst, mp)
+    b.run()  # warm-up (also restores nothing: re-seed coordinates below)
+    for inst, (x0, _) in zip(insts, items):
+        inst.coords = x0
+    res = b.run()
+    st = runtime.last_run_stats()
+    conv = sum(r.status == abi.RES_CONVERGED for r in res)
+    batched = len(items) / (st["kernel_ms"] / 1e3)
+    # plain: the same instances one at a time on the whole GPU (sample)
+    rng = np.random.default_rng(0)
+    idx = rng.choice(len(items), size=min(args.plain_sample, len(items)), replace=False)
+    plain_ms = 0.0
+    for i in idx:
+        inst = runtime.Instance(p, items[i][0])
+        inst.minimise(items[i][1])
+        plain_ms += runtime.last_run_stats()["kernel_ms"]
+    plain = len(idx) / (plain_ms / 1e3)
+    flops32 = st["pairs32"] * 20
+    return {
+        "batched": {"value": batched, "unit": "minimisations/s", "instances": len(items),
+                    "converged": int(conv), "kernel_ms": st["kernel_ms"],
+                    "fp32_tflops": flops32 / (st["kernel_ms"] / 1e3) / 1e12,
+                    "workload": "4096 LJ clusters N~U{13..400}, half Fire(0.1) half Lbfgs(m=5), RMS<1e-6"},
+        "plain": {"value": plain, "unit": "minimisations/s", "sample": int(len(idx))},
+        "batched_vs_plain": batched / plain,
+    }
+
+
+def cpu_baseline(gpu_iters, budget_s=20.0):
+    """CPU restatement (or the reference library where it was built) timed on
+    a bounded number of L-BFGS iterations of the same 192^3 workload; the
+    rate is extrapolated to a full minimisation with the GPU's iteration
+    count (the same algorithm and stopping rule)."""
+    from minim_gb300 import abi
+    from oracle import oracle as O
+    p, x0, mp = pf_setup()
+    kind = "reference" if O.reference_available() else "port"
+    cls = O.Reference if kind == "reference" else O.Oracle
+    inst = cls(p, x0)
+    # time one E+g to size the sample
+    t = time.perf_counter()
+    inst.energy_gradient()
+    t_eval = time.perf_counter() - t
+    iters = max(2, int(budget_s / max(t_eval * 5, 1e-3)))
+    mps = abi.minimiser("lbfgs", m=10, tol=TOL, max_iter=iters - 1)
+    inst = cls(p, x0)
+    t = time.perf_counter()
+    r = inst.minimise(mps)
+    dt = time.perf_counter() - t
+    per_iter = dt / (r.iter + 1 if r.status != 0 else r.iter + 1)
+    rate = 1.0 / (per_iter * max(gpu_iters + 1, 1))
+    return {"value": rate, "unit": "minimisations/s", "cores": 1, "kind": kind,
+            "sample": f"{r.iter + 1} L-BFGS iterations of the 192^3 run ({dt:.1f} s), "
+                      f"extrapolated to {gpu_iters + 1} iterations"}
+
+
+def run_reference(args):
+    cb = cpu_baseline(args.ref_iters_hint, budget_s=args.cpu_budget)
+    return {"metric": METRIC, "value": cb["value"], "unit": cb["unit"], "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 / cb["value"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp64",
+            "data": "synthetic (seeded noise field)", "impl": "reference",
+            "config": {"workload": "PhaseField binary 192^3 periodic, Lbfgs m=10, RMS<1e-7"},
+            "cpu_baseline": cb,
+            "e2e": {"value": cb["value"], "unit": cb["unit"], "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="minim_gb300")
+    ap.add_argument("--batch", type=int, default=4096)
+    ap.add_argument("--plain-sample", type=int, default=16)
+    ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-budget", type=float, default=20.0)
+    ap.add_argument("--ref-iters-hint", type=int, default=600)
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if args.impl == "reference":
+        if rank == 0:
+            print(json.dumps(run_reference(args)))
+        return
+    if world > 1:
+        # replicas: every rank runs its own copy of the workload on its GPU
+        import torch
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        args.no_cpu = rank != 0
+        out = run_gpu(args)
+        t = torch.tensor([out["ms_per_step"]], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        out["ms_per_step"] = float(t.item())
+        out["value"] = world * 1e3 / out["ms_per_step"]
+        out["n_gpus"] = world
+        if rank == 0:
+            print(json.dumps(out))
+        dist.destroy_process_group()
+        return
+    print(json.dumps(run_gpu(args)))
+
+
+if __name__ == "__main__":
+    main()

@@ -149,6 +149,18 @@ typedef struct {
   double latency_ms;    /* serving: submit -> completion wall time */
 } minim_gpu_result;
 
+/* Measurement of the last minimise / batch call, taken by the library on the
+ * stream it launches on: CUDA events around every kernel launch. */
+typedef struct {
+  double kernel_ms;     /* summed device time of the minimiser kernel launches */
+  double wall_ms;       /* host wall time of the call */
+  int64_t launches;     /* minimiser kernel launches in the call */
+  double abytes;        /* algorithmic HBM bytes of the work done (all instances) */
+  double pairs32;       /* Lennard-Jones pair interactions in FP32 */
+  double pairs64;       /* ... and in FP64 */
+  int64_t iterations;   /* minimiser iterations (all instances) */
+} minim_gpu_run_stats;
+
 typedef struct minim_gpu_instance_s* minim_gpu_handle;
 typedef struct minim_gpu_batch_s* minim_gpu_batch;
 typedef struct minim_gpu_server_s* minim_gpu_server;
@@ -162,6 +174,8 @@ void minim_gpu_default_pf(minim_gpu_pf_params* out);
 void minim_gpu_default_bah(minim_gpu_bah_params* out);
 /* Number of potential/minimiser kernel launches issued by this process. */
 int64_t minim_gpu_launch_count(void);
+/* Statistics of the most recent minimise / batch_run call. */
+int minim_gpu_last_run_stats(minim_gpu_run_stats* out);
 
 /* ---- single instances ------------------------------------------------------ */
 /* Copies the host arrays into device-owned buffers; the caller keeps its own.
@@ -218,6 +232,24 @@ int minim_gpu_server_poll(minim_gpu_server s, uint64_t* ids, minim_gpu_result* r
 int minim_gpu_server_take(minim_gpu_server s, uint64_t id, double* x, size_t ndof);
 int minim_gpu_server_cancel(minim_gpu_server s, uint64_t id);
 int minim_gpu_server_destroy(minim_gpu_server s);
+
+/* ---- set-up introspection (host only; no GPU needed) ------------------------
+ * These expose the host-side set-up so it can be compared with the reference
+ * library: BarAndHinge elements in the order of BarAndHinge::init
+ * (src/potentials/BarAndHinge.cpp:16-67; topology of computeBondList /
+ * computeHingeList, lines 70-147), the greedy element colouring used by the
+ * gradient scatter, and PhaseField::init/initLocal products (kappa, kappaP,
+ * nodeVol, surfaceArea; src/potentials/PhaseField.cpp:78-235). */
+int minim_gpu_bah_elements(const minim_gpu_bah_params* q, const double* x0, size_t ndof, int cap,
+                           int* nbar, int* bars, double* bar_par, int* nhinge, int* hinges,
+                           double* hinge_par);
+int minim_gpu_bah_colouring(const minim_gpu_bah_params* q, const double* x0, size_t ndof,
+                            int* nbar_colors, int* nhinge_colors, int* valid);
+/* kernel_variant: 1 = general PhaseField kernel, 3 = binary kernel without
+ * optional terms. */
+int minim_gpu_pf_setup(const minim_gpu_pf_params* q, const double* x0, size_t ndof, double* kappa,
+                       double* kappaP, int* nk, double* node_vol, double* surface_area,
+                       int* kernel_variant);
 
 #ifdef __cplusplus
 }

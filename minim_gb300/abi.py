@@ -82,6 +82,12 @@ class Result(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class RunStats(C.Structure):
+    _fields_ = [("kernel_ms", C.c_double), ("wall_ms", C.c_double), ("launches", C.c_int64),
+                ("abytes", C.c_double), ("pairs32", C.c_double), ("pairs64", C.c_double),
+                ("iterations", C.c_int64)]
+
+
 class ServerConfig(C.Structure):
     _fields_ = [("max_bytes", C.c_size_t), ("max_slots", C.c_int), ("slice_iters", C.c_int),
                 ("threads_per_cta", C.c_int)]

@@ -1,0 +1,1008 @@
+// capi.cpp -- host runtime behind include/minim_gpu.h.
+//
+// One process, one GPU (the current CUDA device, which must be sm_103).
+// Device memory comes from the stream-ordered pool (cudaMallocAsync with a
+// release threshold that keeps freed blocks cached), so admitting and
+// retiring thousands of instances does not hit the driver allocator.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <deque>
+#include <mutex>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "engine.h"
+#include "minim_gpu.h"
+#include "setup.h"
+
+using namespace mg;
+
+namespace {
+
+thread_local std::string g_err;
+std::atomic<int64_t> g_launches{0};
+minim_gpu_run_stats g_stats{};
+std::recursive_mutex g_mu;
+
+struct ApiError {
+  int code;
+  std::string msg;
+};
+
+#define CK(call)                                                                              \
+  do {                                                                                        \
+    cudaError_t e_ = (call);                                                                  \
+    if (e_ != cudaSuccess)                                                                    \
+      throw ApiError{e_ == cudaErrorMemoryAllocation ? MINIM_GPU_ERR_OOM : MINIM_GPU_ERR_CUDA, \
+                     std::string(#call) + ": " + cudaGetErrorString(e_)};                     \
+  } while (0)
+
+double now_ms() {
+  using namespace std::chrono;
+  return duration<double, std::milli>(steady_clock::now().time_since_epoch()).count();
+}
+
+// ---- device ------------------------------------------------------------------
+struct Dev {
+  int ok = 0;
+  int id = 0;
+  int nsm = 0;
+  std::string why;
+  cudaStream_t s = nullptr;             // runtime stream (allocations, copies)
+  cudaStream_t ks[4] = {nullptr, nullptr, nullptr, nullptr};  // one per kernel kind
+};
+
+Dev& dev() {
+  static Dev d;
+  static bool inited = false;
+  if (inited) return d;
+  inited = true;
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+    d.why = "no CUDA device";
+    return d;
+  }
+  cudaGetDevice(&d.id);
+  cudaDeviceProp p;
+  cudaGetDeviceProperties(&p, d.id);
+  if (!(p.major == 10 && p.minor == 3)) {
+    d.why = std::string("the kernels are built for sm_103a; device is sm_") + std::to_string(p.major) +
+            std::to_string(p.minor);
+    return d;
+  }
+  d.nsm = p.multiProcessorCount;
+  cudaStreamCreateWithFlags(&d.s, cudaStreamNonBlocking);
+  for (auto& k : d.ks) cudaStreamCreateWithFlags(&k, cudaStreamNonBlocking);
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, d.id) == cudaSuccess) {
+    uint64_t thr = UINT64_MAX;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+  }
+  d.ok = 1;
+  return d;
+}
+
+Dev& need_dev() {
+  Dev& d = dev();
+  if (!d.ok) throw ApiError{MINIM_GPU_ERR_NO_DEVICE, "minim_gpu: " + d.why};
+  return d;
+}
+
+void* dalloc(size_t bytes) {
+  if (bytes == 0) bytes = 256;
+  void* p = nullptr;
+  CK(cudaMallocAsync(&p, bytes, need_dev().s));
+  return p;
+}
+void dfree(void* p) {
+  if (p) cudaFreeAsync(p, dev().s);
+}
+template <typename T>
+T* upload(const std::vector<T>& v) {
+  if (v.empty()) return nullptr;
+  T* p = (T*)dalloc(v.size() * sizeof(T));
+  CK(cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, dev().s));
+  return p;
+}
+
+// ---- kernel table ---------------------------------------------------------------
+struct Kern {
+  int (*batch)(const InstDesc*, int, int*, int, int, int, size_t, void*);
+  int (*grid)(const InstDesc*, int, const EvalIO*, int, GridSyncState*, double*, int, int, size_t, void*);
+  int (*occ)(int, int, size_t, int*);
+};
+Kern kern(int kk) {
+  switch (kk) {
+    case K_LJ: return {mg_launch_batch_lj, mg_launch_grid_lj, mg_occupancy_lj};
+    case K_PF: return {mg_launch_batch_pf, mg_launch_grid_pf, mg_occupancy_pf};
+    case K_BAH: return {mg_launch_batch_bah, mg_launch_grid_bah, mg_occupancy_bah};
+    default: return {mg_launch_batch_pf1, mg_launch_grid_pf1, mg_occupancy_pf1};
+  }
+}
+const size_t kLjTileBytes = 1024 * 32;  // 1024 particles of 4 doubles
+size_t pot_smem(int kk) { return kk == K_LJ ? kLjTileBytes : 0; }
+
+// ---- workspace layout --------------------------------------------------------------
+struct WsLayout {
+  size_t x32[2], x64[2], g[2], S, Y, V, total;
+  int nS, nY;
+  bool fp64;
+};
+size_t align256(size_t v) { return (v + 255) & ~(size_t)255; }
+WsLayout ws_layout(size_t n, const minim_gpu_minimiser_params& mp) {
+  WsLayout L{};
+  size_t o = 0;
+  auto take = [&](size_t bytes) { size_t r = o; o += align256(bytes); return r; };
+  L.fp64 = mp.precision != MINIM_PREC_FP32;
+  L.nS = mp.method == MINIM_LBFGS ? mp.m + 1 : (mp.method == MINIM_FIRE ? 1 : 0);
+  L.nY = mp.method == MINIM_LBFGS ? mp.m + 1 : 0;
+  for (int k = 0; k < 2; k++) L.x32[k] = take(n * 4);
+  for (int k = 0; k < 2; k++) L.x64[k] = L.fp64 ? take(n * 8) : (size_t)-1;
+  for (int k = 0; k < 2; k++) L.g[k] = take(n * 4);
+  L.S = L.nS ? take((size_t)L.nS * n * 4) : (size_t)-1;
+  L.Y = L.nY ? take((size_t)L.nY * n * 4) : (size_t)-1;
+  L.V = mp.method == MINIM_FIRE ? take(n * 4) : (size_t)-1;
+  L.total = o;
+  return L;
+}
+void ws_apply(InstDesc& d, char* base, const WsLayout& L) {
+  for (int k = 0; k < 2; k++) {
+    d.X32[k] = (float*)(base + L.x32[k]);
+    d.X64[k] = L.fp64 ? (double*)(base + L.x64[k]) : nullptr;
+    d.G[k] = (float*)(base + L.g[k]);
+  }
+  d.Sb = L.nS ? (float*)(base + L.S) : nullptr;
+  d.Yb = L.nY ? (float*)(base + L.Y) : nullptr;
+  d.V = L.V != (size_t)-1 ? (float*)(base + L.V) : nullptr;
+}
+
+void check_mp(const minim_gpu_minimiser_params& mp) {
+  if (mp.method < 0 || mp.method > 2) throw ApiError{MINIM_GPU_ERR_INVALID, "unknown minimiser method"};
+  if (mp.linesearch != MINIM_LS_BACKTRACKING && mp.linesearch != MINIM_LS_NONE)
+    throw ApiError{MINIM_GPU_ERR_INVALID, "Invalid line search method."};
+  if (mp.method == MINIM_LBFGS && (mp.m < 1 || mp.m > MINIM_MAXM))
+    throw ApiError{MINIM_GPU_ERR_INVALID, "Lbfgs: m must be between 1 and 16 on the device"};
+  if (mp.precision < 0 || mp.precision > 2) throw ApiError{MINIM_GPU_ERR_INVALID, "unknown precision"};
+}
+
+MinParams to_mp(const minim_gpu_minimiser_params& q, double tol) {
+  MinParams p{};
+  p.method = q.method;
+  p.linesearch = q.linesearch;
+  p.max_iter = q.max_iter;
+  p.m = q.method == MINIM_LBFGS ? q.m : 0;
+  p.precision = q.precision;
+  p.tol = tol;
+  p.max_step = q.max_step;
+  p.init_step = q.init_step;
+  p.dt_max = q.dt_max;
+  p.alpha = q.alpha;
+  return p;
+}
+
+MinScalars fresh_scalars() {
+  MinScalars s;
+  std::memset(&s, 0, sizeof s);
+  s.status = ST_RUNNING;
+  return s;
+}
+
+void fill_result(minim_gpu_result* r, const MinScalars& s, size_t n) {
+  std::memset(r, 0, sizeof *r);
+  r->status = s.status;
+  r->iter = s.iter;
+  r->fp64_iters = s.fp64_iters;
+  r->evals = s.evals;
+  r->energy = s.E;
+  r->rms = std::sqrt(s.gg / (double)n);
+  r->dt_max = s.dtmax;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Instances
+// ---------------------------------------------------------------------------
+struct minim_gpu_instance_s {
+  int kind = 0;
+  int kk = 0;        // kernel kind
+  size_t n = 0;
+  InstDesc d{};      // potential part + resident pointers
+  std::vector<void*> owned;
+  double default_tol = 1e-6;
+  BahHost bah;
+  std::vector<unsigned char> fixed;
+  size_t pot_bytes = 0;
+  // grid-launch resources (lazy)
+  InstDesc* d_desc = nullptr;
+  EvalIO* d_io = nullptr;
+  GridSyncState* d_bar = nullptr;
+  double* d_partials = nullptr;
+  double* d_tmp = nullptr;   // n doubles: API coordinates / vectors
+  double* d_g = nullptr;     // n doubles: API gradient
+  double* d_e = nullptr;
+  int gblocks = 0, gthreads = 256;
+  // single-instance workspace (lazy)
+  void* ws = nullptr;
+  size_t ws_bytes = 0;
+  MinScalars* d_st = nullptr;
+
+  void* own(void* p) {
+    if (p) owned.push_back(p);
+    return p;
+  }
+  template <typename T>
+  T* own_upload(const std::vector<T>& v) {
+    T* p = upload(v);
+    own(p);
+    pot_bytes += v.size() * sizeof(T);
+    return p;
+  }
+  ~minim_gpu_instance_s() {
+    for (void* p : owned) dfree(p);
+    dfree(ws);
+  }
+};
+
+namespace {
+
+void upload_bah_arrays(minim_gpu_instance_s* h) {
+  BahDevArrays A = bah_arrays(h->bah, h->fixed);
+  PotBAH& P = h->d.bah;
+  P.nvert = h->bah.nvert;
+  P.nbar = (int)A.bars.size();
+  P.nhinge = (int)A.hinges.size();
+  P.bars = h->own_upload(A.bars);
+  P.bar_par = h->own_upload(A.bpar);
+  P.hinges = h->own_upload(A.hinges);
+  P.hinge_par = h->own_upload(A.hpar);
+  P.nbar_colors = (int)A.bar_off.size() - 1;
+  P.nhinge_colors = (int)A.hinge_off.size() - 1;
+  P.bar_color_off = h->own_upload(A.bar_off);
+  P.hinge_color_off = h->own_upload(A.hinge_off);
+  P.node_el = h->own_upload(A.node_el);
+  P.nforce = (int)h->bah.force.size();
+  P.force = h->own_upload(h->bah.force);
+  P.wall_on = h->bah.wall_on;
+  P.wall_adh = h->bah.wall_adh;
+  P.wall_eps = h->bah.wall_eps;
+  P.wall_sig = h->bah.wall_sig;
+}
+
+minim_gpu_instance_s* create_instance(int kind, const void* params, const double* x0, size_t ndof) {
+  need_dev();
+  if (!params || !x0 || ndof == 0) throw ApiError{MINIM_GPU_ERR_INVALID, "null parameters or empty coordinates"};
+  if (ndof > 0x7fffffffULL) throw ApiError{MINIM_GPU_ERR_INVALID, "too many degrees of freedom"};
+  auto h = new minim_gpu_instance_s();
+  try {
+    h->kind = kind;
+    h->n = ndof;
+    h->d.kind = kind;
+    h->d.ndof = (int)ndof;
+    if (kind == MINIM_GPU_LJ) {
+      auto q = (const minim_gpu_lj_params*)params;
+      if (q->ndim < 2 || q->ndim > 3 || ndof % q->ndim)
+        throw ApiError{MINIM_GPU_ERR_INVALID, "LjNd: Length of coords must be a multiple of the number of dimensions."};
+      h->kk = K_LJ;
+      h->d.lj.ndim = q->ndim;
+      h->d.lj.np = (int)(ndof / q->ndim);
+      h->d.lj.s6 = std::pow(q->sigma, 6);
+      h->d.lj.eps = q->epsilon;
+    } else if (kind == MINIM_GPU_PF) {
+      PfHost H = setup_pf(*(const minim_gpu_pf_params*)params, x0, ndof);
+      h->kk = H.kernel_kind;
+      h->default_tol = H.default_tol;
+      h->d.pf = H.pot;
+      h->d.pf.aux = h->own_upload(H.aux);
+      h->d.pf.wet = h->own_upload(H.wet);
+      h->d.pf.kappa_node = h->own_upload(H.kappa_node);
+      h->d.pf.kappaP_node = h->own_upload(H.kappaP_node);
+      h->d.pf.ff_init = h->own_upload(H.ff_init);
+    } else if (kind == MINIM_GPU_BAH) {
+      h->kk = K_BAH;
+      h->bah = setup_bah(*(const minim_gpu_bah_params*)params, x0, ndof);
+      upload_bah_arrays(h);
+      h->d.GA = (double*)h->own(dalloc(ndof * sizeof(double)));
+    } else {
+      throw ApiError{MINIM_GPU_ERR_INVALID, "unknown potential kind"};
+    }
+    h->d.kind = kind;
+    h->d.xres = (double*)h->own(dalloc(ndof * sizeof(double)));
+    CK(cudaMemcpyAsync(h->d.xres, x0, ndof * sizeof(double), cudaMemcpyHostToDevice, dev().s));
+    CK(cudaStreamSynchronize(dev().s));
+  } catch (...) {
+    delete h;
+    throw;
+  }
+  return h;
+}
+
+void ensure_grid(minim_gpu_instance_s* h) {
+  Dev& D = need_dev();
+  if (h->d_desc) return;
+  int per_sm = 0;
+  CK((cudaError_t)kern(h->kk).occ(1, h->gthreads, pot_smem(h->kk), &per_sm));
+  if (per_sm < 1) throw ApiError{MINIM_GPU_ERR_CUDA, "grid kernel does not fit on an SM"};
+  h->gblocks = D.nsm * per_sm;
+  h->d_desc = (InstDesc*)h->own(dalloc(sizeof(InstDesc)));
+  h->d_io = (EvalIO*)h->own(dalloc(sizeof(EvalIO)));
+  h->d_bar = (GridSyncState*)h->own(dalloc(sizeof(GridSyncState)));
+  h->d_partials = (double*)h->own(dalloc(2 * (size_t)h->gblocks * 8 * sizeof(double)));
+  h->d_e = (double*)h->own(dalloc(sizeof(double)));
+  h->d_tmp = (double*)h->own(dalloc(h->n * sizeof(double)));
+  h->d_g = (double*)h->own(dalloc(h->n * sizeof(double)));
+}
+
+void launch_grid(minim_gpu_instance_s* h, int op, int slice) {
+  Dev& D = need_dev();
+  CK(cudaMemsetAsync(h->d_bar, 0, sizeof(GridSyncState), D.s));
+  CK((cudaError_t)kern(h->kk).grid(h->d_desc, op, h->d_io, slice, h->d_bar, h->d_partials, h->gthreads,
+                                    h->gblocks, pot_smem(h->kk), D.s));
+  g_launches++;
+}
+
+int grid_error(minim_gpu_instance_s* h) {
+  GridSyncState b;
+  CK(cudaMemcpyAsync(&b, h->d_bar, sizeof b, cudaMemcpyDeviceToHost, dev().s));
+  CK(cudaStreamSynchronize(dev().s));
+  return b.err;
+}
+
+void do_eval(minim_gpu_instance_s* h, const double* x, double* e, double* g) {
+  Dev& D = need_dev();
+  ensure_grid(h);
+  const double* xd = h->d.xres;
+  if (x) {
+    CK(cudaMemcpyAsync(h->d_tmp, x, h->n * sizeof(double), cudaMemcpyHostToDevice, D.s));
+    xd = h->d_tmp;
+  }
+  EvalIO io{xd, g ? h->d_g : nullptr, h->d_e, nullptr};
+  InstDesc d = h->d;
+  d.fixed = h->d.fixed;
+  CK(cudaMemcpyAsync(h->d_desc, &d, sizeof d, cudaMemcpyHostToDevice, D.s));
+  CK(cudaMemcpyAsync(h->d_io, &io, sizeof io, cudaMemcpyHostToDevice, D.s));
+  launch_grid(h, OP_EVAL, 0);
+  double ev = 0;
+  CK(cudaMemcpyAsync(&ev, h->d_e, sizeof(double), cudaMemcpyDeviceToHost, D.s));
+  if (g) CK(cudaMemcpyAsync(g, h->d_g, h->n * sizeof(double), cudaMemcpyDeviceToHost, D.s));
+  CK(cudaStreamSynchronize(D.s));
+  if (grid_error(h)) throw ApiError{MINIM_GPU_ERR_RUNTIME, "device barrier timed out"};
+  if (e) *e = ev;
+}
+
+void do_minimise(minim_gpu_instance_s* h, const minim_gpu_minimiser_params& mp, minim_gpu_result* res) {
+  Dev& D = need_dev();
+  check_mp(mp);
+  ensure_grid(h);
+  const double tol = mp.tol >= 0 ? mp.tol : h->default_tol;
+  WsLayout L = ws_layout(h->n, mp);
+  const size_t need = L.total + align256(sizeof(MinScalars));
+  if (need > h->ws_bytes) {
+    dfree(h->ws);
+    h->ws = dalloc(need);
+    h->ws_bytes = need;
+  }
+  InstDesc d = h->d;
+  ws_apply(d, (char*)h->ws, L);
+  d.mp = to_mp(mp, tol);
+  h->d_st = (MinScalars*)((char*)h->ws + L.total);
+  d.st = h->d_st;
+  MinScalars s = fresh_scalars();
+  CK(cudaMemcpyAsync(h->d_st, &s, sizeof s, cudaMemcpyHostToDevice, D.s));
+  CK(cudaMemcpyAsync(h->d_desc, &d, sizeof d, cudaMemcpyHostToDevice, D.s));
+  int slice = 64;
+  const double t0 = now_ms();
+  minim_gpu_run_stats stats{};
+  cudaEvent_t ev0, ev1;
+  CK(cudaEventCreate(&ev0));
+  CK(cudaEventCreate(&ev1));
+  for (;;) {
+    CK(cudaEventRecord(ev0, D.s));
+    launch_grid(h, OP_MINIMISE, slice);
+    CK(cudaEventRecord(ev1, D.s));
+    CK(cudaMemcpyAsync(&s, h->d_st, sizeof s, cudaMemcpyDeviceToHost, D.s));
+    CK(cudaStreamSynchronize(D.s));
+    float ms = 0;
+    CK(cudaEventElapsedTime(&ms, ev0, ev1));
+    stats.kernel_ms += ms;
+    stats.launches++;
+    if (s.status != ST_RUNNING) break;
+    if (grid_error(h)) {
+      s.status = ST_TIMEOUT;
+      break;
+    }
+    slice = std::min(slice * 2, 4096);
+  }
+  cudaEventDestroy(ev0);
+  cudaEventDestroy(ev1);
+  stats.wall_ms = now_ms() - t0;
+  stats.abytes = s.abytes;
+  stats.pairs32 = s.pairs32;
+  stats.pairs64 = s.pairs64;
+  stats.iterations = s.iter + (s.status == ST_CONVERGED ? 1 : 0);
+  g_stats = stats;
+  if (res) fill_result(res, s, h->n);
+}
+
+template <class F>
+int guarded(F&& f) {
+  std::lock_guard<std::recursive_mutex> lk(g_mu);
+  try {
+    f();
+    return MINIM_GPU_OK;
+  } catch (const ApiError& e) {
+    g_err = e.msg;
+    return e.code;
+  } catch (const SetupError& e) {
+    g_err = e.what();
+    return e.code;
+  } catch (const std::bad_alloc&) {
+    g_err = "host allocation failed";
+    return MINIM_GPU_ERR_OOM;
+  } catch (const std::exception& e) {
+    g_err = e.what();
+    return MINIM_GPU_ERR_RUNTIME;
+  }
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Batches
+// ---------------------------------------------------------------------------
+struct minim_gpu_batch_s {
+  std::vector<minim_gpu_handle> inst;
+  std::vector<minim_gpu_minimiser_params> mp;
+};
+
+namespace {
+
+int default_threads(int kk, const std::vector<InstDesc>& ds) {
+  if (kk == K_LJ) {
+    int nmax = 0;
+    for (auto& d : ds) nmax = std::max(nmax, d.lj.np);
+    return nmax <= 96 ? 64 : (nmax <= 192 ? 128 : 256);
+  }
+  return 256;
+}
+
+double cost_of(const InstDesc& d, int kk) {
+  if (kk == K_LJ) return (double)d.lj.np * d.lj.np;
+  if (kk == K_BAH) return (double)d.bah.nbar + 4.0 * d.bah.nhinge + d.ndof;
+  return (double)d.ndof;
+}
+
+// Runs the given instances with the batch kernels (one launch per kernel
+// kind, the kinds concurrently on their own streams).  descs[i].st must
+// point into d_st.  Returns when all launches are done.
+void run_batch(std::vector<InstDesc>& descs, const std::vector<int>& kks, MinScalars* d_st,
+               const std::vector<MinScalars>& st_init, int slice, int threads) {
+  Dev& D = need_dev();
+  const int n = (int)descs.size();
+  if (n == 0) return;
+  if (!st_init.empty())
+    CK(cudaMemcpyAsync(d_st, st_init.data(), n * sizeof(MinScalars), cudaMemcpyHostToDevice, D.s));
+  // group by kernel kind, largest first within a group
+  std::vector<int> order(n);
+  for (int i = 0; i < n; i++) order[i] = i;
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+    if (kks[a] != kks[b]) return kks[a] < kks[b];
+    return cost_of(descs[a], kks[a]) > cost_of(descs[b], kks[b]);
+  });
+  std::vector<InstDesc> sorted(n);
+  for (int i = 0; i < n; i++) sorted[i] = descs[order[i]];
+  InstDesc* d_descs = (InstDesc*)dalloc(n * sizeof(InstDesc));
+  int* d_counters = (int*)dalloc(4 * sizeof(int));
+  CK(cudaMemcpyAsync(d_descs, sorted.data(), n * sizeof(InstDesc), cudaMemcpyHostToDevice, D.s));
+  CK(cudaMemsetAsync(d_counters, 0, 4 * sizeof(int), D.s));
+  cudaEvent_t ready, t_end;
+  CK(cudaEventCreate(&ready));
+  CK(cudaEventCreate(&t_end));
+  CK(cudaEventRecord(ready, D.s));
+  int i0 = 0;
+  std::vector<cudaEvent_t> done;
+  while (i0 < n) {
+    const int kk = kks[order[i0]];
+    int i1 = i0;
+    while (i1 < n && kks[order[i1]] == kk) i1++;
+    std::vector<InstDesc> grp(sorted.begin() + i0, sorted.begin() + i1);
+    const int thr = threads > 0 ? threads : default_threads(kk, grp);
+    const size_t smem = pot_smem(kk);
+    int per_sm = 0;
+    CK((cudaError_t)kern(kk).occ(0, thr, smem, &per_sm));
+    if (per_sm < 1) throw ApiError{MINIM_GPU_ERR_CUDA, "batch kernel does not fit on an SM"};
+    const int blocks = std::min(i1 - i0, D.nsm * per_sm);
+    cudaStream_t ks = D.ks[kk];
+    CK(cudaStreamWaitEvent(ks, ready, 0));
+    CK((cudaError_t)kern(kk).batch(d_descs + i0, i1 - i0, d_counters + kk, slice, thr, blocks, smem, ks));
+    g_launches++;
+    cudaEvent_t ev;
+    CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    CK(cudaEventRecord(ev, ks));
+    done.push_back(ev);
+    i0 = i1;
+  }
+  for (auto ev : done) {
+    CK(cudaStreamWaitEvent(D.s, ev, 0));
+    cudaEventDestroy(ev);
+  }
+  CK(cudaEventRecord(t_end, D.s));
+  CK(cudaEventSynchronize(t_end));
+  float ms = 0;
+  CK(cudaEventElapsedTime(&ms, ready, t_end));
+  g_stats.kernel_ms = ms;
+  g_stats.launches = (int64_t)done.size();
+  cudaEventDestroy(ready);
+  cudaEventDestroy(t_end);
+  dfree(d_descs);
+  dfree(d_counters);
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Server (continuous batching)
+// ---------------------------------------------------------------------------
+namespace {
+struct Request {
+  uint64_t id = 0;
+  minim_gpu_instance_s* inst = nullptr;
+  minim_gpu_minimiser_params mp{};
+  double tol = 0;
+  int state = 0;  // 0 queued, 1 resident, 2 done
+  int slot = -1;
+  void* ws = nullptr;
+  size_t bytes = 0;
+  double t_submit = 0, t_done = 0;
+  minim_gpu_result res{};
+  bool polled = false;
+};
+}  // namespace
+
+struct minim_gpu_server_s {
+  minim_gpu_server_config cfg{};
+  uint64_t next_id = 1;
+  std::unordered_map<uint64_t, Request> reqs;
+  std::deque<uint64_t> queue;
+  std::vector<uint64_t> slots;    // slot -> request id (0 = free)
+  std::vector<uint64_t> done;     // finished, not yet polled
+  size_t bytes_in_use = 0;
+  MinScalars* d_st = nullptr;     // one per slot
+  std::vector<InstDesc> descs;    // per slot (valid where resident)
+  ~minim_gpu_server_s() {
+    for (auto& kv : reqs) {
+      dfree(kv.second.ws);
+      delete kv.second.inst;
+    }
+    dfree(d_st);
+  }
+};
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+extern "C" {
+
+int minim_gpu_abi_version(void) { return MINIM_GPU_ABI_VERSION; }
+
+int minim_gpu_last_error(char* buf, size_t len) {
+  if (buf && len) {
+    std::strncpy(buf, g_err.c_str(), len - 1);
+    buf[len - 1] = 0;
+  }
+  return (int)g_err.size();
+}
+
+int64_t minim_gpu_launch_count(void) { return g_launches.load(); }
+
+int minim_gpu_last_run_stats(minim_gpu_run_stats* out) {
+  return guarded([&] { *out = g_stats; });
+}
+
+void minim_gpu_default_minimiser(int method, minim_gpu_minimiser_params* p) {
+  std::memset(p, 0, sizeof *p);
+  p->method = method;
+  p->linesearch = MINIM_LS_BACKTRACKING;
+  p->max_iter = 100000;
+  p->tol = -1;
+  p->m = 5;
+  p->max_step = 0;
+  p->init_step = 1;
+  p->dt_max = 0;
+  p->alpha = 0.1;
+  p->precision = MINIM_PREC_MIXED;
+}
+
+void minim_gpu_default_pf(minim_gpu_pf_params* p) {
+  std::memset(p, 0, sizeof *p);
+  p->grid[0] = p->grid[1] = p->grid[2] = 1;
+  p->nfluid = 1;
+  p->resolution = 1;
+  p->density_constraint = MINIM_PF_DENSITY_HARD;
+  p->density_const = 1;
+  p->vol_const = 0.01;
+}
+
+void minim_gpu_default_bah(minim_gpu_bah_params* p) {
+  std::memset(p, 0, sizeof *p);
+  p->bond_stride = 2;
+  p->hinge_stride = 4;
+  p->modulus = 1;
+  p->poisson_ratio = 0.3;
+  p->wall_epsilon = 1e-12;
+  p->wall_sigma = 1e-5;
+}
+
+int minim_gpu_instance_create(int kind, const void* params, const double* x0, size_t ndof,
+                              minim_gpu_handle* out) {
+  return guarded([&] {
+    if (!out) throw ApiError{MINIM_GPU_ERR_INVALID, "null output handle"};
+    *out = create_instance(kind, params, x0, ndof);
+  });
+}
+
+int minim_gpu_instance_destroy(minim_gpu_handle h) {
+  return guarded([&] { delete h; });
+}
+
+int minim_gpu_instance_ndof(minim_gpu_handle h, size_t* n) {
+  return guarded([&] { *n = h->n; });
+}
+
+int minim_gpu_instance_default_tol(minim_gpu_handle h, double* tol) {
+  return guarded([&] { *tol = h->default_tol; });
+}
+
+int minim_gpu_instance_set_coords(minim_gpu_handle h, const double* x) {
+  return guarded([&] {
+    CK(cudaMemcpyAsync(h->d.xres, x, h->n * sizeof(double), cudaMemcpyHostToDevice, need_dev().s));
+    CK(cudaStreamSynchronize(dev().s));
+  });
+}
+
+int minim_gpu_instance_get_coords(minim_gpu_handle h, double* x) {
+  return guarded([&] {
+    CK(cudaMemcpyAsync(x, h->d.xres, h->n * sizeof(double), cudaMemcpyDeviceToHost, need_dev().s));
+    CK(cudaStreamSynchronize(dev().s));
+  });
+}
+
+int minim_gpu_instance_set_fixed(minim_gpu_handle h, const int* idof, size_t n) {
+  return guarded([&] {
+    std::vector<unsigned char> f(h->n, 0);
+    for (size_t i = 0; i < n; i++) {
+      if (idof[i] < 0 || (size_t)idof[i] >= h->n) throw ApiError{MINIM_GPU_ERR_INVALID, "fixed dof out of range"};
+      f[idof[i]] = 1;
+    }
+    h->fixed = n ? f : std::vector<unsigned char>();
+    h->d.fixed = h->own_upload(h->fixed);
+    if (h->kind == MINIM_GPU_BAH) upload_bah_arrays(h);
+    CK(cudaStreamSynchronize(dev().s));
+  });
+}
+
+int minim_gpu_energy_gradient(minim_gpu_handle h, const double* x, double* e, double* g) {
+  return guarded([&] { do_eval(h, x, e, g); });
+}
+
+int minim_gpu_apply_constraints(minim_gpu_handle h, double* v) {
+  return guarded([&] {
+    Dev& D = need_dev();
+    ensure_grid(h);
+    CK(cudaMemcpyAsync(h->d_tmp, v, h->n * sizeof(double), cudaMemcpyHostToDevice, D.s));
+    EvalIO io{nullptr, nullptr, nullptr, h->d_tmp};
+    CK(cudaMemcpyAsync(h->d_desc, &h->d, sizeof(InstDesc), cudaMemcpyHostToDevice, D.s));
+    CK(cudaMemcpyAsync(h->d_io, &io, sizeof io, cudaMemcpyHostToDevice, D.s));
+    launch_grid(h, OP_CONSTRAIN, 0);
+    CK(cudaMemcpyAsync(v, h->d_tmp, h->n * sizeof(double), cudaMemcpyDeviceToHost, D.s));
+    CK(cudaStreamSynchronize(D.s));
+  });
+}
+
+int minim_gpu_minimise(minim_gpu_handle h, const minim_gpu_minimiser_params* mp, minim_gpu_result* res) {
+  return guarded([&] {
+    if (!mp) throw ApiError{MINIM_GPU_ERR_INVALID, "null minimiser parameters"};
+    do_minimise(h, *mp, res);
+  });
+}
+
+int minim_gpu_batch_create(minim_gpu_batch* out) {
+  return guarded([&] { *out = new minim_gpu_batch_s(); });
+}
+
+int minim_gpu_batch_add(minim_gpu_batch b, minim_gpu_handle h, const minim_gpu_minimiser_params* mp) {
+  return guarded([&] {
+    if (!b || !h || !mp) throw ApiError{MINIM_GPU_ERR_INVALID, "null argument"};
+    check_mp(*mp);
+    b->inst.push_back(h);
+    b->mp.push_back(*mp);
+  });
+}
+
+int minim_gpu_batch_run(minim_gpu_batch b, int threads, minim_gpu_result* results) {
+  return guarded([&] {
+    Dev& D = need_dev();
+    const int n = (int)b->inst.size();
+    if (n == 0) return;
+    std::vector<WsLayout> L(n);
+    std::vector<size_t> off(n);
+    size_t total = 0;
+    for (int i = 0; i < n; i++) {
+      L[i] = ws_layout(b->inst[i]->n, b->mp[i]);
+      off[i] = total;
+      total += L[i].total;
+    }
+    char* arena = (char*)dalloc(total);
+    MinScalars* d_st = (MinScalars*)dalloc(n * sizeof(MinScalars));
+    std::vector<InstDesc> descs(n);
+    std::vector<int> kks(n);
+    for (int i = 0; i < n; i++) {
+      InstDesc d = b->inst[i]->d;
+      ws_apply(d, arena + off[i], L[i]);
+      const double tol = b->mp[i].tol >= 0 ? b->mp[i].tol : b->inst[i]->default_tol;
+      d.mp = to_mp(b->mp[i], tol);
+      d.st = d_st + i;
+      descs[i] = d;
+      kks[i] = b->inst[i]->kk;
+    }
+    std::vector<MinScalars> st(n, fresh_scalars());
+    const double t0 = now_ms();
+    run_batch(descs, kks, d_st, st, 0x7fffffff, threads);
+    CK(cudaMemcpyAsync(st.data(), d_st, n * sizeof(MinScalars), cudaMemcpyDeviceToHost, D.s));
+    CK(cudaStreamSynchronize(D.s));
+    g_stats.wall_ms = now_ms() - t0;
+    g_stats.abytes = g_stats.pairs32 = g_stats.pairs64 = 0;
+    g_stats.iterations = 0;
+    for (auto& s : st) {
+      g_stats.abytes += s.abytes;
+      g_stats.pairs32 += s.pairs32;
+      g_stats.pairs64 += s.pairs64;
+      g_stats.iterations += s.iter + (s.status == ST_CONVERGED ? 1 : 0);
+    }
+    dfree(arena);
+    dfree(d_st);
+    if (results)
+      for (int i = 0; i < n; i++) fill_result(&results[i], st[i], b->inst[i]->n);
+  });
+}
+
+int minim_gpu_batch_destroy(minim_gpu_batch b) {
+  return guarded([&] { delete b; });
+}
+
+int minim_gpu_server_create(const minim_gpu_server_config* cfg, minim_gpu_server* out) {
+  return guarded([&] {
+    need_dev();
+    auto s = new minim_gpu_server_s();
+    if (cfg) s->cfg = *cfg;
+    if (s->cfg.max_slots <= 0) s->cfg.max_slots = 4096;
+    if (s->cfg.slice_iters <= 0) s->cfg.slice_iters = 64;
+    if (s->cfg.max_bytes == 0) {
+      size_t fr = 0, tot = 0;
+      cudaMemGetInfo(&fr, &tot);
+      s->cfg.max_bytes = fr / 2;
+    }
+    s->slots.assign(s->cfg.max_slots, 0);
+    s->descs.resize(s->cfg.max_slots);
+    s->d_st = (MinScalars*)dalloc(s->cfg.max_slots * sizeof(MinScalars));
+    *out = s;
+  });
+}
+
+int minim_gpu_server_submit(minim_gpu_server s, int kind, const void* params, const double* x0, size_t ndof,
+                            const minim_gpu_minimiser_params* mp, uint64_t* request_id) {
+  return guarded([&] {
+    if (!mp) throw ApiError{MINIM_GPU_ERR_INVALID, "null minimiser parameters"};
+    check_mp(*mp);
+    Request r;
+    r.id = s->next_id++;
+    r.inst = create_instance(kind, params, x0, ndof);
+    r.mp = *mp;
+    r.tol = mp->tol >= 0 ? mp->tol : r.inst->default_tol;
+    r.bytes = ws_layout(ndof, *mp).total;
+    r.t_submit = now_ms();
+    if (r.bytes + r.inst->pot_bytes > s->cfg.max_bytes) {
+      r.state = 2;
+      r.res.status = MINIM_RES_REJECTED;
+      r.t_done = r.t_submit;
+      s->done.push_back(r.id);
+    } else {
+      s->queue.push_back(r.id);
+    }
+    if (request_id) *request_id = r.id;
+    s->reqs.emplace(r.id, r);
+  });
+}
+
+int minim_gpu_server_step(minim_gpu_server s, int* n_resident, int* n_queued) {
+  return guarded([&] {
+    Dev& D = need_dev();
+    // admit
+    std::vector<int> admitted;
+    int free_slot = 0;
+    while (!s->queue.empty()) {
+      Request& r = s->reqs[s->queue.front()];
+      if (r.state != 0) {  // cancelled while queued
+        s->queue.pop_front();
+        continue;
+      }
+      if (s->bytes_in_use + r.bytes > s->cfg.max_bytes) break;
+      while (free_slot < s->cfg.max_slots && s->slots[free_slot]) free_slot++;
+      if (free_slot >= s->cfg.max_slots) break;
+      s->queue.pop_front();
+      WsLayout L = ws_layout(r.inst->n, r.mp);
+      r.ws = dalloc(L.total);
+      r.slot = free_slot;
+      r.state = 1;
+      s->slots[free_slot] = r.id;
+      s->bytes_in_use += r.bytes;
+      InstDesc d = r.inst->d;
+      ws_apply(d, (char*)r.ws, L);
+      d.mp = to_mp(r.mp, r.tol);
+      d.st = s->d_st + free_slot;
+      s->descs[free_slot] = d;
+      admitted.push_back(free_slot);
+    }
+    for (int slot : admitted) {
+      MinScalars st = fresh_scalars();
+      CK(cudaMemcpyAsync(s->d_st + slot, &st, sizeof st, cudaMemcpyHostToDevice, D.s));
+    }
+    // one slice on every resident instance
+    std::vector<InstDesc> descs;
+    std::vector<int> kks, slot_of;
+    for (int k = 0; k < s->cfg.max_slots; k++) {
+      if (!s->slots[k]) continue;
+      descs.push_back(s->descs[k]);
+      kks.push_back(s->reqs[s->slots[k]].inst->kk);
+      slot_of.push_back(k);
+    }
+    if (!descs.empty()) {
+      run_batch(descs, kks, s->d_st, {}, s->cfg.slice_iters, s->cfg.threads_per_cta);
+      std::vector<MinScalars> st(s->cfg.max_slots);
+      CK(cudaMemcpyAsync(st.data(), s->d_st, s->cfg.max_slots * sizeof(MinScalars), cudaMemcpyDeviceToHost, D.s));
+      CK(cudaStreamSynchronize(D.s));
+      const double t = now_ms();
+      for (int k : slot_of) {
+        if (st[k].status == ST_RUNNING) continue;
+        Request& r = s->reqs[s->slots[k]];
+        fill_result(&r.res, st[k], r.inst->n);
+        r.t_done = t;
+        r.res.latency_ms = t - r.t_submit;
+        r.state = 2;
+        dfree(r.ws);
+        r.ws = nullptr;
+        s->bytes_in_use -= r.bytes;
+        s->slots[k] = 0;
+        r.slot = -1;
+        s->done.push_back(r.id);
+      }
+    }
+    int res_n = 0;
+    for (auto id : s->slots) res_n += id != 0;
+    if (n_resident) *n_resident = res_n;
+    if (n_queued) *n_queued = (int)s->queue.size();
+  });
+}
+
+int minim_gpu_server_poll(minim_gpu_server s, uint64_t* ids, minim_gpu_result* res, int max, int* n_done) {
+  return guarded([&] {
+    int k = 0;
+    while (k < max && !s->done.empty()) {
+      const uint64_t id = s->done.front();
+      s->done.erase(s->done.begin());
+      Request& r = s->reqs[id];
+      r.polled = true;
+      if (ids) ids[k] = id;
+      if (res) res[k] = r.res;
+      k++;
+    }
+    if (n_done) *n_done = k;
+  });
+}
+
+int minim_gpu_server_take(minim_gpu_server s, uint64_t id, double* x, size_t ndof) {
+  return guarded([&] {
+    auto it = s->reqs.find(id);
+    if (it == s->reqs.end() || it->second.state != 2) throw ApiError{MINIM_GPU_ERR_BUSY, "request not finished"};
+    Request& r = it->second;
+    if (x) {
+      if (ndof != r.inst->n) throw ApiError{MINIM_GPU_ERR_INVALID, "wrong coordinate count"};
+      CK(cudaMemcpyAsync(x, r.inst->d.xres, ndof * sizeof(double), cudaMemcpyDeviceToHost, dev().s));
+      CK(cudaStreamSynchronize(dev().s));
+    }
+    delete r.inst;
+    s->reqs.erase(it);
+  });
+}
+
+int minim_gpu_server_cancel(minim_gpu_server s, uint64_t id) {
+  return guarded([&] {
+    auto it = s->reqs.find(id);
+    if (it == s->reqs.end()) throw ApiError{MINIM_GPU_ERR_BUSY, "unknown request"};
+    Request& r = it->second;
+    if (r.state == 2) return;
+    if (r.state == 1) {
+      s->slots[r.slot] = 0;
+      dfree(r.ws);
+      r.ws = nullptr;
+      s->bytes_in_use -= r.bytes;
+      r.slot = -1;
+    }
+    r.state = 2;
+    r.res.status = MINIM_RES_CANCELLED;
+    r.t_done = now_ms();
+    r.res.latency_ms = r.t_done - r.t_submit;
+    s->done.push_back(id);
+  });
+}
+
+int minim_gpu_server_destroy(minim_gpu_server s) {
+  return guarded([&] { delete s; });
+}
+
+// ---- host-only set-up introspection (no GPU needed) -------------------------
+int minim_gpu_bah_elements(const minim_gpu_bah_params* q, const double* x0, size_t ndof, int cap, int* nbar,
+                           int* bars, double* bar_par, int* nhinge, int* hinges, double* hinge_par) {
+  return guarded([&] {
+    BahHost B = setup_bah(*q, x0, ndof);
+    const int nb = (int)(B.bars.size() / 2), nh = (int)(B.hinges.size() / 4);
+    *nbar = nb;
+    *nhinge = nh;
+    if (nb <= cap) {
+      std::memcpy(bars, B.bars.data(), B.bars.size() * sizeof(int));
+      std::memcpy(bar_par, B.bpar.data(), B.bpar.size() * sizeof(double));
+    }
+    if (nh <= cap) {
+      std::memcpy(hinges, B.hinges.data(), B.hinges.size() * sizeof(int));
+      std::memcpy(hinge_par, B.hpar.data(), B.hpar.size() * sizeof(double));
+    }
+  });
+}
+
+int minim_gpu_bah_colouring(const minim_gpu_bah_params* q, const double* x0, size_t ndof, int* nbar_colors,
+                            int* nhinge_colors, int* valid) {
+  return guarded([&] {
+    BahHost B = setup_bah(*q, x0, ndof);
+    BahDevArrays A = bah_arrays(B, {});
+    *nbar_colors = (int)A.bar_off.size() - 1;
+    *nhinge_colors = (int)A.hinge_off.size() - 1;
+    // every colour must be vertex-disjoint
+    int ok = 1;
+    std::vector<int> seen(B.nvert, -1);
+    for (int c = 0; c < *nbar_colors && ok; c++)
+      for (int e = A.bar_off[c]; e < A.bar_off[c + 1] && ok; e++)
+        for (int v : {A.bars[e].x, A.bars[e].y}) {
+          if (seen[v] == c) ok = 0;
+          seen[v] = c;
+        }
+    std::fill(seen.begin(), seen.end(), -1);
+    for (int c = 0; c < *nhinge_colors && ok; c++)
+      for (int e = A.hinge_off[c]; e < A.hinge_off[c + 1] && ok; e++)
+        for (int v : {A.hinges[e].x, A.hinges[e].y, A.hinges[e].z, A.hinges[e].w}) {
+          if (seen[v] == c) ok = 0;
+          seen[v] = c;
+        }
+    *valid = ok;
+  });
+}
+
+int minim_gpu_pf_setup(const minim_gpu_pf_params* q, const double* x0, size_t ndof, double* kappa,
+                       double* kappaP, int* nk, double* node_vol, double* surface_area, int* kernel_variant) {
+  return guarded([&] {
+    PfHost H = setup_pf(*q, x0, ndof);
+    *nk = (int)H.kappa.size();
+    if (kappa) std::memcpy(kappa, H.kappa.data(), H.kappa.size() * sizeof(double));
+    if (kappaP) std::memcpy(kappaP, H.kappaP.data(), H.kappaP.size() * sizeof(double));
+    if (node_vol) std::memcpy(node_vol, H.node_vol.data(), H.node_vol.size() * sizeof(double));
+    if (surface_area) std::memcpy(surface_area, H.surface_area.data(), H.surface_area.size() * sizeof(double));
+    if (kernel_variant) *kernel_variant = H.kernel_kind;
+  });
+}
+
+}  // extern "C"

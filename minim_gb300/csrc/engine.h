@@ -1,0 +1,177 @@
+// engine.h -- data layout shared by the host runtime and the device kernels.
+//
+// Everything an instance needs on the device lives in one InstDesc (plain
+// data, device pointers): the potential's parameters, the minimiser's
+// parameters, the vector buffers and a pointer to its MinScalars (the
+// minimiser state that persists between launches, so a minimisation can be
+// run in slices and resumed).
+#pragma once
+#include <stddef.h>
+#include <stdint.h>
+#include <vector_types.h>
+
+#define MINIM_MAXM 16
+#define MINIM_MAXF 4
+
+namespace mg {
+
+// ---- potentials -------------------------------------------------------------
+struct PotLJ {
+  int ndim;        // 2 or 3
+  int np;          // particles
+  double s6;       // sigma^6
+  double eps;      // epsilon
+};
+
+enum PfFlags : unsigned {
+  PF_SOLID = 1u << 0,      // aux[] present: node types and solid-neighbour masks
+  PF_CONTACT = 1u << 1,    // wet[] present (binary wetting term)
+  PF_PRESSURE = 1u << 2,
+  PF_SOFT = 1u << 3,       // soft density penalty
+  PF_HARD = 1u << 4,       // hard density projection
+  PF_VOLUME = 1u << 5,     // fixed-volume projection
+  PF_FORCE = 1u << 6,
+  PF_CONFINE = 1u << 7,
+  PF_NODE_KAPPA = 1u << 8, // per-node kappa / kappaP arrays
+  PF_FIXFLUID = 1u << 9,
+};
+
+struct PotPF {
+  int n[3];
+  int nfluid;
+  int ngrid;
+  unsigned flags;
+  // per node: bits 0-3 = node type + 1 (0 = solid, 1 = bulk, 2..8 = surface
+  // types 1..7); bits 4-9 = solid flags of the face neighbours in the order
+  // x-, x+, y-, y+, z-, z+.  NULL when there is no solid.
+  const uint16_t* aux;
+  double vol_of_type[9];    // nodeVol by (type + 1), includes res^3
+  double res, res2;
+  double kappa[MINIM_MAXF], kappaP[MINIM_MAXF];
+  const double* kappa_node;   // ngrid*nfluid (PF_NODE_KAPPA)
+  const double* kappaP_node;
+  const double* wet;          // per node: wettingParam * surfaceArea (PF_CONTACT)
+  double pressure[MINIM_MAXF];
+  unsigned fix_mask;          // fixFluid bits
+  int nvar;                   // variable (non-fixed) fluids
+  double soft_coef;           // densityConst * sigmaMean * res^2
+  double confine_coef[MINIM_MAXF];
+  const double* ff_init;      // ndof (PF_CONFINE)
+  double fmag[MINIM_MAXF];
+  double fnorm[MINIM_MAXF][3];
+  double total_volume2;       // sum nodeVol^2 (PF_VOLUME)
+};
+
+struct PotBAH {
+  int nvert, nbar, nhinge;
+  const int2* bars;           // sorted by colour
+  const double2* bar_par;     // {k, l0}
+  const int4* hinges;         // sorted by colour
+  const double2* hinge_par;   // {k, theta0}
+  int nbar_colors, nhinge_colors;
+  const int* bar_color_off;   // nbar_colors + 1 offsets
+  const int* hinge_color_off;
+  const unsigned char* node_el;  // per vertex: force/wall elements present
+  int nforce;                 // 0, 3 or 3*nvert
+  const double* force;
+  int wall_on, wall_adh;
+  double wall_eps, wall_sig;
+};
+
+// ---- minimiser ------------------------------------------------------------------
+struct MinParams {
+  int method;       // 0 lbfgs, 1 fire, 2 gd
+  int linesearch;   // 0 backtracking, 1 none
+  int max_iter;
+  int m;
+  int precision;    // 0 mixed, 1 fp64, 2 fp32
+  double tol;
+  double max_step, init_step, dt_max, alpha;
+};
+
+enum RunStatus { ST_CONVERGED = 0, ST_MAXITER = 1, ST_NAN = 2, ST_TIMEOUT = 3,
+                 ST_CANCELLED = 4, ST_RUNNING = 5 };
+
+struct MinScalars {
+  int status;
+  int initialised;
+  int iter;          // the reference's loop counter
+  int ii;            // Lbfgs::_i
+  int stage;         // 0: FP32 coordinates, 1: FP64 coordinates
+  int xi, gi;        // which of X[2] / G[2] is current
+  int evals;
+  int fp64_iters;
+  int stall;         // iterations since the best rms improved (stage 0)
+  int nsteps;        // Fire::_nSteps
+  int pbuf, ybuf;    // spare history buffers (direction / new y)
+  int sidx[MINIM_MAXM], yidx[MINIM_MAXM];  // ring slot -> buffer
+  double E;          // energy at the current coordinates
+  double gg;         // g.g at the current coordinates
+  double best_rms;
+  double dt, a, dtmax, gnorm;  // Fire
+  double rho[MINIM_MAXM], sigma[MINIM_MAXM], yy[MINIM_MAXM];
+  // work counters for the roofline: algorithmic HBM bytes of every vector
+  // pass and evaluation, and Lennard-Jones pair interactions per precision
+  double abytes, pairs32, pairs64;
+};
+
+// K_PF1 is the kernel variant for a binary PhaseField with none of the
+// optional terms except pressure (chosen by the host; same results).
+enum Kind { K_LJ = 0, K_PF = 1, K_BAH = 2, K_PF1 = 3 };
+
+struct InstDesc {
+  int kind;
+  int ndof;
+  PotLJ lj;
+  PotPF pf;
+  PotBAH bah;
+  MinParams mp;
+  const unsigned char* fixed;  // per-dof fixed flags, or NULL
+  float* X32[2];
+  double* X64[2];
+  float* G[2];
+  float* Sb;       // (m + 1) * ndof: ring of directions (s = sigma * S)
+  float* Yb;       // (m + 1) * ndof
+  float* V;        // Fire velocity
+  double* GA;      // FP64 gradient accumulator (BarAndHinge scatter), or NULL
+  double* xres;    // resident FP64 coordinates: read at start, written at the end
+  MinScalars* st;
+};
+
+// Bounded software grid barrier state (one per cooperative launch).
+struct GridSyncState {
+  unsigned int count;
+  unsigned int gen;
+  int err;      // set when a barrier wait gave up
+  int pad;
+};
+
+// ---- kernel entry points (engine.cu) ---------------------------------------------
+enum Op { OP_MINIMISE = 0, OP_EVAL = 1, OP_CONSTRAIN = 2 };
+
+struct EvalIO {      // OP_EVAL / OP_CONSTRAIN on one instance, FP64 in/out
+  const double* x;   // coordinates (device), ndof
+  double* g;         // gradient out (device) or NULL
+  double* e;         // energy out (device, 1 double) or NULL
+  double* v;         // OP_CONSTRAIN: vector constrained in place
+};
+
+}  // namespace mg
+
+extern "C" {
+// Launchers, one set per potential kind (engine_{lj,pf,bah}.cu).  Each
+// returns a cudaError_t value.
+#define MG_DECLARE_LAUNCHERS(NAME)                                                              \
+  int mg_launch_batch_##NAME(const mg::InstDesc* d_insts, int ninst, int* d_counter,             \
+                             int slice_iters, int threads, int blocks, size_t smem, void* stream); \
+  int mg_launch_grid_##NAME(const mg::InstDesc* d_inst, int op, const mg::EvalIO* d_io,           \
+                            int slice_iters, mg::GridSyncState* d_bar, double* d_partials,       \
+                            int threads, int blocks, size_t smem, void* stream);                 \
+  int mg_occupancy_##NAME(int grid, int threads, size_t smem, int* blocks_per_sm);
+MG_DECLARE_LAUNCHERS(lj)
+MG_DECLARE_LAUNCHERS(pf)
+MG_DECLARE_LAUNCHERS(bah)
+MG_DECLARE_LAUNCHERS(pf1)
+// engine_misc.cu: FP64 <-> FP32 vector conversion on a stream
+int mg_convert(const void* src, void* dst, size_t n, int to_float, void* stream);
+}

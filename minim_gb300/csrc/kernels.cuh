@@ -1,0 +1,147 @@
+// engine.cu -- the two persistent kernels and their launchers.
+//
+//   batch_kernel : one CTA per instance.  CTAs pull instance indices from a
+//                  global counter (largest instances first, set by the host),
+//                  run that instance's minimisation for up to `slice`
+//                  iterations entirely on chip, store its state and pull the
+//                  next.  No CTA ever waits on another.
+//   grid_kernel  : one instance on the whole GPU (cooperative launch, bounded
+//                  software grid barrier); also serves the FP64 energy /
+//                  gradient and constraint calls of the C ABI.
+#pragma once
+#include "minimiser.cuh"
+
+namespace mg {
+
+struct SharedScalars {
+  double red[(32 + 1) * MINIM_MAXRED];
+  double rho[MINIM_MAXM], sig[MINIM_MAXM], yy[MINIM_MAXM], alpha[MINIM_MAXM];
+  int sidx[MINIM_MAXM], yidx[MINIM_MAXM];
+  int next, ok;
+};
+
+__device__ __forceinline__ void copy_desc(InstDesc* dst, const InstDesc* src) {
+  const int nw = (int)(sizeof(InstDesc) / sizeof(int));
+  const int* s = reinterpret_cast<const int*>(src);
+  int* d = reinterpret_cast<int*>(dst);
+  for (int i = threadIdx.x; i < nw; i += blockDim.x) d[i] = s[i];
+}
+
+template <class Team, int KIND>
+__device__ void setup_runner(Runner<Team, KIND>& R, SharedScalars& S, const InstDesc& in) {
+  R.n = in.ndof;
+  R.rho = S.rho; R.sig = S.sig; R.yy = S.yy; R.alpha = S.alpha;
+  R.sidx = S.sidx; R.yidx = S.yidx;
+}
+
+template <int KIND>
+__global__ void __launch_bounds__(256)
+batch_kernel(const InstDesc* __restrict__ insts, int ninst, int* counter, int slice, int lj_tile) {
+  __shared__ SharedScalars S;
+  __shared__ __align__(16) InstDesc s_in;
+  extern __shared__ __align__(16) unsigned char dyn[];
+  for (;;) {
+    if (threadIdx.x == 0) S.next = atomicAdd(counter, 1);
+    __syncthreads();
+    const int k = S.next;
+    if (k >= ninst) break;
+    copy_desc(&s_in, &insts[k]);
+    __syncthreads();
+    CtaTeam tm{(int)threadIdx.x, (int)blockDim.x, S.red};
+    Runner<CtaTeam, KIND> R{tm, s_in, dyn, lj_tile};
+    setup_runner(R, S, s_in);
+    R.load(*s_in.st);
+    R.run(slice);
+    R.store(*s_in.st);
+  }
+}
+
+template <class Team, int KIND>
+__device__ void eval_op(Runner<Team, KIND>& R, Team& tm, const InstDesc& in, const EvalIO& io) {
+  CView<double> cv{io.x, nullptr, 0.0};
+  StoreEmit64 em{io.g, in.fixed};
+  const bool want_g = io.g != nullptr;
+  const double ep = R.template pot_eval<double>(cv, nullptr, em, true, want_g);
+  if constexpr (KIND == K_PF) {
+    if (want_g && (in.pf.flags & PF_VOLUME)) {
+      tm.sync();
+      pf_volume_project<double>(tm, in.pf, io.g);
+    }
+  }
+  double v[1] = {ep};
+  tm.reduce(v);
+  if (io.e && tm.block0() && threadIdx.x == 0) *io.e = v[0];
+}
+
+template <class Team, int KIND>
+__device__ void constrain_op(Team& tm, const InstDesc& in, const EvalIO& io) {
+  double* v = io.v;
+  if (in.fixed)
+    for (int i = tm.tid; i < in.ndof; i += tm.nthr)
+      if (in.fixed[i]) v[i] = 0.0;
+  if constexpr (KIND == K_PF) {
+    if (in.pf.flags & (PF_FIXFLUID | PF_HARD)) {
+      tm.sync();
+      pf_local_constrain<double>(tm, in.pf, v);
+    }
+    if (in.pf.flags & PF_VOLUME) {
+      tm.sync();
+      pf_volume_project<double>(tm, in.pf, v);
+    }
+  }
+}
+
+template <int KIND>
+__global__ void __launch_bounds__(256)
+grid_kernel(const InstDesc* __restrict__ inst, int op, const EvalIO* io, int slice,
+            GridSyncState* bar, double* partials, int lj_tile) {
+  __shared__ SharedScalars S;
+  __shared__ __align__(16) InstDesc s_in;
+  extern __shared__ __align__(16) unsigned char dyn[];
+  copy_desc(&s_in, inst);
+  if (threadIdx.x == 0) S.ok = 1;
+  __syncthreads();
+  GridTeam tm{(int)(blockIdx.x * blockDim.x + threadIdx.x), (int)(gridDim.x * blockDim.x), S.red,
+              bar, partials, 0, &S.ok};
+  Runner<GridTeam, KIND> R{tm, s_in, dyn, lj_tile};
+  setup_runner(R, S, s_in);
+  if (op == OP_MINIMISE) {
+    R.load(*s_in.st);
+    R.run(slice);
+    R.store(*s_in.st);
+  } else if (op == OP_EVAL) {
+    eval_op(R, tm, s_in, *io);
+  } else {
+    constrain_op<GridTeam, KIND>(tm, s_in, *io);
+  }
+}
+
+}  // namespace mg
+
+// Instantiates the kernels for one potential kind and defines its launchers
+// (mg_launch_batch_<name>, mg_launch_grid_<name>, occupancy queries).
+#define MG_DEFINE_LAUNCHERS(KIND, NAME)                                                          \
+  extern "C" int mg_launch_batch_##NAME(const mg::InstDesc* d_insts, int ninst, int* d_counter,   \
+                                        int slice_iters, int threads, int blocks, size_t smem,    \
+                                        void* stream) {                                           \
+    const int tile = (int)(smem / sizeof(mg::D4));                                                \
+    mg::batch_kernel<KIND><<<blocks, threads, smem, (cudaStream_t)stream>>>(                     \
+        d_insts, ninst, d_counter, slice_iters, tile);                                            \
+    return (int)cudaGetLastError();                                                               \
+  }                                                                                               \
+  extern "C" int mg_launch_grid_##NAME(const mg::InstDesc* d_inst, int op, const mg::EvalIO* d_io, \
+                                       int slice_iters, mg::GridSyncState* d_bar,                 \
+                                       double* d_partials, int threads, int blocks, size_t smem,  \
+                                       void* stream) {                                            \
+    int tile = (int)(smem / sizeof(mg::D4));                                                      \
+    void* args[] = {(void*)&d_inst, (void*)&op,         (void*)&d_io, (void*)&slice_iters,        \
+                    (void*)&d_bar,  (void*)&d_partials, (void*)&tile};                            \
+    return (int)cudaLaunchCooperativeKernel((const void*)mg::grid_kernel<KIND>, dim3(blocks),     \
+                                            dim3(threads), args, smem, (cudaStream_t)stream);     \
+  }                                                                                               \
+  extern "C" int mg_occupancy_##NAME(int grid, int threads, size_t smem, int* blocks_per_sm) {    \
+    return grid ? (int)cudaOccupancyMaxActiveBlocksPerMultiprocessor(                             \
+                      blocks_per_sm, mg::grid_kernel<KIND>, threads, smem)                        \
+                : (int)cudaOccupancyMaxActiveBlocksPerMultiprocessor(                             \
+                      blocks_per_sm, mg::batch_kernel<KIND>, threads, smem);                      \
+  }

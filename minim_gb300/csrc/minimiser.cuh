@@ -1,0 +1,578 @@
+// minimiser.cuh -- device-resident Lbfgs / Fire / GradDescent iterations.
+//
+// One implementation serves both teams (one CTA per instance in a batch, or
+// the whole grid for a single instance).  It follows the reference's
+// iteration semantics step by step:
+//   Minimiser::minimise           src/Minimiser.cpp:27-38
+//   Lbfgs::iteration/getDirection src/minimisers/Lbfgs.cpp:41-133
+//   Fire::init/iteration          src/minimisers/Fire.cpp:27-90
+//   GradDescent::iteration        src/minimisers/GradDescent.cpp:27-46
+//   backtrackingLinesearch        src/minimisers/linesearch.cpp:8-30
+// Differences of representation, not of algorithm:
+//   * vectors are FP32, every dot product and energy is reduced in FP64;
+//   * a step is kept as (scalar t, direction P): trial points x + t*P are
+//     evaluated on the fly, the accepted point is written by the gradient
+//     evaluation that follows, and s = t*P is stored as (t, P) -- the
+//     reference scales the step by tau = 0.5, which is exact in binary;
+//   * the energy at the current point is carried from the last evaluation
+//     instead of being recomputed at the start of each line search;
+//   * precision MIXED runs FP32 coordinates until converged or stalled, then
+//     continues from the same point with FP64 coordinates (the L-BFGS history
+//     and the FIRE velocity carry over); the final convergence test is FP64.
+#pragma once
+#include "potentials.cuh"
+
+namespace mg {
+
+// Writes the gradient (FP32), applies fixed-dof constraints and accumulates
+// g.g and, for L-BFGS, y = g_new - g_old with P.y and y.y.
+struct FusedEmit {
+  float* G;
+  const float* Gold;
+  const float* P;
+  float* Y;
+  const unsigned char* fixed;
+  Acc gg, py, yy;
+  template <typename T>
+  __device__ __forceinline__ void operator()(int i, T v) {
+    float g = (fixed && fixed[i]) ? 0.f : (float)v;
+    G[i] = g;
+    gg.add(g * g);
+    if (Y) {
+      const float y = g - Gold[i];
+      Y[i] = y;
+      py.add(P[i] * y);
+      yy.add(y * y);
+    }
+  }
+};
+
+// FP64 output (API evaluation)
+struct StoreEmit64 {
+  double* G;
+  const unsigned char* fixed;
+  template <typename T>
+  __device__ __forceinline__ void operator()(int i, T v) {
+    G[i] = (fixed && fixed[i]) ? 0.0 : (double)v;
+  }
+};
+
+template <class Team, int KIND>
+struct Runner {
+  Team& tm;
+  const InstDesc& in;
+  void* smem_pot;     // potential scratch (LJ tiles)
+  int lj_tile;
+  // uniform scalars (every thread holds identical copies)
+  int n, status, initd, iter, ii, stage, xi, gi, evals, fp64_iters, stall, nsteps, pbuf, ybuf;
+  double E, gg, best_rms, dt, a, dtmax, gnorm;
+  double abytes, pairs32, pairs64;
+  // shared arrays (one copy per block; written by thread 0 between barriers)
+  double *rho, *sig, *yy, *alpha;
+  int *sidx, *yidx;
+
+  __device__ float* Sbuf(int b) const { return in.Sb + (size_t)b * n; }
+  __device__ float* Ybuf(int b) const { return in.Yb + (size_t)b * n; }
+  __device__ bool has_constraints() const {
+    if constexpr (KIND == K_PF)
+      return in.fixed != nullptr || (in.pf.flags & (PF_FIXFLUID | PF_HARD | PF_VOLUME));
+    return in.fixed != nullptr;
+  }
+  __device__ bool global_projection() const {
+    return KIND == K_PF && (in.pf.flags & PF_VOLUME);
+  }
+
+  // ---- work accounting -------------------------------------------------------------
+  __device__ double xbytes() const { return stage ? 8.0 : 4.0; }
+  // one potential evaluation: coordinates read (plus the direction for a
+  // trial point), gradient written; pair count for Lennard-Jones
+  __device__ void count_eval(bool trial, bool want_g) {
+    double b = xbytes() + (trial ? 4.0 : 0.0) + (want_g ? 4.0 : 0.0);
+    if constexpr (KIND == K_LJ) {
+      const double np = in.lj.np;
+      const double pairs = want_g ? np * (np - 1) : 0.5 * np * (np - 1);
+      if (stage) pairs64 += pairs; else pairs32 += pairs;
+    }
+    abytes += b * n;
+  }
+
+  // ---- potential dispatch -------------------------------------------------------
+  template <typename T, class Emit>
+  __device__ double pot_eval(CView<T> cv, T* xw, Emit& em, bool want_e, bool want_g) {
+    if constexpr (KIND == K_LJ) {
+      return lj_eval<T>(tm, in.lj, cv, xw, &em, want_e, want_g, smem_pot, lj_tile);
+    } else if constexpr (KIND == K_PF) {
+      return pf_eval<T>(tm, in.pf, cv, xw, &em, want_e, want_g);
+    } else if constexpr (KIND == K_PF1) {
+      return pf1_eval<T>(tm, in.pf, cv, xw, &em, want_e, want_g);
+    } else {
+      return bah_eval<T>(tm, in.bah, cv, xw, in.GA, &em, want_e, want_g);
+    }
+  }
+
+  // Energy (energy-only semantics) and constrained gradient at X[xi] + t*P.
+  // write_x: the point is also written to X[1-xi] and becomes current.
+  // With want_y the difference to the current gradient goes to Ybuf(ybuf)
+  // and py = P.y, yyv = y.y are returned.  The new gradient becomes current.
+  __device__ void grad_eval(double t, const float* P, bool write_x, bool want_y, double& py,
+                            double& yyv) {
+    float* Gn = in.G[1 - gi];
+    const bool proj = global_projection();
+    // with a global projection the gradient is finished in a second pass
+    FusedEmit em{Gn, in.G[gi], P, (want_y && !proj) ? Ybuf(ybuf) : nullptr, in.fixed};
+    double ep;
+    if (stage == 0) {
+      CView<float> cv{in.X32[xi], P, (float)t};
+      ep = pot_eval<float>(cv, write_x ? in.X32[1 - xi] : nullptr, em, true, true);
+    } else {
+      CView<double> cv{in.X64[xi], P, t};
+      ep = pot_eval<double>(cv, write_x ? in.X64[1 - xi] : nullptr, em, true, true);
+    }
+    if (proj) {
+      em.gg = Acc();
+      tm.sync();
+      if constexpr (KIND == K_PF) pf_volume_project<float>(tm, in.pf, Gn);
+      const float* Go = in.G[gi];
+      float* Y = want_y ? Ybuf(ybuf) : nullptr;
+      for (int i = tm.tid; i < n; i += tm.nthr) {
+        const float g = Gn[i];
+        em.gg.add(g * g);
+        if (Y) {
+          const float y = g - Go[i];
+          Y[i] = y;
+          em.py.add(P[i] * y);
+          em.yy.add(y * y);
+        }
+      }
+    }
+    double v[4] = {ep, em.gg.total(), em.py.total(), em.yy.total()};
+    tm.reduce(v);
+    E = v[0];
+    gg = v[1];
+    py = v[2];
+    yyv = v[3];
+    evals++;
+    count_eval(P != nullptr, true);
+    if (write_x) abytes += xbytes() * n;
+    if (want_y) abytes += 8.0 * n;
+    gi = 1 - gi;
+    if (write_x) xi = 1 - xi;
+  }
+
+  __device__ double energy_at(double t, const float* P) {
+    FusedEmit ne{nullptr, nullptr, nullptr, nullptr, nullptr};
+    double ep;
+    if (stage == 0) {
+      CView<float> cv{in.X32[xi], P, (float)t};
+      ep = pot_eval<float>(cv, nullptr, ne, true, false);
+    } else {
+      CView<double> cv{in.X64[xi], P, t};
+      ep = pot_eval<double>(cv, nullptr, ne, true, false);
+    }
+    double v[1] = {ep};
+    tm.reduce(v);
+    evals++;
+    count_eval(P != nullptr, false);
+    return v[0];
+  }
+
+  // State::applyConstraints on the direction P, then returns g.P
+  __device__ double constrain_dir(float* P) {
+    if (in.fixed) {
+      for (int i = tm.tid; i < n; i += tm.nthr)
+        if (in.fixed[i]) P[i] = 0.f;
+    }
+    if constexpr (KIND == K_PF) {
+      if (in.pf.flags & (PF_FIXFLUID | PF_HARD)) {
+        tm.sync();
+        pf_local_constrain<float>(tm, in.pf, P);
+      }
+      if (global_projection()) {
+        tm.sync();
+        pf_volume_project<float>(tm, in.pf, P);
+      }
+    }
+    tm.sync();
+    const float* G = in.G[gi];
+    Acc d;
+    for (int i = tm.tid; i < n; i += tm.nthr) d.add(G[i] * P[i]);
+    double v[1] = {d.total()};
+    tm.reduce(v);
+    return v[0];
+  }
+
+  // backtrackingLinesearch: the step is t0 * P with g.step = gs <= 0.
+  // Returns the accepted multiplier (t0 * tau^k, or t0 * tau^10 when no
+  // trial passed -- that last point is taken without being evaluated).
+  __device__ double linesearch(const float* P, double t0, double gs, bool& exhausted) {
+    const double c = 0.5, tau = 0.5;
+    double thr = -c * gs;
+    const double e0 = E;
+    double t = t0;
+    exhausted = true;
+    for (int k = 0; k < 10; k++) {
+      const double e = energy_at(t, P);
+      if (!tm.ok()) return t;
+      if (e0 - e >= thr) { exhausted = false; break; }
+      t = t * tau;
+      thr = thr * tau;
+    }
+    return t;
+  }
+
+  // ---- L-BFGS ---------------------------------------------------------------------
+  // Fused two-loop recursion (Lbfgs::getDirection): each pass finishes the
+  // previous axpy and computes the next dot product, so a direction costs
+  // 2*min(m,i)+1 passes and as many reductions.  Writes P = Sbuf(pbuf) and
+  // returns the scale folded into the step (initStep/|g| or maxStep cap).
+  __device__ double lbfgs_direction(double& gp) {
+    float* P = Sbuf(pbuf);
+    const float* G = in.G[gi];
+    const int m = in.mp.m;
+    if (ii == 0) {
+      for (int i = tm.tid; i < n; i += tm.nthr) P[i] = -G[i];
+      tm.sync();
+      abytes += 8.0 * n;
+      const double gn = sqrt(gg);
+      const double scale = gn > 0 ? in.mp.init_step / gn : 1.0;
+      gp = -gg * scale;
+      return scale;
+    }
+    const int mt = ii < m ? ii : m;
+    const int c = ii % m;
+    abytes += (4.0 * mt + 2.0) * 4.0 * n;  // each history vector read twice, g read, p written
+    double coef = 0.0;
+    const float* ysrc = nullptr;
+    // first loop: newest to oldest
+    for (int j = 0; j < mt; j++) {
+      const int k = (c - 1 - j + m) % m;
+      const float* S = Sbuf(sidx[k]);
+      const float fc = (float)coef;
+      Acc d;
+      for (int i = tm.tid; i < n; i += tm.nthr) {
+        const float q = (j == 0) ? -G[i] : P[i] - fc * ysrc[i];
+        P[i] = q;
+        d.add(q * S[i]);
+      }
+      double v[1] = {d.total()};
+      tm.reduce(v);
+      const double al = rho[k] * sig[k] * v[0];
+      if (threadIdx.x == 0) alpha[k] = al;
+      coef = al;
+      ysrc = Ybuf(yidx[k]);
+    }
+    const int kn = (c - 1 + m) % m;
+    const double gamma = 1.0 / (rho[kn] * yy[kn]);
+    // second loop: oldest to newest
+    double beta = 0.0;
+    for (int j = 0; j <= mt; j++) {
+      const float* Yn = (j < mt) ? Ybuf(yidx[(c - mt + j + m) % m]) : nullptr;
+      Acc d1, d2;
+      if (j == 0) {
+        const float fc = (float)coef, fg = (float)gamma;
+        for (int i = tm.tid; i < n; i += tm.nthr) {
+          const float q = (P[i] - fc * ysrc[i]) * fg;
+          P[i] = q;
+          d1.add(q * Yn[i]);
+        }
+      } else {
+        const int kp = (c - mt + j - 1 + m) % m;
+        const float* Sp = Sbuf(sidx[kp]);
+        const float fc = (float)((alpha[kp] - beta) * sig[kp]);
+        if (Yn) {
+          for (int i = tm.tid; i < n; i += tm.nthr) {
+            const float q = P[i] + fc * Sp[i];
+            P[i] = q;
+            d1.add(q * Yn[i]);
+          }
+        } else {
+          for (int i = tm.tid; i < n; i += tm.nthr) {
+            const float q = P[i] + fc * Sp[i];
+            P[i] = q;
+            d1.add(q * G[i]);
+            d2.add(q * q);
+          }
+        }
+      }
+      double v[2] = {d1.total(), d2.total()};
+      tm.reduce(v);
+      if (Yn) {
+        beta = rho[(c - mt + j + m) % m] * v[0];
+      } else {
+        gp = v[0];
+        double scale = 1.0;
+        if (in.mp.max_step != 0) {
+          const double ss = sqrt(v[1]);
+          if (ss > in.mp.max_step) scale = in.mp.max_step / ss;
+        }
+        gp *= scale;
+        return scale;
+      }
+    }
+    return 1.0;  // not reached
+  }
+
+  __device__ void lbfgs_iteration(bool& exhausted) {
+    double py, yyv;
+    exhausted = false;
+    if (iter == 0) {
+      grad_eval(0.0, nullptr, false, false, py, yyv);
+      ii = 0;
+    } else {
+      ii++;
+    }
+    double gp;
+    double scale = lbfgs_direction(gp);
+    float* P = Sbuf(pbuf);
+    if (has_constraints()) gp = scale * constrain_dir(P);
+    double gs = gp;
+    if (gs > 0) { gs = -gs; scale = -scale; }
+    double t = scale;
+    if (in.mp.linesearch == 0) t = linesearch(P, scale, gs, exhausted);
+    if (!tm.ok()) return;
+    grad_eval(t, P, true, true, py, yyv);
+    const double sy = t * py;
+    if (sy != 0) {
+      const int m = in.mp.m;
+      const int c = ii % m;
+      const int os = sidx[c], oy = yidx[c];
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        sidx[c] = pbuf; yidx[c] = ybuf;
+        rho[c] = 1.0 / sy; sig[c] = t; yy[c] = yyv;
+      }
+      pbuf = os; ybuf = oy;
+      __syncthreads();
+    } else {
+      ii--;
+    }
+  }
+
+  // ---- FIRE -----------------------------------------------------------------------
+  __device__ void fire_iteration(bool& exhausted) {
+    const int nMin = 5;
+    const double fInc = 1.1, fDec = 0.5, fA = 0.99, aStart = 0.1;
+    double py, yyv;
+    exhausted = false;
+    if (iter == 0) {
+      dt = dtmax;
+      grad_eval(0.0, nullptr, false, false, py, yyv);
+      gnorm = sqrt(gg);
+    }
+    const float* G = in.G[gi];
+    float* Vv = in.V;
+    Acc d1, d2;
+    for (int i = tm.tid; i < n; i += tm.nthr) {
+      const float v = Vv[i];
+      d1.add(v * G[i]);
+      d2.add(v * v);
+    }
+    double r[2] = {d1.total(), d2.total()};
+    tm.reduce(r);
+    abytes += 8.0 * n;
+    const double p = -r[0];
+    double c1, c2;
+    if (p > 0) {
+      const double vnorm = sqrt(r[1]);
+      c1 = 1 - a;
+      c2 = a * vnorm / gnorm + dt;
+      nsteps++;
+    } else {
+      c1 = 0.0;
+      c2 = dt;
+      nsteps = 0;
+    }
+    if (p > 0 && nsteps > nMin) {
+      a = a * fA;
+      dt = dt * fInc;
+      if (dt > dtmax) dt = dtmax;
+    } else if (p <= 0) {
+      a = aStart;
+      dt = dt * fDec;
+    }
+    float* P = Sbuf(0);
+    const float f1 = (float)c1, f2 = (float)c2, fdt = (float)dt;
+    Acc dg;
+    for (int i = tm.tid; i < n; i += tm.nthr) {
+      const float v = (p > 0) ? f1 * Vv[i] - f2 * G[i] : -f2 * G[i];
+      Vv[i] = v;
+      const float s = fdt * v;
+      P[i] = s;
+      dg.add(G[i] * s);
+    }
+    abytes += 16.0 * n;
+    double gs;
+    if (has_constraints()) {
+      gs = constrain_dir(P);
+    } else {
+      double v[1] = {dg.total()};
+      tm.reduce(v);
+      gs = v[0];
+    }
+    double t = 1.0;
+    if (in.mp.linesearch == 0) t = linesearch(P, 1.0, gs, exhausted);
+    if (!tm.ok()) return;
+    grad_eval(t, P, true, false, py, yyv);
+    gnorm = sqrt(gg);
+  }
+
+  // ---- gradient descent -------------------------------------------------------------
+  __device__ void gd_iteration(bool& exhausted) {
+    double py, yyv;
+    exhausted = false;
+    grad_eval(0.0, nullptr, false, false, py, yyv);
+    const float* G = in.G[gi];
+    const double gs = -in.mp.alpha * gg;
+    double t = -in.mp.alpha;
+    if (in.mp.linesearch == 0) t = linesearch(G, -in.mp.alpha, gs, exhausted);
+    if (!tm.ok()) return;
+    // x += t * g (materialise the accepted point)
+    if (stage == 0) {
+      const float* X = in.X32[xi];
+      float* Xn = in.X32[1 - xi];
+      CView<float> cv{X, G, (float)t};
+      for (int i = tm.tid; i < n; i += tm.nthr) Xn[i] = cv(i);
+    } else {
+      const double* X = in.X64[xi];
+      double* Xn = in.X64[1 - xi];
+      CView<double> cv{X, G, t};
+      for (int i = tm.tid; i < n; i += tm.nthr) Xn[i] = cv(i);
+    }
+    xi = 1 - xi;
+    tm.sync();
+    abytes += (2.0 * xbytes() + 4.0) * n;
+  }
+
+  // ---- precision switch -------------------------------------------------------------
+  __device__ void to_fp64() {
+    const float* X = in.X32[xi];
+    double* X64 = in.X64[xi];
+    for (int i = tm.tid; i < n; i += tm.nthr) X64[i] = (double)X[i];
+    tm.sync();
+    abytes += 12.0 * n;
+    stage = 1;
+  }
+
+  __device__ double rms() const { return sqrt(gg / n); }
+
+  // ---- driver -------------------------------------------------------------------------
+  __device__ void load(const MinScalars& s) {
+    status = s.status; initd = s.initialised; iter = s.iter; ii = s.ii; stage = s.stage; xi = s.xi; gi = s.gi;
+    evals = s.evals; fp64_iters = s.fp64_iters; stall = s.stall; nsteps = s.nsteps;
+    pbuf = s.pbuf; ybuf = s.ybuf; E = s.E; gg = s.gg; best_rms = s.best_rms;
+    dt = s.dt; a = s.a; dtmax = s.dtmax; gnorm = s.gnorm;
+    abytes = s.abytes; pairs32 = s.pairs32; pairs64 = s.pairs64;
+    for (int k = threadIdx.x; k < MINIM_MAXM; k += blockDim.x) {
+      rho[k] = s.rho[k]; sig[k] = s.sigma[k]; yy[k] = s.yy[k];
+      sidx[k] = s.sidx[k]; yidx[k] = s.yidx[k]; alpha[k] = 0.0;
+    }
+    __syncthreads();
+  }
+
+  __device__ void store(MinScalars& s) {
+    __syncthreads();
+    if (tm.block0() && threadIdx.x == 0) {
+      s.status = status; s.iter = iter; s.ii = ii; s.stage = stage; s.xi = xi; s.gi = gi;
+      s.evals = evals; s.fp64_iters = fp64_iters; s.stall = stall; s.nsteps = nsteps;
+      s.pbuf = pbuf; s.ybuf = ybuf; s.E = E; s.gg = gg; s.best_rms = best_rms;
+      s.dt = dt; s.a = a; s.dtmax = dtmax; s.gnorm = gnorm; s.initialised = 1;
+      s.abytes = abytes; s.pairs32 = pairs32; s.pairs64 = pairs64;
+      for (int k = 0; k < MINIM_MAXM; k++) {
+        s.rho[k] = rho[k]; s.sigma[k] = sig[k]; s.yy[k] = yy[k];
+        s.sidx[k] = sidx[k]; s.yidx[k] = yidx[k];
+      }
+    }
+    __syncthreads();
+  }
+
+  // Minimiser::minimise, resumable: runs at most `slice` iterations.
+  __device__ void run(int slice) {
+    const MinParams& mp = in.mp;
+    if (status != ST_RUNNING) return;
+    const bool mixed = (mp.precision == 0);
+    if (!initd) {
+      // Minimiser::init.  In FP64 mode the host has written the exact input
+      // to X64[0], so the FP64 stage starts from it directly.
+      initd = 1;
+      {
+        const double* xr = in.xres;
+        float* X32 = in.X32[0];
+        double* X64 = in.X64[0];
+        for (int i = tm.tid; i < n; i += tm.nthr) {
+          const double v = xr[i];
+          X32[i] = (float)v;
+          if (X64) X64[i] = v;
+        }
+        tm.sync();
+        xi = 0;
+        gi = 0;
+      }
+      if (mp.precision == 1) stage = 1;
+      if (mp.method == 0) {
+        ii = 0;
+        if (threadIdx.x == 0)
+          for (int k = 0; k < MINIM_MAXM; k++) {
+            rho[k] = 0; sig[k] = 0; yy[k] = 0; sidx[k] = k; yidx[k] = k;
+          }
+        pbuf = mp.m; ybuf = mp.m;
+        __syncthreads();
+      } else if (mp.method == 1) {
+        for (int i = tm.tid; i < n; i += tm.nthr) in.V[i] = 0.f;
+        tm.sync();
+        a = 0.1; nsteps = 0;
+        dtmax = mp.dt_max;
+        if (dtmax == 0) {
+          double py, yyv;
+          grad_eval(0.0, nullptr, false, false, py, yyv);
+          const double gn = sqrt(gg);
+          dtmax = (gn != 0) ? 0.1 / sqrt(gn) : 1.0;
+        }
+      }
+      best_rms = 1e300;
+      stall = 0;
+    }
+    for (int s = 0; s < slice; s++) {
+      if (iter > mp.max_iter) { status = ST_MAXITER; break; }
+      bool exhausted = false;
+      if (mp.method == 0) lbfgs_iteration(exhausted);
+      else if (mp.method == 1) fire_iteration(exhausted);
+      else gd_iteration(exhausted);
+      if (!tm.ok()) { status = ST_TIMEOUT; break; }
+      if (stage == 1) fp64_iters++;
+      if (!isfinite(E) || !isfinite(gg)) { status = ST_NAN; break; }
+      const double r = rms();
+      bool conv = r < mp.tol;
+      if (stage == 0 && mixed) {
+        if (r < 0.999 * best_rms) { best_rms = r; stall = 0; }
+        else stall++;
+        if (conv || exhausted || stall >= 100) {
+          to_fp64();
+          if (mp.method != 2) {
+            double py, yyv;
+            grad_eval(0.0, nullptr, false, false, py, yyv);
+            if (mp.method == 1) gnorm = sqrt(gg);
+            conv = rms() < mp.tol;
+          } else {
+            conv = false;  // the next iteration's FP64 gradient decides
+          }
+        }
+      }
+      if (conv) { status = ST_CONVERGED; break; }
+      iter++;
+    }
+    if (status != ST_RUNNING) {
+      // hand the final coordinates back to the resident FP64 copy
+      double* xr = in.xres;
+      if (stage == 1) {
+        const double* X = in.X64[xi];
+        for (int i = tm.tid; i < n; i += tm.nthr) xr[i] = X[i];
+      } else {
+        const float* X = in.X32[xi];
+        for (int i = tm.tid; i < n; i += tm.nthr) xr[i] = (double)X[i];
+      }
+      tm.sync();
+    }
+  }
+};
+
+}  // namespace mg

@@ -1,0 +1,651 @@
+// potentials.cuh -- device energy/gradient of LjNd, PhaseField and BarAndHinge.
+//
+// Each evaluator is a template over the coordinate type T (float for the FP32
+// stage, double for the FP64 stage and the FP64 API call) and the team.  The
+// coordinates are read through a CView (x + t*p, so line-search trial points
+// are never materialised), optionally written out (the accepted point), and
+// the gradient is handed DOF by DOF to an Emit functor exactly once per DOF.
+// The return value is the calling thread's share of the energy.
+#pragma once
+#include "common.cuh"
+
+namespace mg {
+
+// coordinates x + t * p (p may be NULL); one rounding, the same everywhere
+template <typename T>
+struct CView {
+  const T* x;
+  const float* p;
+  T t;
+  __device__ __forceinline__ T operator()(int i) const;
+};
+template <>
+__device__ __forceinline__ float CView<float>::operator()(int i) const {
+  return p ? __fadd_rn(x[i], __fmul_rn(t, p[i])) : x[i];
+}
+template <>
+__device__ __forceinline__ double CView<double>::operator()(int i) const {
+  return p ? __dadd_rn(x[i], __dmul_rn(t, (double)p[i])) : x[i];
+}
+
+template <typename T> struct EAcc;
+template <> struct EAcc<float> {
+  Acc a;
+  __device__ __forceinline__ void add(float v) { a.add(v); }
+  __device__ __forceinline__ double total() const { return a.total(); }
+};
+template <> struct EAcc<double> {
+  double d = 0.0;
+  __device__ __forceinline__ void add(double v) { d += v; }
+  __device__ __forceinline__ double total() const { return d; }
+};
+
+struct NoEmit {
+  template <typename T>
+  __device__ __forceinline__ void operator()(int, T) {}
+};
+
+// ===========================================================================
+// LjNd: all i<j pairs (src/potentials/LjNd.cpp:12-53).  Each thread owns
+// particles i and sums the force from every j (no scatter, deterministic);
+// the energy counts each pair once (j > i).  Coordinates are staged through
+// shared memory in tiles.
+// ===========================================================================
+struct alignas(16) F4 { float x, y, z, w; };
+struct alignas(16) D4 { double x, y, z, w; };
+template <typename T> struct Vec4T;
+template <> struct Vec4T<float> { using type = F4; };
+template <> struct Vec4T<double> { using type = D4; };
+
+template <typename T>
+__device__ __forceinline__ T lj_rcp(T r2);
+template <>
+__device__ __forceinline__ float lj_rcp<float>(float r2) { return __frcp_rn(r2); }
+template <>
+__device__ __forceinline__ double lj_rcp<double>(double r2) { return 1.0 / r2; }
+
+template <typename T, class Team, class Emit>
+__device__ __noinline__ double lj_eval(Team& tm, const PotLJ& P, CView<T> cv, T* xw, Emit* emp,
+                                       bool want_e, bool want_g, void* smem, int tile) {
+  Emit emit = *emp;
+  using V4 = typename Vec4T<T>::type;
+  V4* sx = reinterpret_cast<V4*>(smem);
+  const int N = P.np, nd = P.ndim;
+  const T s6 = (T)P.s6;
+  if (xw) {
+    for (int i = tm.tid; i < N * nd; i += tm.nthr) xw[i] = cv(i);
+  }
+  EAcc<T> e;
+  const int step = tm.nthr;
+  // every thread of every block runs the same number of outer rounds
+  const int rounds = (N + step - 1) / step;
+  for (int r = 0; r < rounds; r++) {
+    const int i = r * step + tm.tid;
+    const bool act = i < N;
+    T xi = 0, yi = 0, zi = 0;
+    if (act) {
+      xi = cv(nd * i);
+      yi = cv(nd * i + 1);
+      zi = (nd == 3) ? cv(nd * i + 2) : (T)0;
+    }
+    T fx = 0, fy = 0, fz = 0;
+    for (int j0 = 0; j0 < N; j0 += tile) {
+      const int nt = min(tile, N - j0);
+      __syncthreads();
+      for (int j = threadIdx.x; j < nt; j += blockDim.x) {
+        const int jj = j0 + j;
+        V4 v;
+        v.x = cv(nd * jj);
+        v.y = cv(nd * jj + 1);
+        v.z = (nd == 3) ? cv(nd * jj + 2) : (T)0;
+        v.w = 0;
+        sx[j] = v;
+      }
+      __syncthreads();
+      if (act) {
+        if (want_g) {
+          for (int j = 0; j < nt; j++) {
+            const V4 b = sx[j];
+            const T dx = xi - b.x, dy = yi - b.y, dz = zi - b.z;
+            const T r2 = dx * dx + dy * dy + dz * dz;
+            const bool self = (j0 + j == i);
+            const T inv = lj_rcp<T>(self ? (T)1 : r2);
+            const T lj6 = s6 * inv * inv * inv;
+            const T lj12 = lj6 * lj6;
+            const T f = self ? (T)0 : (2 * lj12 - lj6) * inv;
+            fx += dx * f;
+            fy += dy * f;
+            fz += dz * f;
+            if (want_e && (j0 + j > i)) e.add(lj12 - lj6);
+          }
+        } else if (want_e) {
+          for (int j = max(0, i + 1 - j0); j < nt; j++) {
+            const V4 b = sx[j];
+            const T dx = xi - b.x, dy = yi - b.y, dz = zi - b.z;
+            const T r2 = dx * dx + dy * dy + dz * dz;
+            const T inv = lj_rcp<T>(r2);
+            const T lj6 = s6 * inv * inv * inv;
+            e.add(lj6 * lj6 - lj6);
+          }
+        }
+      }
+    }
+    if (act && want_g) {
+      const T c = (T)(-24.0 * P.eps);
+      emit(nd * i, c * fx);
+      emit(nd * i + 1, c * fy);
+      if (nd == 3) emit(nd * i + 2, c * fz);
+    }
+  }
+  __syncthreads();
+  *emp = emit;
+  return 4.0 * P.eps * e.total();
+}
+
+// ===========================================================================
+// PhaseField (MODEL_BASIC), gather form of PhaseField::energyGradient
+// (src/potentials/PhaseField.cpp:238-288, 365-393, 432-537) followed by the
+// node-local parts of specialisedConstraints (fixFluid, hard density, lines
+// 580-612).  Each node computes its own bulk and gradient terms and collects
+// the contributions that the reference scatters into it from its two
+// neighbours in every direction, so every DOF is written exactly once.
+// ===========================================================================
+__device__ __forceinline__ int pf_type1(const PotPF& P, int node) {  // type + 1
+  return P.aux ? (int)(P.aux[node] & 15u) : 1;
+}
+
+template <typename T, class Team, class Emit>
+__device__ __noinline__ double pf_eval(Team& tm, const PotPF& P, CView<T> cv, T* xw, Emit* emp,
+                                       bool want_e, bool want_g) {
+  constexpr int NFMAX = MINIM_MAXF;
+  Emit emit = *emp;
+  const int nf = P.nfluid;
+  const int nx = P.n[0], ny = P.n[1], nz = P.n[2];
+  const int ng = P.ngrid;
+  const unsigned fl = P.flags;
+  const T res2 = (T)P.res2;
+  EAcc<T> e;
+  for (int iG = tm.tid; iG < ng; iG += tm.nthr) {
+    const int z = iG % nz, y = (iG / nz) % ny, x = iG / (ny * nz);
+    int nb[6];
+    nb[0] = ((x == 0 ? nx - 1 : x - 1) * ny + y) * nz + z;
+    nb[1] = ((x == nx - 1 ? 0 : x + 1) * ny + y) * nz + z;
+    nb[2] = (x * ny + (y == 0 ? ny - 1 : y - 1)) * nz + z;
+    nb[3] = (x * ny + (y == ny - 1 ? 0 : y + 1)) * nz + z;
+    nb[4] = (x * ny + y) * nz + (z == 0 ? nz - 1 : z - 1);
+    nb[5] = (x * ny + y) * nz + (z == nz - 1 ? 0 : z + 1);
+    const unsigned aux_i = P.aux ? P.aux[iG] : 1u;
+    const int t1 = (int)(aux_i & 15u);
+    const bool solid_i = (t1 == 0);
+    const unsigned mask_i = aux_i >> 4;
+    const T V = (T)P.vol_of_type[t1];
+    unsigned aux_nb[6];
+#pragma unroll
+    for (int k = 0; k < 6; k++) aux_nb[k] = P.aux ? P.aux[nb[k]] : 1u;
+
+    T c[NFMAX], g[NFMAX];
+#pragma unroll
+    for (int f = 0; f < NFMAX; f++) {
+      if (f < nf) {
+        c[f] = cv(iG * nf + f);
+        if (xw) xw[iG * nf + f] = c[f];
+        g[f] = 0;
+      }
+    }
+    T rd = -1;  // soft density: sum c - 1
+    if (fl & PF_SOFT) {
+#pragma unroll
+      for (int f = 0; f < NFMAX; f++)
+        if (f < nf) rd += c[f];
+    }
+    bool force_e_done = false;  // energy-only semantics of forceEnergy
+#pragma unroll
+    for (int f = 0; f < NFMAX; f++) {
+      if (f >= nf) break;
+      const int dof = iG * nf + f;
+      const T cc = c[f];
+      const T kap = (fl & PF_NODE_KAPPA) ? (T)P.kappa_node[dof] : (T)P.kappa[f];
+      const T kP = (fl & PF_NODE_KAPPA) ? (T)P.kappaP_node[dof] : (T)P.kappaP[f];
+      T gv = 0;
+      // bulk
+      if (nf == 1) {
+        const T fac = kap / 16 * V;
+        const T a = (cc + 1) * (cc - 1);
+        if (want_e) e.add(fac * a * a);
+        gv += fac * 4 * cc * (cc * cc - 1);
+      } else {
+        const T fac = (T)0.5 * kap * V;
+        const T a = cc * (cc - 1);
+        if (want_e) e.add(fac * a * a);
+        gv += fac * 2 * cc * (cc - 1) * (2 * cc - 1);
+      }
+      // gradient energy
+      const T coefk = ((nf == 1) ? (T)0.25 : (T)0.5) / res2;
+      const T Fi = coefk * kP * V;
+      T eg = 0;
+#pragma unroll
+      for (int d = 0; d < 3; d++) {
+        if (P.n[d] == 1) continue;
+        const int im = nb[2 * d], ip = nb[2 * d + 1];
+        const T cm = cv(im * nf + f), cp = cv(ip * nf + f);
+        const bool sm = (mask_i >> (2 * d)) & 1u, sp = (mask_i >> (2 * d + 1)) & 1u;
+        const T gm = cc - cm, gp = cc - cp;
+        if (!sm && !sp) {
+          eg += (T)0.5 * (gm * gm + gp * gp);
+          gv += Fi * (gm + gp);
+        } else if (!sp) {
+          eg += gp * gp;
+          gv += Fi * 2 * gp;
+        } else if (!sm) {
+          eg += gm * gm;
+          gv += Fi * 2 * gm;
+        }
+        if (!solid_i) {
+          if (!sp) {  // term of node p whose minus neighbour is this node
+            const unsigned ap = aux_nb[2 * d + 1];
+            const T Vp = (T)P.vol_of_type[ap & 15u];
+            const T kPp = (fl & PF_NODE_KAPPA) ? (T)P.kappaP_node[ip * nf + f] : kP;
+            const T Fp = coefk * kPp * Vp;
+            const bool pp_solid = ((ap >> 4) >> (2 * d + 1)) & 1u;
+            gv -= (pp_solid ? (T)2 : (T)1) * Fp * (cp - cc);
+          }
+          if (!sm) {  // term of node m whose plus neighbour is this node
+            const unsigned am = aux_nb[2 * d];
+            const T Vm = (T)P.vol_of_type[am & 15u];
+            const T kPm = (fl & PF_NODE_KAPPA) ? (T)P.kappaP_node[im * nf + f] : kP;
+            const T Fm = coefk * kPm * Vm;
+            const bool mm_solid = ((am >> 4) >> (2 * d)) & 1u;
+            gv -= (mm_solid ? (T)2 : (T)1) * Fm * (cm - cc);
+          }
+        }
+      }
+      if (want_e) e.add(Fi * eg);
+      // surface (binary only)
+      if ((fl & PF_CONTACT) && nf == 1) {
+        const T w = (T)P.wet[iG];
+        if (w != 0) {
+          if (want_e) e.add(w * (cc * cc * cc / 3 - cc - (T)(2.0 / 3)));
+          gv += w * (cc * cc - 1);
+        }
+      }
+      // pressure
+      if ((fl & PF_PRESSURE) && P.pressure[f] != 0 && !((P.fix_mask >> f) & 1u)) {
+        const T pr = (T)P.pressure[f];
+        if (nf == 1) {
+          if (want_e) e.add(-pr * ((T)0.5 * (cc + 1) * V));
+          gv -= (T)0.5 * pr * V;
+        } else {
+          if (want_e) e.add(-pr * (cc * V));
+          gv -= pr * V;
+        }
+      }
+      // soft density
+      if ((fl & PF_SOFT) && nf > 1) {
+        const T sc = (T)P.soft_coef;
+        if (want_e && f == 0) e.add(sc * rd * rd);
+        gv += 2 * sc * rd;
+      }
+      // body force
+      if ((fl & PF_FORCE) && !solid_i && P.fmag[f] != 0) {
+        const T cf = (nf == 1) ? (T)0.5 * (1 + cc) : cc;
+        if (cf >= (T)0.01) {
+          const T co0 = (T)(x - (nx - 1) / 2.0), co1 = (T)(y - (ny - 1) / 2.0),
+                  co2 = (T)(z - (nz - 1) / 2.0);
+          const T h = -(co0 * (T)P.fnorm[f][0] + co1 * (T)P.fnorm[f][1] + co2 * (T)P.fnorm[f][2]) *
+                      (T)P.res;
+          const T epc = V * (T)P.fmag[f] * h;
+          if (want_e && !force_e_done) e.add(cf * epc);
+          force_e_done = true;
+          gv += (nf == 1) ? (T)0.5 * epc : epc;
+        }
+      }
+      // diffuse-solid confinement
+      if ((fl & PF_CONFINE) && P.confine_coef[f] != 0) {
+        const T c0 = (T)P.ff_init[dof];
+        if ((c0 - (T)0.5) * (cc - (T)0.5) < 0) {
+          const T coef = (T)P.confine_coef[f];
+          if (want_e) e.add(coef * (cc - (T)0.5) * (cc - (T)0.5));
+          gv += coef * 2 * (cc - (T)0.5);
+        }
+      }
+      g[f] = gv;
+    }
+    if (want_g) {
+      // node-local constraints: fixed fluids, then the hard density projection
+      if (fl & PF_FIXFLUID) {
+#pragma unroll
+        for (int f = 0; f < NFMAX; f++)
+          if (f < nf && ((P.fix_mask >> f) & 1u)) g[f] = 0;
+      }
+      if ((fl & PF_HARD) && nf > 1) {
+        T comp = 0;
+#pragma unroll
+        for (int f = 0; f < NFMAX; f++)
+          if (f < nf && !((P.fix_mask >> f) & 1u)) comp += g[f];
+        comp *= (T)1 / (T)P.nvar;
+#pragma unroll
+        for (int f = 0; f < NFMAX; f++)
+          if (f < nf && !((P.fix_mask >> f) & 1u)) g[f] -= comp;
+      }
+#pragma unroll
+      for (int f = 0; f < NFMAX; f++)
+        if (f < nf) emit(iG * nf + f, g[f]);
+    }
+  }
+  *emp = emit;
+  return e.total();
+}
+
+// Binary fluid (nFluid == 1) without solid, contact angle, force or
+// confinement: the 7-point stencil of the bulk and gradient terms plus the
+// optional pressure term.  Same arithmetic as pf_eval for this case.
+template <typename T, class Team, class Emit>
+__device__ __noinline__ double pf1_eval(Team& tm, const PotPF& P, CView<T> cv, T* xw, Emit* emp,
+                                        bool want_e, bool want_g) {
+  Emit emit = *emp;
+  const int nx = P.n[0], ny = P.n[1], nz = P.n[2];
+  const int ng = P.ngrid;
+  const T V = (T)P.vol_of_type[1];
+  const T kap = (T)P.kappa[0];
+  const T fb = kap / 16 * V;                      // bulk factor
+  const T Fi = (T)0.25 / (T)P.res2 * (T)P.kappaP[0] * V;  // gradient factor
+  const T pr = (P.flags & PF_PRESSURE) ? (T)P.pressure[0] : (T)0;
+  const bool dx_on = nx > 1, dy_on = ny > 1, dz_on = nz > 1;
+  EAcc<T> e;
+  for (int iG = tm.tid; iG < ng; iG += tm.nthr) {
+    const int z = iG % nz, y = (iG / nz) % ny, x = iG / (ny * nz);
+    const T c = cv(iG);
+    if (xw) xw[iG] = c;
+    const T a = (c + 1) * (c - 1);
+    T g = fb * 4 * c * (c * c - 1);
+    T eg = 0, lap = 0;
+    if (dx_on) {
+      const T cm = cv(((x == 0 ? nx - 1 : x - 1) * ny + y) * nz + z);
+      const T cp = cv(((x == nx - 1 ? 0 : x + 1) * ny + y) * nz + z);
+      const T gm = c - cm, gp = c - cp;
+      eg += (T)0.5 * (gm * gm + gp * gp);
+      lap += gm + gp;
+    }
+    if (dy_on) {
+      const T cm = cv((x * ny + (y == 0 ? ny - 1 : y - 1)) * nz + z);
+      const T cp = cv((x * ny + (y == ny - 1 ? 0 : y + 1)) * nz + z);
+      const T gm = c - cm, gp = c - cp;
+      eg += (T)0.5 * (gm * gm + gp * gp);
+      lap += gm + gp;
+    }
+    if (dz_on) {
+      const T cm = cv(iG - z + (z == 0 ? nz - 1 : z - 1));
+      const T cp = cv(iG - z + (z == nz - 1 ? 0 : z + 1));
+      const T gm = c - cm, gp = c - cp;
+      eg += (T)0.5 * (gm * gm + gp * gp);
+      lap += gm + gp;
+    }
+    // own term F*(gm+gp) plus the two neighbours' terms, which contribute
+    // the same amount again when nothing is solid
+    g += 2 * Fi * lap;
+    if (want_e) {
+      e.add(fb * a * a);
+      e.add(Fi * eg);
+    }
+    if (pr != 0) {
+      if (want_e) e.add(-pr * ((T)0.5 * (c + 1) * V));
+      g -= (T)0.5 * pr * V;
+    }
+    if (want_g) emit(iG, g);
+  }
+  *emp = emit;
+  return e.total();
+}
+
+// PhaseField node-local constraints on an arbitrary vector (a step):
+// fixFluid zeroing and the hard density projection.
+template <typename T, class Team>
+__device__ void pf_local_constrain(Team& tm, const PotPF& P, T* v) {
+  const int nf = P.nfluid;
+  for (int iG = tm.tid; iG < P.ngrid; iG += tm.nthr) {
+    T* w = v + (size_t)iG * nf;
+    if (P.flags & PF_FIXFLUID)
+      for (int f = 0; f < nf; f++)
+        if ((P.fix_mask >> f) & 1u) w[f] = 0;
+    if ((P.flags & PF_HARD) && nf > 1) {
+      T comp = 0;
+      for (int f = 0; f < nf; f++)
+        if (!((P.fix_mask >> f) & 1u)) comp += w[f];
+      comp *= (T)1 / (T)P.nvar;
+      for (int f = 0; f < nf; f++)
+        if (!((P.fix_mask >> f) & 1u)) w[f] -= comp;
+    }
+  }
+}
+
+// Fixed-volume projection (specialisedConstraints lines 614-658):
+// per variable fluid, remove the component along the (density-orthogonal)
+// node-volume vector.  One reduction over the grid.
+template <typename T, class Team>
+__device__ void pf_volume_project(Team& tm, const PotPF& P, T* v) {
+  const int nf = P.nfluid;
+  const bool hard = (P.flags & PF_HARD) != 0;
+  double part[MINIM_MAXF];
+#pragma unroll
+  for (int f = 0; f < MINIM_MAXF; f++) part[f] = 0.0;
+  for (int iG = tm.tid; iG < P.ngrid; iG += tm.nthr) {
+    const double V = P.vol_of_type[pf_type1(P, iG)];
+    const T* w = v + (size_t)iG * nf;
+    double sv = 0.0;
+    if (hard)
+      for (int f = 0; f < nf; f++)
+        if (!((P.fix_mask >> f) & 1u)) sv += (double)w[f];
+#pragma unroll
+    for (int f = 0; f < MINIM_MAXF; f++) {
+      if (f < nf && !((P.fix_mask >> f) & 1u))
+        part[f] += ((double)w[f] - (hard ? sv / P.nvar : 0.0)) * V;
+    }
+  }
+  tm.reduce(part);
+  double comp[MINIM_MAXF], csum = 0.0;
+#pragma unroll
+  for (int f = 0; f < MINIM_MAXF; f++) {
+    comp[f] = (f < nf && !((P.fix_mask >> f) & 1u)) ? part[f] / P.total_volume2 : 0.0;
+    csum += comp[f];
+  }
+  for (int iG = tm.tid; iG < P.ngrid; iG += tm.nthr) {
+    const double V = P.vol_of_type[pf_type1(P, iG)];
+    T* w = v + (size_t)iG * nf;
+    for (int f = 0; f < nf; f++) {
+      if ((P.fix_mask >> f) & 1u) continue;
+      double d = comp[f] * V;
+      if (hard) d -= csum * V / P.nvar;
+      w[f] = (T)((double)w[f] - d);
+    }
+  }
+  tm.sync();
+}
+
+// ===========================================================================
+// BarAndHinge (src/potentials/BarAndHinge.cpp:269-387).  Bars and hinges are
+// pre-sorted into colours (no two elements of a colour share a vertex), so
+// each colour scatters into the FP64 accumulator without atomics and the
+// result is deterministic.  The dihedral angle uses the atan2 form of the
+// reference's acos expression (same angle, accurate near 0 and pi).
+// ===========================================================================
+template <typename T>
+__device__ __forceinline__ T bah_atan2(T y, T x);
+template <>
+__device__ __forceinline__ float bah_atan2<float>(float y, float x) { return atan2f(y, x); }
+template <>
+__device__ __forceinline__ double bah_atan2<double>(double y, double x) { return atan2(y, x); }
+template <typename T>
+__device__ __forceinline__ T bah_fmod(T a, T b);
+template <>
+__device__ __forceinline__ float bah_fmod<float>(float a, float b) { return fmodf(a, b); }
+template <>
+__device__ __forceinline__ double bah_fmod<double>(double a, double b) { return fmod(a, b); }
+template <typename T>
+__device__ __forceinline__ T bah_sqrt(T a);
+template <>
+__device__ __forceinline__ float bah_sqrt<float>(float a) { return sqrtf(a); }
+template <>
+__device__ __forceinline__ double bah_sqrt<double>(double a) { return sqrt(a); }
+
+template <typename T>
+__device__ __forceinline__ void bah_bar(const PotBAH& P, const CView<T>& cv, int b, T& e, T* gl, T* gr,
+                                        bool want_g) {
+  const int2 nd = P.bars[b];
+  const double2 pr = P.bar_par[b];
+  const T dx = cv(3 * nd.x) - cv(3 * nd.y);
+  const T dy = cv(3 * nd.x + 1) - cv(3 * nd.y + 1);
+  const T dz = cv(3 * nd.x + 2) - cv(3 * nd.y + 2);
+  const T l = bah_sqrt<T>(dx * dx + dy * dy + dz * dz);
+  const T dl = l - (T)pr.y;
+  const T k = (T)pr.x;
+  e = (T)0.5 * k * dl * dl;
+  if (want_g) {
+    const T gf = 2 * k * dl / l;  // the reference's factor of 2
+    gl[0] = gf * dx; gl[1] = gf * dy; gl[2] = gf * dz;
+    gr[0] = -gl[0]; gr[1] = -gl[1]; gr[2] = -gl[2];
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ void bah_hinge(const PotBAH& P, const CView<T>& cv, int h, T& e, T (*gq)[3],
+                                          bool want_g) {
+  const int4 nd = P.hinges[h];
+  const double2 pr = P.hinge_par[h];
+  T x1[3], x2[3], x3[3], x4[3];
+#pragma unroll
+  for (int d = 0; d < 3; d++) {
+    x1[d] = cv(3 * nd.x + d); x2[d] = cv(3 * nd.y + d);
+    x3[d] = cv(3 * nd.z + d); x4[d] = cv(3 * nd.w + d);
+  }
+  T b1[3], b2[3], b3[3];
+#pragma unroll
+  for (int d = 0; d < 3; d++) { b1[d] = x2[d] - x1[d]; b2[d] = x3[d] - x2[d]; b3[d] = x4[d] - x3[d]; }
+  const T b2sq = b2[0] * b2[0] + b2[1] * b2[1] + b2[2] * b2[2];
+  const T b2m = bah_sqrt<T>(b2sq);
+  const T n1[3] = {b1[1] * b2[2] - b1[2] * b2[1], b1[2] * b2[0] - b1[0] * b2[2], b1[0] * b2[1] - b1[1] * b2[0]};
+  const T n2[3] = {b2[1] * b3[2] - b2[2] * b3[1], b2[2] * b3[0] - b2[0] * b3[2], b2[0] * b3[1] - b2[1] * b3[0]};
+  const T n1sq = n1[0] * n1[0] + n1[1] * n1[1] + n1[2] * n1[2];
+  const T n2sq = n2[0] * n2[0] + n2[1] * n2[1] + n2[2] * n2[2];
+  const T n1n2 = n1[0] * n2[0] + n1[1] * n2[1] + n1[2] * n2[2];
+  const T n1b3 = n1[0] * b3[0] + n1[1] * b3[1] + n1[2] * b3[2];
+  // acos(n1.n2/|n1||n2|) = atan2(|n1 x n2|, n1.n2) and |n1 x n2| = |b2| |n1.b3|
+  const T twopi = (T)(2.0 * 3.14159265358979323846);
+  const T pi = (T)3.14159265358979323846;
+  T th = bah_atan2<T>(b2m * (n1b3 >= 0 ? n1b3 : -n1b3), n1n2);
+  if (n1b3 < 0) th = twopi - th;
+  T dth = th - (T)pr.y;
+  dth = bah_fmod<T>(dth + pi, twopi) - pi;
+  const T k = (T)pr.x;
+  e = (T)0.5 * k * dth * dth;
+  if (want_g) {
+    const T gf = k * dth;
+    const T s1 = b2m / n1sq, s2 = b2m / n2sq;
+    const T sk1 = -(b1[0] * b2[0] + b1[1] * b2[1] + b1[2] * b2[2]) / b2sq;
+    const T sk2 = -(b3[0] * b2[0] + b3[1] * b2[1] + b3[2] * b2[2]) / b2sq;
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+      const T a1 = s1 * n1[d], a2 = s2 * n2[d];
+      gq[0][d] = -gf * a1;
+      gq[1][d] = gf * ((1 - sk1) * a1 - sk2 * a2);
+      gq[2][d] = -gf * ((1 - sk2) * a2 - sk1 * a1);
+      gq[3][d] = gf * a2;
+    }
+  }
+}
+
+// Per-vertex external force and substrate wall (lines 359-387); returns the
+// energy and the z-gradient of vertex v.
+template <typename T>
+__device__ __forceinline__ void bah_vertex(const PotBAH& P, const CView<T>& cv, int v, T& e, T& gz) {
+  e = 0; gz = 0;
+  if (!P.node_el[v]) return;
+  double fz = 0;
+  if (P.nforce == 3) fz = P.force[2];
+  else if (P.nforce > 0) fz = P.force[3 * v + 2];
+  const T z = cv(3 * v + 2);
+  e -= (T)fz * z;
+  gz -= (T)fz;
+  if (P.wall_on) {
+    if (!P.wall_adh && z > 0) return;
+    const double sig = P.wall_sig;
+    const T r0 = (T)(0.858374218932559 * sig);
+    T h = z + r0;
+    if (h < r0 / 2) h = r0 / 2;
+    const T q = (T)sig / h;
+    const T q3 = q * q * q;
+    const T lj9 = (T)(2.0 / 15) * q3 * q3 * q3;
+    const T lj3 = q3;
+    const double s3 = sig * sig * sig;
+    const T lj9_0 = (T)(0.5270462766947298 * s3 * s3 * s3);
+    const T lj3_0 = (T)(1.5811388300841895 * s3);
+    e += (T)P.wall_eps * ((lj9 - lj9_0) - (lj3 - lj3_0));
+    gz -= (T)P.wall_eps * (9 * lj9 - 3 * lj3) / h;
+  }
+}
+
+template <typename T, class Team, class Emit>
+__device__ __noinline__ double bah_eval(Team& tm, const PotBAH& P, CView<T> cv, T* xw, double* GA,
+                                        Emit* emp, bool want_e, bool want_g) {
+  Emit emit = *emp;
+  EAcc<T> e;
+  const int nv = P.nvert;
+  for (int v = tm.tid; v < nv; v += tm.nthr) {
+    if (xw) {
+      xw[3 * v] = cv(3 * v); xw[3 * v + 1] = cv(3 * v + 1); xw[3 * v + 2] = cv(3 * v + 2);
+    }
+    T ev, gz;
+    bah_vertex<T>(P, cv, v, ev, gz);
+    if (want_e) e.add(ev);
+    if (want_g) {
+      GA[3 * v] = 0.0; GA[3 * v + 1] = 0.0; GA[3 * v + 2] = (double)gz;
+    }
+  }
+  if (!want_g) {
+    for (int b = tm.tid; b < P.nbar; b += tm.nthr) {
+      T eb; bah_bar<T>(P, cv, b, eb, nullptr, nullptr, false);
+      e.add(eb);
+    }
+    for (int h = tm.tid; h < P.nhinge; h += tm.nthr) {
+      T eh; bah_hinge<T>(P, cv, h, eh, nullptr, false);
+      e.add(eh);
+    }
+    *emp = emit;
+    return e.total();
+  }
+  tm.sync();
+  for (int c = 0; c < P.nbar_colors; c++) {
+    const int b0 = P.bar_color_off[c], b1 = P.bar_color_off[c + 1];
+    for (int b = b0 + tm.tid; b < b1; b += tm.nthr) {
+      T eb, gl[3], gr[3];
+      bah_bar<T>(P, cv, b, eb, gl, gr, true);
+      if (want_e) e.add(eb);
+      const int2 nd = P.bars[b];
+#pragma unroll
+      for (int d = 0; d < 3; d++) {
+        GA[3 * nd.x + d] += (double)gl[d];
+        GA[3 * nd.y + d] += (double)gr[d];
+      }
+    }
+    tm.sync();
+  }
+  for (int c = 0; c < P.nhinge_colors; c++) {
+    const int h0 = P.hinge_color_off[c], h1 = P.hinge_color_off[c + 1];
+    for (int h = h0 + tm.tid; h < h1; h += tm.nthr) {
+      T eh, gq[4][3];
+      bah_hinge<T>(P, cv, h, eh, gq, true);
+      if (want_e) e.add(eh);
+      const int4 nd = P.hinges[h];
+      const int vs[4] = {nd.x, nd.y, nd.z, nd.w};
+#pragma unroll
+      for (int q = 0; q < 4; q++)
+#pragma unroll
+        for (int d = 0; d < 3; d++) GA[3 * vs[q] + d] += (double)gq[q][d];
+    }
+    tm.sync();
+  }
+  for (int i = tm.tid; i < 3 * nv; i += tm.nthr) emit(i, (T)GA[i]);
+  *emp = emit;
+  return e.total();
+}
+
+}  // namespace mg

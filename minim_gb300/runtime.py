@@ -1,0 +1,311 @@
+"""ctypes binding of libminim_gb300.so (the C ABI of include/minim_gpu.h).
+
+This is the call path tests and bench.py use: every compute call goes through
+the C ABI into the CUDA kernels.  There is no CPU fallback: without the
+library or without an sm_103 GPU every call raises.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import abi
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libminim_gb300.so")
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+_lib = None
+
+# every symbol declared in include/minim_gpu.h
+EXPORTS = [
+    "minim_gpu_abi_version", "minim_gpu_last_error", "minim_gpu_default_minimiser",
+    "minim_gpu_default_pf", "minim_gpu_default_bah", "minim_gpu_launch_count",
+    "minim_gpu_last_run_stats",
+    "minim_gpu_instance_create", "minim_gpu_instance_destroy", "minim_gpu_instance_ndof",
+    "minim_gpu_instance_default_tol", "minim_gpu_instance_set_coords",
+    "minim_gpu_instance_get_coords", "minim_gpu_instance_set_fixed", "minim_gpu_energy_gradient",
+    "minim_gpu_apply_constraints", "minim_gpu_minimise", "minim_gpu_batch_create",
+    "minim_gpu_batch_add", "minim_gpu_batch_run", "minim_gpu_batch_destroy",
+    "minim_gpu_server_create", "minim_gpu_server_submit", "minim_gpu_server_step",
+    "minim_gpu_server_poll", "minim_gpu_server_take", "minim_gpu_server_cancel",
+    "minim_gpu_server_destroy", "minim_gpu_bah_elements", "minim_gpu_bah_colouring",
+    "minim_gpu_pf_setup",
+]
+
+
+class MinimGpuError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"minim_gpu error {code}: {msg}")
+        self.code = code
+
+
+def load(path=LIB_PATH):
+    """Load the engine library (building it first if it is missing)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        from . import build as _build
+        _build.build()
+    lib = C.CDLL(path)
+    P = C.c_void_p
+    sig = {
+        "minim_gpu_abi_version": ([], C.c_int),
+        "minim_gpu_last_error": ([C.c_char_p, C.c_size_t], C.c_int),
+        "minim_gpu_launch_count": ([], C.c_int64),
+        "minim_gpu_last_run_stats": ([C.POINTER(abi.RunStats)], C.c_int),
+        "minim_gpu_instance_create": ([C.c_int, P, _dp, C.c_size_t, C.POINTER(P)], C.c_int),
+        "minim_gpu_instance_destroy": ([P], C.c_int),
+        "minim_gpu_instance_default_tol": ([P, _dp], C.c_int),
+        "minim_gpu_instance_set_coords": ([P, _dp], C.c_int),
+        "minim_gpu_instance_get_coords": ([P, _dp], C.c_int),
+        "minim_gpu_instance_set_fixed": ([P, _ip, C.c_size_t], C.c_int),
+        "minim_gpu_energy_gradient": ([P, _dp, _dp, _dp], C.c_int),
+        "minim_gpu_apply_constraints": ([P, _dp], C.c_int),
+        "minim_gpu_minimise": ([P, C.POINTER(abi.MinimiserParams), C.POINTER(abi.Result)], C.c_int),
+        "minim_gpu_batch_create": ([C.POINTER(P)], C.c_int),
+        "minim_gpu_batch_add": ([P, P, C.POINTER(abi.MinimiserParams)], C.c_int),
+        "minim_gpu_batch_run": ([P, C.c_int, C.POINTER(abi.Result)], C.c_int),
+        "minim_gpu_batch_destroy": ([P], C.c_int),
+        "minim_gpu_server_create": ([C.POINTER(abi.ServerConfig), C.POINTER(P)], C.c_int),
+        "minim_gpu_server_submit": ([P, C.c_int, P, _dp, C.c_size_t, C.POINTER(abi.MinimiserParams),
+                                     C.POINTER(C.c_uint64)], C.c_int),
+        "minim_gpu_server_step": ([P, _ip, _ip], C.c_int),
+        "minim_gpu_server_poll": ([P, C.POINTER(C.c_uint64), C.POINTER(abi.Result), C.c_int, _ip],
+                                  C.c_int),
+        "minim_gpu_server_take": ([P, C.c_uint64, _dp, C.c_size_t], C.c_int),
+        "minim_gpu_server_cancel": ([P, C.c_uint64], C.c_int),
+        "minim_gpu_server_destroy": ([P], C.c_int),
+        "minim_gpu_bah_elements": ([P, _dp, C.c_size_t, C.c_int, _ip, _ip, _dp, _ip, _ip, _dp],
+                                   C.c_int),
+        "minim_gpu_bah_colouring": ([P, _dp, C.c_size_t, _ip, _ip, _ip], C.c_int),
+        "minim_gpu_pf_setup": ([P, _dp, C.c_size_t, _dp, _dp, _ip, _dp, _dp, _ip], C.c_int),
+    }
+    for name, (args, res) in sig.items():
+        f = getattr(lib, name)
+        f.argtypes = args
+        f.restype = res
+    _lib = lib
+    return lib
+
+
+def _check(rc):
+    if rc != 0:
+        buf = C.create_string_buffer(1024)
+        _lib.minim_gpu_last_error(buf, 1024)
+        raise MinimGpuError(rc, buf.value.decode())
+
+
+def _vec(x):
+    return np.ascontiguousarray(np.asarray(x, dtype=np.float64).ravel())
+
+
+def launch_count():
+    return load().minim_gpu_launch_count()
+
+
+def last_run_stats():
+    s = abi.RunStats()
+    _check(load().minim_gpu_last_run_stats(C.byref(s)))
+    return {k: getattr(s, k) for k, _ in s._fields_}
+
+
+class Instance:
+    """A device-resident State: potential + coordinates (C ABI instance)."""
+
+    def __init__(self, params, x0, fixed=None):
+        lib = load()
+        self.params = params
+        x = _vec(x0)
+        self.ndof = x.size
+        h = C.c_void_p()
+        _check(lib.minim_gpu_instance_create(params.kind, params.ptr(), x.ctypes.data_as(_dp),
+                                             x.size, C.byref(h)))
+        self.h = h
+        if fixed is not None and len(fixed):
+            self.set_fixed(fixed)
+
+    def close(self):
+        if getattr(self, "h", None) is not None and _lib is not None:
+            _lib.minim_gpu_instance_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def default_tol(self):
+        t = C.c_double()
+        _check(_lib.minim_gpu_instance_default_tol(self.h, C.byref(t)))
+        return t.value
+
+    @property
+    def coords(self):
+        x = np.zeros(self.ndof)
+        _check(_lib.minim_gpu_instance_get_coords(self.h, x.ctypes.data_as(_dp)))
+        return x
+
+    @coords.setter
+    def coords(self, x):
+        xv = _vec(x)
+        _check(_lib.minim_gpu_instance_set_coords(self.h, xv.ctypes.data_as(_dp)))
+
+    def set_fixed(self, idof):
+        a = np.ascontiguousarray(np.asarray(idof, dtype=np.int32))
+        _check(_lib.minim_gpu_instance_set_fixed(self.h, a.ctypes.data_as(_ip), a.size))
+
+    def energy_gradient(self, x=None, energy=True, gradient=True):
+        xv = None if x is None else _vec(x)
+        e = C.c_double()
+        g = np.zeros(self.ndof) if gradient else None
+        _check(_lib.minim_gpu_energy_gradient(
+            self.h, None if xv is None else xv.ctypes.data_as(_dp), C.byref(e) if energy else None,
+            None if g is None else g.ctypes.data_as(_dp)))
+        return (e.value if energy else None), g
+
+    def energy(self, x=None):
+        return self.energy_gradient(x, gradient=False)[0]
+
+    def gradient(self, x=None):
+        return self.energy_gradient(x, energy=False)[1]
+
+    def apply_constraints(self, v):
+        a = _vec(v).copy()
+        _check(_lib.minim_gpu_apply_constraints(self.h, a.ctypes.data_as(_dp)))
+        return a
+
+    def minimise(self, mp):
+        r = abi.Result()
+        _check(_lib.minim_gpu_minimise(self.h, C.byref(mp), C.byref(r)))
+        return r
+
+
+class Batch:
+    """Many instances minimised together by the persistent batch kernels."""
+
+    def __init__(self):
+        lib = load()
+        h = C.c_void_p()
+        _check(lib.minim_gpu_batch_create(C.byref(h)))
+        self.h = h
+        self.items = []
+
+    def add(self, inst, mp):
+        _check(_lib.minim_gpu_batch_add(self.h, inst.h, C.byref(mp)))
+        self.items.append((inst, mp))
+
+    def run(self, threads=0):
+        res = (abi.Result * len(self.items))()
+        _check(_lib.minim_gpu_batch_run(self.h, threads, res))
+        return list(res)
+
+    def close(self):
+        if getattr(self, "h", None) is not None and _lib is not None:
+            _lib.minim_gpu_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Server:
+    """Continuous batching: submit requests, step, poll results."""
+
+    def __init__(self, max_bytes=0, max_slots=0, slice_iters=0, threads=0):
+        lib = load()
+        cfg = abi.ServerConfig(max_bytes, max_slots, slice_iters, threads)
+        h = C.c_void_p()
+        _check(lib.minim_gpu_server_create(C.byref(cfg), C.byref(h)))
+        self.h = h
+        self.ndof = {}
+
+    def submit(self, params, x0, mp):
+        x = _vec(x0)
+        rid = C.c_uint64()
+        _check(_lib.minim_gpu_server_submit(self.h, params.kind, params.ptr(), x.ctypes.data_as(_dp),
+                                            x.size, C.byref(mp), C.byref(rid)))
+        self.ndof[rid.value] = x.size
+        return rid.value
+
+    def step(self):
+        nr, nq = C.c_int(), C.c_int()
+        _check(_lib.minim_gpu_server_step(self.h, C.byref(nr), C.byref(nq)))
+        return nr.value, nq.value
+
+    def poll(self, max_n=4096):
+        ids = (C.c_uint64 * max_n)()
+        res = (abi.Result * max_n)()
+        n = C.c_int()
+        _check(_lib.minim_gpu_server_poll(self.h, ids, res, max_n, C.byref(n)))
+        return [(ids[i], res[i]) for i in range(n.value)]
+
+    def take(self, rid):
+        x = np.zeros(self.ndof[rid])
+        _check(_lib.minim_gpu_server_take(self.h, rid, x.ctypes.data_as(_dp), x.size))
+        del self.ndof[rid]
+        return x
+
+    def cancel(self, rid):
+        _check(_lib.minim_gpu_server_cancel(self.h, rid))
+
+    def close(self):
+        if getattr(self, "h", None) is not None and _lib is not None:
+            _lib.minim_gpu_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+# ---- host-only set-up introspection (no GPU needed) ------------------------------
+def bah_elements(params, x0):
+    lib = load()
+    x = _vec(x0)
+    cap = 4 * x.size + 64
+    nb, nh = C.c_int(), C.c_int()
+    b = np.zeros(2 * cap, np.int32)
+    h = np.zeros(4 * cap, np.int32)
+    bp = np.zeros(2 * cap)
+    hp = np.zeros(2 * cap)
+    _check(lib.minim_gpu_bah_elements(params.ptr(), x.ctypes.data_as(_dp), x.size, cap, C.byref(nb),
+                                      b.ctypes.data_as(_ip), bp.ctypes.data_as(_dp), C.byref(nh),
+                                      h.ctypes.data_as(_ip), hp.ctypes.data_as(_dp)))
+    return (b[: 2 * nb.value].reshape(-1, 2), bp[: 2 * nb.value].reshape(-1, 2),
+            h[: 4 * nh.value].reshape(-1, 4), hp[: 2 * nh.value].reshape(-1, 2))
+
+
+def bah_colouring(params, x0):
+    lib = load()
+    x = _vec(x0)
+    nb, nh, ok = C.c_int(), C.c_int(), C.c_int()
+    _check(lib.minim_gpu_bah_colouring(params.ptr(), x.ctypes.data_as(_dp), x.size, C.byref(nb),
+                                       C.byref(nh), C.byref(ok)))
+    return nb.value, nh.value, bool(ok.value)
+
+
+def pf_setup(params, x0):
+    lib = load()
+    x = _vec(x0)
+    s = params.struct
+    ng = int(np.prod(s.grid[:]))
+    k = np.zeros(ng * s.nfluid + 8)
+    kp = np.zeros(ng * s.nfluid + 8)
+    nv = np.zeros(ng)
+    sa = np.zeros(ng)
+    nk, var = C.c_int(), C.c_int()
+    _check(lib.minim_gpu_pf_setup(params.ptr(), x.ctypes.data_as(_dp), x.size, k.ctypes.data_as(_dp),
+                                  kp.ctypes.data_as(_dp), C.byref(nk), nv.ctypes.data_as(_dp),
+                                  sa.ctypes.data_as(_dp), C.byref(var)))
+    return {"kappa": k[: nk.value], "kappaP": kp[: nk.value], "node_vol": nv, "surface_area": sa,
+            "kernel_variant": var.value}

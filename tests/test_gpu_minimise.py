@@ -1,0 +1,207 @@
+"""Minimisation parity on the GPU (single-instance grid path and batched
+path) against the FP64 oracle.
+
+Parity protocol (LJ landscapes are chaotic, so trajectories may part):
+  * the returned point is a minimum under the oracle: FP64 RMS(g) < tol;
+  * the returned energy equals the oracle's energy at that point to 1e-8
+    relative (absolute floor 1e-8 * max(|E|, |E_init|) near zero);
+  * for the reference's known-answer cases (BarAndHinge hinge minima) the
+    coordinates match the analytic minima to 1e-4, as the reference test does;
+  * in FP64 mode small cases follow the oracle to the same minimum.
+"""
+import numpy as np
+import pytest
+
+from minim_gb300 import abi, runtime
+from oracle.oracle import Oracle
+from tests.workloads import lj_cluster, pf_noise, pf_simplex, sheet
+
+pytestmark = pytest.mark.gpu
+
+
+def check_minimum(p, x0, x, res, tol, fixed=None):
+    ora = Oracle(p, x0, fixed=fixed)
+    e, g = ora.energy_gradient(x)
+    e_init = ora.energy(x0)
+    floor = 1e-8 * max(abs(e), abs(e_init))
+    assert abs(res.energy - e) <= max(1e-8 * abs(e), floor), (res.energy, e)
+    rms = np.sqrt(np.mean(g ** 2))
+    assert rms < tol, rms
+    return e
+
+
+@pytest.mark.parametrize("method,ls", [("lbfgs", None), ("fire", "backtracking"), ("gd", None)])
+@pytest.mark.parametrize("prec", ["mixed", "fp64"])
+def test_lj_grid_path(method, ls, prec):
+    x0 = lj_cluster(13, seed=11)
+    p = abi.lj()
+    inst = runtime.Instance(p, x0)
+    tol = 1e-6 if method != "gd" else 1e-5
+    mp = abi.minimiser(method, linesearch=ls, tol=tol, precision=prec, max_iter=200000)
+    r = inst.minimise(mp)
+    assert r.status == abi.RES_CONVERGED, r.as_dict()
+    check_minimum(p, x0, inst.coords, r, tol)
+
+
+def test_lj_fp64_follows_oracle():
+    x0 = lj_cluster(20, seed=12)
+    p = abi.lj()
+    mp = abi.minimiser("lbfgs", tol=1e-6, precision="fp64")
+    inst = runtime.Instance(p, x0)
+    r = inst.minimise(mp)
+    ora = Oracle(p, x0)
+    ro = ora.minimise(mp)
+    assert r.status == abi.RES_CONVERGED
+    assert abs(r.energy - ro.energy) <= 1e-8 * abs(ro.energy)
+    assert np.max(np.abs(inst.coords - ora.coords)) < 1e-4
+
+
+def test_fire_first_step():
+    # Fire().setMaxIter(0): one iteration from v = 0 moves x by -dt^2/2 * g
+    # with dt = dtMax = 0.1/sqrt(|g|) (reference test/unit/Fire_test.cpp:25-40)
+    x0 = lj_cluster(8, seed=13)
+    p = abi.lj()
+    mp = abi.minimiser("fire", linesearch="backtracking", max_iter=0, precision="fp64")
+    inst = runtime.Instance(p, x0)
+    g = inst.gradient()
+    inst.minimise(mp)
+    dt = 0.1 / np.sqrt(np.linalg.norm(g))
+    expect = x0 - 0.5 * dt * dt * g
+    assert np.allclose(inst.coords, expect, rtol=0, atol=1e-12)
+
+
+@pytest.mark.parametrize("target,expected", [
+    (1e-6, "a"), (np.pi / 2, "b"), (np.pi, "c"), (3 * np.pi / 2, "d"), (2 * np.pi - 1e-6, "e")])
+@pytest.mark.parametrize("path", ["grid", "batch"])
+def test_bah_hinge_minima(target, expected, path):
+    # reference test/unit/BarAndHinge_test.cpp:13-56
+    s2 = np.sqrt(2)
+    dz = s2 / 2
+    exp = {
+        "a": [0, 0, 0.5 + dz, 0, -s2, 0.5 - dz, 0, s2, 0.5 - dz, 0, 0, 0.5 + dz],
+        "b": [-1, 0, 1, 0, -s2, 0, 0, s2, 0, 1, 0, 1],
+        "c": [-s2, 0, 0.5, 0, -s2, 0.5, 0, s2, 0.5, s2, 0, 0.5],
+        "d": [-1, 0, 0, 0, -s2, 1, 0, s2, 1, 1, 0, 0],
+        "e": [0, 0, 0.5 - dz, 0, -s2, 0.5 + dz, 0, s2, 0.5 + dz, 0, 0, 0.5 - dz],
+    }[expected]
+    x0 = np.array([-1, 0, 1, 0, -s2, 0, 0, s2, 0, 1, 0, 1.0])
+    p = abi.bar_and_hinge(triangulation=[[0, 1, 2], [1, 3, 2]], rigidity=(100, 1), theta0=[target])
+    inst = runtime.Instance(p, x0)
+    mp = abi.minimiser("lbfgs")
+    if path == "grid":
+        r = inst.minimise(mp)
+    else:
+        b = runtime.Batch()
+        b.add(inst, mp)
+        r = b.run()[0]
+    assert r.status == abi.RES_CONVERGED, r.as_dict()
+    assert np.allclose(inst.coords, exp, atol=1e-4), inst.coords
+
+
+def test_batch_lj_mixed_methods():
+    p = abi.lj()
+    insts, x0s, mps = [], [], []
+    for i, n in enumerate([13, 38, 55, 13, 100, 7, 150, 26]):
+        x0 = lj_cluster(n, seed=100 + i)
+        meth = ["lbfgs", "fire", "gd", "lbfgs"][i % 4]
+        mp = abi.minimiser(meth, linesearch="backtracking" if meth == "fire" else None,
+                           dt_max=0.0, tol=1e-6 if meth != "gd" else 1e-5, max_iter=200000)
+        insts.append(runtime.Instance(p, x0))
+        x0s.append(x0)
+        mps.append(mp)
+    b = runtime.Batch()
+    for inst, mp in zip(insts, mps):
+        b.add(inst, mp)
+    res = b.run()
+    for inst, x0, mp, r in zip(insts, x0s, mps, res):
+        assert r.status == abi.RES_CONVERGED, r.as_dict()
+        check_minimum(p, x0, inst.coords, r, mp.tol)
+
+
+def test_batch_alone_equals_mixed():
+    p = abi.lj()
+    x0 = lj_cluster(40, seed=200)
+    mp = abi.minimiser("lbfgs", tol=1e-6)
+    a = runtime.Instance(p, x0)
+    ba = runtime.Batch()
+    ba.add(a, mp)
+    ra = ba.run(threads=128)[0]
+    others = [runtime.Instance(p, lj_cluster(n, seed=300 + n)) for n in (13, 80, 120, 33)]
+    b = runtime.Instance(p, x0)
+    bb = runtime.Batch()
+    for o in others[:2]:
+        bb.add(o, mp)
+    bb.add(b, mp)
+    for o in others[2:]:
+        bb.add(o, mp)
+    rb = bb.run(threads=128)[2]
+    assert ra.iter == rb.iter and ra.energy == rb.energy
+    assert np.array_equal(a.coords, b.coords)
+
+
+def test_pf_binary_minimise():
+    grid = (12, 12, 12)
+    x0 = pf_noise(grid, seed=21)
+    p = abi.phase_field(grid)
+    inst = runtime.Instance(p, x0)
+    mp = abi.minimiser("lbfgs", m=10, tol=1e-7)
+    r = inst.minimise(mp)
+    assert r.status == abi.RES_CONVERGED, r.as_dict()
+    check_minimum(p, x0, inst.coords, r, 1e-7)
+
+
+def test_pf_ternary_volume_minimise_batch():
+    shape = (24, 24, 1)
+    p = abi.phase_field(shape, nfluid=3, volume_fixed=True)
+    x0 = pf_simplex(shape, 3, seed=22)
+    inst = runtime.Instance(p, x0)
+    mp = abi.minimiser("lbfgs", tol=1e-7, max_iter=20000)
+    b = runtime.Batch()
+    b.add(inst, mp)
+    r = b.run()[0]
+    assert r.status == abi.RES_CONVERGED, r.as_dict()
+    x = inst.coords
+    check_minimum(p, x0, x, r, 1e-7)
+    # the projection keeps each fluid's volume and the per-node density
+    v0 = x0.reshape(-1, 3).sum(axis=0)
+    v1 = x.reshape(-1, 3).sum(axis=0)
+    assert np.allclose(v0, v1, rtol=0, atol=1e-6 * x0.size)
+    assert np.allclose(x.reshape(-1, 3).sum(axis=1), 1.0, atol=1e-6)
+
+
+def test_bah_sheet_minimise_batch():
+    flat, tris, pert = sheet(10, seed=23)
+    p = abi.bar_and_hinge(triangulation=tris, rigidity=(1, 0.01))
+    inst = runtime.Instance(p, flat)
+    inst.coords = pert
+    mp = abi.minimiser("lbfgs", tol=1e-7)
+    b = runtime.Batch()
+    b.add(inst, mp)
+    r = b.run()[0]
+    assert r.status == abi.RES_CONVERGED, r.as_dict()
+    ora = Oracle(p, flat)
+    e, g = ora.energy_gradient(inst.coords)
+    assert np.sqrt(np.mean(g ** 2)) < 1e-7
+    assert abs(r.energy - e) <= 1e-8 * max(abs(e), abs(ora.energy(pert)))
+
+
+def test_server_roundtrip():
+    p = abi.lj()
+    srv = runtime.Server(slice_iters=32)
+    ids = {}
+    for i, n in enumerate([13, 30, 60, 13, 90]):
+        x0 = lj_cluster(n, seed=400 + i)
+        ids[srv.submit(p, x0, abi.minimiser("lbfgs", tol=1e-6))] = x0
+    done = {}
+    for _ in range(10000):
+        srv.step()
+        for rid, r in srv.poll():
+            done[rid] = r
+        if len(done) == len(ids):
+            break
+    assert len(done) == len(ids)
+    for rid, r in done.items():
+        assert r.status == abi.RES_CONVERGED
+        assert r.latency_ms > 0
+        x = srv.take(rid)
+        check_minimum(p, ids[rid], x, r, 1e-6)
