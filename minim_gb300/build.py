@@ -20,7 +20,11 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU = ["engine_lj.cu", "engine_pf.cu", "engine_pf1.cu", "engine_bah.cu", "engine_misc.cu"]
 CPP = ["setup.cpp", "capi.cpp"]
+API = ["api_core.cpp", "api_minimisers.cpp", "api_potentials.cpp"]  # source-compatible C++ API
 HEADERS = ["common.cuh", "potentials.cuh", "minimiser.cuh", "kernels.cuh", "engine.h", "setup.h"]
+API_HEADERS = ["minim.h", "State.h", "Potential.h", "Minimiser.h", "Communicator.h", "minimisers/Lbfgs.h",
+               "minimisers/Fire.h", "minimisers/GradDescent.h", "potentials/LjNd.h", "potentials/PhaseField.h",
+               "potentials/BarAndHinge.h", "utils/vec.h", "utils/mpi.h", "utils/print.h"]
 
 
 def _deps():
@@ -60,6 +64,14 @@ def build(verbose=False, force=False):
         if force or _stale(obj, [src] + _deps()):
             jobs.append(["g++", "-O2", "-std=c++17", "-fPIC", "-Wall", "-I" + os.path.join(CUDA, "include")]
                         + inc + ["-c", src, "-o", obj])
+    api_deps = [os.path.join(REPO, "include", "minim", h) for h in API_HEADERS] + _deps()
+    for f in API:
+        src = os.path.join(HERE, "cpp", f)
+        obj = os.path.join(BUILD, f + ".o")
+        objs.append(obj)
+        if force or _stale(obj, [src] + api_deps):
+            jobs.append(["g++", "-O2", "-std=c++17", "-fPIC", "-Wall", "-I" + os.path.join(REPO, "include"),
+                         "-I" + os.path.join(REPO, "include", "minim"), "-c", src, "-o", obj])
     if jobs:
         with cf.ThreadPoolExecutor(max_workers=min(len(jobs), os.cpu_count() or 4)) as ex:
             logs = list(ex.map(_run, jobs))
