@@ -273,6 +273,20 @@ def run_reference(args):
                     "d2h_bytes_per_step": 0}}
 
 
+def run_profile_case(iters):
+    """One short minimisation of the headline workload (a single launch of
+    the fused minimiser kernel) for profiler captures."""
+    from minim_gb300 import abi, runtime
+    p, x0, _ = pf_setup()
+    mp = abi.minimiser("lbfgs", m=10, tol=TOL, max_iter=iters - 1, precision="fp32")
+    inst = runtime.Instance(p, x0)
+    r = inst.minimise(mp)
+    st = runtime.last_run_stats()
+    print(json.dumps({"profile_case": "PhaseField 192^3 Lbfgs m=10", "iterations": iters,
+                      "kernel_ms": st["kernel_ms"], "launches": st["launches"],
+                      "abytes_per_launch": st["abytes"] / max(st["launches"], 1), "status": r.status}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -285,7 +299,12 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=20.0)
     ap.add_argument("--ref-iters-hint", type=int, default=600)
+    ap.add_argument("--profile", type=int, default=0,
+                    help="run one short minimisation of N iterations (profiler capture) and exit")
     args = ap.parse_args()
+    if args.profile:
+        run_profile_case(args.profile)
+        return
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     if args.impl == "reference":

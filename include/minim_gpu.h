@@ -159,6 +159,10 @@ typedef struct {
   double pairs32;       /* Lennard-Jones pair interactions in FP32 */
   double pairs64;       /* ... and in FP64 */
   int64_t iterations;   /* minimiser iterations (all instances) */
+  int64_t fp64_iterations; /* ... of which with FP64 coordinates */
+  /* instances whose FP64 stage started because: [1] FP32 converged, [2] the
+   * line search failed twice in a row, [3] the gradient stalled near tol */
+  int64_t switches[4];
 } minim_gpu_run_stats;
 
 typedef struct minim_gpu_instance_s* minim_gpu_handle;

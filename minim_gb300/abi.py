@@ -85,7 +85,8 @@ class Result(C.Structure):
 class RunStats(C.Structure):
     _fields_ = [("kernel_ms", C.c_double), ("wall_ms", C.c_double), ("launches", C.c_int64),
                 ("abytes", C.c_double), ("pairs32", C.c_double), ("pairs64", C.c_double),
-                ("iterations", C.c_int64)]
+                ("iterations", C.c_int64), ("fp64_iterations", C.c_int64),
+                ("switches", C.c_int64 * 4)]
 
 
 class ServerConfig(C.Structure):

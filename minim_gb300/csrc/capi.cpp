@@ -426,6 +426,8 @@ void do_minimise(minim_gpu_instance_s* h, const minim_gpu_minimiser_params& mp, 
   stats.pairs32 = s.pairs32;
   stats.pairs64 = s.pairs64;
   stats.iterations = s.iter + (s.status == ST_CONVERGED ? 1 : 0);
+  stats.fp64_iterations = s.fp64_iters;
+  if (s.switch_reason > 0 && s.switch_reason < 4) stats.switches[s.switch_reason]++;
   g_stats = stats;
   if (res) fill_result(res, s, h->n);
 }
@@ -759,7 +761,11 @@ int minim_gpu_batch_run(minim_gpu_batch b, int threads, minim_gpu_result* result
     g_stats.wall_ms = now_ms() - t0;
     g_stats.abytes = g_stats.pairs32 = g_stats.pairs64 = 0;
     g_stats.iterations = 0;
+    g_stats.fp64_iterations = 0;
+    for (auto& k : g_stats.switches) k = 0;
     for (auto& s : st) {
+      g_stats.fp64_iterations += s.fp64_iters;
+      if (s.switch_reason > 0 && s.switch_reason < 4) g_stats.switches[s.switch_reason]++;
       g_stats.abytes += s.abytes;
       g_stats.pairs32 += s.pairs32;
       g_stats.pairs64 += s.pairs64;

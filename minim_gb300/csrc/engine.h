@@ -104,6 +104,9 @@ struct MinScalars {
   int stall;         // iterations since the best rms improved (stage 0)
   int nsteps;        // Fire::_nSteps
   int pbuf, ybuf;    // spare history buffers (direction / new y)
+  int exhausted_run; // consecutive line searches that found no Armijo point
+  int switch_reason; // why the FP64 stage started: 1 converged in FP32,
+                     // 2 line search exhausted twice, 3 stalled near tol
   int sidx[MINIM_MAXM], yidx[MINIM_MAXM];  // ring slot -> buffer
   double E;          // energy at the current coordinates
   double gg;         // g.g at the current coordinates

@@ -65,6 +65,7 @@ struct Runner {
   int lj_tile;
   // uniform scalars (every thread holds identical copies)
   int n, status, initd, iter, ii, stage, xi, gi, evals, fp64_iters, stall, nsteps, pbuf, ybuf;
+  int exhausted_run, switch_reason;
   double E, gg, best_rms, dt, a, dtmax, gnorm;
   double abytes, pairs32, pairs64;
   // shared arrays (one copy per block; written by thread 0 between barriers)
@@ -459,7 +460,8 @@ struct Runner {
   __device__ void load(const MinScalars& s) {
     status = s.status; initd = s.initialised; iter = s.iter; ii = s.ii; stage = s.stage; xi = s.xi; gi = s.gi;
     evals = s.evals; fp64_iters = s.fp64_iters; stall = s.stall; nsteps = s.nsteps;
-    pbuf = s.pbuf; ybuf = s.ybuf; E = s.E; gg = s.gg; best_rms = s.best_rms;
+    pbuf = s.pbuf; ybuf = s.ybuf; E = s.E;
+    exhausted_run = s.exhausted_run; switch_reason = s.switch_reason; gg = s.gg; best_rms = s.best_rms;
     dt = s.dt; a = s.a; dtmax = s.dtmax; gnorm = s.gnorm;
     abytes = s.abytes; pairs32 = s.pairs32; pairs64 = s.pairs64;
     for (int k = threadIdx.x; k < MINIM_MAXM; k += blockDim.x) {
@@ -474,7 +476,8 @@ struct Runner {
     if (tm.block0() && threadIdx.x == 0) {
       s.status = status; s.iter = iter; s.ii = ii; s.stage = stage; s.xi = xi; s.gi = gi;
       s.evals = evals; s.fp64_iters = fp64_iters; s.stall = stall; s.nsteps = nsteps;
-      s.pbuf = pbuf; s.ybuf = ybuf; s.E = E; s.gg = gg; s.best_rms = best_rms;
+      s.pbuf = pbuf; s.ybuf = ybuf; s.E = E;
+      s.exhausted_run = exhausted_run; s.switch_reason = switch_reason; s.gg = gg; s.best_rms = best_rms;
       s.dt = dt; s.a = a; s.dtmax = dtmax; s.gnorm = gnorm; s.initialised = 1;
       s.abytes = abytes; s.pairs32 = pairs32; s.pairs64 = pairs64;
       for (int k = 0; k < MINIM_MAXM; k++) {
@@ -543,9 +546,18 @@ struct Runner {
       const double r = rms();
       bool conv = r < mp.tol;
       if (stage == 0 && mixed) {
+        // Leave the FP32 stage when FP32 has done what it can: converged in
+        // FP32; the line search found no Armijo point twice in a row (the
+        // FP32 energy no longer resolves the decrease); or the RMS gradient
+        // has not improved by 0.1% for 100 iterations while within 100x of
+        // the tolerance (the FP32 gradient floor).  A run that stalls far
+        // from the tolerance is not limited by precision and stays in FP32.
         if (r < 0.999 * best_rms) { best_rms = r; stall = 0; }
         else stall++;
-        if (conv || exhausted || stall >= 100) {
+        exhausted_run = exhausted ? exhausted_run + 1 : 0;
+        int why = conv ? 1 : (exhausted_run >= 2 ? 2 : ((stall >= 100 && r < 100.0 * mp.tol) ? 3 : 0));
+        if (why) {
+          switch_reason = why;
           to_fp64();
           if (mp.method != 2) {
             double py, yyv;

@@ -109,7 +109,9 @@ def launch_count():
 def last_run_stats():
     s = abi.RunStats()
     _check(load().minim_gpu_last_run_stats(C.byref(s)))
-    return {k: getattr(s, k) for k, _ in s._fields_}
+    d = {k: getattr(s, k) for k, _ in s._fields_}
+    d["switches"] = list(s.switches)
+    return d
 
 
 class Instance:
