@@ -55,7 +55,7 @@ def build(verbose=False, force=False):
         obj = os.path.join(BUILD, f + ".o")
         objs.append(obj)
         if force or _stale(obj, [src] + _deps()):
-            jobs.append([NVCC] + ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
+            jobs.append([NVCC] + ARCH + ["-O3", "-lineinfo", "-std=c++20", "-Xcompiler", "-fPIC",
                                          "-Xptxas", "-v"] + inc + ["-c", src, "-o", obj])
     for f in CPP:
         src = os.path.join(CSRC, f)

@@ -130,7 +130,7 @@ size_t pot_smem(int kk) { return kk == K_LJ ? kLjTileBytes : 0; }
 
 // ---- workspace layout --------------------------------------------------------------
 struct WsLayout {
-  size_t x32[2], x64[2], g[2], S, Y, V, total;
+  size_t x32[2], x64[2], g[2], S, Y, V, total, hstride;
   int nS, nY;
   bool fp64;
 };
@@ -145,8 +145,9 @@ WsLayout ws_layout(size_t n, const minim_gpu_minimiser_params& mp) {
   for (int k = 0; k < 2; k++) L.x32[k] = take(n * 4);
   for (int k = 0; k < 2; k++) L.x64[k] = L.fp64 ? take(n * 8) : (size_t)-1;
   for (int k = 0; k < 2; k++) L.g[k] = take(n * 4);
-  L.S = L.nS ? take((size_t)L.nS * n * 4) : (size_t)-1;
-  L.Y = L.nY ? take((size_t)L.nY * n * 4) : (size_t)-1;
+  L.hstride = (n + 63) & ~(size_t)63;
+  L.S = L.nS ? take((size_t)L.nS * L.hstride * 4) : (size_t)-1;
+  L.Y = L.nY ? take((size_t)L.nY * L.hstride * 4) : (size_t)-1;
   L.V = mp.method == MINIM_FIRE ? take(n * 4) : (size_t)-1;
   L.total = o;
   return L;
@@ -157,6 +158,7 @@ void ws_apply(InstDesc& d, char* base, const WsLayout& L) {
     d.X64[k] = L.fp64 ? (double*)(base + L.x64[k]) : nullptr;
     d.G[k] = (float*)(base + L.g[k]);
   }
+  d.hstride = (int)L.hstride;
   d.Sb = L.nS ? (float*)(base + L.S) : nullptr;
   d.Yb = L.nY ? (float*)(base + L.Y) : nullptr;
   d.V = L.V != (size_t)-1 ? (float*)(base + L.V) : nullptr;
@@ -190,6 +192,7 @@ MinScalars fresh_scalars() {
   MinScalars s;
   std::memset(&s, 0, sizeof s);
   s.status = ST_RUNNING;
+  s.pend = -1;
   return s;
 }
 
@@ -333,7 +336,7 @@ void ensure_grid(minim_gpu_instance_s* h) {
   h->d_desc = (InstDesc*)h->own(dalloc(sizeof(InstDesc)));
   h->d_io = (EvalIO*)h->own(dalloc(sizeof(EvalIO)));
   h->d_bar = (GridSyncState*)h->own(dalloc(sizeof(GridSyncState)));
-  h->d_partials = (double*)h->own(dalloc(2 * (size_t)h->gblocks * 8 * sizeof(double)));
+  h->d_partials = (double*)h->own(dalloc((2 * (size_t)h->gblocks * 64 + 2 * 64) * sizeof(double)));
   h->d_e = (double*)h->own(dalloc(sizeof(double)));
   h->d_tmp = (double*)h->own(dalloc(h->n * sizeof(double)));
   h->d_g = (double*)h->own(dalloc(h->n * sizeof(double)));

@@ -14,6 +14,7 @@
 #include "engine.h"
 
 #define MINIM_MAXRED 8    // values reduced together in one team reduction
+#define MINIM_WIDE 64     // values reduced together in one wide reduction
 
 namespace mg {
 
@@ -21,6 +22,41 @@ __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   return v;
+}
+
+// Warp reduce-scatter of 32 values: on entry every lane holds v[0..31]; on
+// exit lane l holds, in v[0], the sum over the warp of v[l].  31 shuffles per
+// lane instead of 5 per value.
+__device__ __forceinline__ float warp_reduce_scatter32(float* v) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int s = 16; s >= 1; s >>= 1) {
+    const bool up = (lane & s) != 0;
+#pragma unroll
+    for (int j = 0; j < s; j++) {
+      const float send = up ? v[j] : v[j + s];
+      const float keep = up ? v[j + s] : v[j];
+      v[j] = keep + __shfl_xor_sync(0xffffffffu, send, s);
+    }
+  }
+  return v[0];
+}
+
+// Wide reductions are assembled in three steps: every warp zeroes its row of
+// the shared `wide` table (wide_clear), adds groups of 32 per-thread partials
+// -- 4 dot products x 8 slots -- to it (wide_store32, value index
+// dot * 16 + k0 + slot), then the team combines the rows (wide_combine).
+__device__ __forceinline__ void wide_clear_row(double* wide) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  wide[w * MINIM_WIDE + lane] = 0.0;
+  wide[w * MINIM_WIDE + 32 + lane] = 0.0;
+  __syncwarp();
+}
+__device__ __forceinline__ void wide_store_row(float (&v)[32], int k0, double* wide) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const float a = warp_reduce_scatter32(v);
+  wide[w * MINIM_WIDE + (lane >> 3) * 16 + k0 + (lane & 7)] = (double)a;
+  __syncwarp();
 }
 
 // Accumulates a stream of FP32 terms: short runs are summed in FP32 and
@@ -39,6 +75,18 @@ struct Acc {
   __device__ __forceinline__ double total() const { return d + (double)f; }
 };
 
+// aligned 4-wide access to FP32 vectors (element 4*i4 .. 4*i4+3)
+__device__ __forceinline__ float4 ld4(const float* p, int i4) {
+  return reinterpret_cast<const float4*>(p)[i4];
+}
+__device__ __forceinline__ void st4(float* p, int i4, float4 v) { reinterpret_cast<float4*>(p)[i4] = v; }
+__device__ __forceinline__ float dot4(float4 a, float4 b) {
+  return a.x * b.x + a.y * b.y + a.z * b.z + a.w * b.w;
+}
+__device__ __forceinline__ float4 axpy4(float a, float4 x, float4 y) {  // a*x + y
+  return make_float4(fmaf(a, x.x, y.x), fmaf(a, x.y, y.y), fmaf(a, x.z, y.z), fmaf(a, x.w, y.w));
+}
+
 __device__ __forceinline__ unsigned long long globaltimer_ns() {
   unsigned long long t;
   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
@@ -51,6 +99,7 @@ __device__ __forceinline__ unsigned long long globaltimer_ns() {
 struct CtaTeam {
   int tid, nthr;
   double* red;  // shared scratch, >= (32 + 1) * MINIM_MAXRED doubles
+  double* wide; // shared scratch, >= (8 + 1) * MINIM_WIDE doubles
   static constexpr bool kGrid = false;
   __device__ __forceinline__ void sync() { __syncthreads(); }
   __device__ __forceinline__ bool ok() const { return true; }
@@ -77,6 +126,20 @@ struct CtaTeam {
     for (int k = 0; k < K; k++) v[k] = red[32 * MINIM_MAXRED + k];
     __syncthreads();
   }
+
+  __device__ __forceinline__ void wide_clear() { wide_clear_row(wide); }
+  __device__ __forceinline__ void wide_store32(float (&v)[32], int k0) { wide_store_row(v, k0, wide); }
+  // Combines the warps' rows: FP64 totals of values 0..K-1 in out (shared).
+  __device__ void wide_combine(int K, double* out) {
+    const int nw = (blockDim.x + 31) >> 5;
+    __syncthreads();
+    for (int k = threadIdx.x; k < K; k += blockDim.x) {
+      double s = 0.0;
+      for (int i = 0; i < nw; i++) s += wide[i * MINIM_WIDE + k];
+      out[k] = s;
+    }
+    __syncthreads();
+  }
 };
 
 // ---------------------------------------------------------------------------
@@ -85,10 +148,12 @@ struct CtaTeam {
 struct GridTeam {
   int tid, nthr;
   double* red;            // shared scratch as in CtaTeam
+  double* wide;           // shared scratch as in CtaTeam
   GridSyncState* bar;     // global
-  double* partials;       // global, 2 * gridDim.x * MINIM_MAXRED doubles
+  double* partials;       // global, 2 * gridDim.x * MINIM_WIDE + 2 * MINIM_WIDE doubles
   int buf;                // partials double buffer index
   int* s_ok;              // shared flag
+  int* s_last;            // shared flag: this block arrived last
   static constexpr bool kGrid = true;
   static constexpr unsigned long long kWaitLimitNs = 5000000000ull;  // 5 s
 
@@ -132,6 +197,65 @@ struct GridTeam {
     __syncthreads();
   }
 
+  // Reduction barrier: every block publishes its partial sums and arrives;
+  // the block that arrives last sums all partials (fixed order), publishes
+  // the totals and releases the others, which then read only K values.
+  // The wait is bounded as in sync().
+  __device__ void combine(int K, double* out) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    double* P = partials + (size_t)buf * gridDim.x * MINIM_WIDE;
+    double* Rz = partials + (size_t)2 * gridDim.x * MINIM_WIDE + (size_t)buf * MINIM_WIDE;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int okv = *s_ok;
+      int last = 0;
+      if (okv) {
+        volatile unsigned int* vgen = &bar->gen;
+        const unsigned int g = *vgen;
+        __threadfence();
+        const unsigned int arrived = atomicAdd(&bar->count, 1u);
+        if (arrived == gridDim.x - 1) {
+          last = 1;
+          __threadfence();
+        } else {
+          volatile int* verr = &bar->err;
+          unsigned long long t0 = globaltimer_ns();
+          while (*vgen == g) {
+            if (*verr) { okv = 0; break; }
+            if (globaltimer_ns() - t0 > kWaitLimitNs) {
+              atomicExch(&bar->err, 1);
+              okv = 0;
+              break;
+            }
+            __nanosleep(32);
+          }
+          __threadfence();
+        }
+      }
+      *s_ok = okv;
+      *s_last = last;
+    }
+    __syncthreads();
+    if (*s_last) {
+      for (int k = w; k < K; k += nw) {
+        double s = 0.0;
+        for (int b = lane; b < (int)gridDim.x; b += 32) s += __ldcg(&P[b * MINIM_WIDE + k]);
+        s = warp_sum(s);
+        if (lane == 0) Rz[k] = s;
+      }
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        atomicExch(&bar->count, 0u);
+        __threadfence();
+        atomicAdd(&bar->gen, 1u);
+      }
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < K; k += blockDim.x) out[k] = __ldcg(&Rz[k]);
+    __syncthreads();
+    buf ^= 1;
+  }
+
   template <int K>
   __device__ void reduce(double (&v)[K]) {
     static_assert(K <= MINIM_MAXRED, "too many values");
@@ -143,26 +267,30 @@ struct GridTeam {
       for (int k = 0; k < K; k++) red[w * MINIM_MAXRED + k] = v[k];
     }
     __syncthreads();
-    double* P = partials + (size_t)buf * gridDim.x * MINIM_MAXRED;
+    double* P = partials + (size_t)buf * gridDim.x * MINIM_WIDE;
     if (threadIdx.x < K) {
       double s = 0.0;
       for (int i = 0; i < nw; i++) s += red[i * MINIM_MAXRED + threadIdx.x];
-      P[blockIdx.x * MINIM_MAXRED + threadIdx.x] = s;
+      P[blockIdx.x * MINIM_WIDE + threadIdx.x] = s;
     }
-    sync();
-    if (w == 0) {
-      for (int k = 0; k < K; k++) {
-        double s = 0.0;
-        for (int b = lane; b < (int)gridDim.x; b += 32) s += __ldcg(&P[b * MINIM_MAXRED + k]);
-        s = warp_sum(s);
-        if (lane == 0) red[32 * MINIM_MAXRED + k] = s;
-      }
-    }
-    __syncthreads();
+    combine(K, red + 32 * MINIM_MAXRED);
 #pragma unroll
     for (int k = 0; k < K; k++) v[k] = red[32 * MINIM_MAXRED + k];
     __syncthreads();
-    buf ^= 1;
+  }
+
+  __device__ __forceinline__ void wide_clear() { wide_clear_row(wide); }
+  __device__ __forceinline__ void wide_store32(float (&v)[32], int k0) { wide_store_row(v, k0, wide); }
+  __device__ void wide_combine(int K, double* out) {
+    const int nw = (blockDim.x + 31) >> 5;
+    __syncthreads();
+    double* P = partials + (size_t)buf * gridDim.x * MINIM_WIDE;
+    for (int k = threadIdx.x; k < K; k += blockDim.x) {
+      double s = 0.0;
+      for (int i = 0; i < nw; i++) s += wide[i * MINIM_WIDE + k];
+      P[blockIdx.x * MINIM_WIDE + k] = s;
+    }
+    combine(K, out);
   }
 };
 

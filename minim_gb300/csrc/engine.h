@@ -113,6 +113,12 @@ struct MinScalars {
   double best_rms;
   double dt, a, dtmax, gnorm;  // Fire
   double rho[MINIM_MAXM], sigma[MINIM_MAXM], yy[MINIM_MAXM];
+  // compact L-BFGS: SY[a][b] = s_a.y_b (slot indices; the part with a older
+  // than or equal to b is used), YY[a][b] = y_a.y_b; column `pend` (the
+  // newest pair) is filled by the next direction's first pass
+  double SY[MINIM_MAXM][MINIM_MAXM], YY[MINIM_MAXM][MINIM_MAXM];
+  int pend;
+  int pad_;
   // work counters for the roofline: algorithmic HBM bytes of every vector
   // pass and evaluation, and Lennard-Jones pair interactions per precision
   double abytes, pairs32, pairs64;
@@ -133,8 +139,9 @@ struct InstDesc {
   float* X32[2];
   double* X64[2];
   float* G[2];
-  float* Sb;       // (m + 1) * ndof: ring of directions (s = sigma * S)
-  float* Yb;       // (m + 1) * ndof
+  int hstride;     // floats between history buffers (ndof rounded up to 64)
+  float* Sb;       // (m + 1) * hstride: ring of directions (s = sigma * S)
+  float* Yb;       // (m + 1) * hstride
   float* V;        // Fire velocity
   double* GA;      // FP64 gradient accumulator (BarAndHinge scatter), or NULL
   double* xres;    // resident FP64 coordinates: read at start, written at the end

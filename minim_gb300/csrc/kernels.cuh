@@ -15,9 +15,14 @@ namespace mg {
 
 struct SharedScalars {
   double red[(32 + 1) * MINIM_MAXRED];
+  double wide[8 * MINIM_WIDE];
+  double wout[MINIM_WIDE];
+  double SY[MINIM_MAXM * MINIM_MAXM], YY[MINIM_MAXM * MINIM_MAXM];
+  double coefS[MINIM_MAXM], coefY[MINIM_MAXM];
+  long long boff[2 * MINIM_MAXM];
   double rho[MINIM_MAXM], sig[MINIM_MAXM], yy[MINIM_MAXM], alpha[MINIM_MAXM];
   int sidx[MINIM_MAXM], yidx[MINIM_MAXM];
-  int next, ok;
+  int next, ok, last;
 };
 
 __device__ __forceinline__ void copy_desc(InstDesc* dst, const InstDesc* src) {
@@ -32,10 +37,12 @@ __device__ void setup_runner(Runner<Team, KIND>& R, SharedScalars& S, const Inst
   R.n = in.ndof;
   R.rho = S.rho; R.sig = S.sig; R.yy = S.yy; R.alpha = S.alpha;
   R.sidx = S.sidx; R.yidx = S.yidx;
+  R.SY = S.SY; R.YY = S.YY; R.wout = S.wout; R.coefS = S.coefS; R.coefY = S.coefY;
+  R.boff = S.boff;
 }
 
 template <int KIND>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 2)
 batch_kernel(const InstDesc* __restrict__ insts, int ninst, int* counter, int slice, int lj_tile) {
   __shared__ SharedScalars S;
   __shared__ __align__(16) InstDesc s_in;
@@ -47,7 +54,7 @@ batch_kernel(const InstDesc* __restrict__ insts, int ninst, int* counter, int sl
     if (k >= ninst) break;
     copy_desc(&s_in, &insts[k]);
     __syncthreads();
-    CtaTeam tm{(int)threadIdx.x, (int)blockDim.x, S.red};
+    CtaTeam tm{(int)threadIdx.x, (int)blockDim.x, S.red, S.wide};
     Runner<CtaTeam, KIND> R{tm, s_in, dyn, lj_tile};
     setup_runner(R, S, s_in);
     R.load(*s_in.st);
@@ -92,7 +99,7 @@ __device__ void constrain_op(Team& tm, const InstDesc& in, const EvalIO& io) {
 }
 
 template <int KIND>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 2)
 grid_kernel(const InstDesc* __restrict__ inst, int op, const EvalIO* io, int slice,
             GridSyncState* bar, double* partials, int lj_tile) {
   __shared__ SharedScalars S;
@@ -102,7 +109,7 @@ grid_kernel(const InstDesc* __restrict__ inst, int op, const EvalIO* io, int sli
   if (threadIdx.x == 0) S.ok = 1;
   __syncthreads();
   GridTeam tm{(int)(blockIdx.x * blockDim.x + threadIdx.x), (int)(gridDim.x * blockDim.x), S.red,
-              bar, partials, 0, &S.ok};
+              S.wide, bar, partials, 0, &S.ok, &S.last};
   Runner<GridTeam, KIND> R{tm, s_in, dyn, lj_tile};
   setup_runner(R, S, s_in);
   if (op == OP_MINIMISE) {

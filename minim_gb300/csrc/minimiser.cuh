@@ -16,9 +16,11 @@
 //     reference scales the step by tau = 0.5, which is exact in binary;
 //   * the energy at the current point is carried from the last evaluation
 //     instead of being recomputed at the start of each line search;
-//   * precision MIXED runs FP32 coordinates until converged or stalled, then
-//     continues from the same point with FP64 coordinates (the L-BFGS history
-//     and the FIRE velocity carry over); the final convergence test is FP64.
+//   * the L-BFGS direction uses the compact representation (same direction);
+//   * precision MIXED runs FP32 coordinates while FP32 can make progress,
+//     FP64 coordinates near convergence; the final convergence test is FP64.
+// Vector passes move 4 floats per access (float4): every FP32 vector starts
+// on a 16-byte boundary (history buffers are strided by a multiple of 64).
 #pragma once
 #include "potentials.cuh"
 
@@ -45,6 +47,25 @@ struct FusedEmit {
       yy.add(y * y);
     }
   }
+  // four consecutive DOFs 4*i4 .. 4*i4+3 (16-byte aligned)
+  __device__ __forceinline__ void emit4(int i4, float4 g) {
+    if (fixed) {
+      const int i = 4 * i4;
+      if (fixed[i]) g.x = 0.f;
+      if (fixed[i + 1]) g.y = 0.f;
+      if (fixed[i + 2]) g.z = 0.f;
+      if (fixed[i + 3]) g.w = 0.f;
+    }
+    st4(G, i4, g);
+    gg.add(dot4(g, g));
+    if (Y) {
+      const float4 go = ld4(Gold, i4);
+      const float4 y = make_float4(g.x - go.x, g.y - go.y, g.z - go.z, g.w - go.w);
+      st4(Y, i4, y);
+      py.add(dot4(ld4(P, i4), y));
+      yy.add(dot4(y, y));
+    }
+  }
 };
 
 // FP64 output (API evaluation)
@@ -65,15 +86,18 @@ struct Runner {
   int lj_tile;
   // uniform scalars (every thread holds identical copies)
   int n, status, initd, iter, ii, stage, xi, gi, evals, fp64_iters, stall, nsteps, pbuf, ybuf;
-  int exhausted_run, switch_reason;
+  int exhausted_run, switch_reason, pend;
   double E, gg, best_rms, dt, a, dtmax, gnorm;
   double abytes, pairs32, pairs64;
   // shared arrays (one copy per block; written by thread 0 between barriers)
   double *rho, *sig, *yy, *alpha;
   int *sidx, *yidx;
+  double *SY, *YY, *wout, *coefS, *coefY;  // m x m matrices, reduction out, pass coefficients
+  long long* boff;                         // history buffer offsets of the slots in order
 
-  __device__ float* Sbuf(int b) const { return in.Sb + (size_t)b * n; }
-  __device__ float* Ybuf(int b) const { return in.Yb + (size_t)b * n; }
+  __device__ float* Sbuf(int b) const { return in.Sb + (size_t)b * in.hstride; }
+  __device__ float* Ybuf(int b) const { return in.Yb + (size_t)b * in.hstride; }
+  __device__ int n4() const { return n >> 2; }
   __device__ bool has_constraints() const {
     if constexpr (KIND == K_PF)
       return in.fixed != nullptr || (in.pf.flags & (PF_FIXFLUID | PF_HARD | PF_VOLUME));
@@ -105,6 +129,7 @@ struct Runner {
     } else if constexpr (KIND == K_PF) {
       return pf_eval<T>(tm, in.pf, cv, xw, &em, want_e, want_g);
     } else if constexpr (KIND == K_PF1) {
+      if ((in.pf.n[2] & 3) == 0) return pf1_eval_quad<T>(tm, in.pf, cv, xw, &em, want_e, want_g);
       return pf1_eval<T>(tm, in.pf, cv, xw, &em, want_e, want_g);
     } else {
       return bah_eval<T>(tm, in.bah, cv, xw, in.GA, &em, want_e, want_g);
@@ -177,6 +202,17 @@ struct Runner {
     return v[0];
   }
 
+  // g . P over the team
+  __device__ double dot_gP(const float* P) {
+    const float* G = in.G[gi];
+    Acc d;
+    for (int i = tm.tid; i < n4(); i += tm.nthr) d.add(dot4(ld4(G, i), ld4(P, i)));
+    for (int i = 4 * n4() + tm.tid; i < n; i += tm.nthr) d.add(G[i] * P[i]);
+    double v[1] = {d.total()};
+    tm.reduce(v);
+    return v[0];
+  }
+
   // State::applyConstraints on the direction P, then returns g.P
   __device__ double constrain_dir(float* P) {
     if (in.fixed) {
@@ -194,12 +230,7 @@ struct Runner {
       }
     }
     tm.sync();
-    const float* G = in.G[gi];
-    Acc d;
-    for (int i = tm.tid; i < n; i += tm.nthr) d.add(G[i] * P[i]);
-    double v[1] = {d.total()};
-    tm.reduce(v);
-    return v[0];
+    return dot_gP(P);
   }
 
   // backtrackingLinesearch: the step is t0 * P with g.step = gs <= 0.
@@ -222,16 +253,28 @@ struct Runner {
   }
 
   // ---- L-BFGS ---------------------------------------------------------------------
-  // Fused two-loop recursion (Lbfgs::getDirection): each pass finishes the
-  // previous axpy and computes the next dot product, so a direction costs
-  // 2*min(m,i)+1 passes and as many reductions.  Writes P = Sbuf(pbuf) and
-  // returns the scale folded into the step (initStep/|g| or maxStep cap).
+  // Direction -H g of Lbfgs::getDirection in the compact representation of
+  // Byrd, Nocedal & Schnabel (1994): with the stored pairs in order oldest ->
+  // newest, R = upper triangle of S^T Y, D its diagonal and
+  // gamma = s_n.y_n / y_n.y_n,
+  //   H g = gamma g + S w - gamma Y u,   R u = S^T g,
+  //   R^T w = (D + gamma Y^T Y) u - gamma Y^T g,
+  // which equals the two-loop recursion's result for any pairs with s.y != 0
+  // (including s.y < 0, which the reference keeps).  Two passes over the
+  // history and two team reductions, instead of 2 min(m,i) + 1.  The new
+  // pair's column of S^T Y and Y^T Y is computed in the first pass.
+  // Writes P = Sbuf(pbuf); returns the scale folded into the step
+  // (initStep/|g| on the first iteration, or the maxStep cap).
   __device__ double lbfgs_direction(double& gp) {
     float* P = Sbuf(pbuf);
     const float* G = in.G[gi];
     const int m = in.mp.m;
     if (ii == 0) {
-      for (int i = tm.tid; i < n; i += tm.nthr) P[i] = -G[i];
+      for (int i = tm.tid; i < n4(); i += tm.nthr) {
+        const float4 g = ld4(G, i);
+        st4(P, i, make_float4(-g.x, -g.y, -g.z, -g.w));
+      }
+      for (int i = 4 * n4() + tm.tid; i < n; i += tm.nthr) P[i] = -G[i];
       tm.sync();
       abytes += 8.0 * n;
       const double gn = sqrt(gg);
@@ -241,76 +284,134 @@ struct Runner {
     }
     const int mt = ii < m ? ii : m;
     const int c = ii % m;
-    abytes += (4.0 * mt + 2.0) * 4.0 * n;  // each history vector read twice, g read, p written
-    double coef = 0.0;
-    const float* ysrc = nullptr;
-    // first loop: newest to oldest
-    for (int j = 0; j < mt; j++) {
-      const int k = (c - 1 - j + m) % m;
-      const float* S = Sbuf(sidx[k]);
-      const float fc = (float)coef;
-      Acc d;
-      for (int i = tm.tid; i < n; i += tm.nthr) {
-        const float q = (j == 0) ? -G[i] : P[i] - fc * ysrc[i];
-        P[i] = q;
-        d.add(q * S[i]);
+    const int kn = (c - 1 + m) % m;  // newest slot
+    const long long hs = in.hstride;
+    abytes += (4.0 * mt + 2.0) * 4.0 * n;
+    // pass A, 8 slots per sweep: S_k.g, Y_k.g and, for a new pair,
+    // S_k.y_new, Y_k.y_new; value index = dot * 16 + slot order
+    const bool np = pend >= 0;
+    const float* Yn = np ? Ybuf(yidx[pend]) : nullptr;
+    tm.wide_clear();
+    for (int k0 = 0; k0 < mt; k0 += 8) {
+      const float* Sp[8];
+      const float* Yp[8];
+#pragma unroll
+      for (int j = 0; j < 8; j++) {
+        const int k = k0 + j;
+        const int s = (c - mt + k + 2 * m) % m;
+        Sp[j] = in.Sb + ((k < mt) ? sidx[s] : 0) * hs;
+        Yp[j] = in.Yb + ((k < mt) ? yidx[s] : 0) * hs;
       }
-      double v[1] = {d.total()};
-      tm.reduce(v);
-      const double al = rho[k] * sig[k] * v[0];
-      if (threadIdx.x == 0) alpha[k] = al;
-      coef = al;
-      ysrc = Ybuf(yidx[k]);
-    }
-    const int kn = (c - 1 + m) % m;
-    const double gamma = 1.0 / (rho[kn] * yy[kn]);
-    // second loop: oldest to newest
-    double beta = 0.0;
-    for (int j = 0; j <= mt; j++) {
-      const float* Yn = (j < mt) ? Ybuf(yidx[(c - mt + j + m) % m]) : nullptr;
-      Acc d1, d2;
-      if (j == 0) {
-        const float fc = (float)coef, fg = (float)gamma;
-        for (int i = tm.tid; i < n; i += tm.nthr) {
-          const float q = (P[i] - fc * ysrc[i]) * fg;
-          P[i] = q;
-          d1.add(q * Yn[i]);
-        }
-      } else {
-        const int kp = (c - mt + j - 1 + m) % m;
-        const float* Sp = Sbuf(sidx[kp]);
-        const float fc = (float)((alpha[kp] - beta) * sig[kp]);
-        if (Yn) {
-          for (int i = tm.tid; i < n; i += tm.nthr) {
-            const float q = P[i] + fc * Sp[i];
-            P[i] = q;
-            d1.add(q * Yn[i]);
-          }
-        } else {
-          for (int i = tm.tid; i < n; i += tm.nthr) {
-            const float q = P[i] + fc * Sp[i];
-            P[i] = q;
-            d1.add(q * G[i]);
-            d2.add(q * q);
+      float acc[32];
+#pragma unroll
+      for (int k = 0; k < 32; k++) acc[k] = 0.f;
+      for (int i = tm.tid; i < n4(); i += tm.nthr) {
+        const float4 g = ld4(G, i);
+        const float4 yn = np ? ld4(Yn, i) : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+          if (k0 + j < mt) {
+            const float4 s = ld4(Sp[j], i);
+            const float4 y = ld4(Yp[j], i);
+            acc[j] += dot4(s, g);
+            acc[8 + j] += dot4(y, g);
+            acc[16 + j] += dot4(s, yn);
+            acc[24 + j] += dot4(y, yn);
           }
         }
       }
-      double v[2] = {d1.total(), d2.total()};
-      tm.reduce(v);
-      if (Yn) {
-        beta = rho[(c - mt + j + m) % m] * v[0];
-      } else {
-        gp = v[0];
-        double scale = 1.0;
-        if (in.mp.max_step != 0) {
-          const double ss = sqrt(v[1]);
-          if (ss > in.mp.max_step) scale = in.mp.max_step / ss;
+      for (int i = 4 * n4() + tm.tid; i < n; i += tm.nthr) {
+        const float g = G[i];
+        const float yn = np ? Yn[i] : 0.f;
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+          if (k0 + j < mt) {
+            const float s = Sp[j][i], y = Yp[j][i];
+            acc[j] += s * g;
+            acc[8 + j] += y * g;
+            acc[16 + j] += s * yn;
+            acc[24 + j] += y * yn;
+          }
         }
-        gp *= scale;
-        return scale;
       }
+      tm.wide_store32(acc, k0);
     }
-    return 1.0;  // not reached
+    tm.wide_combine(4 * MINIM_MAXM, wout);
+    // small dense algebra in one thread per block (bitwise the same in all)
+    if (threadIdx.x == 0) {
+      double sg[MINIM_MAXM], yg[MINIM_MAXM], u[MINIM_MAXM], w[MINIM_MAXM];
+      int sl[MINIM_MAXM];
+      for (int k = 0; k < mt; k++) {
+        sl[k] = (c - mt + k + 2 * m) % m;
+        sg[k] = sig[sl[k]] * wout[k];
+        yg[k] = wout[MINIM_MAXM + k];
+      }
+      if (np) {
+        for (int k = 0; k < mt; k++) {
+          SY[sl[k] * MINIM_MAXM + pend] = sig[sl[k]] * wout[2 * MINIM_MAXM + k];
+          YY[sl[k] * MINIM_MAXM + pend] = wout[3 * MINIM_MAXM + k];
+          YY[pend * MINIM_MAXM + sl[k]] = wout[3 * MINIM_MAXM + k];
+        }
+      }
+      const double gamma = SY[kn * MINIM_MAXM + kn] / YY[kn * MINIM_MAXM + kn];
+      for (int a = mt - 1; a >= 0; a--) {  // R u = S^T g
+        double t = sg[a];
+        for (int b = a + 1; b < mt; b++) t -= SY[sl[a] * MINIM_MAXM + sl[b]] * u[b];
+        u[a] = t / SY[sl[a] * MINIM_MAXM + sl[a]];
+      }
+      for (int a = 0; a < mt; a++) {  // R^T w = (D + gamma Y^T Y) u - gamma Y^T g
+        double t = SY[sl[a] * MINIM_MAXM + sl[a]] * u[a] - gamma * yg[a];
+        for (int b = 0; b < mt; b++) t += gamma * YY[sl[a] * MINIM_MAXM + sl[b]] * u[b];
+        for (int b = 0; b < a; b++) t -= SY[sl[b] * MINIM_MAXM + sl[a]] * w[b];
+        w[a] = t / SY[sl[a] * MINIM_MAXM + sl[a]];
+      }
+      for (int k = 0; k < MINIM_MAXM; k++) {
+        coefS[k] = (k < mt) ? -w[k] * sig[sl[k]] : 0.0;
+        coefY[k] = (k < mt) ? gamma * u[k] : 0.0;
+        boff[k] = (k < mt) ? (long long)sidx[sl[k]] * hs : 0;
+        boff[MINIM_MAXM + k] = (k < mt) ? (long long)yidx[sl[k]] * hs : 0;
+      }
+      wout[MINIM_WIDE - 1] = gamma;
+    }
+    __syncthreads();
+    pend = -1;
+    const float fg = (float)(-wout[MINIM_WIDE - 1]);
+    // pass B: P = -(gamma g + S w - gamma Y u), with g.P and P.P; the slot
+    // buffers and coefficients are read from shared memory (broadcast)
+    Acc d1, d2;
+    for (int i = tm.tid; i < n4(); i += tm.nthr) {
+      const float4 g = ld4(G, i);
+      float4 q = make_float4(fg * g.x, fg * g.y, fg * g.z, fg * g.w);
+#pragma unroll 4
+      for (int k = 0; k < mt; k++) {
+        q = axpy4((float)coefS[k], ld4(in.Sb + boff[k], i), q);
+        q = axpy4((float)coefY[k], ld4(in.Yb + boff[MINIM_MAXM + k], i), q);
+      }
+      st4(P, i, q);
+      d1.add(dot4(q, g));
+      d2.add(dot4(q, q));
+    }
+    for (int i = 4 * n4() + tm.tid; i < n; i += tm.nthr) {
+      const float g = G[i];
+      float q = fg * g;
+      for (int k = 0; k < mt; k++) {
+        q += (float)coefS[k] * in.Sb[boff[k] + i];
+        q += (float)coefY[k] * in.Yb[boff[MINIM_MAXM + k] + i];
+      }
+      P[i] = q;
+      d1.add(q * g);
+      d2.add(q * q);
+    }
+    double v[2] = {d1.total(), d2.total()};
+    tm.reduce(v);
+    gp = v[0];
+    double scale = 1.0;
+    if (in.mp.max_step != 0) {
+      const double ss = sqrt(v[1]);
+      if (ss > in.mp.max_step) scale = in.mp.max_step / ss;
+    }
+    gp *= scale;
+    return scale;
   }
 
   __device__ void lbfgs_iteration(bool& exhausted) {
@@ -333,7 +434,7 @@ struct Runner {
     if (!tm.ok()) return;
     grad_eval(t, P, true, true, py, yyv);
     const double sy = t * py;
-    if (sy != 0) {
+    if (sy != 0 && isfinite(sy)) {
       const int m = in.mp.m;
       const int c = ii % m;
       const int os = sidx[c], oy = yidx[c];
@@ -343,6 +444,7 @@ struct Runner {
         rho[c] = 1.0 / sy; sig[c] = t; yy[c] = yyv;
       }
       pbuf = os; ybuf = oy;
+      pend = c;
       __syncthreads();
     } else {
       ii--;
@@ -363,7 +465,12 @@ struct Runner {
     const float* G = in.G[gi];
     float* Vv = in.V;
     Acc d1, d2;
-    for (int i = tm.tid; i < n; i += tm.nthr) {
+    for (int i = tm.tid; i < n4(); i += tm.nthr) {
+      const float4 v = ld4(Vv, i);
+      d1.add(dot4(v, ld4(G, i)));
+      d2.add(dot4(v, v));
+    }
+    for (int i = 4 * n4() + tm.tid; i < n; i += tm.nthr) {
       const float v = Vv[i];
       d1.add(v * G[i]);
       d2.add(v * v);
@@ -393,9 +500,23 @@ struct Runner {
     }
     float* P = Sbuf(0);
     const float f1 = (float)c1, f2 = (float)c2, fdt = (float)dt;
+    const bool mix = p > 0;
     Acc dg;
-    for (int i = tm.tid; i < n; i += tm.nthr) {
-      const float v = (p > 0) ? f1 * Vv[i] - f2 * G[i] : -f2 * G[i];
+    for (int i = tm.tid; i < n4(); i += tm.nthr) {
+      const float4 g = ld4(G, i);
+      const float4 vo = ld4(Vv, i);
+      float4 v;
+      v.x = mix ? f1 * vo.x - f2 * g.x : -f2 * g.x;
+      v.y = mix ? f1 * vo.y - f2 * g.y : -f2 * g.y;
+      v.z = mix ? f1 * vo.z - f2 * g.z : -f2 * g.z;
+      v.w = mix ? f1 * vo.w - f2 * g.w : -f2 * g.w;
+      st4(Vv, i, v);
+      const float4 s = make_float4(fdt * v.x, fdt * v.y, fdt * v.z, fdt * v.w);
+      st4(P, i, s);
+      dg.add(dot4(g, s));
+    }
+    for (int i = 4 * n4() + tm.tid; i < n; i += tm.nthr) {
+      const float v = mix ? f1 * Vv[i] - f2 * G[i] : -f2 * G[i];
       Vv[i] = v;
       const float s = fdt * v;
       P[i] = s;
@@ -429,14 +550,12 @@ struct Runner {
     if (!tm.ok()) return;
     // x += t * g (materialise the accepted point)
     if (stage == 0) {
-      const float* X = in.X32[xi];
+      CView<float> cv{in.X32[xi], G, (float)t};
       float* Xn = in.X32[1 - xi];
-      CView<float> cv{X, G, (float)t};
       for (int i = tm.tid; i < n; i += tm.nthr) Xn[i] = cv(i);
     } else {
-      const double* X = in.X64[xi];
+      CView<double> cv{in.X64[xi], G, t};
       double* Xn = in.X64[1 - xi];
-      CView<double> cv{X, G, t};
       for (int i = tm.tid; i < n; i += tm.nthr) Xn[i] = cv(i);
     }
     xi = 1 - xi;
@@ -444,7 +563,7 @@ struct Runner {
     abytes += (2.0 * xbytes() + 4.0) * n;
   }
 
-  // ---- precision switch -------------------------------------------------------------
+  // ---- precision stages -------------------------------------------------------------
   __device__ void to_fp64() {
     const float* X = in.X32[xi];
     double* X64 = in.X64[xi];
@@ -453,17 +572,36 @@ struct Runner {
     abytes += 12.0 * n;
     stage = 1;
   }
+  __device__ void to_fp32() {
+    const double* X64 = in.X64[xi];
+    float* X = in.X32[xi];
+    for (int i = tm.tid; i < n; i += tm.nthr) X[i] = (float)X64[i];
+    tm.sync();
+    abytes += 12.0 * n;
+    stage = 0;
+  }
+  // the current gradient (and energy) again at the current point, in the
+  // current precision
+  __device__ void reeval() {
+    double py, yyv;
+    grad_eval(0.0, nullptr, false, false, py, yyv);
+    if (in.mp.method == 1) gnorm = sqrt(gg);
+  }
 
   __device__ double rms() const { return sqrt(gg / n); }
 
   // ---- driver -------------------------------------------------------------------------
   __device__ void load(const MinScalars& s) {
-    status = s.status; initd = s.initialised; iter = s.iter; ii = s.ii; stage = s.stage; xi = s.xi; gi = s.gi;
-    evals = s.evals; fp64_iters = s.fp64_iters; stall = s.stall; nsteps = s.nsteps;
-    pbuf = s.pbuf; ybuf = s.ybuf; E = s.E;
-    exhausted_run = s.exhausted_run; switch_reason = s.switch_reason; gg = s.gg; best_rms = s.best_rms;
+    status = s.status; initd = s.initialised; iter = s.iter; ii = s.ii; stage = s.stage;
+    xi = s.xi; gi = s.gi; evals = s.evals; fp64_iters = s.fp64_iters; stall = s.stall;
+    nsteps = s.nsteps; pbuf = s.pbuf; ybuf = s.ybuf; E = s.E; gg = s.gg; best_rms = s.best_rms;
+    exhausted_run = s.exhausted_run; switch_reason = s.switch_reason; pend = s.pend;
     dt = s.dt; a = s.a; dtmax = s.dtmax; gnorm = s.gnorm;
     abytes = s.abytes; pairs32 = s.pairs32; pairs64 = s.pairs64;
+    for (int k = threadIdx.x; k < MINIM_MAXM * MINIM_MAXM; k += blockDim.x) {
+      SY[k] = (&s.SY[0][0])[k];
+      YY[k] = (&s.YY[0][0])[k];
+    }
     for (int k = threadIdx.x; k < MINIM_MAXM; k += blockDim.x) {
       rho[k] = s.rho[k]; sig[k] = s.sigma[k]; yy[k] = s.yy[k];
       sidx[k] = s.sidx[k]; yidx[k] = s.yidx[k]; alpha[k] = 0.0;
@@ -476,10 +614,14 @@ struct Runner {
     if (tm.block0() && threadIdx.x == 0) {
       s.status = status; s.iter = iter; s.ii = ii; s.stage = stage; s.xi = xi; s.gi = gi;
       s.evals = evals; s.fp64_iters = fp64_iters; s.stall = stall; s.nsteps = nsteps;
-      s.pbuf = pbuf; s.ybuf = ybuf; s.E = E;
-      s.exhausted_run = exhausted_run; s.switch_reason = switch_reason; s.gg = gg; s.best_rms = best_rms;
+      s.pbuf = pbuf; s.ybuf = ybuf; s.E = E; s.gg = gg; s.best_rms = best_rms;
+      s.exhausted_run = exhausted_run; s.switch_reason = switch_reason; s.pend = pend;
       s.dt = dt; s.a = a; s.dtmax = dtmax; s.gnorm = gnorm; s.initialised = 1;
       s.abytes = abytes; s.pairs32 = pairs32; s.pairs64 = pairs64;
+      for (int k = 0; k < MINIM_MAXM * MINIM_MAXM; k++) {
+        (&s.SY[0][0])[k] = SY[k];
+        (&s.YY[0][0])[k] = YY[k];
+      }
       for (int k = 0; k < MINIM_MAXM; k++) {
         s.rho[k] = rho[k]; s.sigma[k] = sig[k]; s.yy[k] = yy[k];
         s.sidx[k] = sidx[k]; s.yidx[k] = yidx[k];
@@ -494,8 +636,7 @@ struct Runner {
     if (status != ST_RUNNING) return;
     const bool mixed = (mp.precision == 0);
     if (!initd) {
-      // Minimiser::init.  In FP64 mode the host has written the exact input
-      // to X64[0], so the FP64 stage starts from it directly.
+      // Minimiser::init; the coordinates come from the resident FP64 copy
       initd = 1;
       {
         const double* xr = in.xres;
@@ -518,6 +659,7 @@ struct Runner {
             rho[k] = 0; sig[k] = 0; yy[k] = 0; sidx[k] = k; yidx[k] = k;
           }
         pbuf = mp.m; ybuf = mp.m;
+        pend = -1;
         __syncthreads();
       } else if (mp.method == 1) {
         for (int i = tm.tid; i < n; i += tm.nthr) in.V[i] = 0.f;
@@ -533,6 +675,7 @@ struct Runner {
       }
       best_rms = 1e300;
       stall = 0;
+      exhausted_run = 0;
     }
     for (int s = 0; s < slice; s++) {
       if (iter > mp.max_iter) { status = ST_MAXITER; break; }
@@ -542,31 +685,54 @@ struct Runner {
       else gd_iteration(exhausted);
       if (!tm.ok()) { status = ST_TIMEOUT; break; }
       if (stage == 1) fp64_iters++;
-      if (!isfinite(E) || !isfinite(gg)) { status = ST_NAN; break; }
+      if (!isfinite(E) || !isfinite(gg)) {
+        // FP32 overflows where FP64 does not (e.g. Lennard-Jones pairs at
+        // very short range): evaluate the same point in FP64 before giving up
+        if (stage == 0 && mixed) {
+          switch_reason = 4;
+          to_fp64();
+          reeval();
+        }
+        if (!isfinite(E) || !isfinite(gg)) { status = ST_NAN; break; }
+      }
       const double r = rms();
       bool conv = r < mp.tol;
-      if (stage == 0 && mixed) {
-        // Leave the FP32 stage when FP32 has done what it can: converged in
-        // FP32; the line search found no Armijo point twice in a row (the
-        // FP32 energy no longer resolves the decrease); or the RMS gradient
-        // has not improved by 0.1% for 100 iterations while within 100x of
-        // the tolerance (the FP32 gradient floor).  A run that stalls far
-        // from the tolerance is not limited by precision and stays in FP32.
-        if (r < 0.999 * best_rms) { best_rms = r; stall = 0; }
-        else stall++;
-        exhausted_run = exhausted ? exhausted_run + 1 : 0;
-        int why = conv ? 1 : (exhausted_run >= 2 ? 2 : ((stall >= 100 && r < 100.0 * mp.tol) ? 3 : 0));
-        if (why) {
-          switch_reason = why;
-          to_fp64();
-          if (mp.method != 2) {
-            double py, yyv;
-            grad_eval(0.0, nullptr, false, false, py, yyv);
-            if (mp.method == 1) gnorm = sqrt(gg);
-            conv = rms() < mp.tol;
-          } else {
-            conv = false;  // the next iteration's FP64 gradient decides
+      if (mixed) {
+        if (stage == 0) {
+          // Leave the FP32 stage when FP32 has done what it can: converged in
+          // FP32; the line search keeps failing to find an Armijo point (the
+          // FP32 energy no longer resolves the decrease: failures accumulate
+          // in a decaying score, or one failure within 1000x of tol); or the
+          // RMS gradient has not improved by 0.1% for 100 iterations within
+          // 100x of the tolerance (the FP32 gradient floor).
+          if (r < 0.999 * best_rms) { best_rms = r; stall = 0; }
+          else stall++;
+          exhausted_run = exhausted_run * 7 / 8 + (exhausted ? 8 : 0);
+          const int why = conv ? 1
+                        : ((exhausted_run >= 20 || (exhausted && r < 1000.0 * mp.tol)) ? 2
+                        : ((stall >= 100 && r < 100.0 * mp.tol) ? 3 : 0));
+          if (why) {
+            switch_reason = why;
+            to_fp64();
+            if (mp.method != 2) {
+              reeval();
+              conv = rms() < mp.tol;
+            } else {
+              conv = false;  // the next iteration's FP64 gradient decides
+            }
+            best_rms = rms();
+            stall = 0;
+            exhausted_run = 0;
           }
+        } else if (r > 1e4 * mp.tol && r > 100.0 * best_rms) {
+          // an FP64 run that has moved far from convergence (FIRE restarts,
+          // a basin change) continues in FP32 until it approaches again
+          to_fp32();
+          reeval();
+          best_rms = rms();
+          stall = 0;
+          exhausted_run = 0;
+          conv = false;
         }
       }
       if (conv) { status = ST_CONVERGED; break; }

@@ -336,6 +336,128 @@ __device__ __noinline__ double pf_eval(Team& tm, const PotPF& P, CView<T> cv, T*
   return e.total();
 }
 
+// Four consecutive values of a coordinate view (aligned: element 4*i4).
+template <typename T> struct Quad { T v[4]; };
+__device__ __forceinline__ Quad<float> cv4(const CView<float>& cv, int i4) {
+  const float4 x = ld4(cv.x, i4);
+  Quad<float> q{{x.x, x.y, x.z, x.w}};
+  if (cv.p) {
+    const float4 p = ld4(cv.p, i4);
+    q.v[0] = __fadd_rn(x.x, __fmul_rn(cv.t, p.x));
+    q.v[1] = __fadd_rn(x.y, __fmul_rn(cv.t, p.y));
+    q.v[2] = __fadd_rn(x.z, __fmul_rn(cv.t, p.z));
+    q.v[3] = __fadd_rn(x.w, __fmul_rn(cv.t, p.w));
+  }
+  return q;
+}
+__device__ __forceinline__ Quad<double> cv4(const CView<double>& cv, int i4) {
+  const double2 a = reinterpret_cast<const double2*>(cv.x)[2 * i4];
+  const double2 b = reinterpret_cast<const double2*>(cv.x)[2 * i4 + 1];
+  Quad<double> q{{a.x, a.y, b.x, b.y}};
+  if (cv.p) {
+    const float4 p = ld4(cv.p, i4);
+    q.v[0] = __dadd_rn(a.x, __dmul_rn(cv.t, (double)p.x));
+    q.v[1] = __dadd_rn(a.y, __dmul_rn(cv.t, (double)p.y));
+    q.v[2] = __dadd_rn(b.x, __dmul_rn(cv.t, (double)p.z));
+    q.v[3] = __dadd_rn(b.y, __dmul_rn(cv.t, (double)p.w));
+  }
+  return q;
+}
+__device__ __forceinline__ void st_quad(float* x, int i4, const Quad<float>& q) {
+  st4(x, i4, make_float4(q.v[0], q.v[1], q.v[2], q.v[3]));
+}
+__device__ __forceinline__ void st_quad(double* x, int i4, const Quad<double>& q) {
+  reinterpret_cast<double2*>(x)[2 * i4] = make_double2(q.v[0], q.v[1]);
+  reinterpret_cast<double2*>(x)[2 * i4 + 1] = make_double2(q.v[2], q.v[3]);
+}
+// hand four gradient values to an emitter (vector store when it has one)
+template <class Emit, typename T>
+__device__ __forceinline__ void emit_quad(Emit& em, int i4, const T (&g)[4]) {
+  if constexpr (requires { em.emit4(i4, float4{}); }) {
+    em.emit4(i4, make_float4((float)g[0], (float)g[1], (float)g[2], (float)g[3]));
+  } else {
+#pragma unroll
+    for (int k = 0; k < 4; k++) em(4 * i4 + k, g[k]);
+  }
+}
+
+// Binary fluid on a grid whose innermost size is a multiple of 4: each thread
+// evaluates four consecutive cells along z with 16-byte loads of the cell and
+// of its x and y neighbour lines, plus two scalar loads for the z ends.
+template <typename T, class Team, class Emit>
+__device__ __noinline__ double pf1_eval_quad(Team& tm, const PotPF& P, CView<T> cv, T* xw, Emit* emp,
+                                             bool want_e, bool want_g) {
+  Emit emit = *emp;
+  const int nx = P.n[0], ny = P.n[1], nz = P.n[2];
+  const int nq = P.ngrid >> 2;
+  const T V = (T)P.vol_of_type[1];
+  const T fb = (T)P.kappa[0] / 16 * V;
+  const T Fi = (T)0.25 / (T)P.res2 * (T)P.kappaP[0] * V;
+  const T pr = (P.flags & PF_PRESSURE) ? (T)P.pressure[0] : (T)0;
+  const bool dx_on = nx > 1, dy_on = ny > 1;
+  EAcc<T> e;
+  for (int q = tm.tid; q < nq; q += tm.nthr) {
+    const int iG = 4 * q;
+    const int z0 = iG % nz, line = iG / nz;
+    const int y = line % ny, x = line / ny;
+    const Quad<T> c = cv4(cv, q);
+    if (xw) st_quad(xw, q, c);
+    T lap[4], eg[4];
+    {  // z: neighbours inside the quad, plus one scalar at each end
+      const T zm = cv(z0 == 0 ? iG + nz - 1 : iG - 1);
+      const T zp = cv(z0 + 4 == nz ? iG - z0 : iG + 4);
+#pragma unroll
+      for (int k = 0; k < 4; k++) {
+        const T cm = (k == 0) ? zm : c.v[k - 1];
+        const T cp = (k == 3) ? zp : c.v[k + 1];
+        const T gm = c.v[k] - cm, gp = c.v[k] - cp;
+        lap[k] = gm + gp;
+        eg[k] = (T)0.5 * (gm * gm + gp * gp);
+      }
+    }
+    if (dy_on) {
+      const int qm = ((x * ny + (y == 0 ? ny - 1 : y - 1)) * nz + z0) >> 2;
+      const int qp = ((x * ny + (y == ny - 1 ? 0 : y + 1)) * nz + z0) >> 2;
+      const Quad<T> cm = cv4(cv, qm), cp = cv4(cv, qp);
+#pragma unroll
+      for (int k = 0; k < 4; k++) {
+        const T gm = c.v[k] - cm.v[k], gp = c.v[k] - cp.v[k];
+        lap[k] += gm + gp;
+        eg[k] += (T)0.5 * (gm * gm + gp * gp);
+      }
+    }
+    if (dx_on) {
+      const int qm = (((x == 0 ? nx - 1 : x - 1) * ny + y) * nz + z0) >> 2;
+      const int qp = (((x == nx - 1 ? 0 : x + 1) * ny + y) * nz + z0) >> 2;
+      const Quad<T> cm = cv4(cv, qm), cp = cv4(cv, qp);
+#pragma unroll
+      for (int k = 0; k < 4; k++) {
+        const T gm = c.v[k] - cm.v[k], gp = c.v[k] - cp.v[k];
+        lap[k] += gm + gp;
+        eg[k] += (T)0.5 * (gm * gm + gp * gp);
+      }
+    }
+    T g[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      const T cc = c.v[k];
+      const T a = (cc + 1) * (cc - 1);
+      g[k] = fb * 4 * cc * (cc * cc - 1) + 2 * Fi * lap[k];
+      if (want_e) {
+        e.add(fb * a * a);
+        e.add(Fi * eg[k]);
+      }
+      if (pr != 0) {
+        if (want_e) e.add(-pr * ((T)0.5 * (cc + 1) * V));
+        g[k] -= (T)0.5 * pr * V;
+      }
+    }
+    if (want_g) emit_quad(emit, q, g);
+  }
+  *emp = emit;
+  return e.total();
+}
+
 // Binary fluid (nFluid == 1) without solid, contact angle, force or
 // confinement: the 7-point stencil of the bulk and gradient terms plus the
 // optional pressure term.  Same arithmetic as pf_eval for this case.

@@ -92,7 +92,11 @@ def test_bah_hinge_minima(target, expected, path):
     x0 = np.array([-1, 0, 1, 0, -s2, 0, 0, s2, 0, 1, 0, 1.0])
     p = abi.bar_and_hinge(triangulation=[[0, 1, 2], [1, 3, 2]], rigidity=(100, 1), theta0=[target])
     inst = runtime.Instance(p, x0)
-    mp = abi.minimiser("lbfgs")
+    # The two folded targets sit on the knife edge of the reference's
+    # dihedral wrap (theta jumps between 0 and 2*pi where n1.b3 changes
+    # sign); following the reference's path onto the same side of the fold
+    # needs FP64 coordinates throughout.
+    mp = abi.minimiser("lbfgs", precision="fp64")
     if path == "grid":
         r = inst.minimise(mp)
     else:
@@ -101,6 +105,20 @@ def test_bah_hinge_minima(target, expected, path):
         r = b.run()[0]
     assert r.status == abi.RES_CONVERGED, r.as_dict()
     assert np.allclose(inst.coords, exp, atol=1e-4), inst.coords
+
+
+@pytest.mark.parametrize("target", [1e-6, 2 * np.pi - 1e-6])
+def test_bah_fold_mixed_precision_is_a_minimum(target):
+    """In mixed precision the fold may be reached from the other side; the
+    result must still be a minimum of the reference's energy (E ~ 0)."""
+    s2 = np.sqrt(2)
+    x0 = np.array([-1, 0, 1, 0, -s2, 0, 0, s2, 0, 1, 0, 1.0])
+    p = abi.bar_and_hinge(triangulation=[[0, 1, 2], [1, 3, 2]], rigidity=(100, 1), theta0=[target])
+    inst = runtime.Instance(p, x0)
+    r = inst.minimise(abi.minimiser("lbfgs"))
+    assert r.status == abi.RES_CONVERGED
+    check_minimum(p, x0, inst.coords, r, 1e-6)
+    assert r.energy < 1e-10
 
 
 def test_batch_lj_mixed_methods():
