@@ -163,6 +163,10 @@ typedef struct {
   /* instances whose FP64 stage started because: [1] FP32 converged, [2] the
    * line search failed twice in a row, [3] the gradient stalled near tol */
   int64_t switches[4];
+  /* device time in gradient evaluations, line-search trial evaluations and
+   * L-BFGS direction passes (single-instance calls; summed over instances
+   * for batches) */
+  double phase_ms[3];
 } minim_gpu_run_stats;
 
 typedef struct minim_gpu_instance_s* minim_gpu_handle;

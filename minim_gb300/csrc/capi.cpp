@@ -227,6 +227,7 @@ struct minim_gpu_instance_s {
   EvalIO* d_io = nullptr;
   GridSyncState* d_bar = nullptr;
   double* d_partials = nullptr;
+  size_t partials_bytes = 0;
   double* d_tmp = nullptr;   // n doubles: API coordinates / vectors
   double* d_g = nullptr;     // n doubles: API gradient
   double* d_e = nullptr;
@@ -336,7 +337,8 @@ void ensure_grid(minim_gpu_instance_s* h) {
   h->d_desc = (InstDesc*)h->own(dalloc(sizeof(InstDesc)));
   h->d_io = (EvalIO*)h->own(dalloc(sizeof(EvalIO)));
   h->d_bar = (GridSyncState*)h->own(dalloc(sizeof(GridSyncState)));
-  h->d_partials = (double*)h->own(dalloc((2 * (size_t)h->gblocks * 64 + 2 * 64) * sizeof(double)));
+  h->partials_bytes = (2 * (size_t)h->gblocks * 64 + 2 * 64) * sizeof(double) + (size_t)h->gblocks * 4;
+  h->d_partials = (double*)h->own(dalloc(h->partials_bytes));
   h->d_e = (double*)h->own(dalloc(sizeof(double)));
   h->d_tmp = (double*)h->own(dalloc(h->n * sizeof(double)));
   h->d_g = (double*)h->own(dalloc(h->n * sizeof(double)));
@@ -345,6 +347,9 @@ void ensure_grid(minim_gpu_instance_s* h) {
 void launch_grid(minim_gpu_instance_s* h, int op, int slice) {
   Dev& D = need_dev();
   CK(cudaMemsetAsync(h->d_bar, 0, sizeof(GridSyncState), D.s));
+  // barrier flags and epochs restart at 0 in every launch
+  const size_t flag_off = (2 * (size_t)h->gblocks * 64 + 2 * 64) * sizeof(double);
+  CK(cudaMemsetAsync((char*)h->d_partials + flag_off, 0, h->partials_bytes - flag_off, D.s));
   CK((cudaError_t)kern(h->kk).grid(h->d_desc, op, h->d_io, slice, h->d_bar, h->d_partials, h->gthreads,
                                     h->gblocks, pot_smem(h->kk), D.s));
   g_launches++;
@@ -430,6 +435,7 @@ void do_minimise(minim_gpu_instance_s* h, const minim_gpu_minimiser_params& mp, 
   stats.pairs64 = s.pairs64;
   stats.iterations = s.iter + (s.status == ST_CONVERGED ? 1 : 0);
   stats.fp64_iterations = s.fp64_iters;
+  for (int k = 0; k < 3; k++) stats.phase_ms[k] = s.tphase[k] * 1e-6;
   if (s.switch_reason > 0 && s.switch_reason < 4) stats.switches[s.switch_reason]++;
   g_stats = stats;
   if (res) fill_result(res, s, h->n);
@@ -766,7 +772,9 @@ int minim_gpu_batch_run(minim_gpu_batch b, int threads, minim_gpu_result* result
     g_stats.iterations = 0;
     g_stats.fp64_iterations = 0;
     for (auto& k : g_stats.switches) k = 0;
+    for (auto& k : g_stats.phase_ms) k = 0;
     for (auto& s : st) {
+      for (int k = 0; k < 3; k++) g_stats.phase_ms[k] += s.tphase[k] * 1e-6;
       g_stats.fp64_iterations += s.fp64_iters;
       if (s.switch_reason > 0 && s.switch_reason < 4) g_stats.switches[s.switch_reason]++;
       g_stats.abytes += s.abytes;

@@ -150,104 +150,80 @@ struct GridTeam {
   double* red;            // shared scratch as in CtaTeam
   double* wide;           // shared scratch as in CtaTeam
   GridSyncState* bar;     // global
-  double* partials;       // global, 2 * gridDim.x * MINIM_WIDE + 2 * MINIM_WIDE doubles
+  double* partials;       // global: 2 * gridDim.x * MINIM_WIDE partials, 2 * MINIM_WIDE
+                          // totals, then gridDim.x unsigned flags
   int buf;                // partials double buffer index
   int* s_ok;              // shared flag
-  int* s_last;            // shared flag: this block arrived last
+  unsigned int epoch;     // barriers passed in this launch (uniform)
   static constexpr bool kGrid = true;
   static constexpr unsigned long long kWaitLimitNs = 5000000000ull;  // 5 s
 
   __device__ __forceinline__ bool block0() const { return blockIdx.x == 0; }
   __device__ __forceinline__ bool ok() const { return *s_ok != 0; }
 
-  // Sense-counting barrier over all blocks.  Every wait is bounded: after
-  // kWaitLimitNs the block records an error and leaves; blocks arriving
-  // later see the error flag and leave too, so the kernel always returns.
-  __device__ void sync() {
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      int okv = *s_ok;
-      if (okv) {
-        volatile unsigned int* vgen = &bar->gen;
-        volatile int* verr = &bar->err;
-        unsigned int g = *vgen;
-        __threadfence();
-        unsigned int arrived = atomicAdd(&bar->count, 1u);
-        if (arrived == gridDim.x - 1) {
-          atomicExch(&bar->count, 0u);
-          __threadfence();
-          atomicAdd(&bar->gen, 1u);
-        } else {
-          unsigned long long t0 = globaltimer_ns();
-          while (*vgen == g) {
-            if (*verr) { okv = 0; break; }
-            if (globaltimer_ns() - t0 > kWaitLimitNs) {
-              atomicExch(&bar->err, 1);
-              okv = 0;
-              break;
-            }
-            __nanosleep(64);
-          }
-        }
-        __threadfence();
-        if (*verr) okv = 0;
+  // Bounded wait until *p reaches `want` (or an error was recorded).
+  __device__ bool wait_value(volatile unsigned int* p, unsigned int want) {
+    volatile int* verr = &bar->err;
+    unsigned long long t0 = 0;
+    while (*p < want) {
+      if (*verr) return false;
+      const unsigned long long t = globaltimer_ns();
+      if (t0 == 0) {
+        t0 = t;
+      } else if (t - t0 > kWaitLimitNs) {
+        atomicExch(&bar->err, 1);
+        return false;
       }
-      *s_ok = okv;
+      __nanosleep(32);
     }
-    __syncthreads();
+    return true;
   }
 
-  // Reduction barrier: every block publishes its partial sums and arrives;
-  // the block that arrives last sums all partials (fixed order), publishes
-  // the totals and releases the others, which then read only K values.
-  // The wait is bounded as in sync().
-  __device__ void combine(int K, double* out) {
+  // Flag barrier with an optional reduction.  Every block publishes the
+  // barrier's epoch in its own flag (no contended atomics); block 0 waits for
+  // all flags in parallel, sums the blocks' K partials in a fixed order into
+  // the published totals, then releases the others by publishing the epoch.
+  // Every wait is bounded (kWaitLimitNs): a block that gives up records an
+  // error; later barriers see it and return at once, so the kernel always
+  // finishes (status TIMEOUT).
+  __device__ void arrive_release(int K, double* out) {
+    unsigned int* flags =
+        reinterpret_cast<unsigned int*>(partials + (size_t)2 * gridDim.x * MINIM_WIDE + 2 * MINIM_WIDE);
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
     double* P = partials + (size_t)buf * gridDim.x * MINIM_WIDE;
     double* Rz = partials + (size_t)2 * gridDim.x * MINIM_WIDE + (size_t)buf * MINIM_WIDE;
+    const unsigned int ep = ++epoch;
     __syncthreads();
-    if (threadIdx.x == 0) {
-      int okv = *s_ok;
-      int last = 0;
-      if (okv) {
-        volatile unsigned int* vgen = &bar->gen;
-        const unsigned int g = *vgen;
-        __threadfence();
-        const unsigned int arrived = atomicAdd(&bar->count, 1u);
-        if (arrived == gridDim.x - 1) {
-          last = 1;
-          __threadfence();
-        } else {
-          volatile int* verr = &bar->err;
-          unsigned long long t0 = globaltimer_ns();
-          while (*vgen == g) {
-            if (*verr) { okv = 0; break; }
-            if (globaltimer_ns() - t0 > kWaitLimitNs) {
-              atomicExch(&bar->err, 1);
-              okv = 0;
-              break;
-            }
-            __nanosleep(32);
-          }
-          __threadfence();
-        }
-      }
-      *s_ok = okv;
-      *s_last = last;
-    }
+    const bool okb = *s_ok != 0;
     __syncthreads();
-    if (*s_last) {
-      for (int k = w; k < K; k += nw) {
-        double s = 0.0;
-        for (int b = lane; b < (int)gridDim.x; b += 32) s += __ldcg(&P[b * MINIM_WIDE + k]);
-        s = warp_sum(s);
-        if (lane == 0) Rz[k] = s;
-      }
-      __syncthreads();
+    if (okb) {
       if (threadIdx.x == 0) {
-        atomicExch(&bar->count, 0u);
         __threadfence();
-        atomicAdd(&bar->gen, 1u);
+        *(volatile unsigned int*)&flags[blockIdx.x] = ep;
+      }
+      if (blockIdx.x == 0) {
+        bool okv = true;
+        for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x)
+          okv = wait_value((volatile unsigned int*)&flags[b], ep) && okv;
+        if (!okv) *s_ok = 0;
+        __threadfence();
+        __syncthreads();
+        if (*s_ok) {
+          for (int k = w; k < K; k += nw) {
+            double s = 0.0;
+            for (int b = lane; b < (int)gridDim.x; b += 32) s += __ldcg(&P[b * MINIM_WIDE + k]);
+            s = warp_sum(s);
+            if (lane == 0) Rz[k] = s;
+          }
+          __syncthreads();
+          if (threadIdx.x == 0) {
+            __threadfence();
+            *(volatile unsigned int*)&bar->gen = ep;
+          }
+        }
+      } else if (threadIdx.x == 0) {
+        if (!wait_value((volatile unsigned int*)&bar->gen, ep)) *s_ok = 0;
+        __threadfence();
       }
     }
     __syncthreads();
@@ -255,6 +231,8 @@ struct GridTeam {
     __syncthreads();
     buf ^= 1;
   }
+
+  __device__ void sync() { arrive_release(0, nullptr); }
 
   template <int K>
   __device__ void reduce(double (&v)[K]) {
@@ -273,7 +251,7 @@ struct GridTeam {
       for (int i = 0; i < nw; i++) s += red[i * MINIM_MAXRED + threadIdx.x];
       P[blockIdx.x * MINIM_WIDE + threadIdx.x] = s;
     }
-    combine(K, red + 32 * MINIM_MAXRED);
+    arrive_release(K, red + 32 * MINIM_MAXRED);
 #pragma unroll
     for (int k = 0; k < K; k++) v[k] = red[32 * MINIM_MAXRED + k];
     __syncthreads();
@@ -290,7 +268,7 @@ struct GridTeam {
       for (int i = 0; i < nw; i++) s += wide[i * MINIM_WIDE + k];
       P[blockIdx.x * MINIM_WIDE + k] = s;
     }
-    combine(K, out);
+    arrive_release(K, out);
   }
 };
 

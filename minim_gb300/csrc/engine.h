@@ -118,10 +118,13 @@ struct MinScalars {
   // newest pair) is filled by the next direction's first pass
   double SY[MINIM_MAXM][MINIM_MAXM], YY[MINIM_MAXM][MINIM_MAXM];
   int pend;
-  int pad_;
+  int cool;          // iterations before a stalled run may re-enter FP64
   // work counters for the roofline: algorithmic HBM bytes of every vector
   // pass and evaluation, and Lennard-Jones pair interactions per precision
   double abytes, pairs32, pairs64;
+  // device time (ns, block 0) in gradient evaluations, line-search trial
+  // evaluations and L-BFGS direction passes
+  double tphase[3];
 };
 
 // K_PF1 is the kernel variant for a binary PhaseField with none of the

@@ -109,7 +109,7 @@ grid_kernel(const InstDesc* __restrict__ inst, int op, const EvalIO* io, int sli
   if (threadIdx.x == 0) S.ok = 1;
   __syncthreads();
   GridTeam tm{(int)(blockIdx.x * blockDim.x + threadIdx.x), (int)(gridDim.x * blockDim.x), S.red,
-              S.wide, bar, partials, 0, &S.ok, &S.last};
+              S.wide, bar, partials, 0, &S.ok, 0u};
   Runner<GridTeam, KIND> R{tm, s_in, dyn, lj_tile};
   setup_runner(R, S, s_in);
   if (op == OP_MINIMISE) {

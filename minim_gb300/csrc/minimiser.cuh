@@ -86,9 +86,10 @@ struct Runner {
   int lj_tile;
   // uniform scalars (every thread holds identical copies)
   int n, status, initd, iter, ii, stage, xi, gi, evals, fp64_iters, stall, nsteps, pbuf, ybuf;
-  int exhausted_run, switch_reason, pend;
+  int exhausted_run, switch_reason, pend, cool;
   double E, gg, best_rms, dt, a, dtmax, gnorm;
   double abytes, pairs32, pairs64;
+  double tph[3];
   // shared arrays (one copy per block; written by thread 0 between barriers)
   double *rho, *sig, *yy, *alpha;
   int *sidx, *yidx;
@@ -125,6 +126,14 @@ struct Runner {
   template <typename T, class Emit>
   __device__ double pot_eval(CView<T> cv, T* xw, Emit& em, bool want_e, bool want_g) {
     if constexpr (KIND == K_LJ) {
+      if constexpr (!Team::kGrid) {
+        // batched path: each pair once, when positions and forces of all
+        // particles fit the tile buffer
+        const int ntp = ((in.lj.np + 31) >> 5) + (((in.lj.np + 31) >> 5) & 1);
+        if (want_g && (size_t)32 * ntp * 7 * sizeof(T) <= (size_t)lj_tile * sizeof(D4) &&
+            (blockDim.x & 31) == 0)
+          return lj_eval_sym<T>(tm, in.lj, cv, xw, &em, want_e, smem_pot);
+      }
       return lj_eval<T>(tm, in.lj, cv, xw, &em, want_e, want_g, smem_pot, lj_tile);
     } else if constexpr (KIND == K_PF) {
       return pf_eval<T>(tm, in.pf, cv, xw, &em, want_e, want_g);
@@ -142,6 +151,7 @@ struct Runner {
   // and py = P.y, yyv = y.y are returned.  The new gradient becomes current.
   __device__ void grad_eval(double t, const float* P, bool write_x, bool want_y, double& py,
                             double& yyv) {
+    const unsigned long long t_start = globaltimer_ns();
     float* Gn = in.G[1 - gi];
     const bool proj = global_projection();
     // with a global projection the gradient is finished in a second pass
@@ -183,9 +193,11 @@ struct Runner {
     if (want_y) abytes += 8.0 * n;
     gi = 1 - gi;
     if (write_x) xi = 1 - xi;
+    tph[0] += (double)(globaltimer_ns() - t_start);
   }
 
   __device__ double energy_at(double t, const float* P) {
+    const unsigned long long t_start = globaltimer_ns();
     FusedEmit ne{nullptr, nullptr, nullptr, nullptr, nullptr};
     double ep;
     if (stage == 0) {
@@ -199,6 +211,7 @@ struct Runner {
     tm.reduce(v);
     evals++;
     count_eval(P != nullptr, false);
+    tph[1] += (double)(globaltimer_ns() - t_start);
     return v[0];
   }
 
@@ -424,7 +437,9 @@ struct Runner {
       ii++;
     }
     double gp;
+    const unsigned long long t_dir = globaltimer_ns();
     double scale = lbfgs_direction(gp);
+    tph[2] += (double)(globaltimer_ns() - t_dir);
     float* P = Sbuf(pbuf);
     if (has_constraints()) gp = scale * constrain_dir(P);
     double gs = gp;
@@ -595,9 +610,10 @@ struct Runner {
     status = s.status; initd = s.initialised; iter = s.iter; ii = s.ii; stage = s.stage;
     xi = s.xi; gi = s.gi; evals = s.evals; fp64_iters = s.fp64_iters; stall = s.stall;
     nsteps = s.nsteps; pbuf = s.pbuf; ybuf = s.ybuf; E = s.E; gg = s.gg; best_rms = s.best_rms;
-    exhausted_run = s.exhausted_run; switch_reason = s.switch_reason; pend = s.pend;
+    exhausted_run = s.exhausted_run; switch_reason = s.switch_reason; pend = s.pend; cool = s.cool;
     dt = s.dt; a = s.a; dtmax = s.dtmax; gnorm = s.gnorm;
     abytes = s.abytes; pairs32 = s.pairs32; pairs64 = s.pairs64;
+    tph[0] = s.tphase[0]; tph[1] = s.tphase[1]; tph[2] = s.tphase[2];
     for (int k = threadIdx.x; k < MINIM_MAXM * MINIM_MAXM; k += blockDim.x) {
       SY[k] = (&s.SY[0][0])[k];
       YY[k] = (&s.YY[0][0])[k];
@@ -615,9 +631,10 @@ struct Runner {
       s.status = status; s.iter = iter; s.ii = ii; s.stage = stage; s.xi = xi; s.gi = gi;
       s.evals = evals; s.fp64_iters = fp64_iters; s.stall = stall; s.nsteps = nsteps;
       s.pbuf = pbuf; s.ybuf = ybuf; s.E = E; s.gg = gg; s.best_rms = best_rms;
-      s.exhausted_run = exhausted_run; s.switch_reason = switch_reason; s.pend = pend;
+      s.exhausted_run = exhausted_run; s.switch_reason = switch_reason; s.pend = pend; s.cool = cool;
       s.dt = dt; s.a = a; s.dtmax = dtmax; s.gnorm = gnorm; s.initialised = 1;
       s.abytes = abytes; s.pairs32 = pairs32; s.pairs64 = pairs64;
+      s.tphase[0] = tph[0]; s.tphase[1] = tph[1]; s.tphase[2] = tph[2];
       for (int k = 0; k < MINIM_MAXM * MINIM_MAXM; k++) {
         (&s.SY[0][0])[k] = SY[k];
         (&s.YY[0][0])[k] = YY[k];
@@ -676,6 +693,7 @@ struct Runner {
       best_rms = 1e300;
       stall = 0;
       exhausted_run = 0;
+      cool = 0;
     }
     for (int s = 0; s < slice; s++) {
       if (iter > mp.max_iter) { status = ST_MAXITER; break; }
@@ -698,6 +716,7 @@ struct Runner {
       const double r = rms();
       bool conv = r < mp.tol;
       if (mixed) {
+        if (cool > 0) cool--;
         if (stage == 0) {
           // Leave the FP32 stage when FP32 has done what it can: converged in
           // FP32; the line search keeps failing to find an Armijo point (the
@@ -710,7 +729,7 @@ struct Runner {
           exhausted_run = exhausted_run * 7 / 8 + (exhausted ? 8 : 0);
           const int why = conv ? 1
                         : ((exhausted_run >= 20 || (exhausted && r < 1000.0 * mp.tol)) ? 2
-                        : ((stall >= 100 && r < 100.0 * mp.tol) ? 3 : 0));
+                        : ((stall >= 100 && r < 100.0 * mp.tol && cool == 0) ? 3 : 0));
           if (why) {
             switch_reason = why;
             to_fp64();
@@ -724,15 +743,24 @@ struct Runner {
             stall = 0;
             exhausted_run = 0;
           }
-        } else if (r > 1e4 * mp.tol && r > 100.0 * best_rms) {
-          // an FP64 run that has moved far from convergence (FIRE restarts,
-          // a basin change) continues in FP32 until it approaches again
-          to_fp32();
-          reeval();
-          best_rms = rms();
-          stall = 0;
-          exhausted_run = 0;
-          conv = false;
+        } else {
+          // An FP64 run that has moved far from convergence (FIRE restarts,
+          // a basin change), or that has not improved its RMS gradient by 1%
+          // in 2000 iterations (an orbit that will not converge), continues
+          // in FP32; a stalled run may re-enter FP64 on a stall only after
+          // 5000 more iterations.
+          if (r < 0.99 * best_rms) { best_rms = r; stall = 0; }
+          else stall++;
+          const bool far = r > 1e4 * mp.tol && r > 100.0 * best_rms;
+          if (far || stall >= 2000) {
+            if (!far) cool = 5000;
+            to_fp32();
+            reeval();
+            best_rms = rms();
+            stall = 0;
+            exhausted_run = 0;
+            conv = false;
+          }
         }
       }
       if (conv) { status = ST_CONVERGED; break; }

@@ -142,6 +142,119 @@ __device__ __noinline__ double lj_eval(Team& tm, const PotLJ& P, CView<T> cv, T*
   return 4.0 * P.eps * e.total();
 }
 
+// Symmetric all-pairs evaluation for one CTA (the batched path): each
+// unordered pair is computed once.  Particles are grouped in tiles of 32;
+// tile pairs are scheduled round-robin (circle method) so that within a
+// round every tile belongs to one warp.  The warp keeps its i tile in lanes
+// and rotates the j tile's positions and forces through the lanes with
+// shuffles (32 steps return them home), then adds both tiles' forces to
+// shared-memory accumulators -- no atomics, and the summation order per
+// particle is fixed by the round order, so results are deterministic.  Tiles
+// are padded with particles 1e6 sigma apart, which contribute nothing
+// measurable.  Shared memory: positions (4 T) and forces (3 T) per particle.
+template <typename T, class Emit>
+__device__ __noinline__ double lj_eval_sym(CtaTeam& tm, const PotLJ& P, CView<T> cv, T* xw, Emit* emp,
+                                           bool want_e, void* smem) {
+  using V4 = typename Vec4T<T>::type;
+  Emit emit = *emp;
+  const int N = P.np, nd = P.ndim;
+  const int nt = (N + 31) >> 5;            // tiles
+  const int ntp = nt + (nt & 1);           // even count for the schedule (last may be empty)
+  V4* sx = reinterpret_cast<V4*>(smem);
+  T* sf = reinterpret_cast<T*>(sx + 32 * ntp);  // 3 per particle
+  const T s6 = (T)P.s6;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int j = threadIdx.x; j < 32 * ntp; j += blockDim.x) {
+    V4 v;
+    if (j < N) {
+      v.x = cv(nd * j);
+      v.y = cv(nd * j + 1);
+      v.z = (nd == 3) ? cv(nd * j + 2) : (T)0;
+      if (xw) {
+        xw[nd * j] = v.x;
+        xw[nd * j + 1] = v.y;
+        if (nd == 3) xw[nd * j + 2] = v.z;
+      }
+    } else {
+      v.x = (T)(1e6 * (double)(j + 1));
+      v.y = 0;
+      v.z = 0;
+    }
+    v.w = 0;
+    sx[j] = v;
+    sf[3 * j] = 0;
+    sf[3 * j + 1] = 0;
+    sf[3 * j + 2] = 0;
+  }
+  __syncthreads();
+  EAcc<T> e;
+  // diagonal tiles: each lane pairs with the 31 others of its tile (every
+  // pair twice, half the energy each), force on the own particle only
+  for (int t = w; t < nt; t += nw) {
+    const int i = 32 * t + lane;
+    const V4 a = sx[i];
+    T fx = 0, fy = 0, fz = 0, ee = 0;
+    for (int s = 1; s < 32; s++) {
+      const V4 b = sx[32 * t + ((lane + s) & 31)];
+      const T dx = a.x - b.x, dy = a.y - b.y, dz = a.z - b.z;
+      const T inv = lj_rcp<T>(dx * dx + dy * dy + dz * dz);
+      const T lj6 = s6 * inv * inv * inv;
+      const T lj12 = lj6 * lj6;
+      const T f = (2 * lj12 - lj6) * inv;
+      fx += dx * f; fy += dy * f; fz += dz * f;
+      ee += lj12 - lj6;
+    }
+    sf[3 * i] += fx; sf[3 * i + 1] += fy; sf[3 * i + 2] += fz;
+    if (want_e && i < N) e.add((T)0.5 * ee);
+  }
+  __syncthreads();
+  // off-diagonal tile pairs, circle-method rounds
+  const int half = ntp >> 1;
+  for (int r = 0; r < ntp - 1; r++) {
+    for (int k = w; k < half; k += nw) {
+      int I, J;
+      if (k == 0) { I = ntp - 1; J = r; }
+      else { I = (r + k) % (ntp - 1); J = (r - k + (ntp - 1)) % (ntp - 1); }
+      if (I >= nt || J >= nt) continue;   // the empty padding tile
+      const int i = 32 * I + lane;
+      const V4 a = sx[i];
+      V4 b = sx[32 * J + lane];
+      T fx = 0, fy = 0, fz = 0, gx = 0, gy = 0, gz = 0, ee = 0;
+      const int src = (lane + 1) & 31;
+      for (int s = 0; s < 32; s++) {
+        const T dx = a.x - b.x, dy = a.y - b.y, dz = a.z - b.z;
+        const T inv = lj_rcp<T>(dx * dx + dy * dy + dz * dz);
+        const T lj6 = s6 * inv * inv * inv;
+        const T lj12 = lj6 * lj6;
+        const T f = (2 * lj12 - lj6) * inv;
+        fx += dx * f; fy += dy * f; fz += dz * f;
+        gx -= dx * f; gy -= dy * f; gz -= dz * f;
+        ee += lj12 - lj6;
+        b.x = __shfl_sync(0xffffffffu, b.x, src);
+        b.y = __shfl_sync(0xffffffffu, b.y, src);
+        b.z = __shfl_sync(0xffffffffu, b.z, src);
+        gx = __shfl_sync(0xffffffffu, gx, src);
+        gy = __shfl_sync(0xffffffffu, gy, src);
+        gz = __shfl_sync(0xffffffffu, gz, src);
+      }
+      const int j = 32 * J + lane;
+      sf[3 * i] += fx; sf[3 * i + 1] += fy; sf[3 * i + 2] += fz;
+      sf[3 * j] += gx; sf[3 * j + 1] += gy; sf[3 * j + 2] += gz;
+      if (want_e) e.add(ee);
+    }
+    __syncthreads();
+  }
+  const T c = (T)(-24.0 * P.eps);
+  for (int i = threadIdx.x; i < N; i += blockDim.x) {
+    emit(nd * i, c * sf[3 * i]);
+    emit(nd * i + 1, c * sf[3 * i + 1]);
+    if (nd == 3) emit(nd * i + 2, c * sf[3 * i + 2]);
+  }
+  __syncthreads();
+  *emp = emit;
+  return 4.0 * P.eps * e.total();
+}
+
 // ===========================================================================
 // PhaseField (MODEL_BASIC), gather form of PhaseField::energyGradient
 // (src/potentials/PhaseField.cpp:238-288, 365-393, 432-537) followed by the

@@ -111,6 +111,7 @@ def last_run_stats():
     _check(load().minim_gpu_last_run_stats(C.byref(s)))
     d = {k: getattr(s, k) for k, _ in s._fields_}
     d["switches"] = list(s.switches)
+    d["phase_ms"] = list(s.phase_ms)
     return d
 
 
