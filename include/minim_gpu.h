@@ -259,6 +259,26 @@ int minim_gpu_pf_setup(const minim_gpu_pf_params* q, const double* x0, size_t nd
                        double* kappaP, int* nk, double* node_vol, double* surface_area,
                        int* kernel_variant);
 
+/* ---- allocation-free minimisation (no counterpart in the reference) ------
+ * Minimises one Lennard-Jones cluster (LjNd energy, the given minimiser) in
+ * one CTA without allocating any memory: for callers that cannot call the
+ * device allocator -- code embedded in a runtime whose caching allocator
+ * already holds the GPU's memory, or a loop that must stay out of the
+ * driver's allocator.  x_dev (device memory, ndof doubles) holds the start
+ * and receives the minimum; the workspace is a fixed 1 MiB device array
+ * inside this library, at most 3072 degrees of freedom (1024 particles in
+ * 3-D; larger calls return MINIM_GPU_ERR_INVALID).  Work is queued on
+ * `stream` (a cudaStream_t, NULL = legacy default stream) and the call
+ * returns after synchronising that stream.  The first call on a device (with
+ * that device current) looks up the array's device address; make it before
+ * any stream capture.  All calls share the one array: calls that overlap on
+ * the GPU race and must be serialised by the caller.  The tolerance
+ * mp->tol < 0 means 1e-6.  Results equal minim_gpu_batch_run with 256
+ * threads per CTA. */
+int minim_gpu_lj_minimise_noalloc(const minim_gpu_lj_params* p, double* x_dev, size_t ndof,
+                                  const minim_gpu_minimiser_params* mp, minim_gpu_result* res,
+                                  void* stream);
+
 #ifdef __cplusplus
 }
 #endif

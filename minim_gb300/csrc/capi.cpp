@@ -602,6 +602,10 @@ extern "C" {
 
 int minim_gpu_abi_version(void) { return MINIM_GPU_ABI_VERSION; }
 
+// Sets the calling thread's last-error message (for entry points defined in
+// other translation units).
+void mg_set_last_error(const char* msg) { g_err = msg ? msg : ""; }
+
 int minim_gpu_last_error(char* buf, size_t len) {
   if (buf && len) {
     std::strncpy(buf, g_err.c_str(), len - 1);

@@ -31,7 +31,7 @@ EXPORTS = [
     "minim_gpu_server_create", "minim_gpu_server_submit", "minim_gpu_server_step",
     "minim_gpu_server_poll", "minim_gpu_server_take", "minim_gpu_server_cancel",
     "minim_gpu_server_destroy", "minim_gpu_bah_elements", "minim_gpu_bah_colouring",
-    "minim_gpu_pf_setup",
+    "minim_gpu_pf_setup", "minim_gpu_lj_minimise_noalloc",
 ]
 
 
@@ -82,6 +82,8 @@ def load(path=LIB_PATH):
                                    C.c_int),
         "minim_gpu_bah_colouring": ([P, _dp, C.c_size_t, _ip, _ip, _ip], C.c_int),
         "minim_gpu_pf_setup": ([P, _dp, C.c_size_t, _dp, _dp, _ip, _dp, _dp, _ip], C.c_int),
+        "minim_gpu_lj_minimise_noalloc": ([P, C.c_void_p, C.c_size_t, C.POINTER(abi.MinimiserParams),
+                                           C.POINTER(abi.Result), C.c_void_p], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)
@@ -312,3 +314,14 @@ def pf_setup(params, x0):
                                   sa.ctypes.data_as(_dp), C.byref(var)))
     return {"kappa": k[: nk.value], "kappaP": kp[: nk.value], "node_vol": nv, "surface_area": sa,
             "kernel_variant": var.value}
+
+
+def lj_minimise_noalloc(params, x_dev_ptr, ndof, mp, stream=0):
+    """Allocation-free LJ minimisation of the device coordinates at x_dev_ptr
+    (ndof doubles, overwritten with the minimum) on `stream` (a cudaStream_t
+    handle as an integer, 0 = default stream).  Returns the Result."""
+    lib = load()
+    r = abi.Result()
+    _check(lib.minim_gpu_lj_minimise_noalloc(params.ptr(), C.c_void_p(x_dev_ptr), ndof, C.byref(mp),
+                                             C.byref(r), C.c_void_p(stream)))
+    return r
