@@ -35,6 +35,12 @@ sys.path.insert(0, HERE)
 GRID = (192, 192, 192)
 TOL = 1e-7
 METRIC = "converged minimisations/s batched vs plain on GB300 at ΔE/E<1e-8; p50/p99 ms"
+# DRAM bytes per algorithmic byte of the PhaseField 192^3 minimiser kernel,
+# from one ncu capture of a 20-iteration launch of the same kernel
+# (dram__bytes_read.sum + dram__bytes_write.sum = 26.21 GB against the
+# kernel's own count of 22.93 GB; profiles/grid_kernel_pf1_192cubed.md).
+# Traffic per step = this ratio x the step's algorithmic bytes.
+PF_TRAFFIC_PER_ALGO_BYTE = 26.21 / 22.93
 
 
 def _peaks():
@@ -172,8 +178,10 @@ def run_gpu(args):
 
     hbm_peak, peak_kind = _peaks()
     achieved = abytes / (kernel_ms / 1e3) / 1e9
+    traffic = PF_TRAFFIC_PER_ALGO_BYTE * abytes / args.steps
     roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                "frac": achieved / hbm_peak, "traffic": None, "peak_source": peak_kind,
+                "frac": achieved / hbm_peak, "traffic": traffic, "traffic_unit": "bytes/step",
+                "algorithmic_bytes_per_step": abytes / args.steps, "peak_source": peak_kind,
                 "kernel": "grid_kernel<K_PF1> (fused L-BFGS minimiser)"}
 
     out = {
@@ -243,28 +251,29 @@ def run_batched(args):
 
 def cpu_baseline(gpu_iters, budget_s=20.0):
     """CPU restatement (or the reference library where it was built) timed on
-    a bounded number of L-BFGS iterations of the same 192^3 workload; the
-    rate is extrapolated to a full minimisation with the GPU's iteration
-    count (the same algorithm and stopping rule)."""
+    all host threads over a bounded number of L-BFGS iterations of the same
+    192^3 workload; the rate is extrapolated to a full minimisation with the
+    GPU's iteration count (the same algorithm and stopping rule)."""
     from minim_gb300 import abi
     from oracle import oracle as O
     p, x0, mp = pf_setup()
     kind = "reference" if O.reference_available() else "port"
     cls = O.Reference if kind == "reference" else O.Oracle
-    inst = cls(p, x0)
+    threads = os.cpu_count() or 1
+    inst = cls(p, x0, threads=threads)
     # time one E+g to size the sample
     t = time.perf_counter()
     inst.energy_gradient()
     t_eval = time.perf_counter() - t
     iters = max(2, int(budget_s / max(t_eval * 5, 1e-3)))
     mps = abi.minimiser("lbfgs", m=10, tol=TOL, max_iter=iters - 1)
-    inst = cls(p, x0)
+    inst = cls(p, x0, threads=threads)
     t = time.perf_counter()
     r = inst.minimise(mps)
     dt = time.perf_counter() - t
     per_iter = dt / (r.iter + 1 if r.status != 0 else r.iter + 1)
     rate = 1.0 / (per_iter * max(gpu_iters + 1, 1))
-    return {"value": rate, "unit": "minimisations/s", "cores": 1, "kind": kind,
+    return {"value": rate, "unit": "minimisations/s", "cores": threads, "kind": kind,
             "sample": f"{r.iter + 1} L-BFGS iterations of the 192^3 run ({dt:.1f} s), "
                       f"extrapolated to {gpu_iters + 1} iterations"}
 

@@ -10,6 +10,7 @@
 #include <atomic>
 #include <chrono>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <deque>
 #include <mutex>
@@ -127,6 +128,33 @@ Kern kern(int kk) {
 }
 const size_t kLjTileBytes = 1024 * 32;  // 1024 particles of 4 doubles
 size_t pot_smem(int kk) { return kk == K_LJ ? kLjTileBytes : 0; }
+// Grid launches of the grid-sized potentials can stream the minimiser's
+// vector passes through a ring of kStages shared-memory stages of
+// MINIM_GPU_STAGE_KB kilobytes each (at most 50; 4 x 22.5 KB keeps two
+// blocks of 256 threads per SM).  The default, 0, reads global memory
+// directly with L2 prefetch one sweep step ahead, which measures faster.
+const int kStages = 4;
+int stage_bytes_cfg() {
+  static const int v = [] {
+    const char* e = std::getenv("MINIM_GPU_STAGE_KB");
+    double kb = e ? std::atof(e) : 0.0;
+    kb = kb < 0 ? 0 : (kb > 50 ? 50 : kb);
+    return ((int)(kb * 1024) / 256) * 256;
+  }();
+  return v;
+}
+int grid_stage_bytes(int kk) { return kk == K_LJ ? 0 : stage_bytes_cfg(); }
+// L2 prefetch distance of the grid launches' sweeps, in sweep steps
+// (MINIM_GPU_PREFETCH, default 1; 0 disables it).
+int prefetch_cfg() {
+  static const int v = [] {
+    const char* e = std::getenv("MINIM_GPU_PREFETCH");
+    const int d = e ? std::atoi(e) : 1;
+    return d < 0 ? 0 : (d > 8 ? 8 : d);
+  }();
+  return v;
+}
+size_t grid_smem(int kk) { return kk == K_LJ ? kLjTileBytes : kStages * (size_t)stage_bytes_cfg(); }
 
 // ---- workspace layout --------------------------------------------------------------
 struct WsLayout {
@@ -146,6 +174,9 @@ WsLayout ws_layout(size_t n, const minim_gpu_minimiser_params& mp) {
   for (int k = 0; k < 2; k++) L.x64[k] = L.fp64 ? take(n * 8) : (size_t)-1;
   for (int k = 0; k < 2; k++) L.g[k] = take(n * 4);
   L.hstride = (n + 63) & ~(size_t)63;
+  // the direction pass addresses history slots with 32-bit float4 offsets
+  if ((size_t)(L.nS > L.nY ? L.nS : L.nY) * L.hstride >= ((size_t)1 << 33))
+    throw ApiError{MINIM_GPU_ERR_INVALID, "instance too large for the history layout"};
   L.S = L.nS ? take((size_t)L.nS * L.hstride * 4) : (size_t)-1;
   L.Y = L.nY ? take((size_t)L.nY * L.hstride * 4) : (size_t)-1;
   L.V = mp.method == MINIM_FIRE ? take(n * 4) : (size_t)-1;
@@ -331,7 +362,7 @@ void ensure_grid(minim_gpu_instance_s* h) {
   Dev& D = need_dev();
   if (h->d_desc) return;
   int per_sm = 0;
-  CK((cudaError_t)kern(h->kk).occ(1, h->gthreads, pot_smem(h->kk), &per_sm));
+  CK((cudaError_t)kern(h->kk).occ(1, h->gthreads, grid_smem(h->kk), &per_sm));
   if (per_sm < 1) throw ApiError{MINIM_GPU_ERR_CUDA, "grid kernel does not fit on an SM"};
   h->gblocks = D.nsm * per_sm;
   h->d_desc = (InstDesc*)h->own(dalloc(sizeof(InstDesc)));
@@ -351,7 +382,7 @@ void launch_grid(minim_gpu_instance_s* h, int op, int slice) {
   const size_t flag_off = (2 * (size_t)h->gblocks * 64 + 2 * 64) * sizeof(double);
   CK(cudaMemsetAsync((char*)h->d_partials + flag_off, 0, h->partials_bytes - flag_off, D.s));
   CK((cudaError_t)kern(h->kk).grid(h->d_desc, op, h->d_io, slice, h->d_bar, h->d_partials, h->gthreads,
-                                    h->gblocks, pot_smem(h->kk), D.s));
+                                    h->gblocks, grid_smem(h->kk), D.s));
   g_launches++;
 }
 
@@ -399,6 +430,9 @@ void do_minimise(minim_gpu_instance_s* h, const minim_gpu_minimiser_params& mp, 
   InstDesc d = h->d;
   ws_apply(d, (char*)h->ws, L);
   d.mp = to_mp(mp, tol);
+  d.stage_bytes = grid_stage_bytes(h->kk);
+  d.pf_dist = prefetch_cfg();
+  d.pf.pf_dist = d.pf_dist;
   h->d_st = (MinScalars*)((char*)h->ws + L.total);
   d.st = h->d_st;
   MinScalars s = fresh_scalars();

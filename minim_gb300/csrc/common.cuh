@@ -15,6 +15,7 @@
 
 #define MINIM_MAXRED 8    // values reduced together in one team reduction
 #define MINIM_WIDE 64     // values reduced together in one wide reduction
+#define MINIM_NSTAGE 4    // shared-memory stages of a staged vector pass
 
 namespace mg {
 
@@ -59,20 +60,23 @@ __device__ __forceinline__ void wide_store_row(float (&v)[32], int k0, double* w
   __syncwarp();
 }
 
-// Accumulates a stream of FP32 terms: short runs are summed in FP32 and
-// flushed into an FP64 total (the FP64 pipe is a scarce resource on GB300;
-// the FP32 run length bounds the FP32 rounding).
+// Accumulates a stream of FP32 terms with compensated (TwoSum) FP32
+// arithmetic: the sum and its running rounding error together carry about
+// 48 bits, and no per-term work touches the FP64 pipe, which on GB300 runs at
+// 1/64 of the FP32 rate.  The order of additions is fixed, so results are
+// deterministic.
 struct Acc {
-  double d;
-  float f;
-  int n;
-  __device__ __forceinline__ Acc() : d(0.0), f(0.f), n(0) {}
+  float s, c;  // running sum and its rounding error (Neumaier / TwoSum, all FP32)
+  double d;    // FP64 terms
+  __device__ __forceinline__ Acc() : s(0.f), c(0.f), d(0.0) {}
   __device__ __forceinline__ void add(float v) {
-    f += v;
-    if (++n == 8) { d += (double)f; f = 0.f; n = 0; }
+    const float t = __fadd_rn(s, v);
+    const float bp = __fsub_rn(t, s);
+    c = __fadd_rn(c, __fadd_rn(__fsub_rn(s, __fsub_rn(t, bp)), __fsub_rn(v, bp)));
+    s = t;
   }
   __device__ __forceinline__ void add(double v) { d += v; }
-  __device__ __forceinline__ double total() const { return d + (double)f; }
+  __device__ __forceinline__ double total() const { return d + ((double)s + (double)c); }
 };
 
 // aligned 4-wide access to FP32 vectors (element 4*i4 .. 4*i4+3)
@@ -87,17 +91,178 @@ __device__ __forceinline__ float4 axpy4(float a, float4 x, float4 y) {  // a*x +
   return make_float4(fmaf(a, x.x, y.x), fmaf(a, x.y, y.y), fmaf(a, x.z, y.z), fmaf(a, x.w, y.w));
 }
 
+// L2 prefetch of the 128-byte line that holds float4 element i4 of p.  One
+// lane in eight issues it (eight consecutive float4 share a line; callers
+// keep i4 of lane 0 of each group a multiple of 8).  A prefetch holds no
+// register, so the passes keep more bytes in flight than their loads alone.
+__device__ __forceinline__ void prefetch_line(const float* p, int i4) {
+  if ((threadIdx.x & 7) == 0) asm volatile("prefetch.global.L2 [%0];" ::"l"(p + 4 * (size_t)i4));
+}
+
 __device__ __forceinline__ unsigned long long globaltimer_ns() {
   unsigned long long t;
   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
   return t;
 }
 
+// ---- bulk copies into shared memory (cp.async.bulk + mbarrier) -----------------
+// A stage is a shared buffer with an mbarrier.  One thread announces the
+// bytes the stage will receive (arrive.expect_tx) and issues the copies; the
+// mbarrier's phase completes when all bytes have landed, and every thread
+// waits on that phase before reading.  Addresses and sizes are multiples of
+// 16 bytes.
+__device__ __forceinline__ unsigned smem_u32(const void* p) {
+  return (unsigned)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_init_fence() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void proxy_async_fence() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long* bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes, unsigned long long* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(unsigned long long* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+// The spin itself carries no memory clobber (nothing the compiler holds in
+// registers is reloaded per poll); a compiler fence after the loop keeps the
+// reads of the landed data below the wait, whose acquire makes them visible.
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity));
+  return ok != 0;
+}
+// Bounded wait for the given phase parity (false after `limit_ns`).
+__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity,
+                                          unsigned long long limit_ns) {
+  bool ok = true;
+  if (!mbar_try_wait(bar, parity)) {
+    const unsigned long long t0 = globaltimer_ns();
+    while (!mbar_try_wait(bar, parity)) {
+      if (globaltimer_ns() - t0 > limit_ns) {
+        ok = false;
+        break;
+      }
+    }
+  }
+  asm volatile("" ::: "memory");
+  return ok;
+}
+
+// A ring of MINIM_NSTAGE shared stages streaming chunks of nv vectors into a
+// block: each stage has a "full" mbarrier (the chunk's bytes have landed)
+// and an "empty" one (every warp is done with it).  The block's chunks are
+// cidx = blockIdx.x + j * gridDim.x; a chunk holds `ch` floats of each
+// vector.  Thread 0 fills the ring ahead; warp 0, after releasing chunk j,
+// waits until all warps have, and refills that stage with chunk j +
+// MINIM_NSTAGE, so warps never wait on one another except through the data.
+// Uses are numbered per launch (sq), which fixes the barriers' phase
+// parities.  All state lives in registers (no member access through memory).
+struct StageRing {
+  char* base;                 // shared: MINIM_NSTAGE stages of stage_bytes
+  unsigned long long* full;   // shared mbarriers
+  unsigned long long* empty;
+  int* err;                   // shared: a wait gave up
+  int stage_bytes, n, ch, nv, mine, j, issued;
+  unsigned sq;
+
+  __device__ __forceinline__ float* buf(int s) const {
+    return reinterpret_cast<float*>(base + (size_t)s * stage_bytes);
+  }
+  template <class VecFn>
+  __device__ __forceinline__ void issue(int s, int cidx, VecFn vec) const {
+    const int i0 = cidx * ch;
+    const int cnt = min(ch, n - i0);
+    const unsigned bytes = (unsigned)((cnt * 4 + 15) & ~15);
+    float* dst = buf(s);
+    proxy_async_fence();
+    mbar_expect_tx(&full[s], bytes * (unsigned)nv);
+    for (int v = 0; v < nv; v++) bulk_g2s(dst + (size_t)v * ch, vec(v) + i0, bytes, &full[s]);
+  }
+  // all threads; `ok` false skips the sweep
+  template <class VecFn>
+  __device__ __forceinline__ void begin(bool ok, VecFn vec) {
+    const int nch = (n + ch - 1) / ch;
+    mine = ok && (int)blockIdx.x < nch ? (nch - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+    j = 0;
+    issued = 0;
+    if (threadIdx.x == 0) {
+      *err = 0;
+      for (; issued < min(MINIM_NSTAGE, mine); issued++)
+        issue((sq + issued) % MINIM_NSTAGE, blockIdx.x + issued * gridDim.x, vec);
+    }
+    __syncthreads();
+  }
+  __device__ __forceinline__ int i0() const { return ((int)blockIdx.x + j * (int)gridDim.x) * ch; }
+  __device__ __forceinline__ int count() const { return min(ch, n - i0()); }
+  // wait for chunk j; null if the block must stop
+  __device__ __forceinline__ const float* acquire() {
+    const unsigned u = sq + (unsigned)j;
+    if (*(volatile int*)err) return nullptr;
+    if (!mbar_wait(&full[u % MINIM_NSTAGE], (u / MINIM_NSTAGE) & 1u, 5000000000ull)) {
+      *(volatile int*)err = 1;
+      return nullptr;
+    }
+    return buf(u % MINIM_NSTAGE);
+  }
+  template <class VecFn>
+  __device__ __forceinline__ void release(VecFn vec) {
+    const unsigned u = sq + (unsigned)j;
+    const int s = u % MINIM_NSTAGE;
+    __syncwarp();
+    if ((threadIdx.x & 31) == 0) mbar_arrive(&empty[s]);
+    if (threadIdx.x < 32 && j + MINIM_NSTAGE < mine) {
+      const bool ok = mbar_wait(&empty[s], (u / MINIM_NSTAGE) & 1u, 5000000000ull);
+      if (threadIdx.x == 0) {
+        if (ok) {
+          issue(s, blockIdx.x + (j + MINIM_NSTAGE) * gridDim.x, vec);
+          issued++;
+        } else {
+          *(volatile int*)err = 1;
+        }
+      }
+      __syncwarp();
+    }
+    j++;
+  }
+  // all threads, after the loop; false if a wait gave up (the copies still
+  // in flight have been given bounded time to land)
+  __device__ __forceinline__ bool end() {
+    __syncthreads();
+    const bool bad = *(volatile int*)err != 0;
+    if (bad && threadIdx.x == 0)
+      for (int k = 0; k < issued; k++) {
+        const unsigned u = sq + (unsigned)k;
+        mbar_wait(&full[u % MINIM_NSTAGE], (u / MINIM_NSTAGE) & 1u, 5000000000ull);
+      }
+    sq += (unsigned)mine;
+    return !bad;
+  }
+};
+
 // ---------------------------------------------------------------------------
 // Team = one CTA
 // ---------------------------------------------------------------------------
 struct CtaTeam {
-  int tid, nthr;
+  // thread index and count come from special registers, never from memory
+  __device__ __forceinline__ int tid() const { return threadIdx.x; }
+  __device__ __forceinline__ int nthr() const { return blockDim.x; }
   double* red;  // shared scratch, >= (32 + 1) * MINIM_MAXRED doubles
   double* wide; // shared scratch, >= (8 + 1) * MINIM_WIDE doubles
   static constexpr bool kGrid = false;
@@ -142,16 +307,20 @@ struct CtaTeam {
   }
 };
 
+struct D4q {
+  double x, y, z, w;
+};
+
 // ---------------------------------------------------------------------------
 // Team = whole grid (cooperative launch), with a bounded software barrier
 // ---------------------------------------------------------------------------
 struct GridTeam {
-  int tid, nthr;
+  __device__ __forceinline__ int tid() const { return blockIdx.x * blockDim.x + threadIdx.x; }
+  __device__ __forceinline__ int nthr() const { return gridDim.x * blockDim.x; }
   double* red;            // shared scratch as in CtaTeam
   double* wide;           // shared scratch as in CtaTeam
   GridSyncState* bar;     // global
-  double* partials;       // global: 2 * gridDim.x * MINIM_WIDE partials, 2 * MINIM_WIDE
-                          // totals, then gridDim.x unsigned flags
+  double* partials;       // global: 2 * gridDim.x * MINIM_WIDE partials (double-buffered rows)
   int buf;                // partials double buffer index
   int* s_ok;              // shared flag
   unsigned int epoch;     // barriers passed in this launch (uniform)
@@ -160,13 +329,24 @@ struct GridTeam {
 
   __device__ __forceinline__ bool block0() const { return blockIdx.x == 0; }
   __device__ __forceinline__ bool ok() const { return *s_ok != 0; }
+  // records a failed wait: this block stops, the others stop at their next
+  // barrier (status TIMEOUT)
+  __device__ void fail() {
+    if (threadIdx.x == 0) {
+      atomicExch(&bar->err, 1);
+      *s_ok = 0;
+    }
+  }
 
-  // Bounded wait until *p reaches `want` (or an error was recorded).
-  __device__ bool wait_value(volatile unsigned int* p, unsigned int want) {
-    volatile int* verr = &bar->err;
+  // Bounded wait until the arrival counter reaches `want` (or an error was
+  // recorded by any block).
+  __device__ bool wait_count(unsigned int want) {
     unsigned long long t0 = 0;
-    while (*p < want) {
-      if (*verr) return false;
+    for (;;) {
+      unsigned int c;
+      asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(c) : "l"(&bar->count) : "memory");
+      if (c >= want) return true;
+      if (*(volatile int*)&bar->err) return false;
       const unsigned long long t = globaltimer_ns();
       if (t0 == 0) {
         t0 = t;
@@ -174,60 +354,81 @@ struct GridTeam {
         atomicExch(&bar->err, 1);
         return false;
       }
-      __nanosleep(32);
+      __nanosleep(20);
     }
-    return true;
   }
 
-  // Flag barrier with an optional reduction.  Every block publishes the
-  // barrier's epoch in its own flag (no contended atomics); block 0 waits for
-  // all flags in parallel, sums the blocks' K partials in a fixed order into
-  // the published totals, then releases the others by publishing the epoch.
-  // Every wait is bounded (kWaitLimitNs): a block that gives up records an
-  // error; later barriers see it and return at once, so the kernel always
-  // finishes (status TIMEOUT).
-  __device__ void arrive_release(int K, double* out) {
-    unsigned int* flags =
-        reinterpret_cast<unsigned int*>(partials + (size_t)2 * gridDim.x * MINIM_WIDE + 2 * MINIM_WIDE);
+  // Every block sums the K (<= 64) partials of all blocks' rows in block
+  // order, so all blocks hold bitwise the same totals without a second round
+  // trip: one double4 load per (block, 4 values) spread over the threads
+  // (all issued at once), butterflies across the lanes that share a column,
+  // then a fixed-order sum over warps through `wide` (free during barriers).
+  __device__ void sum_rows(const double* P, int K, double* out) {
+    const int nq = (K + 3) >> 2;  // double4 columns
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
-    double* P = partials + (size_t)buf * gridDim.x * MINIM_WIDE;
-    double* Rz = partials + (size_t)2 * gridDim.x * MINIM_WIDE + (size_t)buf * MINIM_WIDE;
-    const unsigned int ep = ++epoch;
-    __syncthreads();
-    const bool okb = *s_ok != 0;
-    __syncthreads();
-    if (okb) {
-      if (threadIdx.x == 0) {
-        __threadfence();
-        *(volatile unsigned int*)&flags[blockIdx.x] = ep;
+    const int nqp = nq <= 1 ? 1 : nq <= 2 ? 2 : nq <= 4 ? 4 : nq <= 8 ? 8 : 16;
+    const int q = threadIdx.x & (nqp - 1);
+    const int r0 = threadIdx.x / nqp, rs = blockDim.x / nqp;
+    const int G = gridDim.x;
+    // four consecutive partials of row b (L2, 2 x 16-byte loads)
+    auto ld = [&](int b) {
+      const double2* r = reinterpret_cast<const double2*>(P + (size_t)b * MINIM_WIDE) + 2 * q;
+      const double2 lo = __ldcg(r), hi = __ldcg(r + 1);
+      return D4q{lo.x, lo.y, hi.x, hi.y};
+    };
+    D4q acc{0.0, 0.0, 0.0, 0.0};
+    if (q < nq) {
+      int b = r0;
+      for (; b + 3 * rs < G; b += 4 * rs) {
+        const D4q v0 = ld(b), v1 = ld(b + rs), v2 = ld(b + 2 * rs), v3 = ld(b + 3 * rs);
+        acc.x += v0.x; acc.y += v0.y; acc.z += v0.z; acc.w += v0.w;
+        acc.x += v1.x; acc.y += v1.y; acc.z += v1.z; acc.w += v1.w;
+        acc.x += v2.x; acc.y += v2.y; acc.z += v2.z; acc.w += v2.w;
+        acc.x += v3.x; acc.y += v3.y; acc.z += v3.z; acc.w += v3.w;
       }
-      if (blockIdx.x == 0) {
-        bool okv = true;
-        for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x)
-          okv = wait_value((volatile unsigned int*)&flags[b], ep) && okv;
-        if (!okv) *s_ok = 0;
-        __threadfence();
-        __syncthreads();
-        if (*s_ok) {
-          for (int k = w; k < K; k += nw) {
-            double s = 0.0;
-            for (int b = lane; b < (int)gridDim.x; b += 32) s += __ldcg(&P[b * MINIM_WIDE + k]);
-            s = warp_sum(s);
-            if (lane == 0) Rz[k] = s;
-          }
-          __syncthreads();
-          if (threadIdx.x == 0) {
-            __threadfence();
-            *(volatile unsigned int*)&bar->gen = ep;
-          }
-        }
-      } else if (threadIdx.x == 0) {
-        if (!wait_value((volatile unsigned int*)&bar->gen, ep)) *s_ok = 0;
-        __threadfence();
+      for (; b < G; b += rs) {
+        const D4q v = ld(b);
+        acc.x += v.x; acc.y += v.y; acc.z += v.z; acc.w += v.w;
       }
     }
+    for (int off = 16; off >= nqp; off >>= 1) {
+      acc.x += __shfl_xor_sync(0xffffffffu, acc.x, off);
+      acc.y += __shfl_xor_sync(0xffffffffu, acc.y, off);
+      acc.z += __shfl_xor_sync(0xffffffffu, acc.z, off);
+      acc.w += __shfl_xor_sync(0xffffffffu, acc.w, off);
+    }
+    // columns of warp w: lanes 0 .. min(nqp, 32) - 1 (nqp <= 16)
+    if (lane < nqp && q < nq) {
+      double* d = wide + (size_t)w * MINIM_WIDE + 4 * q;
+      d[0] = acc.x; d[1] = acc.y; d[2] = acc.z; d[3] = acc.w;
+    }
     __syncthreads();
-    for (int k = threadIdx.x; k < K; k += blockDim.x) out[k] = __ldcg(&Rz[k]);
+    for (int k = threadIdx.x; k < K; k += blockDim.x) {
+      double t = 0.0;
+      for (int i = 0; i < nw; i++) t += wide[i * MINIM_WIDE + k];
+      out[k] = t;
+    }
+  }
+
+  // Counter barrier with an optional reduction.  Every block adds 1 to the
+  // launch's arrival counter after its partials are written (fence, then a
+  // fire-and-forget atomic), waits until all blocks have arrived at this
+  // barrier (epoch * gridDim.x arrivals), and then sums every block's K
+  // partials itself.  Every wait is bounded (kWaitLimitNs): a block that
+  // gives up records an error; later barriers see it and return at once, so
+  // the kernel always finishes (status TIMEOUT).
+  __device__ void arrive_release(int K, double* out) {
+    const double* P = partials + (size_t)buf * gridDim.x * MINIM_WIDE;
+    const unsigned int ep = ++epoch;
+    __syncthreads();
+    if (threadIdx.x == 0 && *s_ok) {
+      __threadfence();
+      atomicAdd(&bar->count, 1u);
+      if (!wait_count(ep * gridDim.x)) *s_ok = 0;
+      __threadfence();
+    }
+    __syncthreads();
+    if (*s_ok && K > 0) sum_rows(P, K, out);
     __syncthreads();
     buf ^= 1;
   }

@@ -60,6 +60,7 @@ struct PotPF {
   double fmag[MINIM_MAXF];
   double fnorm[MINIM_MAXF][3];
   double total_volume2;       // sum nodeVol^2 (PF_VOLUME)
+  int pf_dist;                // L2 prefetch distance of the stencil sweep (0 = none)
 };
 
 struct PotBAH {
@@ -149,6 +150,8 @@ struct InstDesc {
   double* GA;      // FP64 gradient accumulator (BarAndHinge scatter), or NULL
   double* xres;    // resident FP64 coordinates: read at start, written at the end
   MinScalars* st;
+  int stage_bytes; // grid launches: bytes of each shared staging buffer (0 = none)
+  int pf_dist;     // vector passes: L2 prefetch distance in sweep steps (0 = none)
 };
 
 // Bounded software grid barrier state (one per cooperative launch).

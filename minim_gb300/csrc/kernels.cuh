@@ -18,10 +18,12 @@ struct SharedScalars {
   double wide[8 * MINIM_WIDE];
   double wout[MINIM_WIDE];
   double SY[MINIM_MAXM * MINIM_MAXM], YY[MINIM_MAXM * MINIM_MAXM];
-  double coefS[MINIM_MAXM], coefY[MINIM_MAXM];
+  float coefS[MINIM_MAXM], coefY[MINIM_MAXM];
   long long boff[2 * MINIM_MAXM];
   double rho[MINIM_MAXM], sig[MINIM_MAXM], yy[MINIM_MAXM], alpha[MINIM_MAXM];
   int sidx[MINIM_MAXM], yidx[MINIM_MAXM];
+  unsigned long long mbar[MINIM_NSTAGE], mbar_empty[MINIM_NSTAGE];
+  int stage_err;
   int next, ok, last;
 };
 
@@ -39,6 +41,10 @@ __device__ void setup_runner(Runner<Team, KIND>& R, SharedScalars& S, const Inst
   R.sidx = S.sidx; R.yidx = S.yidx;
   R.SY = S.SY; R.YY = S.YY; R.wout = S.wout; R.coefS = S.coefS; R.coefY = S.coefY;
   R.boff = S.boff;
+  R.mbar = S.mbar;
+  R.mbar_empty = S.mbar_empty;
+  R.stage_err = &S.stage_err;
+  R.sq = 0u;
 }
 
 template <int KIND>
@@ -54,7 +60,7 @@ batch_kernel(const InstDesc* __restrict__ insts, int ninst, int* counter, int sl
     if (k >= ninst) break;
     copy_desc(&s_in, &insts[k]);
     __syncthreads();
-    CtaTeam tm{(int)threadIdx.x, (int)blockDim.x, S.red, S.wide};
+    CtaTeam tm{S.red, S.wide};
     Runner<CtaTeam, KIND> R{tm, s_in, dyn, lj_tile};
     setup_runner(R, S, s_in);
     R.load(*s_in.st);
@@ -84,7 +90,7 @@ template <class Team, int KIND>
 __device__ void constrain_op(Team& tm, const InstDesc& in, const EvalIO& io) {
   double* v = io.v;
   if (in.fixed)
-    for (int i = tm.tid; i < in.ndof; i += tm.nthr)
+    for (int i = tm.tid(); i < in.ndof; i += tm.nthr())
       if (in.fixed[i]) v[i] = 0.0;
   if constexpr (KIND == K_PF) {
     if (in.pf.flags & (PF_FIXFLUID | PF_HARD)) {
@@ -106,9 +112,17 @@ grid_kernel(const InstDesc* __restrict__ inst, int op, const EvalIO* io, int sli
   __shared__ __align__(16) InstDesc s_in;
   extern __shared__ __align__(16) unsigned char dyn[];
   copy_desc(&s_in, inst);
-  if (threadIdx.x == 0) S.ok = 1;
+  if (threadIdx.x == 0) {
+    S.ok = 1;
+    for (int k = 0; k < MINIM_NSTAGE; k++) {
+      mbar_init(&S.mbar[k], 1);
+      mbar_init(&S.mbar_empty[k], (blockDim.x + 31) >> 5);
+    }
+    S.stage_err = 0;
+    mbar_init_fence();
+  }
   __syncthreads();
-  GridTeam tm{(int)(blockIdx.x * blockDim.x + threadIdx.x), (int)(gridDim.x * blockDim.x), S.red,
+  GridTeam tm{S.red,
               S.wide, bar, partials, 0, &S.ok, 0u};
   Runner<GridTeam, KIND> R{tm, s_in, dyn, lj_tile};
   setup_runner(R, S, s_in);
@@ -128,6 +142,15 @@ grid_kernel(const InstDesc* __restrict__ inst, int op, const EvalIO* io, int sli
 // Instantiates the kernels for one potential kind and defines its launchers
 // (mg_launch_batch_<name>, mg_launch_grid_<name>, occupancy queries).
 #define MG_DEFINE_LAUNCHERS(KIND, NAME)                                                          \
+  /* opts the grid kernel in to more than 48 KB of dynamic shared memory */                      \
+  static void mg_grid_smem_##NAME(size_t smem) {                                                  \
+    static size_t done = 0;                                                                       \
+    if (smem > done) {                                                                            \
+      cudaFuncSetAttribute((const void*)mg::grid_kernel<KIND>,                                    \
+                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);               \
+      done = smem;                                                                                \
+    }                                                                                             \
+  }                                                                                               \
   extern "C" int mg_launch_batch_##NAME(const mg::InstDesc* d_insts, int ninst, int* d_counter,   \
                                         int slice_iters, int threads, int blocks, size_t smem,    \
                                         void* stream) {                                           \
@@ -141,12 +164,14 @@ grid_kernel(const InstDesc* __restrict__ inst, int op, const EvalIO* io, int sli
                                        double* d_partials, int threads, int blocks, size_t smem,  \
                                        void* stream) {                                            \
     int tile = (int)(smem / sizeof(mg::D4));                                                      \
+    mg_grid_smem_##NAME(smem);                                                                    \
     void* args[] = {(void*)&d_inst, (void*)&op,         (void*)&d_io, (void*)&slice_iters,        \
                     (void*)&d_bar,  (void*)&d_partials, (void*)&tile};                            \
     return (int)cudaLaunchCooperativeKernel((const void*)mg::grid_kernel<KIND>, dim3(blocks),     \
                                             dim3(threads), args, smem, (cudaStream_t)stream);     \
   }                                                                                               \
   extern "C" int mg_occupancy_##NAME(int grid, int threads, size_t smem, int* blocks_per_sm) {    \
+    if (grid) mg_grid_smem_##NAME(smem);                                                          \
     return grid ? (int)cudaOccupancyMaxActiveBlocksPerMultiprocessor(                             \
                       blocks_per_sm, mg::grid_kernel<KIND>, threads, smem)                        \
                 : (int)cudaOccupancyMaxActiveBlocksPerMultiprocessor(                             \

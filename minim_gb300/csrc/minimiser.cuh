@@ -47,8 +47,23 @@ struct FusedEmit {
       yy.add(y * y);
     }
   }
-  // four consecutive DOFs 4*i4 .. 4*i4+3 (16-byte aligned)
-  __device__ __forceinline__ void emit4(int i4, float4 g) {
+  // four consecutive DOFs 4*i4 .. 4*i4+3 (16-byte aligned); pre4 loads
+  // the old gradient and the direction ahead of the stencil's arithmetic
+  struct Pre4 {
+    float4 go, p;
+  };
+  __device__ __forceinline__ void prefetch4(int i4) const {
+    if (Y) prefetch_line(Gold, i4);
+  }
+  __device__ __forceinline__ Pre4 pre4(int i4) const {
+    Pre4 r{};
+    if (Y) {
+      r.go = ld4(Gold, i4);
+      r.p = ld4(P, i4);
+    }
+    return r;
+  }
+  __device__ __forceinline__ void emit4(int i4, float4 g, const Pre4& pre) {
     if (fixed) {
       const int i = 4 * i4;
       if (fixed[i]) g.x = 0.f;
@@ -59,10 +74,10 @@ struct FusedEmit {
     st4(G, i4, g);
     gg.add(dot4(g, g));
     if (Y) {
-      const float4 go = ld4(Gold, i4);
+      const float4 go = pre.go;
       const float4 y = make_float4(g.x - go.x, g.y - go.y, g.z - go.z, g.w - go.w);
       st4(Y, i4, y);
-      py.add(dot4(ld4(P, i4), y));
+      py.add(dot4(pre.p, y));
       yy.add(dot4(y, y));
     }
   }
@@ -93,8 +108,13 @@ struct Runner {
   // shared arrays (one copy per block; written by thread 0 between barriers)
   double *rho, *sig, *yy, *alpha;
   int *sidx, *yidx;
-  double *SY, *YY, *wout, *coefS, *coefY;  // m x m matrices, reduction out, pass coefficients
+  double *SY, *YY, *wout;  // m x m matrices, reduction out
+  float *coefS, *coefY;     // pass-B coefficients (FP32: no conversion per element)
   long long* boff;                         // history buffer offsets of the slots in order
+  unsigned long long* mbar;                // stage "full" barriers (grid team, shared)
+  unsigned long long* mbar_empty;          // stage "empty" barriers
+  int* stage_err;                          // shared: a stage wait gave up
+  unsigned sq;                             // stage uses so far in this launch (uniform)
 
   __device__ float* Sbuf(int b) const { return in.Sb + (size_t)b * in.hstride; }
   __device__ float* Ybuf(int b) const { return in.Yb + (size_t)b * in.hstride; }
@@ -170,7 +190,7 @@ struct Runner {
       if constexpr (KIND == K_PF) pf_volume_project<float>(tm, in.pf, Gn);
       const float* Go = in.G[gi];
       float* Y = want_y ? Ybuf(ybuf) : nullptr;
-      for (int i = tm.tid; i < n; i += tm.nthr) {
+      for (int i = tm.tid(); i < n; i += tm.nthr()) {
         const float g = Gn[i];
         em.gg.add(g * g);
         if (Y) {
@@ -219,8 +239,8 @@ struct Runner {
   __device__ double dot_gP(const float* P) {
     const float* G = in.G[gi];
     Acc d;
-    for (int i = tm.tid; i < n4(); i += tm.nthr) d.add(dot4(ld4(G, i), ld4(P, i)));
-    for (int i = 4 * n4() + tm.tid; i < n; i += tm.nthr) d.add(G[i] * P[i]);
+    for (int i = tm.tid(); i < n4(); i += tm.nthr()) d.add(dot4(ld4(G, i), ld4(P, i)));
+    for (int i = 4 * n4() + tm.tid(); i < n; i += tm.nthr()) d.add(G[i] * P[i]);
     double v[1] = {d.total()};
     tm.reduce(v);
     return v[0];
@@ -229,7 +249,7 @@ struct Runner {
   // State::applyConstraints on the direction P, then returns g.P
   __device__ double constrain_dir(float* P) {
     if (in.fixed) {
-      for (int i = tm.tid; i < n; i += tm.nthr)
+      for (int i = tm.tid(); i < n; i += tm.nthr())
         if (in.fixed[i]) P[i] = 0.f;
     }
     if constexpr (KIND == K_PF) {
@@ -249,6 +269,9 @@ struct Runner {
   // backtrackingLinesearch: the step is t0 * P with g.step = gs <= 0.
   // Returns the accepted multiplier (t0 * tau^k, or t0 * tau^10 when no
   // trial passed -- that last point is taken without being evaluated).
+  // `exhausted` (for the precision policy only) reports that no trial
+  // passed or that one passed only after 8 or more halvings: the energy no
+  // longer resolves the decrease the gradient predicts.
   __device__ double linesearch(const float* P, double t0, double gs, bool& exhausted) {
     const double c = 0.5, tau = 0.5;
     double thr = -c * gs;
@@ -258,7 +281,7 @@ struct Runner {
     for (int k = 0; k < 10; k++) {
       const double e = energy_at(t, P);
       if (!tm.ok()) return t;
-      if (e0 - e >= thr) { exhausted = false; break; }
+      if (e0 - e >= thr) { exhausted = k >= 8; break; }
       t = t * tau;
       thr = thr * tau;
     }
@@ -283,11 +306,11 @@ struct Runner {
     const float* G = in.G[gi];
     const int m = in.mp.m;
     if (ii == 0) {
-      for (int i = tm.tid; i < n4(); i += tm.nthr) {
+      for (int i = tm.tid(); i < n4(); i += tm.nthr()) {
         const float4 g = ld4(G, i);
         st4(P, i, make_float4(-g.x, -g.y, -g.z, -g.w));
       }
-      for (int i = 4 * n4() + tm.tid; i < n; i += tm.nthr) P[i] = -G[i];
+      for (int i = 4 * n4() + tm.tid(); i < n; i += tm.nthr()) P[i] = -G[i];
       tm.sync();
       abytes += 8.0 * n;
       const double gn = sqrt(gg);
@@ -298,12 +321,80 @@ struct Runner {
     const int mt = ii < m ? ii : m;
     const int c = ii % m;
     const int kn = (c - 1 + m) % m;  // newest slot
-    const long long hs = in.hstride;
     abytes += (4.0 * mt + 2.0) * 4.0 * n;
-    // pass A, 8 slots per sweep: S_k.g, Y_k.g and, for a new pair,
-    // S_k.y_new, Y_k.y_new; value index = dot * 16 + slot order
     const bool np = pend >= 0;
+    const bool staged = stage_chunk(2 + 2 * mt) > 0;
+    if (staged) pass_a_staged(G, mt, c, np);
+    else pass_a_plain(G, mt, c, np);
+    if (!tm.ok()) return 1.0;
+    direction_algebra(mt, c, kn, np);
+    pend = -1;
+    double v[2];
+    if (staged && stage_chunk(1 + 2 * mt) > 0) pass_b_staged(G, P, mt, v);
+    else pass_b_plain(G, P, mt, v);
+    tm.reduce(v);
+    gp = v[0];
+    double scale = 1.0;
+    if (in.mp.max_step != 0) {
+      const double ss = sqrt(v[1]);
+      if (ss > in.mp.max_step) scale = in.mp.max_step / ss;
+    }
+    gp *= scale;
+    return scale;
+  }
+
+  // slot (in age order k = 0 .. mt-1, oldest first) of the history ring
+  __device__ __forceinline__ int slot_of(int k, int mt, int c) const {
+    const int m = in.mp.m;
+    return (c - mt + k + 2 * m) % m;
+  }
+
+  // ---- staging of vector passes through shared memory (grid team) ------------------
+  // Chunk length for nv vectors: the largest multiple of 64 floats whose nv
+  // rows fit one stage (0 = the passes read global memory directly).
+  __device__ int stage_chunk(int nv) const {
+    if constexpr (!Team::kGrid) {
+      return 0;
+    } else {
+      if (in.stage_bytes <= 0) return 0;
+      const int ch = (in.stage_bytes / (4 * nv)) & ~63;
+      return ch >= 64 ? ch : 0;
+    }
+  }
+  __device__ StageRing make_ring(int nv) const {
+    StageRing r;
+    r.base = static_cast<char*>(smem_pot);
+    r.full = mbar;
+    r.empty = mbar_empty;
+    r.err = stage_err;
+    r.stage_bytes = in.stage_bytes;
+    r.n = n;
+    r.nv = nv;
+    r.ch = stage_chunk(nv);
+    r.sq = sq;
+    r.mine = r.j = r.issued = 0;
+    return r;
+  }
+  // after a staged sweep: keep the use count, stop the team on a failed wait
+  __device__ void ring_done(StageRing& r) {
+    const bool ok = r.end();
+    sq = r.sq;
+    if (!ok) {
+      tm.fail();
+      __syncthreads();
+    }
+  }
+
+  // pass A: S_k.g, Y_k.g and, for a new pair, S_k.y_new, Y_k.y_new;
+  // value index = dot * 16 + slot order (oldest first)
+  __device__ __noinline__ void pass_a_plain(const float* G, int mt, int c, bool np) {
+    // everything the loops use is held in registers (no member access
+    // through memory inside them)
+    const long long hs = in.hstride;
+    const int nn = n, nq4 = n >> 2, t0 = tm.tid(), nt = tm.nthr(), pd = in.pf_dist * nt;
     const float* Yn = np ? Ybuf(yidx[pend]) : nullptr;
+    const float* Sb = in.Sb;
+    const float* Yb = in.Yb;
     tm.wide_clear();
     for (int k0 = 0; k0 < mt; k0 += 8) {
       const float* Sp[8];
@@ -311,19 +402,31 @@ struct Runner {
 #pragma unroll
       for (int j = 0; j < 8; j++) {
         const int k = k0 + j;
-        const int s = (c - mt + k + 2 * m) % m;
-        Sp[j] = in.Sb + ((k < mt) ? sidx[s] : 0) * hs;
-        Yp[j] = in.Yb + ((k < mt) ? yidx[s] : 0) * hs;
+        const int s = slot_of(k, mt, c);
+        Sp[j] = Sb + ((k < mt) ? sidx[s] : 0) * hs;
+        Yp[j] = Yb + ((k < mt) ? yidx[s] : 0) * hs;
       }
+      const int nk = min(8, mt - k0);
       float acc[32];
 #pragma unroll
       for (int k = 0; k < 32; k++) acc[k] = 0.f;
-      for (int i = tm.tid; i < n4(); i += tm.nthr) {
+      for (int i = t0; i < nq4; i += nt) {
+        const int ip = i + pd;  // pf_dist sweep steps ahead: fetch into L2 now
+        if (pd > 0 && ip < nq4) {
+          prefetch_line(G, ip);
+          if (np) prefetch_line(Yn, ip);
+#pragma unroll
+          for (int j = 0; j < 8; j++)
+            if (j < nk) {
+              prefetch_line(Sp[j], ip);
+              prefetch_line(Yp[j], ip);
+            }
+        }
         const float4 g = ld4(G, i);
         const float4 yn = np ? ld4(Yn, i) : make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
         for (int j = 0; j < 8; j++) {
-          if (k0 + j < mt) {
+          if (j < nk) {
             const float4 s = ld4(Sp[j], i);
             const float4 y = ld4(Yp[j], i);
             acc[j] += dot4(s, g);
@@ -333,12 +436,12 @@ struct Runner {
           }
         }
       }
-      for (int i = 4 * n4() + tm.tid; i < n; i += tm.nthr) {
+      for (int i = 4 * nq4 + t0; i < nn; i += nt) {
         const float g = G[i];
         const float yn = np ? Yn[i] : 0.f;
 #pragma unroll
         for (int j = 0; j < 8; j++) {
-          if (k0 + j < mt) {
+          if (j < nk) {
             const float s = Sp[j][i], y = Yp[j][i];
             acc[j] += s * g;
             acc[8 + j] += y * g;
@@ -350,7 +453,81 @@ struct Runner {
       tm.wide_store32(acc, k0);
     }
     tm.wide_combine(4 * MINIM_MAXM, wout);
-    // small dense algebra in one thread per block (bitwise the same in all)
+  }
+
+  // pass A through shared memory: vectors g, y_new (when np), S_0..S_mt-1,
+  // Y_0..Y_mt-1 arrive chunk by chunk; all 4 mt sums stay in registers
+  __device__ __noinline__ void pass_a_staged(const float* G, int mt, int c, bool np) {
+    if constexpr (Team::kGrid) {
+      const long long hs = in.hstride;
+      const float* Yn = np ? Ybuf(yidx[pend]) : G;
+      const int nv = 2 + 2 * mt;
+      auto vec = [&](int v) -> const float* {
+        if (v == 0) return G;
+        if (v == 1) return Yn;
+        if (v < 2 + mt) return in.Sb + (long long)sidx[slot_of(v - 2, mt, c)] * hs;
+        return in.Yb + (long long)yidx[slot_of(v - 2 - mt, mt, c)] * hs;
+      };
+      // the block's threads split into one part per group of 8 slots; a
+      // part's threads hold that group's 32 sums (no more live registers
+      // than one group needs)
+      const int ng = (mt + 7) >> 3;
+      const int part_size = blockDim.x / ng;
+      const int part = min((int)threadIdx.x / part_size, ng - 1);
+      const int k0 = 8 * part;
+      const int pt = threadIdx.x - part * part_size;
+      float a0[8], a1[8], a2[8], a3[8];
+#pragma unroll
+      for (int k = 0; k < 8; k++) a0[k] = a1[k] = a2[k] = a3[k] = 0.f;
+      StageRing rg = make_ring(nv);
+      rg.begin(tm.ok(), vec);
+      const int ch = rg.ch;
+      while (rg.j < rg.mine) {
+        const float* sb = rg.acquire();
+        if (!sb) break;
+        if ((int)threadIdx.x < ng * part_size) {
+          const int cnt = rg.count();
+          for (int i = pt; i < cnt; i += part_size) {
+            const float g = sb[i];
+            const float yn = np ? sb[ch + i] : 0.f;
+#pragma unroll
+            for (int k = 0; k < 8; k++) {
+              if (k0 + k < mt) {
+                const float sv = sb[(2 + k0 + k) * ch + i];
+                const float yv = sb[(2 + mt + k0 + k) * ch + i];
+                a0[k] = fmaf(sv, g, a0[k]);
+                a1[k] = fmaf(yv, g, a1[k]);
+                a2[k] = fmaf(sv, yn, a2[k]);
+                a3[k] = fmaf(yv, yn, a3[k]);
+              }
+            }
+          }
+        }
+        rg.release(vec);
+      }
+      ring_done(rg);
+      tm.wide_clear();
+      {
+        float v[32];
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+          v[j] = a0[j];
+          v[8 + j] = a1[j];
+          v[16 + j] = a2[j];
+          v[24 + j] = a3[j];
+        }
+        tm.wide_store32(v, k0);
+      }
+      tm.wide_combine(4 * MINIM_MAXM, wout);
+    }
+  }
+
+  // small dense algebra in one thread per block (bitwise the same in all):
+  // R u = S^T g, R^T w = (D + gamma Y^T Y) u - gamma Y^T g, coefficients of
+  // P = -(gamma g + S w - gamma Y u)
+  __device__ __noinline__ void direction_algebra(int mt, int c, int kn, bool np) {
+    const int m = in.mp.m;
+    const long long hs = in.hstride;
     if (threadIdx.x == 0) {
       double sg[MINIM_MAXM], yg[MINIM_MAXM], u[MINIM_MAXM], w[MINIM_MAXM];
       int sl[MINIM_MAXM];
@@ -379,52 +556,120 @@ struct Runner {
         w[a] = t / SY[sl[a] * MINIM_MAXM + sl[a]];
       }
       for (int k = 0; k < MINIM_MAXM; k++) {
-        coefS[k] = (k < mt) ? -w[k] * sig[sl[k]] : 0.0;
-        coefY[k] = (k < mt) ? gamma * u[k] : 0.0;
+        coefS[k] = (k < mt) ? (float)(-w[k] * sig[sl[k]]) : 0.f;
+        coefY[k] = (k < mt) ? (float)(gamma * u[k]) : 0.f;
         boff[k] = (k < mt) ? (long long)sidx[sl[k]] * hs : 0;
         boff[MINIM_MAXM + k] = (k < mt) ? (long long)yidx[sl[k]] * hs : 0;
       }
       wout[MINIM_WIDE - 1] = gamma;
     }
     __syncthreads();
-    pend = -1;
+  }
+
+  // pass B: P = -(gamma g + S w - gamma Y u), with g.P and P.P; the slot
+  // buffers and coefficients are read from shared memory (broadcast)
+  __device__ __noinline__ void pass_b_plain(const float* G, float* P, int mt, double (&v)[2]) {
+    const int nn = n, nq4 = n >> 2, t0 = tm.tid(), nt = tm.nthr(), pd = in.pf_dist * nt;
     const float fg = (float)(-wout[MINIM_WIDE - 1]);
-    // pass B: P = -(gamma g + S w - gamma Y u), with g.P and P.P; the slot
-    // buffers and coefficients are read from shared memory (broadcast)
+    // slot buffers as 32-bit float4 offsets from the ring bases (the host
+    // keeps (m + 1) * hstride below 2^33 floats)
+    const float4* Sb4 = reinterpret_cast<const float4*>(in.Sb);
+    const float4* Yb4 = reinterpret_cast<const float4*>(in.Yb);
+    unsigned so[MINIM_MAXM], yo[MINIM_MAXM];
+    float cS[MINIM_MAXM], cY[MINIM_MAXM];
+#pragma unroll
+    for (int k = 0; k < MINIM_MAXM; k++) {
+      so[k] = (unsigned)(boff[k] >> 2);
+      yo[k] = (unsigned)(boff[MINIM_MAXM + k] >> 2);
+      cS[k] = coefS[k];
+      cY[k] = coefY[k];
+    }
     Acc d1, d2;
-    for (int i = tm.tid; i < n4(); i += tm.nthr) {
+    for (int i = t0; i < nq4; i += nt) {
+      const int ip = i + pd;  // pf_dist sweep steps ahead: fetch into L2 now
+      if (pd > 0 && ip < nq4) {
+        prefetch_line(G, ip);
+#pragma unroll
+        for (int k = 0; k < MINIM_MAXM; k++)
+          if (k < mt) {
+            prefetch_line(reinterpret_cast<const float*>(Sb4 + so[k]), ip);
+            prefetch_line(reinterpret_cast<const float*>(Yb4 + yo[k]), ip);
+          }
+      }
       const float4 g = ld4(G, i);
       float4 q = make_float4(fg * g.x, fg * g.y, fg * g.z, fg * g.w);
-#pragma unroll 4
-      for (int k = 0; k < mt; k++) {
-        q = axpy4((float)coefS[k], ld4(in.Sb + boff[k], i), q);
-        q = axpy4((float)coefY[k], ld4(in.Yb + boff[MINIM_MAXM + k], i), q);
+#pragma unroll
+      for (int k = 0; k < MINIM_MAXM; k++) {
+        if (k < mt) {
+          q = axpy4(cS[k], Sb4[so[k] + i], q);
+          q = axpy4(cY[k], Yb4[yo[k] + i], q);
+        }
       }
       st4(P, i, q);
       d1.add(dot4(q, g));
       d2.add(dot4(q, q));
     }
-    for (int i = 4 * n4() + tm.tid; i < n; i += tm.nthr) {
+    for (int i = 4 * nq4 + t0; i < nn; i += nt) {
       const float g = G[i];
       float q = fg * g;
       for (int k = 0; k < mt; k++) {
-        q += (float)coefS[k] * in.Sb[boff[k] + i];
-        q += (float)coefY[k] * in.Yb[boff[MINIM_MAXM + k] + i];
+        q += cS[k] * in.Sb[boff[k] + i];
+        q += cY[k] * in.Yb[boff[MINIM_MAXM + k] + i];
       }
       P[i] = q;
       d1.add(q * g);
       d2.add(q * q);
     }
-    double v[2] = {d1.total(), d2.total()};
-    tm.reduce(v);
-    gp = v[0];
-    double scale = 1.0;
-    if (in.mp.max_step != 0) {
-      const double ss = sqrt(v[1]);
-      if (ss > in.mp.max_step) scale = in.mp.max_step / ss;
+    v[0] = d1.total();
+    v[1] = d2.total();
+  }
+
+  // pass B through shared memory: g, S_0..S_mt-1, Y_0..Y_mt-1 arrive chunk by
+  // chunk; P is written straight to global memory
+  __device__ __noinline__ void pass_b_staged(const float* G, float* P, int mt, double (&v)[2]) {
+    if constexpr (Team::kGrid) {
+      const int nv = 1 + 2 * mt;
+      auto vec = [&](int k) -> const float* {
+        if (k == 0) return G;
+        if (k < 1 + mt) return in.Sb + boff[k - 1];
+        return in.Yb + boff[MINIM_MAXM + k - 1 - mt];
+      };
+      const float fg = (float)(-wout[MINIM_WIDE - 1]);
+      float cS[MINIM_MAXM], cY[MINIM_MAXM];
+#pragma unroll
+      for (int k = 0; k < MINIM_MAXM; k++) {
+        cS[k] = coefS[k];
+        cY[k] = coefY[k];
+      }
+      Acc d1, d2;
+      StageRing rg = make_ring(nv);
+      rg.begin(tm.ok(), vec);
+      const int ch = rg.ch;
+      while (rg.j < rg.mine) {
+        const float* sb = rg.acquire();
+        if (!sb) break;
+        const int i0 = rg.i0();
+        const int cnt = rg.count();
+        for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
+          const float g = sb[i];
+          float q = fg * g;
+#pragma unroll
+          for (int k = 0; k < MINIM_MAXM; k++) {
+            if (k < mt) {
+              q = fmaf(cS[k], sb[(1 + k) * ch + i], q);
+              q = fmaf(cY[k], sb[(1 + mt + k) * ch + i], q);
+            }
+          }
+          P[i0 + i] = q;
+          d1.add(q * g);
+          d2.add(q * q);
+        }
+        rg.release(vec);
+      }
+      ring_done(rg);
+      v[0] = d1.total();
+      v[1] = d2.total();
     }
-    gp *= scale;
-    return scale;
   }
 
   __device__ void lbfgs_iteration(bool& exhausted) {
@@ -479,13 +724,14 @@ struct Runner {
     }
     const float* G = in.G[gi];
     float* Vv = in.V;
+    const int nn = n, nq4 = n >> 2, t0 = tm.tid(), nt = tm.nthr();
     Acc d1, d2;
-    for (int i = tm.tid; i < n4(); i += tm.nthr) {
+    for (int i = t0; i < nq4; i += nt) {
       const float4 v = ld4(Vv, i);
       d1.add(dot4(v, ld4(G, i)));
       d2.add(dot4(v, v));
     }
-    for (int i = 4 * n4() + tm.tid; i < n; i += tm.nthr) {
+    for (int i = 4 * nq4 + t0; i < nn; i += nt) {
       const float v = Vv[i];
       d1.add(v * G[i]);
       d2.add(v * v);
@@ -517,7 +763,7 @@ struct Runner {
     const float f1 = (float)c1, f2 = (float)c2, fdt = (float)dt;
     const bool mix = p > 0;
     Acc dg;
-    for (int i = tm.tid; i < n4(); i += tm.nthr) {
+    for (int i = t0; i < nq4; i += nt) {
       const float4 g = ld4(G, i);
       const float4 vo = ld4(Vv, i);
       float4 v;
@@ -530,7 +776,7 @@ struct Runner {
       st4(P, i, s);
       dg.add(dot4(g, s));
     }
-    for (int i = 4 * n4() + tm.tid; i < n; i += tm.nthr) {
+    for (int i = 4 * nq4 + t0; i < nn; i += nt) {
       const float v = mix ? f1 * Vv[i] - f2 * G[i] : -f2 * G[i];
       Vv[i] = v;
       const float s = fdt * v;
@@ -567,11 +813,11 @@ struct Runner {
     if (stage == 0) {
       CView<float> cv{in.X32[xi], G, (float)t};
       float* Xn = in.X32[1 - xi];
-      for (int i = tm.tid; i < n; i += tm.nthr) Xn[i] = cv(i);
+      for (int i = tm.tid(); i < n; i += tm.nthr()) Xn[i] = cv(i);
     } else {
       CView<double> cv{in.X64[xi], G, t};
       double* Xn = in.X64[1 - xi];
-      for (int i = tm.tid; i < n; i += tm.nthr) Xn[i] = cv(i);
+      for (int i = tm.tid(); i < n; i += tm.nthr()) Xn[i] = cv(i);
     }
     xi = 1 - xi;
     tm.sync();
@@ -582,7 +828,7 @@ struct Runner {
   __device__ void to_fp64() {
     const float* X = in.X32[xi];
     double* X64 = in.X64[xi];
-    for (int i = tm.tid; i < n; i += tm.nthr) X64[i] = (double)X[i];
+    for (int i = tm.tid(); i < n; i += tm.nthr()) X64[i] = (double)X[i];
     tm.sync();
     abytes += 12.0 * n;
     stage = 1;
@@ -590,7 +836,7 @@ struct Runner {
   __device__ void to_fp32() {
     const double* X64 = in.X64[xi];
     float* X = in.X32[xi];
-    for (int i = tm.tid; i < n; i += tm.nthr) X[i] = (float)X64[i];
+    for (int i = tm.tid(); i < n; i += tm.nthr()) X[i] = (float)X64[i];
     tm.sync();
     abytes += 12.0 * n;
     stage = 0;
@@ -659,7 +905,7 @@ struct Runner {
         const double* xr = in.xres;
         float* X32 = in.X32[0];
         double* X64 = in.X64[0];
-        for (int i = tm.tid; i < n; i += tm.nthr) {
+        for (int i = tm.tid(); i < n; i += tm.nthr()) {
           const double v = xr[i];
           X32[i] = (float)v;
           if (X64) X64[i] = v;
@@ -679,7 +925,7 @@ struct Runner {
         pend = -1;
         __syncthreads();
       } else if (mp.method == 1) {
-        for (int i = tm.tid; i < n; i += tm.nthr) in.V[i] = 0.f;
+        for (int i = tm.tid(); i < n; i += tm.nthr()) in.V[i] = 0.f;
         tm.sync();
         a = 0.1; nsteps = 0;
         dtmax = mp.dt_max;
@@ -771,10 +1017,10 @@ struct Runner {
       double* xr = in.xres;
       if (stage == 1) {
         const double* X = in.X64[xi];
-        for (int i = tm.tid; i < n; i += tm.nthr) xr[i] = X[i];
+        for (int i = tm.tid(); i < n; i += tm.nthr()) xr[i] = X[i];
       } else {
         const float* X = in.X32[xi];
-        for (int i = tm.tid; i < n; i += tm.nthr) xr[i] = (double)X[i];
+        for (int i = tm.tid(); i < n; i += tm.nthr()) xr[i] = (double)X[i];
       }
       tm.sync();
     }

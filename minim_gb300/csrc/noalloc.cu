@@ -54,7 +54,7 @@ __global__ void __launch_bounds__(256, 2) noalloc_lj_kernel(InstDesc d, int slic
   extern __shared__ __align__(16) unsigned char dyn[];
   if (threadIdx.x == 0) s_in = d;
   __syncthreads();
-  CtaTeam tm{(int)threadIdx.x, (int)blockDim.x, S.red, S.wide};
+  CtaTeam tm{S.red, S.wide};
   Runner<CtaTeam, K_LJ> R{tm, s_in, dyn, lj_tile};
   setup_runner(R, S, s_in);
   R.load(*s_in.st);

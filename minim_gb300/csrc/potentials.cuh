@@ -73,14 +73,14 @@ __device__ __noinline__ double lj_eval(Team& tm, const PotLJ& P, CView<T> cv, T*
   const int N = P.np, nd = P.ndim;
   const T s6 = (T)P.s6;
   if (xw) {
-    for (int i = tm.tid; i < N * nd; i += tm.nthr) xw[i] = cv(i);
+    for (int i = tm.tid(); i < N * nd; i += tm.nthr()) xw[i] = cv(i);
   }
   EAcc<T> e;
-  const int step = tm.nthr;
+  const int step = tm.nthr();
   // every thread of every block runs the same number of outer rounds
   const int rounds = (N + step - 1) / step;
   for (int r = 0; r < rounds; r++) {
-    const int i = r * step + tm.tid;
+    const int i = r * step + tm.tid();
     const bool act = i < N;
     T xi = 0, yi = 0, zi = 0;
     if (act) {
@@ -278,7 +278,7 @@ __device__ __noinline__ double pf_eval(Team& tm, const PotPF& P, CView<T> cv, T*
   const unsigned fl = P.flags;
   const T res2 = (T)P.res2;
   EAcc<T> e;
-  for (int iG = tm.tid; iG < ng; iG += tm.nthr) {
+  for (int iG = tm.tid(); iG < ng; iG += tm.nthr()) {
     const int z = iG % nz, y = (iG / nz) % ny, x = iG / (ny * nz);
     int nb[6];
     nb[0] = ((x == 0 ? nx - 1 : x - 1) * ny + y) * nz + z;
@@ -483,11 +483,21 @@ __device__ __forceinline__ void st_quad(double* x, int i4, const Quad<double>& q
   reinterpret_cast<double2*>(x)[2 * i4] = make_double2(q.v[0], q.v[1]);
   reinterpret_cast<double2*>(x)[2 * i4 + 1] = make_double2(q.v[2], q.v[3]);
 }
-// hand four gradient values to an emitter (vector store when it has one)
-template <class Emit, typename T>
-__device__ __forceinline__ void emit_quad(Emit& em, int i4, const T (&g)[4]) {
-  if constexpr (requires { em.emit4(i4, float4{}); }) {
-    em.emit4(i4, make_float4((float)g[0], (float)g[1], (float)g[2], (float)g[3]));
+// Loads an emitter needs for four values (issued with the stencil's loads),
+// and hands four gradient values to it (vector store when it has one).
+struct NoPre {};
+template <class Emit>
+__device__ __forceinline__ auto emit_pre(const Emit& em, int i4, bool want_g) {
+  if constexpr (requires { em.pre4(i4); }) {
+    return want_g ? em.pre4(i4) : decltype(em.pre4(i4)){};
+  } else {
+    return NoPre{};
+  }
+}
+template <class Emit, typename T, class Pre>
+__device__ __forceinline__ void emit_quad(Emit& em, int i4, const T (&g)[4], const Pre& pre) {
+  if constexpr (requires { em.emit4(i4, float4{}, pre); }) {
+    em.emit4(i4, make_float4((float)g[0], (float)g[1], (float)g[2], (float)g[3]), pre);
   } else {
 #pragma unroll
     for (int k = 0; k < 4; k++) em(4 * i4 + k, g[k]);
@@ -509,43 +519,61 @@ __device__ __noinline__ double pf1_eval_quad(Team& tm, const PotPF& P, CView<T> 
   const T pr = (P.flags & PF_PRESSURE) ? (T)P.pressure[0] : (T)0;
   const bool dx_on = nx > 1, dy_on = ny > 1;
   EAcc<T> e;
-  for (int q = tm.tid; q < nq; q += tm.nthr) {
+  for (int q = tm.tid(); q < nq; q += tm.nthr()) {
+    {  // next sweep step: fetch its lines into L2 now (its neighbour lines are
+       // other threads' own lines in the same window)
+      const int qn = q + P.pf_dist * tm.nthr();
+      if (P.pf_dist > 0 && qn < nq) {
+        const float* xf = reinterpret_cast<const float*>(cv.x);
+        if (sizeof(T) == 8) {  // 8 quads of doubles span two lines
+          prefetch_line(xf, 2 * qn);
+          prefetch_line(xf, 2 * qn + 8);
+        } else {
+          prefetch_line(xf, qn);
+        }
+        if (cv.p) prefetch_line(cv.p, qn);
+        if constexpr (requires { emit.prefetch4(qn); }) {
+          if (want_g) emit.prefetch4(qn);
+        }
+      }
+    }
     const int iG = 4 * q;
     const int z0 = iG % nz, line = iG / nz;
     const int y = line % ny, x = line / ny;
+    // every load of the iteration is issued before any is used (one memory
+    // round trip); a dimension of size 1 reads its own line and adds nothing
+    const int ym = y == 0 ? ny - 1 : y - 1, yp = y == ny - 1 ? 0 : y + 1;
+    const int xm = x == 0 ? nx - 1 : x - 1, xp = x == nx - 1 ? 0 : x + 1;
     const Quad<T> c = cv4(cv, q);
+    const T zm = cv(z0 == 0 ? iG + nz - 1 : iG - 1);
+    const T zp = cv(z0 + 4 == nz ? iG - z0 : iG + 4);
+    const Quad<T> cym = cv4(cv, ((x * ny + ym) * nz + z0) >> 2);
+    const Quad<T> cyp = cv4(cv, ((x * ny + yp) * nz + z0) >> 2);
+    const Quad<T> cxm = cv4(cv, ((xm * ny + y) * nz + z0) >> 2);
+    const Quad<T> cxp = cv4(cv, ((xp * ny + y) * nz + z0) >> 2);
+    auto pre = emit_pre(emit, q, want_g);
     if (xw) st_quad(xw, q, c);
     T lap[4], eg[4];
-    {  // z: neighbours inside the quad, plus one scalar at each end
-      const T zm = cv(z0 == 0 ? iG + nz - 1 : iG - 1);
-      const T zp = cv(z0 + 4 == nz ? iG - z0 : iG + 4);
 #pragma unroll
-      for (int k = 0; k < 4; k++) {
-        const T cm = (k == 0) ? zm : c.v[k - 1];
-        const T cp = (k == 3) ? zp : c.v[k + 1];
-        const T gm = c.v[k] - cm, gp = c.v[k] - cp;
-        lap[k] = gm + gp;
-        eg[k] = (T)0.5 * (gm * gm + gp * gp);
-      }
+    for (int k = 0; k < 4; k++) {  // z: neighbours inside the quad, plus one scalar at each end
+      const T cm = (k == 0) ? zm : c.v[k - 1];
+      const T cp = (k == 3) ? zp : c.v[k + 1];
+      const T gm = c.v[k] - cm, gp = c.v[k] - cp;
+      lap[k] = gm + gp;
+      eg[k] = (T)0.5 * (gm * gm + gp * gp);
     }
     if (dy_on) {
-      const int qm = ((x * ny + (y == 0 ? ny - 1 : y - 1)) * nz + z0) >> 2;
-      const int qp = ((x * ny + (y == ny - 1 ? 0 : y + 1)) * nz + z0) >> 2;
-      const Quad<T> cm = cv4(cv, qm), cp = cv4(cv, qp);
 #pragma unroll
       for (int k = 0; k < 4; k++) {
-        const T gm = c.v[k] - cm.v[k], gp = c.v[k] - cp.v[k];
+        const T gm = c.v[k] - cym.v[k], gp = c.v[k] - cyp.v[k];
         lap[k] += gm + gp;
         eg[k] += (T)0.5 * (gm * gm + gp * gp);
       }
     }
     if (dx_on) {
-      const int qm = (((x == 0 ? nx - 1 : x - 1) * ny + y) * nz + z0) >> 2;
-      const int qp = (((x == nx - 1 ? 0 : x + 1) * ny + y) * nz + z0) >> 2;
-      const Quad<T> cm = cv4(cv, qm), cp = cv4(cv, qp);
 #pragma unroll
       for (int k = 0; k < 4; k++) {
-        const T gm = c.v[k] - cm.v[k], gp = c.v[k] - cp.v[k];
+        const T gm = c.v[k] - cxm.v[k], gp = c.v[k] - cxp.v[k];
         lap[k] += gm + gp;
         eg[k] += (T)0.5 * (gm * gm + gp * gp);
       }
@@ -565,7 +593,7 @@ __device__ __noinline__ double pf1_eval_quad(Team& tm, const PotPF& P, CView<T> 
         g[k] -= (T)0.5 * pr * V;
       }
     }
-    if (want_g) emit_quad(emit, q, g);
+    if (want_g) emit_quad(emit, q, g, pre);
   }
   *emp = emit;
   return e.total();
@@ -587,7 +615,7 @@ __device__ __noinline__ double pf1_eval(Team& tm, const PotPF& P, CView<T> cv, T
   const T pr = (P.flags & PF_PRESSURE) ? (T)P.pressure[0] : (T)0;
   const bool dx_on = nx > 1, dy_on = ny > 1, dz_on = nz > 1;
   EAcc<T> e;
-  for (int iG = tm.tid; iG < ng; iG += tm.nthr) {
+  for (int iG = tm.tid(); iG < ng; iG += tm.nthr()) {
     const int z = iG % nz, y = (iG / nz) % ny, x = iG / (ny * nz);
     const T c = cv(iG);
     if (xw) xw[iG] = c;
@@ -637,7 +665,7 @@ __device__ __noinline__ double pf1_eval(Team& tm, const PotPF& P, CView<T> cv, T
 template <typename T, class Team>
 __device__ void pf_local_constrain(Team& tm, const PotPF& P, T* v) {
   const int nf = P.nfluid;
-  for (int iG = tm.tid; iG < P.ngrid; iG += tm.nthr) {
+  for (int iG = tm.tid(); iG < P.ngrid; iG += tm.nthr()) {
     T* w = v + (size_t)iG * nf;
     if (P.flags & PF_FIXFLUID)
       for (int f = 0; f < nf; f++)
@@ -663,7 +691,7 @@ __device__ void pf_volume_project(Team& tm, const PotPF& P, T* v) {
   double part[MINIM_MAXF];
 #pragma unroll
   for (int f = 0; f < MINIM_MAXF; f++) part[f] = 0.0;
-  for (int iG = tm.tid; iG < P.ngrid; iG += tm.nthr) {
+  for (int iG = tm.tid(); iG < P.ngrid; iG += tm.nthr()) {
     const double V = P.vol_of_type[pf_type1(P, iG)];
     const T* w = v + (size_t)iG * nf;
     double sv = 0.0;
@@ -683,7 +711,7 @@ __device__ void pf_volume_project(Team& tm, const PotPF& P, T* v) {
     comp[f] = (f < nf && !((P.fix_mask >> f) & 1u)) ? part[f] / P.total_volume2 : 0.0;
     csum += comp[f];
   }
-  for (int iG = tm.tid; iG < P.ngrid; iG += tm.nthr) {
+  for (int iG = tm.tid(); iG < P.ngrid; iG += tm.nthr()) {
     const double V = P.vol_of_type[pf_type1(P, iG)];
     T* w = v + (size_t)iG * nf;
     for (int f = 0; f < nf; f++) {
@@ -824,7 +852,7 @@ __device__ __noinline__ double bah_eval(Team& tm, const PotBAH& P, CView<T> cv, 
   Emit emit = *emp;
   EAcc<T> e;
   const int nv = P.nvert;
-  for (int v = tm.tid; v < nv; v += tm.nthr) {
+  for (int v = tm.tid(); v < nv; v += tm.nthr()) {
     if (xw) {
       xw[3 * v] = cv(3 * v); xw[3 * v + 1] = cv(3 * v + 1); xw[3 * v + 2] = cv(3 * v + 2);
     }
@@ -836,11 +864,11 @@ __device__ __noinline__ double bah_eval(Team& tm, const PotBAH& P, CView<T> cv, 
     }
   }
   if (!want_g) {
-    for (int b = tm.tid; b < P.nbar; b += tm.nthr) {
+    for (int b = tm.tid(); b < P.nbar; b += tm.nthr()) {
       T eb; bah_bar<T>(P, cv, b, eb, nullptr, nullptr, false);
       e.add(eb);
     }
-    for (int h = tm.tid; h < P.nhinge; h += tm.nthr) {
+    for (int h = tm.tid(); h < P.nhinge; h += tm.nthr()) {
       T eh; bah_hinge<T>(P, cv, h, eh, nullptr, false);
       e.add(eh);
     }
@@ -850,7 +878,7 @@ __device__ __noinline__ double bah_eval(Team& tm, const PotBAH& P, CView<T> cv, 
   tm.sync();
   for (int c = 0; c < P.nbar_colors; c++) {
     const int b0 = P.bar_color_off[c], b1 = P.bar_color_off[c + 1];
-    for (int b = b0 + tm.tid; b < b1; b += tm.nthr) {
+    for (int b = b0 + tm.tid(); b < b1; b += tm.nthr()) {
       T eb, gl[3], gr[3];
       bah_bar<T>(P, cv, b, eb, gl, gr, true);
       if (want_e) e.add(eb);
@@ -865,7 +893,7 @@ __device__ __noinline__ double bah_eval(Team& tm, const PotBAH& P, CView<T> cv, 
   }
   for (int c = 0; c < P.nhinge_colors; c++) {
     const int h0 = P.hinge_color_off[c], h1 = P.hinge_color_off[c + 1];
-    for (int h = h0 + tm.tid; h < h1; h += tm.nthr) {
+    for (int h = h0 + tm.tid(); h < h1; h += tm.nthr()) {
       T eh, gq[4][3];
       bah_hinge<T>(P, cv, h, eh, gq, true);
       if (want_e) e.add(eh);
@@ -878,7 +906,7 @@ __device__ __noinline__ double bah_eval(Team& tm, const PotBAH& P, CView<T> cv, 
     }
     tm.sync();
   }
-  for (int i = tm.tid; i < 3 * nv; i += tm.nthr) emit(i, (T)GA[i]);
+  for (int i = tm.tid(); i < 3 * nv; i += tm.nthr()) emit(i, (T)GA[i]);
   *emp = emit;
   return e.total();
 }

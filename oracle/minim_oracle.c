@@ -18,6 +18,10 @@
 #include <string.h>
 
 static char g_err[512];
+/* Threaded loops for the all-core CPU timing; with one thread every loop
+ * runs serially in the reference's order (the parity tests use that). */
+#define OMP_FOR _Pragma("omp parallel for if(o->nthreads > 1) num_threads(o->nthreads) schedule(static)")
+
 static int set_err(int code, const char* fmt, ...) {
   va_list ap;
   va_start(ap, fmt);
@@ -83,9 +87,11 @@ struct oracle_inst {
   pf_t pf;
   bah_t bah;
   long evals;
+  int nthreads;  /* > 1: parallel loops (timing runs only); 1: serial reference order */
 };
 
 size_t oracle_ndof(const oracle_inst* o) { return o->ndof; }
+void oracle_set_threads(oracle_inst* o, int nthreads) { o->nthreads = nthreads > 1 ? nthreads : 1; }
 double oracle_default_tol(const oracle_inst* o) { return o->tol_default; }
 
 /* ------------------------------------------------------------------------ */
@@ -357,94 +363,120 @@ static void pf_phase_gradient(const pf_t* p, const double* c, int iGrid, int f, 
  * (365-393), surfaceEnergy (476-487), pressureEnergy (432-454),
  * densityConstraintEnergy (457-473), forceEnergy (490-518) and
  * ffConfinementEnergy (521-537).  Serial order. */
+static void pf_node(const oracle_inst* o, const double* c, int x, int y, int z, double* e, double* g);
+
 static void pf_eg(const oracle_inst* o, const double* c, double* e, double* g) {
+  const pf_t* p = &o->pf;
+  if (o->nthreads > 1 && p->n[0] >= 6) {
+    /* x planes in three colours: a plane writes gradient terms only to its
+     * own plane and the two next to it, so planes of one colour never touch
+     * the same entries; the last nx % 3 planes run serially */
+    const int nx3 = p->n[0] - p->n[0] % 3;
+    double et = 0;
+    for (int col = 0; col < 3; col++) {
+#pragma omp parallel for num_threads(o->nthreads) schedule(static) reduction(+ : et)
+      for (int x = col; x < nx3; x += 3) {
+        double el = 0;
+        for (int y = 0; y < p->n[1]; y++)
+          for (int z = 0; z < p->n[2]; z++) pf_node(o, c, x, y, z, e ? &el : NULL, g);
+        et += el;
+      }
+    }
+    for (int x = nx3; x < p->n[0]; x++)
+      for (int y = 0; y < p->n[1]; y++)
+        for (int z = 0; z < p->n[2]; z++) pf_node(o, c, x, y, z, e ? &et : NULL, g);
+    if (e) *e += et;
+    return;
+  }
+  for (int x = 0; x < p->n[0]; x++)
+    for (int y = 0; y < p->n[1]; y++)
+      for (int z = 0; z < p->n[2]; z++) pf_node(o, c, x, y, z, e, g);
+}
+
+static void pf_node(const oracle_inst* o, const double* c, int x, int y, int z, double* e, double* g) {
   const pf_t* p = &o->pf;
   int nf = p->nfluid;
   double res2 = pow(p->res, 2);
-  for (int x = 0; x < p->n[0]; x++)
-    for (int y = 0; y < p->n[1]; y++)
-      for (int z = 0; z < p->n[2]; z++) {
-        int iG = (x * p->n[1] + y) * p->n[2] + z;
-        int nb[6] = {pf_idx(p, x - 1, y, z), pf_idx(p, x + 1, y, z), pf_idx(p, x, y - 1, z),
-                     pf_idx(p, x, y + 1, z), pf_idx(p, x, y, z - 1), pf_idx(p, x, y, z + 1)};
-        double V = p->node_vol[iG];
-        /* fluidEnergy */
-        for (int f = 0; f < nf; f++) {
-          int iD = iG * nf + f;
-          double cc = c[iD];
-          int iK = (p->nk == nf) ? f : iG * nf + f;
-          if (nf == 1) {
-            double fac = p->kappa[iK] / 16 * V;
-            if (e) *e += fac * pow(cc + 1, 2) * pow(cc - 1, 2);
-            if (g) g[iD] += fac * 4 * cc * (cc * cc - 1);
-          } else {
-            double fac = 0.5 * p->kappa[iK] * V;
-            if (e) *e += fac * pow(cc, 2) * pow(cc - 1, 2);
-            if (g) g[iD] += fac * 2 * cc * (cc - 1) * (2 * cc - 1);
-          }
-          double fac = (nf == 1) ? 0.25 * p->kappaP[iK] * V : 0.5 * p->kappaP[iK] * V;
-          fac = fac / res2;
-          pf_phase_gradient(p, c, iG, f, nb, fac, e, g);
-        }
-        /* surfaceEnergy */
-        if (!(p->surf_area[iG] == 0 || p->ncontact == 0 || p->contact[iG] == 90) && nf == 1) {
-          double w = 1 / sqrt(2.0) * cos(p->contact[iG] * 3.1415926536 / 180);
-          double phi = c[iG];
-          if (e) *e += w * (pow(phi, 3) / 3 - phi - 2.0 / 3) * p->surf_area[iG];
-          if (g) g[iG] += w * (pow(phi, 2) - 1) * p->surf_area[iG];
-        }
-        /* pressureEnergy */
-        for (int f = 0; f < nf; f++) {
-          if (p->pressure[f] == 0 || p->fix_fluid[f]) continue;
-          if (nf == 1) {
-            double vol = 0.5 * (c[iG] + 1) * V;
-            if (e) *e -= p->pressure[f] * vol;
-            if (g) g[iG] -= 0.5 * p->pressure[f] * V;
-          } else {
-            int iD = iG * nf + f;
-            double vol = c[iD] * V;
-            if (e) *e -= p->pressure[f] * vol;
-            if (g) g[iD] -= p->pressure[f] * V;
-          }
-        }
-        /* densityConstraintEnergy */
-        if (nf > 1 && p->density == D_SOFT) {
-          double coef = p->density_const * p->st_mean * res2;
-          double rd = -1;
-          for (int f = 0; f < nf; f++) rd += c[iG * nf + f];
-          if (e) *e += coef * pow(rd, 2);
-          if (g)
-            for (int f = 0; f < nf; f++) g[iG * nf + f] += 2 * coef * rd;
-        }
-        /* forceEnergy (note the reference's early return when no gradient
-         * is requested: only the first qualifying fluid's energy counts) */
-        if (!p->solid[iG] && p->any_force) {
-          double co[3] = {x - (p->n[0] - 1) / 2.0, y - (p->n[1] - 1) / 2.0, z - (p->n[2] - 1) / 2.0};
-          for (int f = 0; f < nf; f++) {
-            if (p->fmag[f] == 0) continue;
-            int iD = iG * nf + f;
-            double cc = (nf == 1) ? 0.5 * (1 + c[iD]) : c[iD];
-            if (cc < 0.01) continue;
-            const double* fn = p->fnorm + 3 * f;
-            double h = -(co[0] * fn[0] + co[1] * fn[1] + co[2] * fn[2]) * p->res;
-            double epc = V * p->fmag[f] * h;
-            if (e) *e += cc * epc;
-            if (!g) break;
-            g[iD] += (nf == 1) ? 0.5 * epc : epc;
-          }
-        }
-        /* ffConfinementEnergy */
-        for (int f = 0; f < nf; f++) {
-          if (p->confine[f] == 0) continue;
-          int iD = iG * nf + f;
-          double coef = p->confine[f] * p->st_mean * res2;
-          double cc = c[iD], c0 = p->ff_init[iD];
-          if ((c0 - 0.5) * (cc - 0.5) < 0) {
-            if (e) *e += coef * pow(cc - 0.5, 2);
-            if (g) g[iD] += coef * 2 * (cc - 0.5);
-          }
-        }
-      }
+  int iG = (x * p->n[1] + y) * p->n[2] + z;
+  int nb[6] = {pf_idx(p, x - 1, y, z), pf_idx(p, x + 1, y, z), pf_idx(p, x, y - 1, z),
+               pf_idx(p, x, y + 1, z), pf_idx(p, x, y, z - 1), pf_idx(p, x, y, z + 1)};
+  double V = p->node_vol[iG];
+  /* fluidEnergy */
+  for (int f = 0; f < nf; f++) {
+    int iD = iG * nf + f;
+    double cc = c[iD];
+    int iK = (p->nk == nf) ? f : iG * nf + f;
+    if (nf == 1) {
+      double fac = p->kappa[iK] / 16 * V;
+      if (e) *e += fac * pow(cc + 1, 2) * pow(cc - 1, 2);
+      if (g) g[iD] += fac * 4 * cc * (cc * cc - 1);
+    } else {
+      double fac = 0.5 * p->kappa[iK] * V;
+      if (e) *e += fac * pow(cc, 2) * pow(cc - 1, 2);
+      if (g) g[iD] += fac * 2 * cc * (cc - 1) * (2 * cc - 1);
+    }
+    double fac = (nf == 1) ? 0.25 * p->kappaP[iK] * V : 0.5 * p->kappaP[iK] * V;
+    fac = fac / res2;
+    pf_phase_gradient(p, c, iG, f, nb, fac, e, g);
+  }
+  /* surfaceEnergy */
+  if (!(p->surf_area[iG] == 0 || p->ncontact == 0 || p->contact[iG] == 90) && nf == 1) {
+    double w = 1 / sqrt(2.0) * cos(p->contact[iG] * 3.1415926536 / 180);
+    double phi = c[iG];
+    if (e) *e += w * (pow(phi, 3) / 3 - phi - 2.0 / 3) * p->surf_area[iG];
+    if (g) g[iG] += w * (pow(phi, 2) - 1) * p->surf_area[iG];
+  }
+  /* pressureEnergy */
+  for (int f = 0; f < nf; f++) {
+    if (p->pressure[f] == 0 || p->fix_fluid[f]) continue;
+    if (nf == 1) {
+      double vol = 0.5 * (c[iG] + 1) * V;
+      if (e) *e -= p->pressure[f] * vol;
+      if (g) g[iG] -= 0.5 * p->pressure[f] * V;
+    } else {
+      int iD = iG * nf + f;
+      double vol = c[iD] * V;
+      if (e) *e -= p->pressure[f] * vol;
+      if (g) g[iD] -= p->pressure[f] * V;
+    }
+  }
+  /* densityConstraintEnergy */
+  if (nf > 1 && p->density == D_SOFT) {
+    double coef = p->density_const * p->st_mean * res2;
+    double rd = -1;
+    for (int f = 0; f < nf; f++) rd += c[iG * nf + f];
+    if (e) *e += coef * pow(rd, 2);
+    if (g)
+      for (int f = 0; f < nf; f++) g[iG * nf + f] += 2 * coef * rd;
+  }
+  /* forceEnergy (note the reference's early return when no gradient
+   * is requested: only the first qualifying fluid's energy counts) */
+  if (!p->solid[iG] && p->any_force) {
+    double co[3] = {x - (p->n[0] - 1) / 2.0, y - (p->n[1] - 1) / 2.0, z - (p->n[2] - 1) / 2.0};
+    for (int f = 0; f < nf; f++) {
+      if (p->fmag[f] == 0) continue;
+      int iD = iG * nf + f;
+      double cc = (nf == 1) ? 0.5 * (1 + c[iD]) : c[iD];
+      if (cc < 0.01) continue;
+      const double* fn = p->fnorm + 3 * f;
+      double h = -(co[0] * fn[0] + co[1] * fn[1] + co[2] * fn[2]) * p->res;
+      double epc = V * p->fmag[f] * h;
+      if (e) *e += cc * epc;
+      if (!g) break;
+      g[iD] += (nf == 1) ? 0.5 * epc : epc;
+    }
+  }
+  /* ffConfinementEnergy */
+  for (int f = 0; f < nf; f++) {
+    if (p->confine[f] == 0) continue;
+    int iD = iG * nf + f;
+    double coef = p->confine[f] * p->st_mean * res2;
+    double cc = c[iD], c0 = p->ff_init[iD];
+    if ((c0 - 0.5) * (cc - 0.5) < 0) {
+      if (e) *e += coef * pow(cc - 0.5, 2);
+      if (g) g[iD] += coef * 2 * (cc - 0.5);
+    }
+  }
 }
 
 /* specialisedConstraints, src/potentials/PhaseField.cpp:580-659 */
@@ -881,8 +913,9 @@ int oracle_apply_constraints(oracle_inst* o, double* v) {
 /* ------------------------------------------------------------------------ */
 /* Vector algebra (Communicator::dotProduct, 1 rank: src/Communicator.cpp:170-173) */
 /* ------------------------------------------------------------------------ */
-static double vdot(const double* a, const double* b, size_t n) {
+static double vdot(const oracle_inst* o, const double* a, const double* b, size_t n) {
   double s = 0;
+#pragma omp parallel for if(o->nthreads > 1) num_threads(o->nthreads) schedule(static) reduction(+ : s)
   for (size_t i = 0; i < n; i++) s += a[i] * b[i];
   return s;
 }
@@ -895,10 +928,12 @@ static double linesearch(oracle_inst* o, double* step, double de0, double* tmp) 
   double t = -c * de0;
   double e0 = st_energy(o, o->x);
   double mult = 1;
+  OMP_FOR
   for (size_t i = 0; i < n; i++) tmp[i] = o->x[i] + step[i];
   for (int k = 0; k < 10; k++) {
     double e = st_energy(o, tmp);
     if (e0 - e >= t) break;
+    OMP_FOR
     for (size_t i = 0; i < n; i++) {
       step[i] = step[i] * tau;
       tmp[i] = o->x[i] + step[i];
@@ -939,42 +974,50 @@ int oracle_minimise(oracle_inst* o, const minim_gpu_minimiser_params* mp, minim_
       /* getDirection */
       int mt = ii < m ? ii : m;
       int ic = ii % m;
+      OMP_FOR
       for (size_t j = 0; j < n; j++) step[j] = -g[j];
       if (ii == 0) {
-        double gnorm = sqrt(vdot(g, g, n));
+        double gnorm = sqrt(vdot(o, g, g, n));
         if (gnorm > 0)
+          OMP_FOR
           for (size_t j = 0; j < n; j++) step[j] *= mp->init_step / gnorm;
       } else {
         for (int i1 = 0; i1 < mt; i1++) {
           int k = ((ic - 1 - i1) + m) % m;
-          alpha[k] = rho[k] * vdot(step, S + (size_t)k * n, n);
+          alpha[k] = rho[k] * vdot(o, step, S + (size_t)k * n, n);
+          OMP_FOR
           for (size_t j = 0; j < n; j++) step[j] -= alpha[k] * Y[(size_t)k * n + j];
         }
         int k = (ic - 1 + m) % m;
-        double gamma = 1 / (rho[k] * vdot(Y + (size_t)k * n, Y + (size_t)k * n, n));
+        double gamma = 1 / (rho[k] * vdot(o, Y + (size_t)k * n, Y + (size_t)k * n, n));
+        OMP_FOR
         for (size_t j = 0; j < n; j++) step[j] *= gamma;
         for (int i1 = 0; i1 < mt; i1++) {
           int kk = ((ic - mt + i1) + m) % m;
-          double beta = rho[kk] * vdot(step, Y + (size_t)kk * n, n);
+          double beta = rho[kk] * vdot(o, step, Y + (size_t)kk * n, n);
+          OMP_FOR
           for (size_t j = 0; j < n; j++) step[j] += (alpha[kk] - beta) * S[(size_t)kk * n + j];
         }
         if (mp->max_step != 0) {
-          double ss = sqrt(vdot(step, step, n));
+          double ss = sqrt(vdot(o, step, step, n));
           if (ss > mp->max_step)
+            OMP_FOR
             for (size_t j = 0; j < n; j++) step[j] *= mp->max_step / ss;
         }
       }
       apply_constraints(o, step);
-      double gs = vdot(g, step, n);
+      double gs = vdot(o, g, step, n);
       if (gs > 0) {
         gs = -gs;
+        OMP_FOR
         for (size_t j = 0; j < n; j++) step[j] = -step[j];
       }
       if (ls) linesearch(o, step, gs, tmp);
       else for (size_t j = 0; j < n; j++) o->x[j] += step[j];
       st_gradient(o, o->x, gn);
+      OMP_FOR
       for (size_t j = 0; j < n; j++) tmp[j] = gn[j] - g[j];
-      double sy = vdot(step, tmp, n);
+      double sy = vdot(o, step, tmp, n);
       if (sy != 0) {
         int c = ii % m;
         memcpy(S + (size_t)c * n, step, n * sizeof(double));
@@ -985,7 +1028,7 @@ int oracle_minimise(oracle_inst* o, const minim_gpu_minimiser_params* mp, minim_
       }
       memcpy(g, gn, n * sizeof(double));
       /* checkConvergence */
-      if (sqrt(vdot(g, g, n) / n) < tol) break;
+      if (sqrt(vdot(o, g, g, n) / n) < tol) break;
     }
     free(S); free(Y); free(rho); free(alpha);
   } else if (mp->method == MINIM_FIRE) {
@@ -996,21 +1039,23 @@ int oracle_minimise(oracle_inst* o, const minim_gpu_minimiser_params* mp, minim_
     int nSteps = 0;
     if (dtmax == 0) { /* Fire::init */
       st_gradient(o, o->x, g);
-      gNorm = sqrt(vdot(g, g, n));
+      gNorm = sqrt(vdot(o, g, g, n));
       dtmax = (gNorm != 0) ? 0.1 / sqrt(gNorm) : 1;
     }
     for (iter = 0; iter <= maxIter; iter++) {
       if (iter == 0) {
         dt = dtmax;
         st_gradient(o, o->x, g);
-        gNorm = sqrt(vdot(g, g, n));
+        gNorm = sqrt(vdot(o, g, g, n));
       }
-      double p = -vdot(v, g, n);
+      double p = -vdot(o, v, g, n);
       if (p > 0) {
-        double vNorm = sqrt(vdot(v, v, n));
+        double vNorm = sqrt(vdot(o, v, v, n));
+        OMP_FOR
         for (size_t j = 0; j < n; j++) v[j] = (1 - a) * v[j] - (a * vNorm / gNorm + dt) * g[j];
         nSteps++;
       } else {
+        OMP_FOR
         for (size_t j = 0; j < n; j++) v[j] = -dt * g[j];
         nSteps = 0;
       }
@@ -1022,30 +1067,34 @@ int oracle_minimise(oracle_inst* o, const minim_gpu_minimiser_params* mp, minim_
         a = aStart;
         dt = dt * fDec;
       }
+      OMP_FOR
       for (size_t j = 0; j < n; j++) step[j] = dt * v[j];
       apply_constraints(o, step);
       if (ls) {
-        double gs = vdot(g, step, n);
+        double gs = vdot(o, g, step, n);
         linesearch(o, step, gs, tmp);
       } else {
+        OMP_FOR
         for (size_t j = 0; j < n; j++) o->x[j] += step[j];
       }
       st_gradient(o, o->x, g);
-      gNorm = sqrt(vdot(g, g, n));
+      gNorm = sqrt(vdot(o, g, g, n));
       if (gNorm / sqrt((double)n) < tol) break;
     }
     free(v);
   } else if (mp->method == MINIM_GD) {
     for (iter = 0; iter <= maxIter; iter++) {
       st_gradient(o, o->x, g);
+      OMP_FOR
       for (size_t j = 0; j < n; j++) step[j] = -mp->alpha * g[j];
       if (ls) {
-        double gs = vdot(g, step, n);
+        double gs = vdot(o, g, step, n);
         linesearch(o, step, gs, tmp);
       } else {
+        OMP_FOR
         for (size_t j = 0; j < n; j++) o->x[j] += step[j];
       }
-      if (sqrt(vdot(g, g, n) / n) < tol) break;
+      if (sqrt(vdot(o, g, g, n) / n) < tol) break;
     }
   } else {
     free(g); free(gn); free(step); free(tmp);
@@ -1059,7 +1108,7 @@ int oracle_minimise(oracle_inst* o, const minim_gpu_minimiser_params* mp, minim_
     long ev = o->evals;
     res->energy = st_energy(o, o->x);
     st_gradient(o, o->x, g);
-    res->rms = sqrt(vdot(g, g, n) / n);
+    res->rms = sqrt(vdot(o, g, g, n) / n);
     res->evals = (int)ev;
     res->dt_max = dtmax;
     if (!(res->energy == res->energy)) res->status = MINIM_RES_NAN;
@@ -1088,6 +1137,7 @@ int oracle_create(int kind, const void* params, const double* x0, size_t ndof,
                   const int* fixed, int nfixed, oracle_inst** out) {
   *out = NULL;
   oracle_inst* o = xcalloc(1, sizeof *o);
+  o->nthreads = 1;
   o->kind = kind;
   o->ndof = ndof;
   o->x = xcalloc(ndof, sizeof(double));

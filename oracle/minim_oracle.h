@@ -26,6 +26,11 @@ int oracle_create(int kind, const void* params, const double* x0, size_t ndof,
                   const int* fixed, int nfixed, oracle_inst** out);
 void oracle_destroy(oracle_inst* o);
 size_t oracle_ndof(const oracle_inst* o);
+/* Threads for the PhaseField evaluation and the minimisers' vector loops
+ * (default 1: serial, in the reference's summation order).  More threads
+ * are for timing the CPU baseline on all host cores; sums then associate
+ * differently. */
+void oracle_set_threads(oracle_inst* o, int nthreads);
 double oracle_default_tol(const oracle_inst* o);
 int oracle_set_coords(oracle_inst* o, const double* x);
 int oracle_get_coords(const oracle_inst* o, double* x);

@@ -56,6 +56,7 @@ def _load_oracle():
                                             C.POINTER(_ip), C.POINTER(_dp)]
         lib.oracle_pf_internals.argtypes = [C.c_void_p, C.POINTER(_dp), C.POINTER(_dp),
                                             C.POINTER(_dp), C.POINTER(_dp), _ip]
+        lib.oracle_set_threads.argtypes = [C.c_void_p, C.c_int]
         _lib = lib
     return _lib
 
@@ -149,7 +150,10 @@ class _Base:
 class Oracle(_Base):
     """FP64 C restatement of the reference path."""
 
-    def __init__(self, params, x0, fixed=None):
+    def __init__(self, params, x0, fixed=None, threads=1):
+        """threads > 1 runs the PhaseField evaluation and the minimisers'
+        vector loops on that many host threads (CPU-baseline timing only);
+        the default 1 keeps the reference's serial summation order."""
         lib = _load_oracle()
         self._lib = lib
         self._create = lib.oracle_create
@@ -159,6 +163,8 @@ class Oracle(_Base):
         self._set = lib.oracle_set_coords
         self._min = lib.oracle_minimise
         super().__init__(params, x0, fixed)
+        if threads > 1:
+            lib.oracle_set_threads(self.h, int(threads))
 
     def _error(self):
         return self._lib.oracle_last_error().decode()

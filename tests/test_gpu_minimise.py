@@ -36,6 +36,18 @@ def check_minimum(p, x0, x, res, tol, fixed=None, gd=False):
     return e
 
 
+@pytest.mark.parametrize("seed", [3, 5, 21, 42, 77])
+def test_lj_grid_mixed_seeds(seed):
+    """Mixed precision must leave the FP32 stage on its own for any start
+    (the line search stops resolving the decrease near the FP32 floor)."""
+    x0 = lj_cluster(13, seed=seed)
+    p = abi.lj()
+    inst = runtime.Instance(p, x0)
+    r = inst.minimise(abi.minimiser("lbfgs", tol=1e-6, max_iter=20000))
+    assert r.status == abi.RES_CONVERGED, r.as_dict()
+    check_minimum(p, x0, inst.coords, r, 1e-6)
+
+
 @pytest.mark.parametrize("method,ls", [("lbfgs", None), ("fire", "backtracking"), ("gd", None)])
 @pytest.mark.parametrize("prec", ["mixed", "fp64"])
 def test_lj_grid_path(method, ls, prec):
