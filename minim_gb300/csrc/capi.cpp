@@ -144,6 +144,15 @@ int stage_bytes_cfg() {
   return v;
 }
 int grid_stage_bytes(int kk) { return kk == K_LJ ? 0 : stage_bytes_cfg(); }
+// The FP32 stage of L-BFGS on a large binary PhaseField runs as a graph of
+// phase kernels (stepped.cu) unless MINIM_GPU_STEPPED=0.
+bool stepped_cfg() {
+  static const bool v = [] {
+    const char* e = std::getenv("MINIM_GPU_STEPPED");
+    return !(e && e[0] == '0');
+  }();
+  return v;
+}
 // L2 prefetch distance of the grid launches' sweeps, in sweep steps
 // (MINIM_GPU_PREFETCH, default 1; 0 disables it).
 int prefetch_cfg() {
@@ -266,6 +275,7 @@ struct minim_gpu_instance_s {
   // single-instance workspace (lazy)
   void* ws = nullptr;
   size_t ws_bytes = 0;
+  void* stepped = nullptr;  // cached graph of the stepped FP32 path
   MinScalars* d_st = nullptr;
 
   void* own(void* p) {
@@ -280,6 +290,10 @@ struct minim_gpu_instance_s {
     return p;
   }
   ~minim_gpu_instance_s() {
+    if (stepped) {
+      cudaStreamSynchronize(dev().s);
+      mg_stepped_free(&stepped);
+    }
     for (void* p : owned) dfree(p);
     dfree(ws);
   }
@@ -444,7 +458,39 @@ void do_minimise(minim_gpu_instance_s* h, const minim_gpu_minimiser_params& mp, 
   cudaEvent_t ev0, ev1;
   CK(cudaEventCreate(&ev0));
   CK(cudaEventCreate(&ev1));
-  for (;;) {
+  const bool stepped = stepped_cfg() && h->kk == K_PF1 && mp.method == MINIM_LBFGS &&
+                       mp.precision != MINIM_PREC_FP64 && h->d.fixed == nullptr && h->n >= ((size_t)1 << 18) &&
+                       L.total < ((size_t)1 << 34);  // signed 32-bit float4 offsets across the workspace
+  if (stepped) {
+    // iteration 0 (set-up) on the persistent kernel, then the FP32 stage as
+    // graph launches until it hands over (precision switch, convergence,
+    // NaN) or stops
+    CK(cudaEventRecord(ev0, D.s));
+    launch_grid(h, OP_MINIMISE, 1);
+    CK(cudaEventRecord(ev1, D.s));
+    CK(cudaMemcpyAsync(&s, h->d_st, sizeof s, cudaMemcpyDeviceToHost, D.s));
+    CK(cudaStreamSynchronize(D.s));
+    float ms = 0;
+    CK(cudaEventElapsedTime(&ms, ev0, ev1));
+    stats.kernel_ms += ms;
+    stats.launches++;
+    if (grid_error(h)) s.status = ST_TIMEOUT;
+    while (s.status == ST_RUNNING && s.stage == 0 && !s.resume) {
+      const int it0 = s.iter;
+      double kernels = 0;
+      CK(cudaEventRecord(ev0, D.s));
+      CK((cudaError_t)mg_stepped_pf1_run(&h->stepped, h->d_desc, h->d_st, mp.m, D.nsm, 4096, D.s, &kernels));
+      CK(cudaEventRecord(ev1, D.s));
+      CK(cudaMemcpyAsync(&s, h->d_st, sizeof s, cudaMemcpyDeviceToHost, D.s));
+      CK(cudaStreamSynchronize(D.s));
+      CK(cudaEventElapsedTime(&ms, ev0, ev1));
+      stats.kernel_ms += ms;
+      stats.launches += (int64_t)kernels;
+      g_launches += (int64_t)kernels;
+      if ((s.iter == it0 && !s.resume) || s.iter > mp.max_iter) break;  // not eligible, or done
+    }
+  }
+  for (; s.status == ST_RUNNING;) {
     CK(cudaEventRecord(ev0, D.s));
     launch_grid(h, OP_MINIMISE, slice);
     CK(cudaEventRecord(ev1, D.s));

@@ -311,6 +311,58 @@ struct D4q {
   double x, y, z, w;
 };
 
+// Sums column k < K (<= 64) of G rows of MINIM_WIDE doubles (row b at
+// P + b * MINIM_WIDE) in row order into out[k], with every thread of the
+// block: one double4 load per (row, 4 columns) spread over the threads (all
+// issued at once), butterflies across the lanes that share a column, then a
+// fixed-order sum over warps through `wide` (8 * MINIM_WIDE doubles of
+// scratch).  Deterministic: the order depends only on G, K and blockDim.
+__device__ inline void sum_rows_fixed(const double* P, int G, int K, double* out, double* wide) {
+  const int nq = (K + 3) >> 2;  // double4 columns
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  const int nqp = nq <= 1 ? 1 : nq <= 2 ? 2 : nq <= 4 ? 4 : nq <= 8 ? 8 : 16;
+  const int q = threadIdx.x & (nqp - 1);
+  const int r0 = threadIdx.x / nqp, rs = blockDim.x / nqp;
+  // four consecutive partials of row b (L2, 2 x 16-byte loads)
+  auto ld = [&](int b) {
+    const double2* r = reinterpret_cast<const double2*>(P + (size_t)b * MINIM_WIDE) + 2 * q;
+    const double2 lo = __ldcg(r), hi = __ldcg(r + 1);
+    return D4q{lo.x, lo.y, hi.x, hi.y};
+  };
+  D4q acc{0.0, 0.0, 0.0, 0.0};
+  if (q < nq) {
+    int b = r0;
+    for (; b + 3 * rs < G; b += 4 * rs) {
+      const D4q v0 = ld(b), v1 = ld(b + rs), v2 = ld(b + 2 * rs), v3 = ld(b + 3 * rs);
+      acc.x += v0.x; acc.y += v0.y; acc.z += v0.z; acc.w += v0.w;
+      acc.x += v1.x; acc.y += v1.y; acc.z += v1.z; acc.w += v1.w;
+      acc.x += v2.x; acc.y += v2.y; acc.z += v2.z; acc.w += v2.w;
+      acc.x += v3.x; acc.y += v3.y; acc.z += v3.z; acc.w += v3.w;
+    }
+    for (; b < G; b += rs) {
+      const D4q v = ld(b);
+      acc.x += v.x; acc.y += v.y; acc.z += v.z; acc.w += v.w;
+    }
+  }
+  for (int off = 16; off >= nqp; off >>= 1) {
+    acc.x += __shfl_xor_sync(0xffffffffu, acc.x, off);
+    acc.y += __shfl_xor_sync(0xffffffffu, acc.y, off);
+    acc.z += __shfl_xor_sync(0xffffffffu, acc.z, off);
+    acc.w += __shfl_xor_sync(0xffffffffu, acc.w, off);
+  }
+  // columns of warp w: lanes 0 .. min(nqp, 32) - 1 (nqp <= 16)
+  if (lane < nqp && q < nq) {
+    double* d = wide + (size_t)w * MINIM_WIDE + 4 * q;
+    d[0] = acc.x; d[1] = acc.y; d[2] = acc.z; d[3] = acc.w;
+  }
+  __syncthreads();
+  for (int k = threadIdx.x; k < K; k += blockDim.x) {
+    double t = 0.0;
+    for (int i = 0; i < nw; i++) t += wide[i * MINIM_WIDE + k];
+    out[k] = t;
+  }
+}
+
 // ---------------------------------------------------------------------------
 // Team = whole grid (cooperative launch), with a bounded software barrier
 // ---------------------------------------------------------------------------
@@ -359,56 +411,9 @@ struct GridTeam {
   }
 
   // Every block sums the K (<= 64) partials of all blocks' rows in block
-  // order, so all blocks hold bitwise the same totals without a second round
-  // trip: one double4 load per (block, 4 values) spread over the threads
-  // (all issued at once), butterflies across the lanes that share a column,
-  // then a fixed-order sum over warps through `wide` (free during barriers).
-  __device__ void sum_rows(const double* P, int K, double* out) {
-    const int nq = (K + 3) >> 2;  // double4 columns
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
-    const int nqp = nq <= 1 ? 1 : nq <= 2 ? 2 : nq <= 4 ? 4 : nq <= 8 ? 8 : 16;
-    const int q = threadIdx.x & (nqp - 1);
-    const int r0 = threadIdx.x / nqp, rs = blockDim.x / nqp;
-    const int G = gridDim.x;
-    // four consecutive partials of row b (L2, 2 x 16-byte loads)
-    auto ld = [&](int b) {
-      const double2* r = reinterpret_cast<const double2*>(P + (size_t)b * MINIM_WIDE) + 2 * q;
-      const double2 lo = __ldcg(r), hi = __ldcg(r + 1);
-      return D4q{lo.x, lo.y, hi.x, hi.y};
-    };
-    D4q acc{0.0, 0.0, 0.0, 0.0};
-    if (q < nq) {
-      int b = r0;
-      for (; b + 3 * rs < G; b += 4 * rs) {
-        const D4q v0 = ld(b), v1 = ld(b + rs), v2 = ld(b + 2 * rs), v3 = ld(b + 3 * rs);
-        acc.x += v0.x; acc.y += v0.y; acc.z += v0.z; acc.w += v0.w;
-        acc.x += v1.x; acc.y += v1.y; acc.z += v1.z; acc.w += v1.w;
-        acc.x += v2.x; acc.y += v2.y; acc.z += v2.z; acc.w += v2.w;
-        acc.x += v3.x; acc.y += v3.y; acc.z += v3.z; acc.w += v3.w;
-      }
-      for (; b < G; b += rs) {
-        const D4q v = ld(b);
-        acc.x += v.x; acc.y += v.y; acc.z += v.z; acc.w += v.w;
-      }
-    }
-    for (int off = 16; off >= nqp; off >>= 1) {
-      acc.x += __shfl_xor_sync(0xffffffffu, acc.x, off);
-      acc.y += __shfl_xor_sync(0xffffffffu, acc.y, off);
-      acc.z += __shfl_xor_sync(0xffffffffu, acc.z, off);
-      acc.w += __shfl_xor_sync(0xffffffffu, acc.w, off);
-    }
-    // columns of warp w: lanes 0 .. min(nqp, 32) - 1 (nqp <= 16)
-    if (lane < nqp && q < nq) {
-      double* d = wide + (size_t)w * MINIM_WIDE + 4 * q;
-      d[0] = acc.x; d[1] = acc.y; d[2] = acc.z; d[3] = acc.w;
-    }
-    __syncthreads();
-    for (int k = threadIdx.x; k < K; k += blockDim.x) {
-      double t = 0.0;
-      for (int i = 0; i < nw; i++) t += wide[i * MINIM_WIDE + k];
-      out[k] = t;
-    }
-  }
+  // order (sum_rows_fixed), so all blocks hold bitwise the same totals
+  // without a second round trip; `wide` is free during barriers.
+  __device__ void sum_rows(const double* P, int K, double* out) { sum_rows_fixed(P, gridDim.x, K, out, wide); }
 
   // Counter barrier with an optional reduction.  Every block adds 1 to the
   // launch's arrival counter after its partials are written (fence, then a

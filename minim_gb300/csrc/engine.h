@@ -120,6 +120,9 @@ struct MinScalars {
   double SY[MINIM_MAXM][MINIM_MAXM], YY[MINIM_MAXM][MINIM_MAXM];
   int pend;
   int cool;          // iterations before a stalled run may re-enter FP64
+  // set by the stepped FP32 path when it hands an iteration's end-of-
+  // iteration bookkeeping (precision switch, convergence) to the kernel
+  int resume, resume_exhausted;
   // work counters for the roofline: algorithmic HBM bytes of every vector
   // pass and evaluation, and Lennard-Jones pair interactions per precision
   double abytes, pairs32, pairs64;
@@ -190,4 +193,10 @@ MG_DECLARE_LAUNCHERS(bah)
 MG_DECLARE_LAUNCHERS(pf1)
 // engine_misc.cu: FP64 <-> FP32 vector conversion on a stream
 int mg_convert(const void* src, void* dst, size_t n, int to_float, void* stream);
+// stepped.cu: up to `slice` FP32 L-BFGS iterations (history m) of a binary
+// PhaseField instance as one graph launch (graph cached in *cache); returns
+// a cudaError_t
+int mg_stepped_pf1_run(void** cache, const mg::InstDesc* d, mg::MinScalars* st, int m, int nsm, int slice,
+                       void* stream, double* kernels);
+void mg_stepped_free(void** cache);
 }

@@ -101,7 +101,7 @@ struct Runner {
   int lj_tile;
   // uniform scalars (every thread holds identical copies)
   int n, status, initd, iter, ii, stage, xi, gi, evals, fp64_iters, stall, nsteps, pbuf, ybuf;
-  int exhausted_run, switch_reason, pend, cool;
+  int exhausted_run, switch_reason, pend, cool, resume, resume_exhausted;
   double E, gg, best_rms, dt, a, dtmax, gnorm;
   double abytes, pairs32, pairs64;
   double tph[3];
@@ -857,6 +857,7 @@ struct Runner {
     xi = s.xi; gi = s.gi; evals = s.evals; fp64_iters = s.fp64_iters; stall = s.stall;
     nsteps = s.nsteps; pbuf = s.pbuf; ybuf = s.ybuf; E = s.E; gg = s.gg; best_rms = s.best_rms;
     exhausted_run = s.exhausted_run; switch_reason = s.switch_reason; pend = s.pend; cool = s.cool;
+    resume = s.resume; resume_exhausted = s.resume_exhausted;
     dt = s.dt; a = s.a; dtmax = s.dtmax; gnorm = s.gnorm;
     abytes = s.abytes; pairs32 = s.pairs32; pairs64 = s.pairs64;
     tph[0] = s.tphase[0]; tph[1] = s.tphase[1]; tph[2] = s.tphase[2];
@@ -878,6 +879,7 @@ struct Runner {
       s.evals = evals; s.fp64_iters = fp64_iters; s.stall = stall; s.nsteps = nsteps;
       s.pbuf = pbuf; s.ybuf = ybuf; s.E = E; s.gg = gg; s.best_rms = best_rms;
       s.exhausted_run = exhausted_run; s.switch_reason = switch_reason; s.pend = pend; s.cool = cool;
+      s.resume = resume; s.resume_exhausted = resume_exhausted;
       s.dt = dt; s.a = a; s.dtmax = dtmax; s.gnorm = gnorm; s.initialised = 1;
       s.abytes = abytes; s.pairs32 = pairs32; s.pairs64 = pairs64;
       s.tphase[0] = tph[0]; s.tphase[1] = tph[1]; s.tphase[2] = tph[2];
@@ -893,62 +895,12 @@ struct Runner {
     __syncthreads();
   }
 
-  // Minimiser::minimise, resumable: runs at most `slice` iterations.
-  __device__ void run(int slice) {
+  // End of an iteration: precision policy, convergence, iteration count.
+  // Returns true when the minimisation has stopped (status set).
+  __device__ bool post_iteration(bool exhausted) {
     const MinParams& mp = in.mp;
-    if (status != ST_RUNNING) return;
     const bool mixed = (mp.precision == 0);
-    if (!initd) {
-      // Minimiser::init; the coordinates come from the resident FP64 copy
-      initd = 1;
-      {
-        const double* xr = in.xres;
-        float* X32 = in.X32[0];
-        double* X64 = in.X64[0];
-        for (int i = tm.tid(); i < n; i += tm.nthr()) {
-          const double v = xr[i];
-          X32[i] = (float)v;
-          if (X64) X64[i] = v;
-        }
-        tm.sync();
-        xi = 0;
-        gi = 0;
-      }
-      if (mp.precision == 1) stage = 1;
-      if (mp.method == 0) {
-        ii = 0;
-        if (threadIdx.x == 0)
-          for (int k = 0; k < MINIM_MAXM; k++) {
-            rho[k] = 0; sig[k] = 0; yy[k] = 0; sidx[k] = k; yidx[k] = k;
-          }
-        pbuf = mp.m; ybuf = mp.m;
-        pend = -1;
-        __syncthreads();
-      } else if (mp.method == 1) {
-        for (int i = tm.tid(); i < n; i += tm.nthr()) in.V[i] = 0.f;
-        tm.sync();
-        a = 0.1; nsteps = 0;
-        dtmax = mp.dt_max;
-        if (dtmax == 0) {
-          double py, yyv;
-          grad_eval(0.0, nullptr, false, false, py, yyv);
-          const double gn = sqrt(gg);
-          dtmax = (gn != 0) ? 0.1 / sqrt(gn) : 1.0;
-        }
-      }
-      best_rms = 1e300;
-      stall = 0;
-      exhausted_run = 0;
-      cool = 0;
-    }
-    for (int s = 0; s < slice; s++) {
-      if (iter > mp.max_iter) { status = ST_MAXITER; break; }
-      bool exhausted = false;
-      if (mp.method == 0) lbfgs_iteration(exhausted);
-      else if (mp.method == 1) fire_iteration(exhausted);
-      else gd_iteration(exhausted);
-      if (!tm.ok()) { status = ST_TIMEOUT; break; }
-      if (stage == 1) fp64_iters++;
+    if (stage == 1) fp64_iters++;
       if (!isfinite(E) || !isfinite(gg)) {
         // FP32 overflows where FP64 does not (e.g. Lennard-Jones pairs at
         // very short range): evaluate the same point in FP64 before giving up
@@ -957,7 +909,7 @@ struct Runner {
           to_fp64();
           reeval();
         }
-        if (!isfinite(E) || !isfinite(gg)) { status = ST_NAN; break; }
+        if (!isfinite(E) || !isfinite(gg)) { status = ST_NAN; return true; }
       }
       const double r = rms();
       bool conv = r < mp.tol;
@@ -1009,8 +961,74 @@ struct Runner {
           }
         }
       }
-      if (conv) { status = ST_CONVERGED; break; }
-      iter++;
+    if (conv) { status = ST_CONVERGED; return true; }
+    iter++;
+    return false;
+  }
+
+  // Minimiser::minimise, resumable: runs at most `slice` iterations.
+  __device__ void run(int slice) {
+    const MinParams& mp = in.mp;
+    if (status != ST_RUNNING) return;
+    const bool mixed = (mp.precision == 0);
+    if (!initd) {
+      // Minimiser::init; the coordinates come from the resident FP64 copy
+      initd = 1;
+      {
+        const double* xr = in.xres;
+        float* X32 = in.X32[0];
+        double* X64 = in.X64[0];
+        for (int i = tm.tid(); i < n; i += tm.nthr()) {
+          const double v = xr[i];
+          X32[i] = (float)v;
+          if (X64) X64[i] = v;
+        }
+        tm.sync();
+        xi = 0;
+        gi = 0;
+      }
+      if (mp.precision == 1) stage = 1;
+      if (mp.method == 0) {
+        ii = 0;
+        if (threadIdx.x == 0)
+          for (int k = 0; k < MINIM_MAXM; k++) {
+            rho[k] = 0; sig[k] = 0; yy[k] = 0; sidx[k] = k; yidx[k] = k;
+          }
+        pbuf = mp.m; ybuf = mp.m;
+        pend = -1;
+        __syncthreads();
+      } else if (mp.method == 1) {
+        for (int i = tm.tid(); i < n; i += tm.nthr()) in.V[i] = 0.f;
+        tm.sync();
+        a = 0.1; nsteps = 0;
+        dtmax = mp.dt_max;
+        if (dtmax == 0) {
+          double py, yyv;
+          grad_eval(0.0, nullptr, false, false, py, yyv);
+          const double gn = sqrt(gg);
+          dtmax = (gn != 0) ? 0.1 / sqrt(gn) : 1.0;
+        }
+      }
+      best_rms = 1e300;
+      stall = 0;
+      exhausted_run = 0;
+      cool = 0;
+    }
+    // an iteration run outside this kernel (the stepped FP32 path) may hand
+    // its end-of-iteration bookkeeping over to here
+    bool done = false;
+    if (resume) {
+      resume = 0;
+      done = post_iteration(resume_exhausted != 0);
+    }
+    for (int s = 0; s < slice && !done; s++) {
+      if (iter > mp.max_iter) { status = ST_MAXITER; break; }
+      bool exhausted = false;
+      if (mp.method == 0) lbfgs_iteration(exhausted);
+      else if (mp.method == 1) fire_iteration(exhausted);
+      else gd_iteration(exhausted);
+      if (!tm.ok()) { status = ST_TIMEOUT; break; }
+      done = post_iteration(exhausted);
     }
     if (status != ST_RUNNING) {
       // hand the final coordinates back to the resident FP64 copy

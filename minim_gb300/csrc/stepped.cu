@@ -1,0 +1,670 @@
+// stepped.cu -- the FP32 stage of an L-BFGS minimisation of one large binary
+// PhaseField as a CUDA graph of phase kernels.
+//
+// The persistent grid kernel holds every phase of the minimiser in one
+// function, so its register budget (128 per thread, 16 warps per SM) is set
+// by the heaviest phase and its sweeps are latency-bound.  Here each phase
+// is its own kernel with its own register allocation and occupancy, and the
+// control flow stays on the device: one graph launch runs up to `slice`
+// iterations as
+//
+//   begin -> WHILE(outer) { dirA -> ctlA -> dirB -> ctlB ->
+//                           WHILE(line search) { eonly -> ctlLS } ->
+//                           grad -> ctlG }
+//
+// Vector kernels write one row of partial sums per block; the controller
+// kernels (one block) sum the rows in a fixed order, run the scalar parts
+// of Lbfgs::iteration / getDirection / backtrackingLinesearch
+// (src/minimisers/Lbfgs.cpp:41-133, src/minimisers/linesearch.cpp:8-30) on
+// the instance's state record, and set the loops' conditions.  Both loops
+// are bounded: the line search by its 10 trials, the outer loop by `slice`
+// iterations per launch.
+//
+// The first iteration and everything outside the FP32 stage (the switch to
+// FP64 coordinates, convergence and NaN handling) stay with the persistent
+// kernel: at the end of each iteration the controller decides on copies of
+// the policy counters whether the minimisation simply continues; if not, it
+// leaves the end-of-iteration bookkeeping to the persistent kernel (state
+// `resume`), which redoes it from the same state.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+
+#include "kernels.cuh"
+
+namespace mg {
+namespace {
+
+struct FlatTeam {
+  __device__ __forceinline__ int tid() const { return blockIdx.x * blockDim.x + threadIdx.x; }
+  __device__ __forceinline__ int nthr() const { return gridDim.x * blockDim.x; }
+};
+
+// Device control block of the stepped path (one per instance).
+struct StepCtl {
+  double t, thr, e0;         // line search: multiplier, Armijo threshold, energy at x
+  double kernels;            // kernel executions (launch count)
+  unsigned long long tmark;  // %globaltimer at the end of the last controller
+  int k, exhausted;          // trials so far; the policy's "line search exhausted"
+  int iters, slice;          // iterations in this launch, at most `slice`
+  int mt;                    // pairs used by this iteration's direction
+  float fg;                  // -gamma
+  float coefS[MINIM_MAXM], coefY[MINIM_MAXM];
+  int so[MINIM_MAXM], yo[MINIM_MAXM];  // slot buffers: float4 offsets from the ring bases
+};
+
+constexpr int kThreads = 256;
+constexpr int kCtlThreads = 256;
+
+// One row of K <= 4 block sums (deterministic: warp butterflies, then warps
+// in order).
+template <int K>
+__device__ void block_row(double (&v)[K], double* row) {
+  __shared__ double red[kThreads / 32][4];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int k = 0; k < K; k++) v[k] = warp_sum(v[k]);
+  if (lane == 0)
+#pragma unroll
+    for (int k = 0; k < K; k++) red[w][k] = v[k];
+  __syncthreads();
+  if ((int)threadIdx.x < K) {
+    double s = 0.0;
+    for (int i = 0; i < nw; i++) s += red[i][threadIdx.x];
+    row[threadIdx.x] = s;
+  }
+}
+
+// ---- vector and stencil kernels -------------------------------------------------
+
+// S_k.g, Y_k.g, S_k.y_new, Y_k.y_new for the pairs of this iteration (row
+// layout: dot * 16 + pair in age order).  M (= Lbfgs m) is a compile-time
+// constant so that every load of a sweep step is unconditional and can be
+// issued before any is used: pairs not yet stored (the first m - 1
+// iterations) read g instead, and their sums are ignored.  The block's
+// threads split into NG parts of at most 8 pairs each (balanced sizes).
+// Offsets are signed: g lies below the ring buffers in the workspace.
+template <int M>
+__global__ void __launch_bounds__(kThreads, 4)
+k_dir_a(const InstDesc* __restrict__ d, const MinScalars* __restrict__ st, double* part) {
+  constexpr int NG = (M + 7) / 8;
+  constexpr int GS = (M + NG - 1) / NG;  // pairs per part
+  __shared__ double wide[8 * MINIM_WIDE];
+  __shared__ int so[16], yo[16];
+  const int n = d->ndof;
+  const long long hs = d->hstride;
+  const int ii = st->ii + 1, mt = ii < M ? ii : M, c = ii % M;
+  const int pend = st->pend;
+  const bool np = pend >= 0;
+  const float* G = d->G[st->gi];
+  const float* Yn = np ? d->Yb + (long long)st->yidx[pend] * hs : G;
+  const float4* Sb4 = reinterpret_cast<const float4*>(d->Sb);
+  const float4* Yb4 = reinterpret_cast<const float4*>(d->Yb);
+  const int gS = (int)(reinterpret_cast<const float4*>(G) - Sb4);
+  const int gY = (int)(reinterpret_cast<const float4*>(G) - Yb4);
+  if (threadIdx.x < 16) {
+    const int k = threadIdx.x;
+    if (k < mt) {
+      const int s = (c - mt + k + 2 * M) % M;
+      so[k] = (int)(((long long)st->sidx[s] * hs) >> 2);
+      yo[k] = (int)(((long long)st->yidx[s] * hs) >> 2);
+    } else {
+      so[k] = gS;
+      yo[k] = gY;
+    }
+  }
+  __syncthreads();
+  const int psz = (blockDim.x / NG) & ~31;
+  const int part_ = min((int)threadIdx.x / psz, NG - 1);
+  const int k0 = GS * part_;
+  const int pt = threadIdx.x - part_ * psz;
+  float acc[4 * GS];
+#pragma unroll
+  for (int k = 0; k < 4 * GS; k++) acc[k] = 0.f;
+  int o_s[GS], o_y[GS];
+#pragma unroll
+  for (int j = 0; j < GS; j++) {
+    o_s[j] = so[min(k0 + j, 15)];
+    o_y[j] = yo[min(k0 + j, 15)];
+  }
+  const int nq4 = n >> 2;
+  const bool active = (int)threadIdx.x < NG * psz;
+  if (active) {
+    for (int i = blockIdx.x * psz + pt; i < nq4; i += gridDim.x * psz) {
+      const float4 g = ld4(G, i);
+      const float4 yn = ld4(Yn, i);
+      float4 sv[GS], yv[GS];
+#pragma unroll
+      for (int j = 0; j < GS; j++) {
+        sv[j] = Sb4[o_s[j] + i];
+        yv[j] = Yb4[o_y[j] + i];
+      }
+#pragma unroll
+      for (int j = 0; j < GS; j++) {
+        acc[j] += dot4(sv[j], g);
+        acc[GS + j] += dot4(yv[j], g);
+        acc[2 * GS + j] += dot4(sv[j], yn);
+        acc[3 * GS + j] += dot4(yv[j], yn);
+      }
+    }
+    if (blockIdx.x == 0)
+      for (int i = 4 * nq4 + pt; i < n; i += psz) {
+        const float g = G[i], yn = Yn[i];
+#pragma unroll
+        for (int j = 0; j < GS; j++) {
+          const float sv = d->Sb[4ll * o_s[j] + i], yv = d->Yb[4ll * o_y[j] + i];
+          acc[j] += sv * g;
+          acc[GS + j] += yv * g;
+          acc[2 * GS + j] += sv * yn;
+          acc[3 * GS + j] += yv * yn;
+        }
+      }
+  }
+  // pairs k0 .. k0 + GS - 1 of this part into the row (dot * 16 + pair)
+  float v[32];
+#pragma unroll
+  for (int j = 0; j < 8; j++) {
+#pragma unroll
+    for (int dd = 0; dd < 4; dd++) v[8 * dd + j] = (j < GS && active) ? acc[dd * GS + min(j, GS - 1)] : 0.f;
+  }
+  wide_clear_row(wide);
+  wide_store_row(v, k0, wide);
+  __syncthreads();
+  for (int k = threadIdx.x; k < MINIM_WIDE; k += blockDim.x) {
+    double sum = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) sum += wide[w * MINIM_WIDE + k];
+    part[(size_t)blockIdx.x * MINIM_WIDE + k] = sum;
+  }
+}
+
+// P = -gamma g - S w + gamma Y u with g.P and P.P (M compile-time, unused
+// pairs read g with weight 0)
+template <int M>
+__global__ void __launch_bounds__(kThreads, 4)
+k_dir_b(const InstDesc* __restrict__ d, const MinScalars* __restrict__ st, const StepCtl* __restrict__ ctl,
+        double* part) {
+  const int n = d->ndof, nq4 = n >> 2, mt = ctl->mt;
+  const float* G = d->G[st->gi];
+  float* P = d->Sb + (long long)st->pbuf * d->hstride;
+  const float4* Sb4 = reinterpret_cast<const float4*>(d->Sb);
+  const float4* Yb4 = reinterpret_cast<const float4*>(d->Yb);
+  const int gS = (int)(reinterpret_cast<const float4*>(G) - Sb4);
+  const int gY = (int)(reinterpret_cast<const float4*>(G) - Yb4);
+  const float fg = ctl->fg;
+  int so[M], yo[M];
+  float cS[M], cY[M];
+#pragma unroll
+  for (int k = 0; k < M; k++) {
+    const bool used = k < mt;
+    so[k] = used ? ctl->so[k] : gS;
+    yo[k] = used ? ctl->yo[k] : gY;
+    cS[k] = used ? ctl->coefS[k] : 0.f;
+    cY[k] = used ? ctl->coefY[k] : 0.f;
+  }
+  Acc d1, d2;
+  const int t0 = blockIdx.x * blockDim.x + threadIdx.x, nt = gridDim.x * blockDim.x;
+  for (int i = t0; i < nq4; i += nt) {
+    const float4 g = ld4(G, i);
+    float4 sv[M], yv[M];
+#pragma unroll
+    for (int k = 0; k < M; k++) {
+      sv[k] = Sb4[so[k] + i];
+      yv[k] = Yb4[yo[k] + i];
+    }
+    float4 q = make_float4(fg * g.x, fg * g.y, fg * g.z, fg * g.w);
+#pragma unroll
+    for (int k = 0; k < M; k++) {
+      q = axpy4(cS[k], sv[k], q);
+      q = axpy4(cY[k], yv[k], q);
+    }
+    st4(P, i, q);
+    d1.add(dot4(q, g));
+    d2.add(dot4(q, q));
+  }
+  for (int i = 4 * nq4 + t0; i < n; i += nt) {
+    const float g = G[i];
+    float q = fg * g;
+#pragma unroll
+    for (int k = 0; k < M; k++) {
+      q = fmaf(cS[k], d->Sb[4ll * so[k] + i], q);
+      q = fmaf(cY[k], d->Yb[4ll * yo[k] + i], q);
+    }
+    P[i] = q;
+    d1.add(q * g);
+    d2.add(q * q);
+  }
+  double v[2] = {d1.total(), d2.total()};
+  block_row<2>(v, part + (size_t)blockIdx.x * MINIM_WIDE);
+}
+
+// Energy at x + t P (line-search trial)
+__global__ void __launch_bounds__(kThreads, 3)
+k_eonly(const InstDesc* __restrict__ d, const MinScalars* __restrict__ st, const StepCtl* __restrict__ ctl,
+        double* part) {
+  FlatTeam tm;
+  const float* P = d->Sb + (long long)st->pbuf * d->hstride;
+  CView<float> cv{d->X32[st->xi], P, (float)ctl->t};
+  FusedEmit ne{nullptr, nullptr, nullptr, nullptr, nullptr};
+  double e;
+  if ((d->pf.n[2] & 3) == 0) e = pf1_eval_quad<float>(tm, d->pf, cv, (float*)nullptr, &ne, true, false);
+  else e = pf1_eval<float>(tm, d->pf, cv, (float*)nullptr, &ne, true, false);
+  double v[1] = {e};
+  block_row<1>(v, part + (size_t)blockIdx.x * MINIM_WIDE);
+}
+
+// Gradient at the accepted point x + t P: writes the point, the gradient and
+// y = g_new - g_old; E, g.g, P.y, y.y
+__global__ void __launch_bounds__(kThreads, 3)
+k_grad(const InstDesc* __restrict__ d, const MinScalars* __restrict__ st, const StepCtl* __restrict__ ctl,
+       double* part) {
+  FlatTeam tm;
+  const int xi = st->xi, gi = st->gi;
+  const float* P = d->Sb + (long long)st->pbuf * d->hstride;
+  CView<float> cv{d->X32[xi], P, (float)ctl->t};
+  FusedEmit em{d->G[1 - gi], d->G[gi], P, d->Yb + (long long)st->ybuf * d->hstride, nullptr};
+  double e;
+  if ((d->pf.n[2] & 3) == 0) e = pf1_eval_quad<float>(tm, d->pf, cv, d->X32[1 - xi], &em, true, true);
+  else e = pf1_eval<float>(tm, d->pf, cv, d->X32[1 - xi], &em, true, true);
+  double v[4] = {e, em.gg.total(), em.py.total(), em.yy.total()};
+  block_row<4>(v, part + (size_t)blockIdx.x * MINIM_WIDE);
+}
+
+// ---- controllers (one block) ----------------------------------------------------
+
+__global__ void k_begin(const InstDesc* __restrict__ d, const MinScalars* __restrict__ st, StepCtl* ctl,
+                        int slice, cudaGraphConditionalHandle outer) {
+  if (threadIdx.x == 0) {
+    ctl->iters = 0;
+    ctl->slice = slice;
+    ctl->kernels = 1;
+    ctl->tmark = globaltimer_ns();
+    const bool go = st->status == ST_RUNNING && st->initialised && st->stage == 0 && st->resume == 0 &&
+                    st->iter > 0 && st->iter <= d->mp.max_iter;
+    cudaGraphSetConditional(outer, go ? 1u : 0u);
+  }
+}
+
+// Device time since the previous controller finished (the phase kernel just
+// run, with its launch) goes to phase ph of the state's phase timers
+// (0 gradient, 1 line-search trials, 2 direction); phase_mark ends it.
+__device__ __forceinline__ void phase_time(MinScalars* st, StepCtl* ctl, int ph) {
+  st->tphase[ph] += (double)(globaltimer_ns() - ctl->tmark);
+}
+__device__ __forceinline__ void phase_mark(StepCtl* ctl) { ctl->tmark = globaltimer_ns(); }
+
+// dirA sums, the compact-form algebra of getDirection, pass-B coefficients
+__global__ void __launch_bounds__(kCtlThreads)
+k_ctl_a(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, const double* part, int nb) {
+  __shared__ double wide[8 * MINIM_WIDE];
+  __shared__ double wout[MINIM_WIDE];
+  sum_rows_fixed(part, nb, MINIM_WIDE, wout, wide);
+  __syncthreads();
+  if (threadIdx.x != 0) return;
+  phase_time(st, ctl, 2);
+  const int m = d->mp.m, n = d->ndof;
+  const long long hs = d->hstride;
+  const int ii = st->ii + 1, mt = ii < m ? ii : m, c = ii % m, kn = (c - 1 + m) % m;
+  const int pend = st->pend;
+  double(*SY)[MINIM_MAXM] = st->SY;
+  double(*YY)[MINIM_MAXM] = st->YY;
+  double sg[MINIM_MAXM], yg[MINIM_MAXM], u[MINIM_MAXM], w[MINIM_MAXM];
+  int sl[MINIM_MAXM];
+  for (int k = 0; k < mt; k++) {
+    sl[k] = (c - mt + k + 2 * m) % m;
+    sg[k] = st->sigma[sl[k]] * wout[k];
+    yg[k] = wout[MINIM_MAXM + k];
+  }
+  if (pend >= 0)
+    for (int k = 0; k < mt; k++) {
+      SY[sl[k]][pend] = st->sigma[sl[k]] * wout[2 * MINIM_MAXM + k];
+      YY[sl[k]][pend] = wout[3 * MINIM_MAXM + k];
+      YY[pend][sl[k]] = wout[3 * MINIM_MAXM + k];
+    }
+  const double gamma = SY[kn][kn] / YY[kn][kn];
+  for (int a = mt - 1; a >= 0; a--) {  // R u = S^T g
+    double t = sg[a];
+    for (int b = a + 1; b < mt; b++) t -= SY[sl[a]][sl[b]] * u[b];
+    u[a] = t / SY[sl[a]][sl[a]];
+  }
+  for (int a = 0; a < mt; a++) {  // R^T w = (D + gamma Y^T Y) u - gamma Y^T g
+    double t = SY[sl[a]][sl[a]] * u[a] - gamma * yg[a];
+    for (int b = 0; b < mt; b++) t += gamma * YY[sl[a]][sl[b]] * u[b];
+    for (int b = 0; b < a; b++) t -= SY[sl[b]][sl[a]] * w[b];
+    w[a] = t / SY[sl[a]][sl[a]];
+  }
+  for (int k = 0; k < MINIM_MAXM; k++) {
+    ctl->coefS[k] = (k < mt) ? (float)(-w[k] * st->sigma[sl[k]]) : 0.f;
+    ctl->coefY[k] = (k < mt) ? (float)(gamma * u[k]) : 0.f;
+    ctl->so[k] = (k < mt) ? (int)(((long long)st->sidx[sl[k]] * hs) >> 2) : 0;
+    ctl->yo[k] = (k < mt) ? (int)(((long long)st->yidx[sl[k]] * hs) >> 2) : 0;
+  }
+  ctl->fg = (float)(-gamma);
+  ctl->mt = mt;
+  st->ii = ii;
+  st->pend = -1;
+  st->abytes += (4.0 * mt + 2.0) * 4.0 * n;
+  phase_mark(ctl);
+}
+
+// dirB sums: step cap, descent check, line-search set-up
+__global__ void __launch_bounds__(kCtlThreads)
+k_ctl_b(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, const double* part, int nb,
+        cudaGraphConditionalHandle ls) {
+  __shared__ double wide[8 * MINIM_WIDE];
+  __shared__ double v[2];
+  sum_rows_fixed(part, nb, 2, v, wide);
+  __syncthreads();
+  if (threadIdx.x != 0) return;
+  phase_time(st, ctl, 2);
+  double gp = v[0], scale = 1.0;
+  if (d->mp.max_step != 0) {
+    const double ss = sqrt(v[1]);
+    if (ss > d->mp.max_step) scale = d->mp.max_step / ss;
+  }
+  gp *= scale;
+  double gs = gp;
+  if (gs > 0) {
+    gs = -gs;
+    scale = -scale;
+  }
+  ctl->t = scale;
+  if (d->mp.linesearch == 0) {
+    ctl->thr = -0.5 * gs;
+    ctl->e0 = st->E;
+    ctl->k = 0;
+    ctl->exhausted = 1;
+    cudaGraphSetConditional(ls, 1u);
+  } else {
+    ctl->exhausted = 0;
+    cudaGraphSetConditional(ls, 0u);
+  }
+  phase_mark(ctl);
+}
+
+// one line-search trial: Armijo test, or halve the step (10 trials at most;
+// after the last failure the halved step is taken unevaluated)
+__global__ void __launch_bounds__(kCtlThreads)
+k_ctl_ls(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, const double* part, int nb,
+         cudaGraphConditionalHandle ls) {
+  __shared__ double wide[8 * MINIM_WIDE];
+  __shared__ double v[1];
+  sum_rows_fixed(part, nb, 1, v, wide);
+  __syncthreads();
+  if (threadIdx.x != 0) return;
+  phase_time(st, ctl, 1);
+  st->evals++;
+  st->abytes += 8.0 * d->ndof;
+  ctl->kernels += 2;
+  bool more = false;
+  if (ctl->e0 - v[0] >= ctl->thr) {
+    ctl->exhausted = ctl->k >= 8;
+  } else {
+    ctl->t *= 0.5;
+    ctl->thr *= 0.5;
+    ctl->k++;
+    more = ctl->k < 10;
+  }
+  cudaGraphSetConditional(ls, more ? 1u : 0u);
+  phase_mark(ctl);
+}
+
+// gradient sums: the pair update of Lbfgs::iteration, then the end-of-
+// iteration decision (continue here, or hand over to the persistent kernel)
+__global__ void __launch_bounds__(kCtlThreads)
+k_ctl_g(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, const double* part, int nb,
+        cudaGraphConditionalHandle outer) {
+  __shared__ double wide[8 * MINIM_WIDE];
+  __shared__ double v[4];
+  sum_rows_fixed(part, nb, 4, v, wide);
+  __syncthreads();
+  if (threadIdx.x != 0) return;
+  phase_time(st, ctl, 0);
+  const MinParams& mp = d->mp;
+  const int n = d->ndof;
+  st->E = v[0];
+  st->gg = v[1];
+  st->evals++;
+  st->abytes += 24.0 * n;
+  st->gi ^= 1;
+  st->xi ^= 1;
+  ctl->kernels += 6;
+  const double t = ctl->t, py = v[2], yyv = v[3];
+  const double sy = t * py;
+  if (sy != 0 && isfinite(sy)) {
+    const int m = mp.m, c = st->ii % m;
+    const int os = st->sidx[c], oy = st->yidx[c];
+    st->sidx[c] = st->pbuf;
+    st->yidx[c] = st->ybuf;
+    st->rho[c] = 1.0 / sy;
+    st->sigma[c] = t;
+    st->yy[c] = yyv;
+    st->pbuf = os;
+    st->ybuf = oy;
+    st->pend = c;
+  } else {
+    st->ii--;
+  }
+  // the persistent kernel's end-of-iteration rules, on copies
+  const bool exh = ctl->exhausted != 0;
+  const bool finite = isfinite(st->E) && isfinite(st->gg);
+  const double r = sqrt(st->gg / n);
+  const bool conv = r < mp.tol;
+  const bool mixed = mp.precision == 0;
+  int cool = st->cool, stall = st->stall, exr = st->exhausted_run, why = 0;
+  double best = st->best_rms;
+  if (mixed) {
+    if (cool > 0) cool--;
+    if (r < 0.999 * best) {
+      best = r;
+      stall = 0;
+    } else {
+      stall++;
+    }
+    exr = exr * 7 / 8 + (exh ? 8 : 0);
+    why = conv ? 1
+               : ((exr >= 20 || (exh && r < 1000.0 * mp.tol))
+                      ? 2
+                      : ((stall >= 100 && r < 100.0 * mp.tol && cool == 0) ? 3 : 0));
+  }
+  bool stop;
+  if (finite && !conv && why == 0) {
+    if (mixed) {
+      st->cool = cool;
+      st->stall = stall;
+      st->exhausted_run = exr;
+      st->best_rms = best;
+    }
+    st->iter++;
+    ctl->iters++;
+    stop = st->iter > mp.max_iter || ctl->iters >= ctl->slice;
+  } else {
+    st->resume = 1;
+    st->resume_exhausted = exh ? 1 : 0;
+    stop = true;
+  }
+  cudaGraphSetConditional(outer, stop ? 0u : 1u);
+  phase_mark(ctl);
+}
+
+int occupancy(const void* f, int threads) {
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, f, threads, 0) != cudaSuccess) return 0;
+  return per_sm;
+}
+
+}  // namespace
+
+// One instance's stepped graph.
+struct SteppedGraph {
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  StepCtl* ctl = nullptr;
+  double* part = nullptr;
+  const MinScalars* st = nullptr;
+  int slice = 0, m = 0;
+};
+
+}  // namespace mg
+
+using namespace mg;
+
+#define SCK(call)               \
+  do {                          \
+    const int e_ = (int)(call); \
+    if (e_ != 0) return e_;     \
+  } while (0)
+
+namespace {
+
+int add_kernel(cudaGraphNode_t* node, cudaGraph_t g, const cudaGraphNode_t* deps, int ndeps, const void* f,
+               int blocks, int threads, void** args) {
+  cudaKernelNodeParams p{};
+  p.func = const_cast<void*>(f);
+  p.gridDim = dim3(blocks);
+  p.blockDim = dim3(threads);
+  p.sharedMemBytes = 0;
+  p.kernelParams = args;
+  return (int)cudaGraphAddKernelNode(node, g, deps, ndeps, &p);
+}
+
+int add_while(cudaGraphNode_t* node, cudaGraph_t g, const cudaGraphNode_t* deps, int ndeps,
+              cudaGraphConditionalHandle h, cudaGraph_t* body) {
+  cudaGraphNodeParams p{};
+  p.type = cudaGraphNodeTypeConditional;
+  p.conditional.handle = h;
+  p.conditional.type = cudaGraphCondTypeWhile;
+  p.conditional.size = 1;
+  SCK(cudaGraphAddNode(node, g, deps, nullptr, (size_t)ndeps, &p));
+  *body = p.conditional.phGraph_out[0];
+  return 0;
+}
+
+template <int M>
+void dir_kernels_m(const void** a, const void** b) {
+  *a = (const void*)k_dir_a<M>;
+  *b = (const void*)k_dir_b<M>;
+}
+// the direction kernels for history length m (1 .. MINIM_MAXM)
+bool dir_kernels(int m, const void** a, const void** b) {
+  switch (m) {
+#define MG_DIR_CASE(M)      \
+  case M:                   \
+    dir_kernels_m<M>(a, b); \
+    return true;
+    MG_DIR_CASE(1) MG_DIR_CASE(2) MG_DIR_CASE(3) MG_DIR_CASE(4) MG_DIR_CASE(5) MG_DIR_CASE(6)
+    MG_DIR_CASE(7) MG_DIR_CASE(8) MG_DIR_CASE(9) MG_DIR_CASE(10) MG_DIR_CASE(11) MG_DIR_CASE(12)
+    MG_DIR_CASE(13) MG_DIR_CASE(14) MG_DIR_CASE(15) MG_DIR_CASE(16)
+#undef MG_DIR_CASE
+    default:
+      return false;
+  }
+}
+
+int build(SteppedGraph* sg, const InstDesc* d, MinScalars* st, int m, int nsm, int slice, cudaStream_t s) {
+  const void* fa = nullptr;
+  const void* fb = nullptr;
+  if (!dir_kernels(m, &fa, &fb)) return (int)cudaErrorInvalidValue;
+  const int occ_a = occupancy(fa, kThreads), occ_b = occupancy(fb, kThreads);
+  const int occ_e = occupancy((const void*)k_eonly, kThreads), occ_g = occupancy((const void*)k_grad, kThreads);
+  if (!occ_a || !occ_b || !occ_e || !occ_g) return (int)cudaErrorInvalidConfiguration;
+  int nb_a = nsm * occ_a, nb_b = nsm * occ_b, nb_e = nsm * occ_e, nb_g = nsm * occ_g;
+  const int nb_max = std::max(std::max(nb_a, nb_b), std::max(nb_e, nb_g));
+  SCK(cudaMallocAsync((void**)&sg->ctl, sizeof(StepCtl), s));
+  SCK(cudaMallocAsync((void**)&sg->part, (size_t)nb_max * MINIM_WIDE * sizeof(double), s));
+  SCK(cudaMemsetAsync(sg->ctl, 0, sizeof(StepCtl), s));
+  sg->st = st;
+  sg->slice = slice;
+  sg->m = m;
+  cudaGraph_t g = nullptr;
+  SCK(cudaGraphCreate(&g, 0));
+  sg->graph = g;
+  cudaGraphConditionalHandle h_outer, h_ls;
+  SCK(cudaGraphConditionalHandleCreate(&h_outer, g, 1, cudaGraphCondAssignDefault));
+  StepCtl* ctl = sg->ctl;
+  double* part = sg->part;
+  cudaGraphNode_t n_begin, n_outer;
+  {
+    void* args[] = {(void*)&d, (void*)&st, (void*)&ctl, (void*)&sg->slice, (void*)&h_outer};
+    SCK(add_kernel(&n_begin, g, nullptr, 0, (const void*)k_begin, 1, 32, args));
+  }
+  cudaGraph_t body;
+  SCK(add_while(&n_outer, g, &n_begin, 1, h_outer, &body));
+  SCK(cudaGraphConditionalHandleCreate(&h_ls, body, 0, 0));
+  cudaGraphNode_t na, nca, nb, ncb, nls, ngr, ncg;
+  {
+    void* args[] = {(void*)&d, (void*)&st, (void*)&part};
+    SCK(add_kernel(&na, body, nullptr, 0, fa, nb_a, kThreads, args));
+  }
+  {
+    void* args[] = {(void*)&d, (void*)&st, (void*)&ctl, (void*)&part, (void*)&nb_a};
+    SCK(add_kernel(&nca, body, &na, 1, (const void*)k_ctl_a, 1, kCtlThreads, args));
+  }
+  {
+    void* args[] = {(void*)&d, (void*)&st, (void*)&ctl, (void*)&part};
+    SCK(add_kernel(&nb, body, &nca, 1, fb, nb_b, kThreads, args));
+  }
+  {
+    void* args[] = {(void*)&d, (void*)&st, (void*)&ctl, (void*)&part, (void*)&nb_b, (void*)&h_ls};
+    SCK(add_kernel(&ncb, body, &nb, 1, (const void*)k_ctl_b, 1, kCtlThreads, args));
+  }
+  cudaGraph_t ls_body;
+  SCK(add_while(&nls, body, &ncb, 1, h_ls, &ls_body));
+  {
+    cudaGraphNode_t ne, ncl;
+    void* args_e[] = {(void*)&d, (void*)&st, (void*)&ctl, (void*)&part};
+    SCK(add_kernel(&ne, ls_body, nullptr, 0, (const void*)k_eonly, nb_e, kThreads, args_e));
+    void* args_c[] = {(void*)&d, (void*)&st, (void*)&ctl, (void*)&part, (void*)&nb_e, (void*)&h_ls};
+    SCK(add_kernel(&ncl, ls_body, &ne, 1, (const void*)k_ctl_ls, 1, kCtlThreads, args_c));
+  }
+  {
+    void* args[] = {(void*)&d, (void*)&st, (void*)&ctl, (void*)&part};
+    SCK(add_kernel(&ngr, body, &nls, 1, (const void*)k_grad, nb_g, kThreads, args));
+  }
+  {
+    void* args[] = {(void*)&d, (void*)&st, (void*)&ctl, (void*)&part, (void*)&nb_g, (void*)&h_outer};
+    SCK(add_kernel(&ncg, body, &ngr, 1, (const void*)k_ctl_g, 1, kCtlThreads, args));
+  }
+  SCK(cudaGraphInstantiate(&sg->exec, g, 0));
+  return 0;
+}
+
+}  // namespace
+
+// Runs up to `slice` FP32 L-BFGS iterations (history m) of the binary
+// PhaseField instance (device descriptor d, state st) as one graph launch on
+// stream s.  The graph is built on the first call for this state record and
+// kept in *cache.  Adds the kernels executed to *kernels.  Returns a
+// cudaError_t.
+extern "C" int mg_stepped_pf1_run(void** cache, const InstDesc* d, MinScalars* st, int m, int nsm, int slice,
+                                  void* stream, double* kernels) {
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  SteppedGraph* sg = static_cast<SteppedGraph*>(*cache);
+  if (sg && (sg->st != st || sg->slice != slice || sg->m != m)) {
+    SCK(cudaStreamSynchronize(s));
+    mg_stepped_free(cache);
+    sg = nullptr;
+  }
+  if (!sg) {
+    sg = new SteppedGraph;
+    *cache = sg;
+    SCK(build(sg, d, st, m, nsm, slice, s));
+  }
+  SCK(cudaGraphLaunch(sg->exec, s));
+  double k = 0;
+  SCK(cudaMemcpyAsync(&k, &sg->ctl->kernels, sizeof(double), cudaMemcpyDeviceToHost, s));
+  SCK(cudaStreamSynchronize(s));
+  if (kernels) *kernels += k;
+  return 0;
+}
+
+extern "C" void mg_stepped_free(void** cache) {
+  SteppedGraph* sg = static_cast<SteppedGraph*>(*cache);
+  if (!sg) return;
+  if (sg->exec) cudaGraphExecDestroy(sg->exec);
+  if (sg->graph) cudaGraphDestroy(sg->graph);
+  if (sg->ctl) cudaFree(sg->ctl);
+  if (sg->part) cudaFree(sg->part);
+  delete sg;
+  *cache = nullptr;
+}

@@ -187,6 +187,64 @@ def test_pf_binary_minimise():
     check_minimum(p, x0, inst.coords, r, 1e-7)
 
 
+@pytest.mark.parametrize("grid,prec", [((64, 64, 64), "mixed"), ((64, 64, 66), "mixed"), ((64, 64, 64), "fp32")])
+def test_pf_binary_minimise_stepped(grid, prec):
+    """Large binary PhaseField: the FP32 stage runs as a graph of phase
+    kernels (quad stencil when nz % 4 == 0, scalar stencil otherwise); the
+    result is a minimum under the oracle, like the persistent path's."""
+    x0 = pf_noise(grid, seed=23, amp=0.05)
+    p = abi.phase_field(grid, interface_size=1.0, surface_tension=1.0)
+    inst = runtime.Instance(p, x0)
+    tol = 1e-7 if prec == "mixed" else 1e-5
+    r = inst.minimise(abi.minimiser("lbfgs", m=10, tol=tol, precision=prec))
+    assert r.status == abi.RES_CONVERGED, r.as_dict()
+    st = runtime.last_run_stats()
+    assert st["launches"] > 20  # phase kernels, not one persistent launch per slice
+    check_minimum(p, x0, inst.coords, r, tol)
+
+
+def test_pf_stepped_max_iter():
+    """The stepped path stops at max_iter like the persistent one."""
+    grid = (64, 64, 64)
+    x0 = pf_noise(grid, seed=25, amp=0.05)
+    inst = runtime.Instance(abi.phase_field(grid, interface_size=1.0, surface_tension=1.0), x0)
+    r = inst.minimise(abi.minimiser("lbfgs", m=10, tol=1e-7, max_iter=19))
+    assert r.status == abi.RES_MAXITER, r.as_dict()
+    assert r.iter == 20
+
+
+def test_pf_stepped_matches_persistent_path():
+    """Same minimisation with the stepped FP32 stage switched off (separate
+    process): same minimum to the tolerance, similar iteration count."""
+    import json
+    import os
+    import subprocess
+    import sys
+    grid = (64, 64, 64)
+    x0 = pf_noise(grid, seed=24, amp=0.05)
+    p = abi.phase_field(grid, interface_size=1.0, surface_tension=1.0)
+    inst = runtime.Instance(p, x0)
+    r = inst.minimise(abi.minimiser("lbfgs", m=10, tol=1e-7))
+    code = (
+        "import json, sys; sys.path.insert(0, '.');"
+        "from minim_gb300 import abi, runtime; from tests.workloads import pf_noise;"
+        "g = (64, 64, 64); x0 = pf_noise(g, seed=24, amp=0.05);"
+        "i = runtime.Instance(abi.phase_field(g, interface_size=1.0, surface_tension=1.0), x0);"
+        "r = i.minimise(abi.minimiser('lbfgs', m=10, tol=1e-7));"
+        "print(json.dumps({'status': r.status, 'iter': r.iter, 'energy': r.energy}))"
+    )
+    repo = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    env = dict(os.environ, MINIM_GPU_STEPPED="0")
+    out = subprocess.run([sys.executable, "-c", code], cwd=repo, env=env, capture_output=True, text=True,
+                         timeout=300)
+    assert out.returncode == 0, out.stderr
+    q = json.loads(out.stdout.strip().splitlines()[-1])
+    assert r.status == q["status"] == abi.RES_CONVERGED
+    e_init = Oracle(p, x0).energy(x0)
+    assert abs(r.energy - q["energy"]) <= 1e-8 * max(abs(r.energy), abs(e_init))
+    assert abs(r.iter - q["iter"]) <= 0.2 * q["iter"] + 10
+
+
 def test_pf_ternary_volume_minimise_batch():
     shape = (24, 24, 1)
     p = abi.phase_field(shape, nfluid=3, volume_fixed=True)
