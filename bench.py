@@ -202,6 +202,8 @@ def run_gpu(args):
     }
     if not args.no_batched:
         out.update(run_batched(args))
+    if args.serve > 0:
+        out.update(run_serving(args))
     if not args.no_cpu:
         out["cpu_baseline"] = cpu_baseline(results[-1].iter, budget_s=args.cpu_budget)
     return out
@@ -247,6 +249,108 @@ def run_batched(args):
         "plain": {"value": plain, "unit": "minimisations/s", "sample": int(len(idx))},
         "batched_vs_plain": batched / plain,
     }
+
+
+def serving_requests(count, rate, seed=7):
+    """A seeded Poisson stream of mixed requests shaped like the serving
+    workload (LjNd clusters, 2-D / 3-D PhaseField grids with and without solid
+    spheres, BarAndHinge sheets), with sizes capped so that the whole stream
+    runs in seconds: LJ N log-uniform in [13, 400], PF sides 64-128 (2-D) or
+    24-48 (3-D), sheets of 32^2 .. 48^2 vertices."""
+    from minim_gb300 import abi, runtime
+    from tests.workloads import Rng, lj_cluster, pf_noise, sheet
+    rng = Rng(seed)
+    u = rng.uniform(6 * count).reshape(count, 6)
+    t = np.cumsum(-np.log(1.0 - u[:, 0]) / rate)
+    reqs = []
+    for i in range(count):
+        kind = int(u[i, 1] * 3)
+        if kind == 0:
+            n = int(np.exp(np.log(13) + u[i, 2] * (np.log(400) - np.log(13))))
+            reqs.append((t[i], "lj", abi.lj(), lj_cluster(n, seed=1000 + i), abi.minimiser("lbfgs", m=5, tol=1e-6)))
+        elif kind == 1:
+            if u[i, 3] < 0.5:
+                side = 64 + int(u[i, 4] * 65)
+                grid = (side, side, 1)
+            else:
+                side = 24 + int(u[i, 4] * 25)
+                grid = (side, side, side)
+            x0 = pf_noise(grid, seed=3000 + i)
+            p = abi.phase_field(grid, interface_size=1.0, surface_tension=1.0)
+            if u[i, 5] < 0.5:
+                # random spheres until about 20 % of the nodes are solid; a
+                # layout with a node shape the reference cannot classify
+                # (PhaseField::getType) is drawn again
+                r2 = Rng(2000 + i)
+                idx = np.indices(grid).reshape(3, -1).T
+                on = np.array(grid) > 1
+                for _ in range(20):
+                    mask = np.zeros(int(np.prod(grid)), bool)
+                    while mask.mean() < 0.2:
+                        c = r2.uniform(3) * np.array(grid)
+                        rad = 3 + r2.uniform() * grid[0] / 8
+                        mask |= (((idx - c) ** 2) * on).sum(axis=1) < rad * rad
+                    ps = abi.phase_field(grid, interface_size=1.0, surface_tension=1.0,
+                                         solid=mask.astype(np.uint8))
+                    try:
+                        runtime.pf_setup(ps, x0)
+                    except runtime.MinimGpuError:
+                        continue
+                    p = ps
+                    break
+            reqs.append((t[i], "pf", p, x0, abi.minimiser("lbfgs", m=5, tol=1e-7)))
+        else:
+            k = 32 + int(u[i, 2] * 17)
+            flat, tris, pert = sheet(k, seed=4000 + i)
+            p0 = abi.bar_and_hinge(triangulation=tris, rigidity=(1, 0.01))
+            _, bpar, _, hpar = runtime.bah_elements(p0, flat)
+            p = abi.bar_and_hinge(triangulation=tris, rigidity=(1, 0.01), length0=bpar[:, 1].copy(),
+                                  theta0=hpar[:, 1].copy())
+            reqs.append((t[i], "bah", p, pert, abi.minimiser("lbfgs", m=5, tol=1e-7)))
+    return reqs
+
+
+def run_serving(args):
+    """Continuous batching under a Poisson arrival stream: requests are
+    submitted when their arrival time has passed, the server admits them as
+    slots and memory free up, and latency is completion minus arrival."""
+    from minim_gb300 import abi, runtime
+    reqs = serving_requests(args.serve, args.serve_rate)
+    srv = runtime.Server()
+    # warm-up: a few requests of each kind
+    for _, _, p, x0, mp in reqs[:6]:
+        srv.submit(p, x0, mp)
+    while srv.ndof:
+        srv.step()
+        for rid, _ in srv.poll():
+            srv.take(rid)
+    arrival, done_t, status = {}, {}, {}
+    t0 = time.perf_counter()
+    nxt = 0
+    while len(done_t) < len(reqs):
+        now = time.perf_counter() - t0
+        while nxt < len(reqs) and reqs[nxt][0] <= now:
+            _, _, p, x0, mp = reqs[nxt]
+            rid = srv.submit(p, x0, mp)
+            arrival[rid] = reqs[nxt][0]
+            nxt += 1
+        if srv.ndof:
+            srv.step()
+        elif nxt < len(reqs):
+            time.sleep(max(0.0, reqs[nxt][0] - (time.perf_counter() - t0)))
+        for rid, r in srv.poll():
+            done_t[rid] = time.perf_counter() - t0
+            status[rid] = r.status
+            srv.take(rid)
+    wall = time.perf_counter() - t0
+    lat = np.array([1e3 * (done_t[r] - arrival[r]) for r in done_t])
+    conv = sum(1 for r in status.values() if r == abi.RES_CONVERGED)
+    srv.close()
+    return {"serving": {"value": conv / wall, "unit": "converged minimisations/s", "requests": len(reqs),
+                        "converged": conv, "wall_s": wall, "p50_ms": float(np.percentile(lat, 50)),
+                        "p99_ms": float(np.percentile(lat, 99)), "arrival_rate": args.serve_rate,
+                        "workload": "Poisson stream of LJ (N 13-400), 2-D/3-D PhaseField (half with 20% solid "
+                                    "spheres) and BarAndHinge sheets (1k-2.3k vertices), Lbfgs"}}
 
 
 def cpu_baseline(gpu_iters, budget_s=20.0):
@@ -313,6 +417,8 @@ def main():
     ap.add_argument("--batch", type=int, default=1024)
     ap.add_argument("--plain-sample", type=int, default=16)
     ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--serve", type=int, default=200, help="requests in the serving stream (0 = skip)")
+    ap.add_argument("--serve-rate", type=float, default=2000.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=20.0)
     ap.add_argument("--ref-iters-hint", type=int, default=600)
