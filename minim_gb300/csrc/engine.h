@@ -196,7 +196,7 @@ int mg_convert(const void* src, void* dst, size_t n, int to_float, void* stream)
 // stepped.cu: up to `slice` FP32 L-BFGS iterations (history m) of a binary
 // PhaseField instance as one graph launch (graph cached in *cache); returns
 // a cudaError_t
-int mg_stepped_pf1_run(void** cache, const mg::InstDesc* d, mg::MinScalars* st, int m, int nsm, int slice,
-                       void* stream, double* kernels);
+int mg_stepped_pf1_run(void** cache, const mg::InstDesc* d, mg::MinScalars* st, int m, const int* grid,
+                       int nsm, int slice, void* stream, double* kernels);
 void mg_stepped_free(void** cache);
 }

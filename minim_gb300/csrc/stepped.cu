@@ -30,6 +30,8 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 
 #include "kernels.cuh"
 
@@ -52,7 +54,26 @@ struct StepCtl {
   float fg;                  // -gamma
   float coefS[MINIM_MAXM], coefY[MINIM_MAXM];
   int so[MINIM_MAXM], yo[MINIM_MAXM];  // slot buffers: float4 offsets from the ring bases
+  // stencil kernels' span (first block's start, last block's end), split
+  // into the gap before, the kernel and the gap after; [0] trials, [1] gradient
+  unsigned long long ks, ke;
+  unsigned kdone;
+  double gap_pre[2], kdur[2], gap_post[2];
 };
+
+// span bookkeeping of a stencil kernel (first block in, last block out)
+__device__ __forceinline__ void span_begin(StepCtl* ctl) {
+  if (blockIdx.x == 0 && threadIdx.x == 0 && threadIdx.y == 0) ctl->ks = globaltimer_ns();
+}
+__device__ __forceinline__ void span_end(StepCtl* ctl) {
+  if (threadIdx.x == 0 && threadIdx.y == 0) {
+    __threadfence();
+    if (atomicAdd(&ctl->kdone, 1u) == gridDim.x - 1) {
+      ctl->ke = globaltimer_ns();
+      ctl->kdone = 0;
+    }
+  }
+}
 
 constexpr int kThreads = 256;
 constexpr int kCtlThreads = 256;
@@ -62,17 +83,19 @@ constexpr int kCtlThreads = 256;
 template <int K>
 __device__ void block_row(double (&v)[K], double* row) {
   __shared__ double red[kThreads / 32][4];
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  // linear thread index (blocks may be 2-D); the block has whole warps
+  const int tl = threadIdx.y * blockDim.x + threadIdx.x;
+  const int lane = tl & 31, w = tl >> 5, nw = (blockDim.x * blockDim.y) >> 5;
 #pragma unroll
   for (int k = 0; k < K; k++) v[k] = warp_sum(v[k]);
   if (lane == 0)
 #pragma unroll
     for (int k = 0; k < K; k++) red[w][k] = v[k];
   __syncthreads();
-  if ((int)threadIdx.x < K) {
+  if (tl < K) {
     double s = 0.0;
-    for (int i = 0; i < nw; i++) s += red[i][threadIdx.x];
-    row[threadIdx.x] = s;
+    for (int i = 0; i < nw; i++) s += red[i][tl];
+    row[tl] = s;
   }
 }
 
@@ -240,8 +263,8 @@ k_dir_b(const InstDesc* __restrict__ d, const MinScalars* __restrict__ st, const
 
 // Energy at x + t P (line-search trial)
 __global__ void __launch_bounds__(kThreads, 3)
-k_eonly(const InstDesc* __restrict__ d, const MinScalars* __restrict__ st, const StepCtl* __restrict__ ctl,
-        double* part) {
+k_eonly(const InstDesc* __restrict__ d, const MinScalars* __restrict__ st, StepCtl* ctl, double* part) {
+  span_begin(ctl);
   FlatTeam tm;
   const float* P = d->Sb + (long long)st->pbuf * d->hstride;
   CView<float> cv{d->X32[st->xi], P, (float)ctl->t};
@@ -251,13 +274,14 @@ k_eonly(const InstDesc* __restrict__ d, const MinScalars* __restrict__ st, const
   else e = pf1_eval<float>(tm, d->pf, cv, (float*)nullptr, &ne, true, false);
   double v[1] = {e};
   block_row<1>(v, part + (size_t)blockIdx.x * MINIM_WIDE);
+  span_end(ctl);
 }
 
 // Gradient at the accepted point x + t P: writes the point, the gradient and
 // y = g_new - g_old; E, g.g, P.y, y.y
 __global__ void __launch_bounds__(kThreads, 3)
-k_grad(const InstDesc* __restrict__ d, const MinScalars* __restrict__ st, const StepCtl* __restrict__ ctl,
-       double* part) {
+k_grad(const InstDesc* __restrict__ d, const MinScalars* __restrict__ st, StepCtl* ctl, double* part) {
+  span_begin(ctl);
   FlatTeam tm;
   const int xi = st->xi, gi = st->gi;
   const float* P = d->Sb + (long long)st->pbuf * d->hstride;
@@ -268,6 +292,109 @@ k_grad(const InstDesc* __restrict__ d, const MinScalars* __restrict__ st, const 
   else e = pf1_eval<float>(tm, d->pf, cv, d->X32[1 - xi], &em, true, true);
   double v[4] = {e, em.gg.total(), em.py.total(), em.yy.total()};
   block_row<4>(v, part + (size_t)blockIdx.x * MINIM_WIDE);
+  span_end(ctl);
+}
+
+// ---- line-shaped stencil (binary PhaseField, nz % 4 == 0) ------------------------
+// Threads are laid out as (nz/4 quads along z) x (lines per block), so a
+// thread's quad index needs no division and each line's x, y come from one
+// division; a quad's four cells are evaluated from 16-byte loads of the quad
+// and of its four neighbour lines plus two scalars at the z ends.  The trial
+// energy is summed per quad in FP32 and per thread with compensation; the
+// gradient variant also writes the point, g and y = g - g_old.
+template <bool WANT_G>
+__global__ void __launch_bounds__(kThreads, WANT_G ? 3 : 4)
+k_lines(const InstDesc* __restrict__ d, const MinScalars* __restrict__ st, StepCtl* ctl, double* part) {
+  span_begin(ctl);
+  const PotPF& Pf = d->pf;
+  const int nx = Pf.n[0], ny = Pf.n[1], nz = Pf.n[2], nz4 = nz >> 2;
+  const int xi = st->xi, gi = st->gi;
+  const float* X = d->X32[xi];
+  const float* Pd = d->Sb + (long long)st->pbuf * d->hstride;
+  const float t = (float)ctl->t;
+  const float V = (float)Pf.vol_of_type[1];
+  const float fb = (float)Pf.kappa[0] / 16 * V;
+  const float Fi = 0.25f / (float)Pf.res2 * (float)Pf.kappaP[0] * V;
+  const float pr = (Pf.flags & PF_PRESSURE) ? (float)Pf.pressure[0] : 0.f;
+  const bool dx_on = nx > 1, dy_on = ny > 1;
+  const int zq = threadIdx.x, nl = nx * ny;
+  const int z0 = 4 * zq;
+  const int izm = z0 == 0 ? nz - 1 : z0 - 1, izp = z0 + 4 == nz ? 0 : z0 + 4;
+  Acc e, gg, py, yy;
+  if (zq < nz4) {
+    for (int l = blockIdx.x * blockDim.y + threadIdx.y; l < nl; l += gridDim.x * blockDim.y) {
+      const int x = l / ny, y = l - x * ny;
+      const int lym = x * ny + (y == 0 ? ny - 1 : y - 1), lyp = x * ny + (y == ny - 1 ? 0 : y + 1);
+      const int lxm = (x == 0 ? nx - 1 : x - 1) * ny + y, lxp = (x == nx - 1 ? 0 : x + 1) * ny + y;
+      const int q = l * nz4 + zq;
+      // every load of the quad first
+      const float4 xc = ld4(X, q), pc = ld4(Pd, q);
+      const float xzm = X[l * nz + izm], pzm = Pd[l * nz + izm];
+      const float xzp = X[l * nz + izp], pzp = Pd[l * nz + izp];
+      const float4 xym = ld4(X, lym * nz4 + zq), pym = ld4(Pd, lym * nz4 + zq);
+      const float4 xyp = ld4(X, lyp * nz4 + zq), pyp = ld4(Pd, lyp * nz4 + zq);
+      const float4 xxm = ld4(X, lxm * nz4 + zq), pxm = ld4(Pd, lxm * nz4 + zq);
+      const float4 xxp = ld4(X, lxp * nz4 + zq), pxp = ld4(Pd, lxp * nz4 + zq);
+      float4 go = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (WANT_G) go = ld4(d->G[gi], q);
+      auto tr = [t](float4 a, float4 b) {
+        return make_float4(__fadd_rn(a.x, __fmul_rn(t, b.x)), __fadd_rn(a.y, __fmul_rn(t, b.y)),
+                           __fadd_rn(a.z, __fmul_rn(t, b.z)), __fadd_rn(a.w, __fmul_rn(t, b.w)));
+      };
+      const float4 c4 = tr(xc, pc);
+      const float cc[4] = {c4.x, c4.y, c4.z, c4.w};
+      const float zm = __fadd_rn(xzm, __fmul_rn(t, pzm)), zp = __fadd_rn(xzp, __fmul_rn(t, pzp));
+      const float4 ym = tr(xym, pym), yp = tr(xyp, pyp), xm = tr(xxm, pxm), xp = tr(xxp, pxp);
+      const float ymv[4] = {ym.x, ym.y, ym.z, ym.w}, ypv[4] = {yp.x, yp.y, yp.z, yp.w};
+      const float xmv[4] = {xm.x, xm.y, xm.z, xm.w}, xpv[4] = {xp.x, xp.y, xp.z, xp.w};
+      float es = 0.f, g[4];
+#pragma unroll
+      for (int j = 0; j < 4; j++) {
+        const float c = cc[j];
+        const float cm = j == 0 ? zm : cc[j - 1], cp = j == 3 ? zp : cc[j + 1];
+        float gm = c - cm, gp = c - cp;
+        float lap = gm + gp, eg = 0.5f * (gm * gm + gp * gp);
+        if (dy_on) {
+          gm = c - ymv[j];
+          gp = c - ypv[j];
+          lap += gm + gp;
+          eg += 0.5f * (gm * gm + gp * gp);
+        }
+        if (dx_on) {
+          gm = c - xmv[j];
+          gp = c - xpv[j];
+          lap += gm + gp;
+          eg += 0.5f * (gm * gm + gp * gp);
+        }
+        const float a = (c + 1) * (c - 1);
+        es += fb * a * a + Fi * eg;
+        if (pr != 0.f) es -= pr * (0.5f * (c + 1) * V);
+        if (WANT_G) {
+          g[j] = fb * 4 * c * (c * c - 1) + 2 * Fi * lap;
+          if (pr != 0.f) g[j] -= 0.5f * pr * V;
+        }
+      }
+      e.add(es);
+      if (WANT_G) {
+        const float4 gv = make_float4(g[0], g[1], g[2], g[3]);
+        st4(d->X32[1 - xi], q, c4);
+        st4(d->G[1 - gi], q, gv);
+        gg.add(dot4(gv, gv));
+        const float4 yv = make_float4(g[0] - go.x, g[1] - go.y, g[2] - go.z, g[3] - go.w);
+        st4(d->Yb + (long long)st->ybuf * d->hstride, q, yv);
+        py.add(dot4(pc, yv));
+        yy.add(dot4(yv, yv));
+      }
+    }
+  }
+  if (WANT_G) {
+    double v[4] = {e.total(), gg.total(), py.total(), yy.total()};
+    block_row<4>(v, part + (size_t)blockIdx.x * MINIM_WIDE);
+  } else {
+    double v[1] = {e.total()};
+    block_row<1>(v, part + (size_t)blockIdx.x * MINIM_WIDE);
+  }
+  span_end(ctl);
 }
 
 // ---- controllers (one block) ----------------------------------------------------
@@ -393,6 +520,12 @@ k_ctl_ls(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, const dou
   __syncthreads();
   if (threadIdx.x != 0) return;
   phase_time(st, ctl, 1);
+  {
+    const unsigned long long now = globaltimer_ns();
+    ctl->gap_pre[0] += (double)(ctl->ks - ctl->tmark);
+    ctl->kdur[0] += (double)(ctl->ke - ctl->ks);
+    ctl->gap_post[0] += (double)(now - ctl->ke);
+  }
   st->evals++;
   st->abytes += 8.0 * d->ndof;
   ctl->kernels += 2;
@@ -420,6 +553,12 @@ k_ctl_g(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, const doub
   __syncthreads();
   if (threadIdx.x != 0) return;
   phase_time(st, ctl, 0);
+  {
+    const unsigned long long now = globaltimer_ns();
+    ctl->gap_pre[1] += (double)(ctl->ks - ctl->tmark);
+    ctl->kdur[1] += (double)(ctl->ke - ctl->ks);
+    ctl->gap_post[1] += (double)(now - ctl->ke);
+  }
   const MinParams& mp = d->mp;
   const int n = d->ndof;
   st->E = v[0];
@@ -518,11 +657,11 @@ using namespace mg;
 namespace {
 
 int add_kernel(cudaGraphNode_t* node, cudaGraph_t g, const cudaGraphNode_t* deps, int ndeps, const void* f,
-               int blocks, int threads, void** args) {
+               int blocks, dim3 threads, void** args) {
   cudaKernelNodeParams p{};
   p.func = const_cast<void*>(f);
   p.gridDim = dim3(blocks);
-  p.blockDim = dim3(threads);
+  p.blockDim = threads;
   p.sharedMemBytes = 0;
   p.kernelParams = args;
   return (int)cudaGraphAddKernelNode(node, g, deps, ndeps, &p);
@@ -561,12 +700,23 @@ bool dir_kernels(int m, const void** a, const void** b) {
   }
 }
 
-int build(SteppedGraph* sg, const InstDesc* d, MinScalars* st, int m, int nsm, int slice, cudaStream_t s) {
+int build(SteppedGraph* sg, const InstDesc* d, MinScalars* st, int m, const int* grid, int nsm, int slice,
+          cudaStream_t s) {
   const void* fa = nullptr;
   const void* fb = nullptr;
   if (!dir_kernels(m, &fa, &fb)) return (int)cudaErrorInvalidValue;
+  // the line-shaped stencil when z splits into quads and a block holds whole
+  // warps of lines (nz / 4 quads x lines per block <= 256 threads)
+  const int nz4 = grid[2] / 4;
+  const bool lines = grid[2] % 4 == 0 && nz4 <= 256;
+  int by = lines ? kThreads / nz4 : 1;
+  while (lines && by > 1 && (nz4 * by) % 32) by--;
+  const bool use_lines = lines && (nz4 * by) % 32 == 0;
+  const dim3 sblock = use_lines ? dim3(nz4, by) : dim3(kThreads);
+  const void* fe = use_lines ? (const void*)k_lines<false> : (const void*)k_eonly;
+  const void* fg = use_lines ? (const void*)k_lines<true> : (const void*)k_grad;
   const int occ_a = occupancy(fa, kThreads), occ_b = occupancy(fb, kThreads);
-  const int occ_e = occupancy((const void*)k_eonly, kThreads), occ_g = occupancy((const void*)k_grad, kThreads);
+  const int occ_e = occupancy(fe, (int)(sblock.x * sblock.y)), occ_g = occupancy(fg, (int)(sblock.x * sblock.y));
   if (!occ_a || !occ_b || !occ_e || !occ_g) return (int)cudaErrorInvalidConfiguration;
   int nb_a = nsm * occ_a, nb_b = nsm * occ_b, nb_e = nsm * occ_e, nb_g = nsm * occ_g;
   const int nb_max = std::max(std::max(nb_a, nb_b), std::max(nb_e, nb_g));
@@ -613,13 +763,13 @@ int build(SteppedGraph* sg, const InstDesc* d, MinScalars* st, int m, int nsm, i
   {
     cudaGraphNode_t ne, ncl;
     void* args_e[] = {(void*)&d, (void*)&st, (void*)&ctl, (void*)&part};
-    SCK(add_kernel(&ne, ls_body, nullptr, 0, (const void*)k_eonly, nb_e, kThreads, args_e));
+    SCK(add_kernel(&ne, ls_body, nullptr, 0, fe, nb_e, sblock, args_e));
     void* args_c[] = {(void*)&d, (void*)&st, (void*)&ctl, (void*)&part, (void*)&nb_e, (void*)&h_ls};
     SCK(add_kernel(&ncl, ls_body, &ne, 1, (const void*)k_ctl_ls, 1, kCtlThreads, args_c));
   }
   {
     void* args[] = {(void*)&d, (void*)&st, (void*)&ctl, (void*)&part};
-    SCK(add_kernel(&ngr, body, &nls, 1, (const void*)k_grad, nb_g, kThreads, args));
+    SCK(add_kernel(&ngr, body, &nls, 1, fg, nb_g, sblock, args));
   }
   {
     void* args[] = {(void*)&d, (void*)&st, (void*)&ctl, (void*)&part, (void*)&nb_g, (void*)&h_outer};
@@ -636,8 +786,8 @@ int build(SteppedGraph* sg, const InstDesc* d, MinScalars* st, int m, int nsm, i
 // stream s.  The graph is built on the first call for this state record and
 // kept in *cache.  Adds the kernels executed to *kernels.  Returns a
 // cudaError_t.
-extern "C" int mg_stepped_pf1_run(void** cache, const InstDesc* d, MinScalars* st, int m, int nsm, int slice,
-                                  void* stream, double* kernels) {
+extern "C" int mg_stepped_pf1_run(void** cache, const InstDesc* d, MinScalars* st, int m, const int* grid,
+                                  int nsm, int slice, void* stream, double* kernels) {
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   SteppedGraph* sg = static_cast<SteppedGraph*>(*cache);
   if (sg && (sg->st != st || sg->slice != slice || sg->m != m)) {
@@ -648,13 +798,19 @@ extern "C" int mg_stepped_pf1_run(void** cache, const InstDesc* d, MinScalars* s
   if (!sg) {
     sg = new SteppedGraph;
     *cache = sg;
-    SCK(build(sg, d, st, m, nsm, slice, s));
+    SCK(build(sg, d, st, m, grid, nsm, slice, s));
   }
   SCK(cudaGraphLaunch(sg->exec, s));
-  double k = 0;
-  SCK(cudaMemcpyAsync(&k, &sg->ctl->kernels, sizeof(double), cudaMemcpyDeviceToHost, s));
+  StepCtl c;
+  SCK(cudaMemcpyAsync(&c, sg->ctl, sizeof c, cudaMemcpyDeviceToHost, s));
   SCK(cudaStreamSynchronize(s));
-  if (kernels) *kernels += k;
+  if (kernels) *kernels += c.kernels;
+  if (std::getenv("MINIM_GPU_STEPPED_TIMING"))  // cumulative over this instance's launches
+    std::fprintf(stderr,
+                 "stepped spans (ms): trials gap %.3f kernel %.3f gap %.3f | gradient gap %.3f kernel %.3f "
+                 "gap %.3f\n",
+                 c.gap_pre[0] * 1e-6, c.kdur[0] * 1e-6, c.gap_post[0] * 1e-6, c.gap_pre[1] * 1e-6,
+                 c.kdur[1] * 1e-6, c.gap_post[1] * 1e-6);
   return 0;
 }
 
