@@ -319,10 +319,12 @@ struct D4q {
 // scratch).  Deterministic: the order depends only on G, K and blockDim.
 __device__ inline void sum_rows_fixed(const double* P, int G, int K, double* out, double* wide) {
   const int nq = (K + 3) >> 2;  // double4 columns
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  // linear thread index (the block may be 2-D; it holds whole warps)
+  const int tl = threadIdx.y * blockDim.x + threadIdx.x, nt = blockDim.x * blockDim.y;
+  const int lane = tl & 31, w = tl >> 5, nw = (nt + 31) >> 5;
   const int nqp = nq <= 1 ? 1 : nq <= 2 ? 2 : nq <= 4 ? 4 : nq <= 8 ? 8 : 16;
-  const int q = threadIdx.x & (nqp - 1);
-  const int r0 = threadIdx.x / nqp, rs = blockDim.x / nqp;
+  const int q = tl & (nqp - 1);
+  const int r0 = tl / nqp, rs = nt / nqp;
   // four consecutive partials of row b (L2, 2 x 16-byte loads)
   auto ld = [&](int b) {
     const double2* r = reinterpret_cast<const double2*>(P + (size_t)b * MINIM_WIDE) + 2 * q;
@@ -356,7 +358,7 @@ __device__ inline void sum_rows_fixed(const double* P, int G, int K, double* out
     d[0] = acc.x; d[1] = acc.y; d[2] = acc.z; d[3] = acc.w;
   }
   __syncthreads();
-  for (int k = threadIdx.x; k < K; k += blockDim.x) {
+  for (int k = tl; k < K; k += nt) {
     double t = 0.0;
     for (int i = 0; i < nw; i++) t += wide[i * MINIM_WIDE + k];
     out[k] = t;

@@ -8,12 +8,11 @@
 // control flow stays on the device: one graph launch runs up to `slice`
 // iterations as
 //
-//   begin -> WHILE(outer) { dirA -> ctlA -> dirB -> ctlB ->
-//                           WHILE(line search) { eonly -> ctlLS } ->
-//                           grad -> ctlG }
+//   begin -> WHILE(outer) { dirA -> dirB -> WHILE(line search) { eonly } -> grad }
 //
-// Vector kernels write one row of partial sums per block; the controller
-// kernels (one block) sum the rows in a fixed order, run the scalar parts
+// Each phase kernel writes one row of partial sums per block; the block that
+// finishes last runs the phase's controller: it sums the rows in a fixed
+// order, runs the scalar parts
 // of Lbfgs::iteration / getDirection / backtrackingLinesearch
 // (src/minimisers/Lbfgs.cpp:41-133, src/minimisers/linesearch.cpp:8-30) on
 // the instance's state record, and set the loops' conditions.  Both loops
@@ -55,7 +54,8 @@ struct StepCtl {
   float coefS[MINIM_MAXM], coefY[MINIM_MAXM];
   int so[MINIM_MAXM], yo[MINIM_MAXM];  // slot buffers: float4 offsets from the ring bases
   // stencil kernels' span (first block's start, last block's end), split
-  // into the gap before, the kernel and the gap after; [0] trials, [1] gradient
+  // into the gap before, the kernel and the controller work after;
+  // [0] trials, [1] gradient
   unsigned long long ks, ke;
   unsigned kdone;
   double gap_pre[2], kdur[2], gap_post[2];
@@ -65,18 +65,26 @@ struct StepCtl {
 __device__ __forceinline__ void span_begin(StepCtl* ctl) {
   if (blockIdx.x == 0 && threadIdx.x == 0 && threadIdx.y == 0) ctl->ks = globaltimer_ns();
 }
-__device__ __forceinline__ void span_end(StepCtl* ctl) {
+// True, in every thread, in the block that finishes last: the blocks count
+// themselves out after writing their partial rows; the last one also marks
+// the kernel's end and sees every other block's row.
+__device__ __forceinline__ bool last_block(StepCtl* ctl) {
+  __shared__ int is_last;
+  __syncthreads();
   if (threadIdx.x == 0 && threadIdx.y == 0) {
     __threadfence();
-    if (atomicAdd(&ctl->kdone, 1u) == gridDim.x - 1) {
+    is_last = atomicAdd(&ctl->kdone, 1u) == gridDim.x - 1;
+    if (is_last) {
       ctl->ke = globaltimer_ns();
       ctl->kdone = 0;
+      __threadfence();
     }
   }
+  __syncthreads();
+  return is_last != 0;
 }
 
 constexpr int kThreads = 256;
-constexpr int kCtlThreads = 256;
 
 // One row of K <= 4 block sums (deterministic: warp butterflies, then warps
 // in order).
@@ -99,6 +107,15 @@ __device__ void block_row(double (&v)[K], double* row) {
   }
 }
 
+// controllers, run by the last block of each phase kernel (defined below)
+__device__ void ctl_a(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, const double* part, int nb);
+__device__ void ctl_b(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, const double* part, int nb,
+                      cudaGraphConditionalHandle ls);
+__device__ void ctl_ls(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, const double* part, int nb,
+                       cudaGraphConditionalHandle ls);
+__device__ void ctl_g(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, const double* part, int nb,
+                      cudaGraphConditionalHandle outer);
+
 // ---- vector and stencil kernels -------------------------------------------------
 
 // S_k.g, Y_k.g, S_k.y_new, Y_k.y_new for the pairs of this iteration (row
@@ -110,7 +127,7 @@ __device__ void block_row(double (&v)[K], double* row) {
 // Offsets are signed: g lies below the ring buffers in the workspace.
 template <int M>
 __global__ void __launch_bounds__(kThreads, 4)
-k_dir_a(const InstDesc* __restrict__ d, const MinScalars* __restrict__ st, double* part) {
+k_dir_a(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, double* part) {
   constexpr int NG = (M + 7) / 8;
   constexpr int GS = (M + NG - 1) / NG;  // pairs per part
   __shared__ double wide[8 * MINIM_WIDE];
@@ -199,14 +216,14 @@ k_dir_a(const InstDesc* __restrict__ d, const MinScalars* __restrict__ st, doubl
     for (int w = 0; w < (int)(blockDim.x >> 5); w++) sum += wide[w * MINIM_WIDE + k];
     part[(size_t)blockIdx.x * MINIM_WIDE + k] = sum;
   }
+  if (last_block(ctl)) ctl_a(d, st, ctl, part, gridDim.x);
 }
 
 // P = -gamma g - S w + gamma Y u with g.P and P.P (M compile-time, unused
 // pairs read g with weight 0)
 template <int M>
 __global__ void __launch_bounds__(kThreads, 4)
-k_dir_b(const InstDesc* __restrict__ d, const MinScalars* __restrict__ st, const StepCtl* __restrict__ ctl,
-        double* part) {
+k_dir_b(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, double* part, cudaGraphConditionalHandle ls) {
   const int n = d->ndof, nq4 = n >> 2, mt = ctl->mt;
   const float* G = d->G[st->gi];
   float* P = d->Sb + (long long)st->pbuf * d->hstride;
@@ -259,11 +276,13 @@ k_dir_b(const InstDesc* __restrict__ d, const MinScalars* __restrict__ st, const
   }
   double v[2] = {d1.total(), d2.total()};
   block_row<2>(v, part + (size_t)blockIdx.x * MINIM_WIDE);
+  if (last_block(ctl)) ctl_b(d, st, ctl, part, gridDim.x, ls);
 }
 
 // Energy at x + t P (line-search trial)
 __global__ void __launch_bounds__(kThreads, 3)
-k_eonly(const InstDesc* __restrict__ d, const MinScalars* __restrict__ st, StepCtl* ctl, double* part) {
+k_eonly(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, double* part,
+        cudaGraphConditionalHandle h) {
   span_begin(ctl);
   FlatTeam tm;
   const float* P = d->Sb + (long long)st->pbuf * d->hstride;
@@ -274,13 +293,14 @@ k_eonly(const InstDesc* __restrict__ d, const MinScalars* __restrict__ st, StepC
   else e = pf1_eval<float>(tm, d->pf, cv, (float*)nullptr, &ne, true, false);
   double v[1] = {e};
   block_row<1>(v, part + (size_t)blockIdx.x * MINIM_WIDE);
-  span_end(ctl);
+  if (last_block(ctl)) ctl_ls(d, st, ctl, part, gridDim.x, h);
 }
 
 // Gradient at the accepted point x + t P: writes the point, the gradient and
 // y = g_new - g_old; E, g.g, P.y, y.y
 __global__ void __launch_bounds__(kThreads, 3)
-k_grad(const InstDesc* __restrict__ d, const MinScalars* __restrict__ st, StepCtl* ctl, double* part) {
+k_grad(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, double* part,
+       cudaGraphConditionalHandle h) {
   span_begin(ctl);
   FlatTeam tm;
   const int xi = st->xi, gi = st->gi;
@@ -292,7 +312,7 @@ k_grad(const InstDesc* __restrict__ d, const MinScalars* __restrict__ st, StepCt
   else e = pf1_eval<float>(tm, d->pf, cv, d->X32[1 - xi], &em, true, true);
   double v[4] = {e, em.gg.total(), em.py.total(), em.yy.total()};
   block_row<4>(v, part + (size_t)blockIdx.x * MINIM_WIDE);
-  span_end(ctl);
+  if (last_block(ctl)) ctl_g(d, st, ctl, part, gridDim.x, h);
 }
 
 // ---- line-shaped stencil (binary PhaseField, nz % 4 == 0) ------------------------
@@ -304,7 +324,8 @@ k_grad(const InstDesc* __restrict__ d, const MinScalars* __restrict__ st, StepCt
 // gradient variant also writes the point, g and y = g - g_old.
 template <bool WANT_G>
 __global__ void __launch_bounds__(kThreads, WANT_G ? 3 : 4)
-k_lines(const InstDesc* __restrict__ d, const MinScalars* __restrict__ st, StepCtl* ctl, double* part) {
+k_lines(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, double* part,
+        cudaGraphConditionalHandle h) {
   span_begin(ctl);
   const PotPF& Pf = d->pf;
   const int nx = Pf.n[0], ny = Pf.n[1], nz = Pf.n[2], nz4 = nz >> 2;
@@ -394,7 +415,10 @@ k_lines(const InstDesc* __restrict__ d, const MinScalars* __restrict__ st, StepC
     double v[1] = {e.total()};
     block_row<1>(v, part + (size_t)blockIdx.x * MINIM_WIDE);
   }
-  span_end(ctl);
+  if (last_block(ctl)) {
+    if (WANT_G) ctl_g(d, st, ctl, part, gridDim.x, h);
+    else ctl_ls(d, st, ctl, part, gridDim.x, h);
+  }
 }
 
 // ---- controllers (one block) ----------------------------------------------------
@@ -421,13 +445,12 @@ __device__ __forceinline__ void phase_time(MinScalars* st, StepCtl* ctl, int ph)
 __device__ __forceinline__ void phase_mark(StepCtl* ctl) { ctl->tmark = globaltimer_ns(); }
 
 // dirA sums, the compact-form algebra of getDirection, pass-B coefficients
-__global__ void __launch_bounds__(kCtlThreads)
-k_ctl_a(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, const double* part, int nb) {
+__device__ void ctl_a(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, const double* part, int nb) {
   __shared__ double wide[8 * MINIM_WIDE];
   __shared__ double wout[MINIM_WIDE];
   sum_rows_fixed(part, nb, MINIM_WIDE, wout, wide);
   __syncthreads();
-  if (threadIdx.x != 0) return;
+  if (threadIdx.x != 0 || threadIdx.y != 0) return;
   phase_time(st, ctl, 2);
   const int m = d->mp.m, n = d->ndof;
   const long long hs = d->hstride;
@@ -475,14 +498,13 @@ k_ctl_a(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, const doub
 }
 
 // dirB sums: step cap, descent check, line-search set-up
-__global__ void __launch_bounds__(kCtlThreads)
-k_ctl_b(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, const double* part, int nb,
+__device__ void ctl_b(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, const double* part, int nb,
         cudaGraphConditionalHandle ls) {
   __shared__ double wide[8 * MINIM_WIDE];
   __shared__ double v[2];
   sum_rows_fixed(part, nb, 2, v, wide);
   __syncthreads();
-  if (threadIdx.x != 0) return;
+  if (threadIdx.x != 0 || threadIdx.y != 0) return;
   phase_time(st, ctl, 2);
   double gp = v[0], scale = 1.0;
   if (d->mp.max_step != 0) {
@@ -511,14 +533,13 @@ k_ctl_b(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, const doub
 
 // one line-search trial: Armijo test, or halve the step (10 trials at most;
 // after the last failure the halved step is taken unevaluated)
-__global__ void __launch_bounds__(kCtlThreads)
-k_ctl_ls(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, const double* part, int nb,
+__device__ void ctl_ls(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, const double* part, int nb,
          cudaGraphConditionalHandle ls) {
   __shared__ double wide[8 * MINIM_WIDE];
   __shared__ double v[1];
   sum_rows_fixed(part, nb, 1, v, wide);
   __syncthreads();
-  if (threadIdx.x != 0) return;
+  if (threadIdx.x != 0 || threadIdx.y != 0) return;
   phase_time(st, ctl, 1);
   {
     const unsigned long long now = globaltimer_ns();
@@ -528,7 +549,7 @@ k_ctl_ls(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, const dou
   }
   st->evals++;
   st->abytes += 8.0 * d->ndof;
-  ctl->kernels += 2;
+  ctl->kernels += 1;
   bool more = false;
   if (ctl->e0 - v[0] >= ctl->thr) {
     ctl->exhausted = ctl->k >= 8;
@@ -544,14 +565,13 @@ k_ctl_ls(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, const dou
 
 // gradient sums: the pair update of Lbfgs::iteration, then the end-of-
 // iteration decision (continue here, or hand over to the persistent kernel)
-__global__ void __launch_bounds__(kCtlThreads)
-k_ctl_g(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, const double* part, int nb,
+__device__ void ctl_g(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, const double* part, int nb,
         cudaGraphConditionalHandle outer) {
   __shared__ double wide[8 * MINIM_WIDE];
   __shared__ double v[4];
   sum_rows_fixed(part, nb, 4, v, wide);
   __syncthreads();
-  if (threadIdx.x != 0) return;
+  if (threadIdx.x != 0 || threadIdx.y != 0) return;
   phase_time(st, ctl, 0);
   {
     const unsigned long long now = globaltimer_ns();
@@ -567,7 +587,7 @@ k_ctl_g(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, const doub
   st->abytes += 24.0 * n;
   st->gi ^= 1;
   st->xi ^= 1;
-  ctl->kernels += 6;
+  ctl->kernels += 3;
   const double t = ctl->t, py = v[2], yyv = v[3];
   const double sy = t * py;
   if (sy != 0 && isfinite(sy)) {
@@ -741,39 +761,25 @@ int build(SteppedGraph* sg, const InstDesc* d, MinScalars* st, int m, const int*
   cudaGraph_t body;
   SCK(add_while(&n_outer, g, &n_begin, 1, h_outer, &body));
   SCK(cudaGraphConditionalHandleCreate(&h_ls, body, 0, 0));
-  cudaGraphNode_t na, nca, nb, ncb, nls, ngr, ncg;
+  cudaGraphNode_t na, nb, nls, ngr;
   {
-    void* args[] = {(void*)&d, (void*)&st, (void*)&part};
+    void* args[] = {(void*)&d, (void*)&st, (void*)&ctl, (void*)&part};
     SCK(add_kernel(&na, body, nullptr, 0, fa, nb_a, kThreads, args));
   }
   {
-    void* args[] = {(void*)&d, (void*)&st, (void*)&ctl, (void*)&part, (void*)&nb_a};
-    SCK(add_kernel(&nca, body, &na, 1, (const void*)k_ctl_a, 1, kCtlThreads, args));
-  }
-  {
-    void* args[] = {(void*)&d, (void*)&st, (void*)&ctl, (void*)&part};
-    SCK(add_kernel(&nb, body, &nca, 1, fb, nb_b, kThreads, args));
-  }
-  {
-    void* args[] = {(void*)&d, (void*)&st, (void*)&ctl, (void*)&part, (void*)&nb_b, (void*)&h_ls};
-    SCK(add_kernel(&ncb, body, &nb, 1, (const void*)k_ctl_b, 1, kCtlThreads, args));
+    void* args[] = {(void*)&d, (void*)&st, (void*)&ctl, (void*)&part, (void*)&h_ls};
+    SCK(add_kernel(&nb, body, &na, 1, fb, nb_b, kThreads, args));
   }
   cudaGraph_t ls_body;
-  SCK(add_while(&nls, body, &ncb, 1, h_ls, &ls_body));
+  SCK(add_while(&nls, body, &nb, 1, h_ls, &ls_body));
   {
-    cudaGraphNode_t ne, ncl;
-    void* args_e[] = {(void*)&d, (void*)&st, (void*)&ctl, (void*)&part};
+    cudaGraphNode_t ne;
+    void* args_e[] = {(void*)&d, (void*)&st, (void*)&ctl, (void*)&part, (void*)&h_ls};
     SCK(add_kernel(&ne, ls_body, nullptr, 0, fe, nb_e, sblock, args_e));
-    void* args_c[] = {(void*)&d, (void*)&st, (void*)&ctl, (void*)&part, (void*)&nb_e, (void*)&h_ls};
-    SCK(add_kernel(&ncl, ls_body, &ne, 1, (const void*)k_ctl_ls, 1, kCtlThreads, args_c));
   }
   {
-    void* args[] = {(void*)&d, (void*)&st, (void*)&ctl, (void*)&part};
+    void* args[] = {(void*)&d, (void*)&st, (void*)&ctl, (void*)&part, (void*)&h_outer};
     SCK(add_kernel(&ngr, body, &nls, 1, fg, nb_g, sblock, args));
-  }
-  {
-    void* args[] = {(void*)&d, (void*)&st, (void*)&ctl, (void*)&part, (void*)&nb_g, (void*)&h_outer};
-    SCK(add_kernel(&ncg, body, &ngr, 1, (const void*)k_ctl_g, 1, kCtlThreads, args));
   }
   SCK(cudaGraphInstantiate(&sg->exec, g, 0));
   return 0;
