@@ -8,7 +8,13 @@
 // control flow stays on the device: one graph launch runs up to `slice`
 // iterations as
 //
-//   begin -> WHILE(outer) { dirA -> dirB -> WHILE(line search) { eonly } -> grad }
+//   begin -> WHILE(outer) { dirA -> dirB -> WHILE(line search) { trial } ->
+//                           IF(no trial accepted) { grad } }
+//
+// A trial evaluates the energy and, in the same pass, the gradient at its
+// point; when the trial is accepted that gradient is the accepted point's
+// (the same values the reference's separate gradient call computes), so the
+// gradient kernel runs only after a line search that accepted no trial.
 //
 // Each phase kernel writes one row of partial sums per block; the block that
 // finishes last runs the phase's controller: it sums the rows in a fixed
@@ -110,11 +116,14 @@ __device__ void block_row(double (&v)[K], double* row) {
 // controllers, run by the last block of each phase kernel (defined below)
 __device__ void ctl_a(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, const double* part, int nb);
 __device__ void ctl_b(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, const double* part, int nb,
-                      cudaGraphConditionalHandle ls);
+                      cudaGraphConditionalHandle ls, cudaGraphConditionalHandle grad, int spec);
 __device__ void ctl_ls(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, const double* part, int nb,
                        cudaGraphConditionalHandle ls);
 __device__ void ctl_g(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, const double* part, int nb,
                       cudaGraphConditionalHandle outer);
+__device__ void ctl_lsg(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, const double* part,
+                        int nb, cudaGraphConditionalHandle ls, cudaGraphConditionalHandle grad,
+                        cudaGraphConditionalHandle outer);
 
 // ---- vector and stencil kernels -------------------------------------------------
 
@@ -223,7 +232,8 @@ k_dir_a(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, double* pa
 // pairs read g with weight 0)
 template <int M>
 __global__ void __launch_bounds__(kThreads, 4)
-k_dir_b(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, double* part, cudaGraphConditionalHandle ls) {
+k_dir_b(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, double* part, cudaGraphConditionalHandle ls,
+        cudaGraphConditionalHandle grad, int spec) {
   const int n = d->ndof, nq4 = n >> 2, mt = ctl->mt;
   const float* G = d->G[st->gi];
   float* P = d->Sb + (long long)st->pbuf * d->hstride;
@@ -276,13 +286,13 @@ k_dir_b(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, double* pa
   }
   double v[2] = {d1.total(), d2.total()};
   block_row<2>(v, part + (size_t)blockIdx.x * MINIM_WIDE);
-  if (last_block(ctl)) ctl_b(d, st, ctl, part, gridDim.x, ls);
+  if (last_block(ctl)) ctl_b(d, st, ctl, part, gridDim.x, ls, grad, spec);
 }
 
 // Energy at x + t P (line-search trial)
 __global__ void __launch_bounds__(kThreads, 3)
-k_eonly(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, double* part,
-        cudaGraphConditionalHandle h) {
+k_eonly(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, double* part, cudaGraphConditionalHandle ls,
+        cudaGraphConditionalHandle grad, cudaGraphConditionalHandle outer) {
   span_begin(ctl);
   FlatTeam tm;
   const float* P = d->Sb + (long long)st->pbuf * d->hstride;
@@ -293,14 +303,15 @@ k_eonly(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, double* pa
   else e = pf1_eval<float>(tm, d->pf, cv, (float*)nullptr, &ne, true, false);
   double v[1] = {e};
   block_row<1>(v, part + (size_t)blockIdx.x * MINIM_WIDE);
-  if (last_block(ctl)) ctl_ls(d, st, ctl, part, gridDim.x, h);
+  if (last_block(ctl)) ctl_ls(d, st, ctl, part, gridDim.x, ls);
 }
 
 // Gradient at the accepted point x + t P: writes the point, the gradient and
 // y = g_new - g_old; E, g.g, P.y, y.y
+template <bool SPEC>
 __global__ void __launch_bounds__(kThreads, 3)
-k_grad(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, double* part,
-       cudaGraphConditionalHandle h) {
+k_grad(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, double* part, cudaGraphConditionalHandle ls,
+       cudaGraphConditionalHandle grad, cudaGraphConditionalHandle outer) {
   span_begin(ctl);
   FlatTeam tm;
   const int xi = st->xi, gi = st->gi;
@@ -312,7 +323,10 @@ k_grad(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, double* par
   else e = pf1_eval<float>(tm, d->pf, cv, d->X32[1 - xi], &em, true, true);
   double v[4] = {e, em.gg.total(), em.py.total(), em.yy.total()};
   block_row<4>(v, part + (size_t)blockIdx.x * MINIM_WIDE);
-  if (last_block(ctl)) ctl_g(d, st, ctl, part, gridDim.x, h);
+  if (last_block(ctl)) {
+    if (SPEC) ctl_lsg(d, st, ctl, part, gridDim.x, ls, grad, outer);
+    else ctl_g(d, st, ctl, part, gridDim.x, outer);
+  }
 }
 
 // ---- line-shaped stencil (binary PhaseField, nz % 4 == 0) ------------------------
@@ -322,10 +336,13 @@ k_grad(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, double* par
 // and of its four neighbour lines plus two scalars at the z ends.  The trial
 // energy is summed per quad in FP32 and per thread with compensation; the
 // gradient variant also writes the point, g and y = g - g_old.
-template <bool WANT_G>
-__global__ void __launch_bounds__(kThreads, WANT_G ? 3 : 4)
-k_lines(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, double* part,
-        cudaGraphConditionalHandle h) {
+// MODE 0: trial energy; 1: gradient at the accepted point; 2: trial energy
+// with the gradient at the trial point (kept when the trial is accepted)
+template <int MODE>
+__global__ void __launch_bounds__(kThreads, MODE ? 3 : 4)
+k_lines(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, double* part, cudaGraphConditionalHandle ls,
+        cudaGraphConditionalHandle grad, cudaGraphConditionalHandle outer) {
+  constexpr bool WANT_G = MODE != 0;
   span_begin(ctl);
   const PotPF& Pf = d->pf;
   const int nx = Pf.n[0], ny = Pf.n[1], nz = Pf.n[2], nz4 = nz >> 2;
@@ -416,8 +433,9 @@ k_lines(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, double* pa
     block_row<1>(v, part + (size_t)blockIdx.x * MINIM_WIDE);
   }
   if (last_block(ctl)) {
-    if (WANT_G) ctl_g(d, st, ctl, part, gridDim.x, h);
-    else ctl_ls(d, st, ctl, part, gridDim.x, h);
+    if (MODE == 0) ctl_ls(d, st, ctl, part, gridDim.x, ls);
+    else if (MODE == 1) ctl_g(d, st, ctl, part, gridDim.x, outer);
+    else ctl_lsg(d, st, ctl, part, gridDim.x, ls, grad, outer);
   }
 }
 
@@ -499,7 +517,7 @@ __device__ void ctl_a(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* c
 
 // dirB sums: step cap, descent check, line-search set-up
 __device__ void ctl_b(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, const double* part, int nb,
-        cudaGraphConditionalHandle ls) {
+                      cudaGraphConditionalHandle ls, cudaGraphConditionalHandle grad, int spec) {
   __shared__ double wide[8 * MINIM_WIDE];
   __shared__ double v[2];
   sum_rows_fixed(part, nb, 2, v, wide);
@@ -524,9 +542,11 @@ __device__ void ctl_b(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* c
     ctl->k = 0;
     ctl->exhausted = 1;
     cudaGraphSetConditional(ls, 1u);
+    if (spec) cudaGraphSetConditional(grad, 0u);
   } else {
     ctl->exhausted = 0;
     cudaGraphSetConditional(ls, 0u);
+    if (spec) cudaGraphSetConditional(grad, 1u);
   }
   phase_mark(ctl);
 }
@@ -563,31 +583,17 @@ __device__ void ctl_ls(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* 
   phase_mark(ctl);
 }
 
-// gradient sums: the pair update of Lbfgs::iteration, then the end-of-
-// iteration decision (continue here, or hand over to the persistent kernel)
-__device__ void ctl_g(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, const double* part, int nb,
-        cudaGraphConditionalHandle outer) {
-  __shared__ double wide[8 * MINIM_WIDE];
-  __shared__ double v[4];
-  sum_rows_fixed(part, nb, 4, v, wide);
-  __syncthreads();
-  if (threadIdx.x != 0 || threadIdx.y != 0) return;
-  phase_time(st, ctl, 0);
-  {
-    const unsigned long long now = globaltimer_ns();
-    ctl->gap_pre[1] += (double)(ctl->ks - ctl->tmark);
-    ctl->kdur[1] += (double)(ctl->ke - ctl->ks);
-    ctl->gap_post[1] += (double)(now - ctl->ke);
-  }
+// The pair update of Lbfgs::iteration with the sums {E, g.g, P.y, y.y} of
+// the gradient at the accepted point, then the end-of-iteration decision
+// (continue here, or hand over to the persistent kernel).  Thread 0.
+__device__ void commit_grad(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, const double* v,
+                            cudaGraphConditionalHandle outer) {
   const MinParams& mp = d->mp;
   const int n = d->ndof;
   st->E = v[0];
   st->gg = v[1];
-  st->evals++;
-  st->abytes += 24.0 * n;
   st->gi ^= 1;
   st->xi ^= 1;
-  ctl->kernels += 3;
   const double t = ctl->t, py = v[2], yyv = v[3];
   const double sy = t * py;
   if (sy != 0 && isfinite(sy)) {
@@ -646,6 +652,71 @@ __device__ void ctl_g(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* c
   phase_mark(ctl);
 }
 
+
+// gradient sums: the pair update of Lbfgs::iteration, then the end-of-
+// iteration decision (continue here, or hand over to the persistent kernel)
+__device__ void ctl_g(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, const double* part, int nb,
+        cudaGraphConditionalHandle outer) {
+  __shared__ double wide[8 * MINIM_WIDE];
+  __shared__ double v[4];
+  sum_rows_fixed(part, nb, 4, v, wide);
+  __syncthreads();
+  if (threadIdx.x != 0 || threadIdx.y != 0) return;
+  phase_time(st, ctl, 0);
+  {
+    const unsigned long long now = globaltimer_ns();
+    ctl->gap_pre[1] += (double)(ctl->ks - ctl->tmark);
+    ctl->kdur[1] += (double)(ctl->ke - ctl->ks);
+    ctl->gap_post[1] += (double)(now - ctl->ke);
+  }
+  st->evals++;
+  st->abytes += 24.0 * d->ndof;
+  ctl->kernels += 3;
+  commit_grad(d, st, ctl, v, outer);
+}
+
+// A line-search trial that also evaluated the gradient at its point (x, g
+// and y written to the next buffers): Armijo test; when it passes, that
+// gradient is the accepted point's and the iteration completes here; when
+// it fails the step is halved (10 trials at most, after which the halved
+// step is taken unevaluated and the gradient kernel runs).
+__device__ void ctl_lsg(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, const double* part,
+                        int nb, cudaGraphConditionalHandle ls, cudaGraphConditionalHandle grad,
+                        cudaGraphConditionalHandle outer) {
+  __shared__ double wide[8 * MINIM_WIDE];
+  __shared__ double v[4];
+  sum_rows_fixed(part, nb, 4, v, wide);
+  __syncthreads();
+  if (threadIdx.x != 0 || threadIdx.y != 0) return;
+  phase_time(st, ctl, 1);
+  {
+    const unsigned long long now = globaltimer_ns();
+    ctl->gap_pre[0] += (double)(ctl->ks - ctl->tmark);
+    ctl->kdur[0] += (double)(ctl->ke - ctl->ks);
+    ctl->gap_post[0] += (double)(now - ctl->ke);
+  }
+  st->evals++;
+  ctl->kernels += 1;
+  if (ctl->e0 - v[0] >= ctl->thr) {
+    ctl->exhausted = ctl->k >= 8;
+    cudaGraphSetConditional(ls, 0u);
+    cudaGraphSetConditional(grad, 0u);
+    st->evals++;
+    st->abytes += 24.0 * d->ndof;
+    ctl->kernels += 2;
+    commit_grad(d, st, ctl, v, outer);
+  } else {
+    st->abytes += 8.0 * d->ndof;
+    ctl->t *= 0.5;
+    ctl->thr *= 0.5;
+    ctl->k++;
+    const bool more = ctl->k < 10;
+    cudaGraphSetConditional(ls, more ? 1u : 0u);
+    cudaGraphSetConditional(grad, more ? 0u : 1u);
+    phase_mark(ctl);
+  }
+}
+
 int occupancy(const void* f, int threads) {
   int per_sm = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, f, threads, 0) != cudaSuccess) return 0;
@@ -687,16 +758,20 @@ int add_kernel(cudaGraphNode_t* node, cudaGraph_t g, const cudaGraphNode_t* deps
   return (int)cudaGraphAddKernelNode(node, g, deps, ndeps, &p);
 }
 
-int add_while(cudaGraphNode_t* node, cudaGraph_t g, const cudaGraphNode_t* deps, int ndeps,
-              cudaGraphConditionalHandle h, cudaGraph_t* body) {
+int add_cond(cudaGraphNode_t* node, cudaGraph_t g, const cudaGraphNode_t* deps, int ndeps,
+             cudaGraphConditionalHandle h, cudaGraphConditionalNodeType type, cudaGraph_t* body) {
   cudaGraphNodeParams p{};
   p.type = cudaGraphNodeTypeConditional;
   p.conditional.handle = h;
-  p.conditional.type = cudaGraphCondTypeWhile;
+  p.conditional.type = type;
   p.conditional.size = 1;
   SCK(cudaGraphAddNode(node, g, deps, nullptr, (size_t)ndeps, &p));
   *body = p.conditional.phGraph_out[0];
   return 0;
+}
+int add_while(cudaGraphNode_t* node, cudaGraph_t g, const cudaGraphNode_t* deps, int ndeps,
+              cudaGraphConditionalHandle h, cudaGraph_t* body) {
+  return add_cond(node, g, deps, ndeps, h, cudaGraphCondTypeWhile, body);
 }
 
 template <int M>
@@ -733,8 +808,13 @@ int build(SteppedGraph* sg, const InstDesc* d, MinScalars* st, int m, const int*
   while (lines && by > 1 && (nz4 * by) % 32) by--;
   const bool use_lines = lines && (nz4 * by) % 32 == 0;
   const dim3 sblock = use_lines ? dim3(nz4, by) : dim3(kThreads);
-  const void* fe = use_lines ? (const void*)k_lines<false> : (const void*)k_eonly;
-  const void* fg = use_lines ? (const void*)k_lines<true> : (const void*)k_grad;
+  // trials that also evaluate the gradient at their point (kept when the
+  // trial is accepted) unless MINIM_GPU_SPECULATIVE=0
+  const char* env = std::getenv("MINIM_GPU_SPECULATIVE");
+  int spec = !(env && env[0] == '0');
+  const void* fe = spec ? (use_lines ? (const void*)k_lines<2> : (const void*)k_grad<true>)
+                        : (use_lines ? (const void*)k_lines<0> : (const void*)k_eonly);
+  const void* fg = use_lines ? (const void*)k_lines<1> : (const void*)k_grad<false>;
   const int occ_a = occupancy(fa, kThreads), occ_b = occupancy(fb, kThreads);
   const int occ_e = occupancy(fe, (int)(sblock.x * sblock.y)), occ_g = occupancy(fg, (int)(sblock.x * sblock.y));
   if (!occ_a || !occ_b || !occ_e || !occ_g) return (int)cudaErrorInvalidConfiguration;
@@ -761,25 +841,32 @@ int build(SteppedGraph* sg, const InstDesc* d, MinScalars* st, int m, const int*
   cudaGraph_t body;
   SCK(add_while(&n_outer, g, &n_begin, 1, h_outer, &body));
   SCK(cudaGraphConditionalHandleCreate(&h_ls, body, 0, 0));
+  cudaGraphConditionalHandle h_grad = 0;
+  if (spec) SCK(cudaGraphConditionalHandleCreate(&h_grad, body, 0, 0));
   cudaGraphNode_t na, nb, nls, ngr;
   {
     void* args[] = {(void*)&d, (void*)&st, (void*)&ctl, (void*)&part};
     SCK(add_kernel(&na, body, nullptr, 0, fa, nb_a, kThreads, args));
   }
   {
-    void* args[] = {(void*)&d, (void*)&st, (void*)&ctl, (void*)&part, (void*)&h_ls};
+    void* args[] = {(void*)&d, (void*)&st, (void*)&ctl, (void*)&part, (void*)&h_ls, (void*)&h_grad, (void*)&spec};
     SCK(add_kernel(&nb, body, &na, 1, fb, nb_b, kThreads, args));
   }
+  void* args_s[] = {(void*)&d, (void*)&st, (void*)&ctl, (void*)&part, (void*)&h_ls, (void*)&h_grad, (void*)&h_outer};
   cudaGraph_t ls_body;
   SCK(add_while(&nls, body, &nb, 1, h_ls, &ls_body));
   {
     cudaGraphNode_t ne;
-    void* args_e[] = {(void*)&d, (void*)&st, (void*)&ctl, (void*)&part, (void*)&h_ls};
-    SCK(add_kernel(&ne, ls_body, nullptr, 0, fe, nb_e, sblock, args_e));
+    SCK(add_kernel(&ne, ls_body, nullptr, 0, fe, nb_e, sblock, args_s));
   }
-  {
-    void* args[] = {(void*)&d, (void*)&st, (void*)&ctl, (void*)&part, (void*)&h_outer};
-    SCK(add_kernel(&ngr, body, &nls, 1, fg, nb_g, sblock, args));
+  if (spec) {
+    // the gradient kernel runs only when no trial was accepted
+    cudaGraph_t g_body;
+    SCK(add_cond(&ngr, body, &nls, 1, h_grad, cudaGraphCondTypeIf, &g_body));
+    cudaGraphNode_t ng;
+    SCK(add_kernel(&ng, g_body, nullptr, 0, fg, nb_g, sblock, args_s));
+  } else {
+    SCK(add_kernel(&ngr, body, &nls, 1, fg, nb_g, sblock, args_s));
   }
   SCK(cudaGraphInstantiate(&sg->exec, g, 0));
   return 0;
