@@ -35,12 +35,13 @@ sys.path.insert(0, HERE)
 GRID = (192, 192, 192)
 TOL = 1e-7
 METRIC = "converged minimisations/s batched vs plain on GB300 at ΔE/E<1e-8; p50/p99 ms"
-# DRAM bytes per algorithmic byte of the PhaseField 192^3 minimiser kernel,
-# from one ncu capture of a 20-iteration launch of the same kernel
-# (dram__bytes_read.sum + dram__bytes_write.sum = 26.21 GB against the
-# kernel's own count of 22.93 GB; profiles/grid_kernel_pf1_192cubed.md).
-# Traffic per step = this ratio x the step's algorithmic bytes.
-PF_TRAFFIC_PER_ALGO_BYTE = 26.21 / 22.93
+# DRAM bytes per algorithmic byte of the PhaseField 192^3 minimisation's
+# FP32 stage (the stepped graph), from one ncu capture of a graph launch
+# running 19 iterations: dram__bytes_read.sum + dram__bytes_write.sum =
+# 23.68 GB against the kernels' own count of 20.77 GB
+# (profiles/stepped_graph_pf1_192cubed.md).  Traffic per step = this ratio x
+# the step's algorithmic bytes.
+PF_TRAFFIC_PER_ALGO_BYTE = 23.68 / 20.77
 
 
 def _peaks():
@@ -182,7 +183,8 @@ def run_gpu(args):
     roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                 "frac": achieved / hbm_peak, "traffic": traffic, "traffic_unit": "bytes/step",
                 "algorithmic_bytes_per_step": abytes / args.steps, "peak_source": peak_kind,
-                "kernel": "grid_kernel<K_PF1> (fused L-BFGS minimiser)"}
+                "kernel": "stepped graph of phase kernels (FP32 L-BFGS stage) + grid_kernel<K_PF1> "
+                          "(set-up iteration, FP64 stage)"}
 
     out = {
         "metric": METRIC, "value": value, "unit": "minimisations/s", "n_gpus": 1,
