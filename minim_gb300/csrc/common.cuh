@@ -79,6 +79,56 @@ struct Acc {
   __device__ __forceinline__ double total() const { return d + ((double)s + (double)c); }
 };
 
+// Double-float numbers: an unevaluated sum hi + lo of two FP32 values with
+// |lo| <= ulp(hi)/2, about 48 significant bits with the FP32 exponent range.
+// Built on the error-free transformations of Knuth (TwoSum) and Dekker
+// (Fast2Sum), with the product's error taken from one fused multiply-add;
+// every operation is a handful of FP32 instructions instead of the FP64 pipe,
+// which runs at 1/64 of the FP32 rate on GB300.  Compile-time rounding is
+// explicit (__fadd_rn etc.) so that no contraction breaks the transformations.
+struct DF {
+  float hi, lo;
+};
+__device__ __forceinline__ DF df_fast2sum(float a, float b) {  // |a| >= |b|
+  const float s = __fadd_rn(a, b);
+  return DF{s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ DF df_2sum(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  return DF{s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb))};
+}
+__device__ __forceinline__ DF df_from(double x) {
+  const float hi = (float)x;
+  return DF{hi, (float)(x - (double)hi)};
+}
+__device__ __forceinline__ DF df_from(float x) { return DF{x, 0.f}; }
+__device__ __forceinline__ double df_to(DF a) { return (double)a.hi + (double)a.lo; }
+__device__ __forceinline__ DF operator+(DF a, DF b) {
+  const DF s = df_2sum(a.hi, b.hi);
+  const DF t = df_2sum(a.lo, b.lo);
+  const DF u = df_fast2sum(s.hi, __fadd_rn(s.lo, t.hi));
+  return df_fast2sum(u.hi, __fadd_rn(u.lo, t.lo));
+}
+__device__ __forceinline__ DF operator-(DF a) { return DF{-a.hi, -a.lo}; }
+__device__ __forceinline__ DF operator-(DF a, DF b) { return a + (-b); }
+__device__ __forceinline__ DF operator*(DF a, DF b) {
+  const float p = __fmul_rn(a.hi, b.hi);
+  float e = __fmaf_rn(a.hi, b.hi, -p);
+  e = __fmaf_rn(a.hi, b.lo, e);
+  e = __fmaf_rn(a.lo, b.hi, e);
+  return df_fast2sum(p, e);
+}
+// 1 / b: the FP32 reciprocal refined by one Newton step in double-float
+__device__ __forceinline__ DF df_rcp(DF b) {
+  const float y = __frcp_rn(b.hi);
+  const DF r = DF{1.f, 0.f} - b * DF{y, 0.f};  // residual 1 - b y
+  return DF{y, 0.f} + DF{y, 0.f} * r;
+}
+__device__ __forceinline__ DF df_shfl(DF a, int src) {
+  return DF{__shfl_sync(0xffffffffu, a.hi, src), __shfl_sync(0xffffffffu, a.lo, src)};
+}
+
 // aligned 4-wide access to FP32 vectors (element 4*i4 .. 4*i4+3)
 __device__ __forceinline__ float4 ld4(const float* p, int i4) {
   return reinterpret_cast<const float4*>(p)[i4];

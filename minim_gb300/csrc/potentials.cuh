@@ -53,88 +53,135 @@ struct NoEmit {
 // ===========================================================================
 struct alignas(16) F4 { float x, y, z, w; };
 struct alignas(16) D4 { double x, y, z, w; };
-template <typename T> struct Vec4T;
-template <> struct Vec4T<float> { using type = F4; };
-template <> struct Vec4T<double> { using type = D4; };
 
-template <typename T>
-__device__ __forceinline__ T lj_rcp(T r2);
-template <>
-__device__ __forceinline__ float lj_rcp<float>(float r2) { return __frcp_rn(r2); }
-template <>
-__device__ __forceinline__ double lj_rcp<double>(double r2) { return 1.0 / r2; }
+// Pair arithmetic type: FP32 in the FP32 stage; double-float (DF, about 48
+// bits) in the FP64 stage and the FP64 API evaluation -- the O(N^2) pair
+// terms stay off the FP64 pipe.  A pair closer than r^2 = 1e-5 sigma^2 (where
+// FP32's exponent range could overflow lj12) is computed in double.
+template <typename T> struct LjC;
+template <> struct LjC<float> {
+  using C = float;
+  __device__ static C from(float x) { return x; }
+  __device__ static double to(C x) { return (double)x; }
+};
+template <> struct LjC<double> {
+  using C = DF;
+  __device__ static C from(double x) { return df_from(x); }
+  __device__ static double to(C x) { return df_to(x); }
+};
+template <typename C> struct CV3 { C x, y, z; };
+
+__device__ __forceinline__ float lj_shfl(float a, int src) { return __shfl_sync(0xffffffffu, a, src); }
+__device__ __forceinline__ DF lj_shfl(DF a, int src) { return df_shfl(a, src); }
+
+// lj6 = s6 / r^6, lj12 = lj6^2 and the force factor f = (2 lj12 - lj6) / r^2
+// of one pair separated by (dx, dy, dz)
+__device__ __forceinline__ void lj_pair(float dx, float dy, float dz, float s6, float& lj6, float& lj12,
+                                        float& f) {
+  const float inv = __frcp_rn(dx * dx + dy * dy + dz * dz);
+  lj6 = s6 * inv * inv * inv;
+  lj12 = lj6 * lj6;
+  f = (lj12 + lj12 - lj6) * inv;
+}
+__device__ __forceinline__ void lj_pair(DF dx, DF dy, DF dz, DF s6, DF& lj6, DF& lj12, DF& f) {
+  const DF r2 = dx * dx + dy * dy + dz * dz;
+  if (r2.hi >= 1e-5f) {
+    const DF inv = df_rcp(r2);
+    const DF inv3 = inv * inv * inv;
+    lj6 = s6 * inv3;
+    lj12 = lj6 * lj6;
+    f = (lj12 + lj12 - lj6) * inv;
+  } else {
+    const double ddx = df_to(dx), ddy = df_to(dy), ddz = df_to(dz);
+    const double inv = 1.0 / (ddx * ddx + ddy * ddy + ddz * ddz);
+    const double l6 = df_to(s6) * inv * inv * inv, l12 = l6 * l6;
+    lj6 = df_from(l6);
+    lj12 = df_from(l12);
+    f = df_from((2 * l12 - l6) * inv);
+  }
+}
+
+// energy accumulator of the pair type
+template <typename C> struct LjAcc;
+template <> struct LjAcc<float> {
+  Acc a;
+  __device__ __forceinline__ void add(float v) { a.add(v); }
+  __device__ __forceinline__ double total() const { return a.total(); }
+};
+template <> struct LjAcc<DF> {
+  DF s{0.f, 0.f};
+  __device__ __forceinline__ void add(DF v) { s = s + v; }
+  __device__ __forceinline__ double total() const { return df_to(s); }
+};
 
 template <typename T, class Team, class Emit>
 __device__ __noinline__ double lj_eval(Team& tm, const PotLJ& P, CView<T> cv, T* xw, Emit* emp,
                                        bool want_e, bool want_g, void* smem, int tile) {
+  using L = LjC<T>;
+  using C = typename L::C;
   Emit emit = *emp;
-  using V4 = typename Vec4T<T>::type;
-  V4* sx = reinterpret_cast<V4*>(smem);
+  CV3<C>* sx = reinterpret_cast<CV3<C>*>(smem);
   const int N = P.np, nd = P.ndim;
-  const T s6 = (T)P.s6;
+  const C s6 = L::from((T)P.s6);
+  const C zero = L::from((T)0);
   if (xw) {
     for (int i = tm.tid(); i < N * nd; i += tm.nthr()) xw[i] = cv(i);
   }
-  EAcc<T> e;
+  LjAcc<C> e;
   const int step = tm.nthr();
   // every thread of every block runs the same number of outer rounds
   const int rounds = (N + step - 1) / step;
   for (int r = 0; r < rounds; r++) {
     const int i = r * step + tm.tid();
     const bool act = i < N;
-    T xi = 0, yi = 0, zi = 0;
+    C xi = zero, yi = zero, zi = zero;
     if (act) {
-      xi = cv(nd * i);
-      yi = cv(nd * i + 1);
-      zi = (nd == 3) ? cv(nd * i + 2) : (T)0;
+      xi = L::from(cv(nd * i));
+      yi = L::from(cv(nd * i + 1));
+      zi = (nd == 3) ? L::from(cv(nd * i + 2)) : zero;
     }
-    T fx = 0, fy = 0, fz = 0;
+    C fx = zero, fy = zero, fz = zero;
     for (int j0 = 0; j0 < N; j0 += tile) {
       const int nt = min(tile, N - j0);
       __syncthreads();
       for (int j = threadIdx.x; j < nt; j += blockDim.x) {
         const int jj = j0 + j;
-        V4 v;
-        v.x = cv(nd * jj);
-        v.y = cv(nd * jj + 1);
-        v.z = (nd == 3) ? cv(nd * jj + 2) : (T)0;
-        v.w = 0;
+        CV3<C> v;
+        v.x = L::from(cv(nd * jj));
+        v.y = L::from(cv(nd * jj + 1));
+        v.z = (nd == 3) ? L::from(cv(nd * jj + 2)) : zero;
         sx[j] = v;
       }
       __syncthreads();
       if (act) {
         if (want_g) {
           for (int j = 0; j < nt; j++) {
-            const V4 b = sx[j];
-            const T dx = xi - b.x, dy = yi - b.y, dz = zi - b.z;
-            const T r2 = dx * dx + dy * dy + dz * dz;
-            const bool self = (j0 + j == i);
-            const T inv = lj_rcp<T>(self ? (T)1 : r2);
-            const T lj6 = s6 * inv * inv * inv;
-            const T lj12 = lj6 * lj6;
-            const T f = self ? (T)0 : (2 * lj12 - lj6) * inv;
-            fx += dx * f;
-            fy += dy * f;
-            fz += dz * f;
+            if (j0 + j == i) continue;
+            const CV3<C> b = sx[j];
+            const C dx = xi - b.x, dy = yi - b.y, dz = zi - b.z;
+            C lj6, lj12, f;
+            lj_pair(dx, dy, dz, s6, lj6, lj12, f);
+            fx = fx + dx * f;
+            fy = fy + dy * f;
+            fz = fz + dz * f;
             if (want_e && (j0 + j > i)) e.add(lj12 - lj6);
           }
         } else if (want_e) {
           for (int j = max(0, i + 1 - j0); j < nt; j++) {
-            const V4 b = sx[j];
-            const T dx = xi - b.x, dy = yi - b.y, dz = zi - b.z;
-            const T r2 = dx * dx + dy * dy + dz * dz;
-            const T inv = lj_rcp<T>(r2);
-            const T lj6 = s6 * inv * inv * inv;
-            e.add(lj6 * lj6 - lj6);
+            const CV3<C> b = sx[j];
+            const C dx = xi - b.x, dy = yi - b.y, dz = zi - b.z;
+            C lj6, lj12, f;
+            lj_pair(dx, dy, dz, s6, lj6, lj12, f);
+            e.add(lj12 - lj6);
           }
         }
       }
     }
     if (act && want_g) {
-      const T c = (T)(-24.0 * P.eps);
-      emit(nd * i, c * fx);
-      emit(nd * i + 1, c * fy);
-      if (nd == 3) emit(nd * i + 2, c * fz);
+      const double c = -24.0 * P.eps;
+      emit(nd * i, (T)(c * L::to(fx)));
+      emit(nd * i + 1, (T)(c * L::to(fy)));
+      if (nd == 3) emit(nd * i + 2, (T)(c * L::to(fz)));
     }
   }
   __syncthreads();
@@ -151,61 +198,62 @@ __device__ __noinline__ double lj_eval(Team& tm, const PotLJ& P, CView<T> cv, T*
 // shared-memory accumulators -- no atomics, and the summation order per
 // particle is fixed by the round order, so results are deterministic.  Tiles
 // are padded with particles 1e6 sigma apart, which contribute nothing
-// measurable.  Shared memory: positions (4 T) and forces (3 T) per particle.
+// measurable.  Shared memory: positions and forces (3 values each) per
+// particle, in the pair arithmetic type.
 template <typename T, class Emit>
 __device__ __noinline__ double lj_eval_sym(CtaTeam& tm, const PotLJ& P, CView<T> cv, T* xw, Emit* emp,
                                            bool want_e, void* smem) {
-  using V4 = typename Vec4T<T>::type;
+  using L = LjC<T>;
+  using C = typename L::C;
   Emit emit = *emp;
   const int N = P.np, nd = P.ndim;
   const int nt = (N + 31) >> 5;            // tiles
   const int ntp = nt + (nt & 1);           // even count for the schedule (last may be empty)
-  V4* sx = reinterpret_cast<V4*>(smem);
-  T* sf = reinterpret_cast<T*>(sx + 32 * ntp);  // 3 per particle
-  const T s6 = (T)P.s6;
+  CV3<C>* sx = reinterpret_cast<CV3<C>*>(smem);
+  C* sf = reinterpret_cast<C*>(sx + 32 * ntp);  // 3 per particle
+  const C s6 = L::from((T)P.s6);
+  const C zero = L::from((T)0);
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
   for (int j = threadIdx.x; j < 32 * ntp; j += blockDim.x) {
-    V4 v;
+    CV3<C> v;
     if (j < N) {
-      v.x = cv(nd * j);
-      v.y = cv(nd * j + 1);
-      v.z = (nd == 3) ? cv(nd * j + 2) : (T)0;
+      const T px = cv(nd * j), py = cv(nd * j + 1), pz = (nd == 3) ? cv(nd * j + 2) : (T)0;
+      v.x = L::from(px);
+      v.y = L::from(py);
+      v.z = L::from(pz);
       if (xw) {
-        xw[nd * j] = v.x;
-        xw[nd * j + 1] = v.y;
-        if (nd == 3) xw[nd * j + 2] = v.z;
+        xw[nd * j] = px;
+        xw[nd * j + 1] = py;
+        if (nd == 3) xw[nd * j + 2] = pz;
       }
     } else {
-      v.x = (T)(1e6 * (double)(j + 1));
-      v.y = 0;
-      v.z = 0;
+      v.x = L::from((T)(1e6 * (double)(j + 1)));
+      v.y = zero;
+      v.z = zero;
     }
-    v.w = 0;
     sx[j] = v;
-    sf[3 * j] = 0;
-    sf[3 * j + 1] = 0;
-    sf[3 * j + 2] = 0;
+    sf[3 * j] = zero;
+    sf[3 * j + 1] = zero;
+    sf[3 * j + 2] = zero;
   }
   __syncthreads();
-  EAcc<T> e;
+  LjAcc<C> e;
   // diagonal tiles: each lane pairs with the 31 others of its tile (every
   // pair twice, half the energy each), force on the own particle only
   for (int t = w; t < nt; t += nw) {
     const int i = 32 * t + lane;
-    const V4 a = sx[i];
-    T fx = 0, fy = 0, fz = 0, ee = 0;
+    const CV3<C> a = sx[i];
+    C fx = zero, fy = zero, fz = zero, ee = zero;
     for (int s = 1; s < 32; s++) {
-      const V4 b = sx[32 * t + ((lane + s) & 31)];
-      const T dx = a.x - b.x, dy = a.y - b.y, dz = a.z - b.z;
-      const T inv = lj_rcp<T>(dx * dx + dy * dy + dz * dz);
-      const T lj6 = s6 * inv * inv * inv;
-      const T lj12 = lj6 * lj6;
-      const T f = (2 * lj12 - lj6) * inv;
-      fx += dx * f; fy += dy * f; fz += dz * f;
-      ee += lj12 - lj6;
+      const CV3<C> b = sx[32 * t + ((lane + s) & 31)];
+      const C dx = a.x - b.x, dy = a.y - b.y, dz = a.z - b.z;
+      C lj6, lj12, f;
+      lj_pair(dx, dy, dz, s6, lj6, lj12, f);
+      fx = fx + dx * f; fy = fy + dy * f; fz = fz + dz * f;
+      ee = ee + (lj12 - lj6);
     }
-    sf[3 * i] += fx; sf[3 * i + 1] += fy; sf[3 * i + 2] += fz;
-    if (want_e && i < N) e.add((T)0.5 * ee);
+    sf[3 * i] = sf[3 * i] + fx; sf[3 * i + 1] = sf[3 * i + 1] + fy; sf[3 * i + 2] = sf[3 * i + 2] + fz;
+    if (want_e && i < N) e.add(ee * L::from((T)0.5));
   }
   __syncthreads();
   // off-diagonal tile pairs, circle-method rounds
@@ -217,38 +265,37 @@ __device__ __noinline__ double lj_eval_sym(CtaTeam& tm, const PotLJ& P, CView<T>
       else { I = (r + k) % (ntp - 1); J = (r - k + (ntp - 1)) % (ntp - 1); }
       if (I >= nt || J >= nt) continue;   // the empty padding tile
       const int i = 32 * I + lane;
-      const V4 a = sx[i];
-      V4 b = sx[32 * J + lane];
-      T fx = 0, fy = 0, fz = 0, gx = 0, gy = 0, gz = 0, ee = 0;
+      const CV3<C> a = sx[i];
+      CV3<C> b = sx[32 * J + lane];
+      C fx = zero, fy = zero, fz = zero, gx = zero, gy = zero, gz = zero, ee = zero;
       const int src = (lane + 1) & 31;
       for (int s = 0; s < 32; s++) {
-        const T dx = a.x - b.x, dy = a.y - b.y, dz = a.z - b.z;
-        const T inv = lj_rcp<T>(dx * dx + dy * dy + dz * dz);
-        const T lj6 = s6 * inv * inv * inv;
-        const T lj12 = lj6 * lj6;
-        const T f = (2 * lj12 - lj6) * inv;
-        fx += dx * f; fy += dy * f; fz += dz * f;
-        gx -= dx * f; gy -= dy * f; gz -= dz * f;
-        ee += lj12 - lj6;
-        b.x = __shfl_sync(0xffffffffu, b.x, src);
-        b.y = __shfl_sync(0xffffffffu, b.y, src);
-        b.z = __shfl_sync(0xffffffffu, b.z, src);
-        gx = __shfl_sync(0xffffffffu, gx, src);
-        gy = __shfl_sync(0xffffffffu, gy, src);
-        gz = __shfl_sync(0xffffffffu, gz, src);
+        const C dx = a.x - b.x, dy = a.y - b.y, dz = a.z - b.z;
+        C lj6, lj12, f;
+        lj_pair(dx, dy, dz, s6, lj6, lj12, f);
+        const C ex = dx * f, ey = dy * f, ez = dz * f;
+        fx = fx + ex; fy = fy + ey; fz = fz + ez;
+        gx = gx - ex; gy = gy - ey; gz = gz - ez;
+        ee = ee + (lj12 - lj6);
+        b.x = lj_shfl(b.x, src);
+        b.y = lj_shfl(b.y, src);
+        b.z = lj_shfl(b.z, src);
+        gx = lj_shfl(gx, src);
+        gy = lj_shfl(gy, src);
+        gz = lj_shfl(gz, src);
       }
       const int j = 32 * J + lane;
-      sf[3 * i] += fx; sf[3 * i + 1] += fy; sf[3 * i + 2] += fz;
-      sf[3 * j] += gx; sf[3 * j + 1] += gy; sf[3 * j + 2] += gz;
+      sf[3 * i] = sf[3 * i] + fx; sf[3 * i + 1] = sf[3 * i + 1] + fy; sf[3 * i + 2] = sf[3 * i + 2] + fz;
+      sf[3 * j] = sf[3 * j] + gx; sf[3 * j + 1] = sf[3 * j + 1] + gy; sf[3 * j + 2] = sf[3 * j + 2] + gz;
       if (want_e) e.add(ee);
     }
     __syncthreads();
   }
-  const T c = (T)(-24.0 * P.eps);
+  const double c = -24.0 * P.eps;
   for (int i = threadIdx.x; i < N; i += blockDim.x) {
-    emit(nd * i, c * sf[3 * i]);
-    emit(nd * i + 1, c * sf[3 * i + 1]);
-    if (nd == 3) emit(nd * i + 2, c * sf[3 * i + 2]);
+    emit(nd * i, (T)(c * L::to(sf[3 * i])));
+    emit(nd * i + 1, (T)(c * L::to(sf[3 * i + 1])));
+    if (nd == 3) emit(nd * i + 2, (T)(c * L::to(sf[3 * i + 2])));
   }
   __syncthreads();
   *emp = emit;
