@@ -204,6 +204,8 @@ def run_gpu(args):
     }
     if not args.no_batched:
         out.update(run_batched(args))
+    if args.mixed > 0:
+        out.update(run_mixed(args))
     if args.serve > 0:
         out.update(run_serving(args))
     if not args.no_cpu:
@@ -251,6 +253,44 @@ def run_batched(args):
         "plain": {"value": plain, "unit": "minimisations/s", "sample": int(len(idx))},
         "batched_vs_plain": batched / plain,
     }
+
+
+def run_mixed(args):
+    """One batch launch of mixed phase-field and mesh instances: 2-D
+    three-fluid PhaseField grids (hard density constraint, fixed volumes,
+    random simplex start) and BarAndHinge sheets (flat jittered rest shape,
+    Gaussian out-of-plane start), all Lbfgs to RMS < 1e-7.  Sizes are capped
+    (grids 64^2 / 128^2, sheets 32^2 .. 64^2 vertices) so that the launch runs
+    in seconds."""
+    from minim_gb300 import abi, runtime
+    from tests.workloads import Rng, pf_simplex, sheet
+    rng = Rng(11)
+    npf, nbah = (2 * args.mixed) // 3, args.mixed - (2 * args.mixed) // 3
+    u = rng.uniform(npf + nbah)
+    insts, items = [], []
+    for i in range(npf):
+        side = 64 if u[i] < 0.5 else 128
+        grid = (side, side, 1)
+        p = abi.phase_field(grid, nfluid=3, volume_fixed=True)
+        insts.append(runtime.Instance(p, pf_simplex(grid, 3, seed=5000 + i)))
+        items.append(("pf", abi.minimiser("lbfgs", tol=1e-7, max_iter=20000)))
+    for i in range(nbah):
+        k = 32 + int(u[npf + i] * 33)
+        flat, tris, pert = sheet(k, seed=6000 + i)
+        inst = runtime.Instance(abi.bar_and_hinge(triangulation=tris, rigidity=(1, 0.01)), flat)
+        inst.coords = pert
+        insts.append(inst)
+        items.append(("bah", abi.minimiser("lbfgs", tol=1e-7, max_iter=20000)))
+    b = runtime.Batch()
+    for inst, (_, mp) in zip(insts, items):
+        b.add(inst, mp)
+    res = b.run()
+    st = runtime.last_run_stats()
+    conv = sum(r.status == abi.RES_CONVERGED for r in res)
+    return {"mixed_batch": {"value": conv / (st["kernel_ms"] / 1e3), "unit": "converged minimisations/s",
+                            "instances": len(items), "converged": int(conv), "kernel_ms": st["kernel_ms"],
+                            "workload": f"{npf} 2-D ternary PhaseField grids (64^2/128^2, fixed volume) + "
+                                        f"{nbah} BarAndHinge sheets (1k-4.2k vertices), Lbfgs RMS<1e-7"}}
 
 
 def serving_requests(count, rate, seed=7):
@@ -420,6 +460,7 @@ def main():
     ap.add_argument("--plain-sample", type=int, default=16)
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--serve", type=int, default=200, help="requests in the serving stream (0 = skip)")
+    ap.add_argument("--mixed", type=int, default=96, help="instances in the mixed PF/BAH batch (0 = skip)")
     ap.add_argument("--serve-rate", type=float, default=2000.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=20.0)
