@@ -464,7 +464,8 @@ def main():
     ap.add_argument("--serve-rate", type=float, default=2000.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-budget", type=float, default=20.0)
-    ap.add_argument("--ref-iters-hint", type=int, default=600)
+    ap.add_argument("--ref-iters-hint", type=int, default=985,
+                    help="iterations of a full minimisation (the GPU run of the same algorithm needs 981-987)")
     ap.add_argument("--profile", type=int, default=0,
                     help="run one short minimisation of N iterations (profiler capture) and exit")
     args = ap.parse_args()
