@@ -119,9 +119,18 @@ __device__ __forceinline__ DF operator*(DF a, DF b) {
   e = __fmaf_rn(a.lo, b.hi, e);
   return df_fast2sum(p, e);
 }
+// 1 / x in FP32: the hardware approximation refined by one Newton-Raphson
+// step, r' = r + r (1 - x r) (within an ulp or so; the correctly rounded
+// reciprocal costs several times more)
+__device__ __forceinline__ float rcp_nr(float x) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return __fmaf_rn(r, __fmaf_rn(-x, r, 1.f), r);
+}
+
 // 1 / b: the FP32 reciprocal refined by one Newton step in double-float
 __device__ __forceinline__ DF df_rcp(DF b) {
-  const float y = __frcp_rn(b.hi);
+  const float y = rcp_nr(b.hi);
   const DF r = DF{1.f, 0.f} - b * DF{y, 0.f};  // residual 1 - b y
   return DF{y, 0.f} + DF{y, 0.f} * r;
 }

@@ -63,11 +63,13 @@ template <> struct LjC<float> {
   using C = float;
   __device__ static C from(float x) { return x; }
   __device__ static double to(C x) { return (double)x; }
+  __device__ static float scaled(double c, C x) { return (float)c * x; }  // no FP64 per DOF
 };
 template <> struct LjC<double> {
   using C = DF;
   __device__ static C from(double x) { return df_from(x); }
   __device__ static double to(C x) { return df_to(x); }
+  __device__ static double scaled(double c, C x) { return c * df_to(x); }
 };
 template <typename C> struct CV3 { C x, y, z; };
 
@@ -78,7 +80,7 @@ __device__ __forceinline__ DF lj_shfl(DF a, int src) { return df_shfl(a, src); }
 // of one pair separated by (dx, dy, dz)
 __device__ __forceinline__ void lj_pair(float dx, float dy, float dz, float s6, float& lj6, float& lj12,
                                         float& f) {
-  const float inv = __frcp_rn(dx * dx + dy * dy + dz * dz);
+  const float inv = rcp_nr(dx * dx + dy * dy + dz * dz);
   lj6 = s6 * inv * inv * inv;
   lj12 = lj6 * lj6;
   f = (lj12 + lj12 - lj6) * inv;
@@ -127,7 +129,7 @@ __device__ __noinline__ double lj_eval(Team& tm, const PotLJ& P, CView<T> cv, T*
   if (xw) {
     for (int i = tm.tid(); i < N * nd; i += tm.nthr()) xw[i] = cv(i);
   }
-  LjAcc<C> e;
+  LjAcc<C> e4[4];
   const int step = tm.nthr();
   // every thread of every block runs the same number of outer rounds
   const int rounds = (N + step - 1) / step;
@@ -154,7 +156,10 @@ __device__ __noinline__ double lj_eval(Team& tm, const PotLJ& P, CView<T> cv, T*
       }
       __syncthreads();
       if (act) {
+        // pair energies go to four compensated accumulators in turn (four
+        // short dependent chains instead of one long one)
         if (want_g) {
+#pragma unroll 4
           for (int j = 0; j < nt; j++) {
             if (j0 + j == i) continue;
             const CV3<C> b = sx[j];
@@ -164,29 +169,30 @@ __device__ __noinline__ double lj_eval(Team& tm, const PotLJ& P, CView<T> cv, T*
             fx = fx + dx * f;
             fy = fy + dy * f;
             fz = fz + dz * f;
-            if (want_e && (j0 + j > i)) e.add(lj12 - lj6);
+            if (want_e && (j0 + j > i)) e4[j & 3].add(lj12 - lj6);
           }
         } else if (want_e) {
+#pragma unroll 4
           for (int j = max(0, i + 1 - j0); j < nt; j++) {
             const CV3<C> b = sx[j];
             const C dx = xi - b.x, dy = yi - b.y, dz = zi - b.z;
             C lj6, lj12, f;
             lj_pair(dx, dy, dz, s6, lj6, lj12, f);
-            e.add(lj12 - lj6);
+            e4[j & 3].add(lj12 - lj6);
           }
         }
       }
     }
     if (act && want_g) {
       const double c = -24.0 * P.eps;
-      emit(nd * i, (T)(c * L::to(fx)));
-      emit(nd * i + 1, (T)(c * L::to(fy)));
-      if (nd == 3) emit(nd * i + 2, (T)(c * L::to(fz)));
+      emit(nd * i, L::scaled(c, fx));
+      emit(nd * i + 1, L::scaled(c, fy));
+      if (nd == 3) emit(nd * i + 2, L::scaled(c, fz));
     }
   }
   __syncthreads();
   *emp = emit;
-  return 4.0 * P.eps * e.total();
+  return 4.0 * P.eps * ((e4[0].total() + e4[1].total()) + (e4[2].total() + e4[3].total()));
 }
 
 // Symmetric all-pairs evaluation for one CTA (the batched path): each
@@ -244,6 +250,7 @@ __device__ __noinline__ double lj_eval_sym(CtaTeam& tm, const PotLJ& P, CView<T>
     const int i = 32 * t + lane;
     const CV3<C> a = sx[i];
     C fx = zero, fy = zero, fz = zero, ee = zero;
+#pragma unroll 4
     for (int s = 1; s < 32; s++) {
       const CV3<C> b = sx[32 * t + ((lane + s) & 31)];
       const C dx = a.x - b.x, dy = a.y - b.y, dz = a.z - b.z;
@@ -269,20 +276,24 @@ __device__ __noinline__ double lj_eval_sym(CtaTeam& tm, const PotLJ& P, CView<T>
       CV3<C> b = sx[32 * J + lane];
       C fx = zero, fy = zero, fz = zero, gx = zero, gy = zero, gz = zero, ee = zero;
       const int src = (lane + 1) & 31;
+      // the next step's j position is fetched first: only the force rotation
+      // (an add and a shuffle) chains one step to the next, so the pair
+      // arithmetic of consecutive steps overlaps
+#pragma unroll 4
       for (int s = 0; s < 32; s++) {
-        const C dx = a.x - b.x, dy = a.y - b.y, dz = a.z - b.z;
+        const CV3<C> bc = b;
+        b.x = lj_shfl(b.x, src);
+        b.y = lj_shfl(b.y, src);
+        b.z = lj_shfl(b.z, src);
+        const C dx = a.x - bc.x, dy = a.y - bc.y, dz = a.z - bc.z;
         C lj6, lj12, f;
         lj_pair(dx, dy, dz, s6, lj6, lj12, f);
         const C ex = dx * f, ey = dy * f, ez = dz * f;
         fx = fx + ex; fy = fy + ey; fz = fz + ez;
-        gx = gx - ex; gy = gy - ey; gz = gz - ez;
+        gx = lj_shfl(gx - ex, src);
+        gy = lj_shfl(gy - ey, src);
+        gz = lj_shfl(gz - ez, src);
         ee = ee + (lj12 - lj6);
-        b.x = lj_shfl(b.x, src);
-        b.y = lj_shfl(b.y, src);
-        b.z = lj_shfl(b.z, src);
-        gx = lj_shfl(gx, src);
-        gy = lj_shfl(gy, src);
-        gz = lj_shfl(gz, src);
       }
       const int j = 32 * J + lane;
       sf[3 * i] = sf[3 * i] + fx; sf[3 * i + 1] = sf[3 * i + 1] + fy; sf[3 * i + 2] = sf[3 * i + 2] + fz;
@@ -293,9 +304,9 @@ __device__ __noinline__ double lj_eval_sym(CtaTeam& tm, const PotLJ& P, CView<T>
   }
   const double c = -24.0 * P.eps;
   for (int i = threadIdx.x; i < N; i += blockDim.x) {
-    emit(nd * i, (T)(c * L::to(sf[3 * i])));
-    emit(nd * i + 1, (T)(c * L::to(sf[3 * i + 1])));
-    if (nd == 3) emit(nd * i + 2, (T)(c * L::to(sf[3 * i + 2])));
+    emit(nd * i, L::scaled(c, sf[3 * i]));
+    emit(nd * i + 1, L::scaled(c, sf[3 * i + 1]));
+    if (nd == 3) emit(nd * i + 2, L::scaled(c, sf[3 * i + 2]));
   }
   __syncthreads();
   *emp = emit;
