@@ -3,13 +3,20 @@
       relaxes to a tanh profile whose fitted width is within 2.5 % of the set
       width (check.py:26-38);
   test/benchmark/pf-volume: a liquid disk under the fixed-volume projection
-      keeps its volume to 0.003 relative (main.cpp:89).
-Both also agree with the FP64 oracle running the same minimisation."""
+      keeps its volume to 0.003 relative (main.cpp:89);
+  test/benchmark/pf-pillar-collapse: the critical pressure at which liquid
+      collapses between two pillars, by bisection, within 100 of
+      -2 gamma cos(theta) / (spacing res) for seven contact angles (check.py).
+The first two also agree with the FP64 oracle running the same minimisation;
+the pillar case with the reference library's own run of the same bisection
+(tests/golden/pillar.npz, made by tests/golden/gen_pillar.py)."""
 import numpy as np
 import pytest
 
 from minim_gb300 import abi, runtime
 from oracle.oracle import Oracle
+from tests import workloads as W
+from tests.golden_io import GOLDEN
 
 pytestmark = pytest.mark.gpu
 
@@ -66,3 +73,53 @@ def test_pf_volume_conservation():
     assert err < 0.003, err
     # the drop stays a drop: the liquid fraction near the centre is ~1
     assert x[:, 0][r < radius - 3].min() > 0.9
+
+
+def test_pf_pillar_collapse():
+    """The seven contact angles run as one batch at every bisection step."""
+    gold = np.load(f"{GOLDEN}/pillar.npz")
+    angles = [float(a) for a in gold["angles"]]
+    solid = W.pillar_solid()
+    # diffuseSolid (src/potentials/PhaseField.cpp:1009-1035), fp64 as in the reference
+    b = runtime.Batch()
+    insts = []
+    for ca in angles:
+        kw = W.pillar_kwargs(ca, diffuse=True)
+        tol = 1e-8 * kw["surface_tension"][0] * W.PILLAR["res"] ** 2
+        inst = runtime.Instance(abi.phase_field(**kw), W.pillar_diffuse_init(solid))
+        insts.append(inst)
+        b.add(inst, abi.minimiser("lbfgs", linesearch="none", max_iter=100, tol=tol, precision="fp64"))
+    res = b.run()
+    b.close()
+    dif = [inst.coords for inst in insts]
+    assert [r.iter for r in res] == list(gold["diffuse_iters"])
+    # 100 iterations without a line search stop far from the minimum, and the
+    # L-BFGS history is FP32 here (FP64 in the reference), so the iterate
+    # agrees to a few 1e-3 rather than to rounding
+    d90 = dif[angles.index(90.0)][0::3]
+    assert np.max(np.abs(d90 - gold["diffused90"])) < 2e-2
+    assert np.allclose([d[0::3].sum() for d in dif], gold["diffused_sum"], rtol=1e-3)
+    assert np.allclose([(d[0::3] ** 2).sum() for d in dif], gold["diffused_sq"], rtol=1e-3)
+    x0s = [W.pillar_fluid(d) for d in dif]
+
+    def run(idx, p):
+        b = runtime.Batch()
+        runs = []
+        for i, pi in zip(idx, p):
+            inst = runtime.Instance(abi.phase_field(**W.pillar_kwargs(angles[i], pressure=pi)), x0s[i])
+            runs.append(inst)
+            b.add(inst, abi.minimiser("lbfgs", linesearch="none", max_iter=5000))
+        out = [(W.pillar_failed(inst.coords), r.iter) for inst, r in zip(runs, b.run())]
+        b.close()
+        return out
+
+    lo, hi, hist = W.pillar_bisect(run, len(angles))
+    crit = 0.5 * (lo + hi)
+    half = 0.5 * (hi - lo)
+    crit_ref = 0.5 * (gold["lo"] + gold["hi"])
+    print("critical pressures", [round(c, 2) for c in crit], "reference", [round(c, 2) for c in crit_ref])
+    for a, c, h, cr in zip(angles, crit, half, crit_ref):
+        # the benchmark's acceptance (check.py: |residual| <= 100)
+        assert abs(c - W.pillar_analytic(a)) <= 100, (a, c)
+        # the reference's bisection lands within a step or two of the same bounds
+        assert abs(c - cr) <= 4 * h + 1e-9, (a, c, cr)

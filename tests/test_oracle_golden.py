@@ -74,3 +74,24 @@ def test_bah_setup():
         b, bp, h, hp = Oracle(p, c["x0"]).bah_elements()
         assert np.array_equal(b, c["bars"]) and np.array_equal(h, c["hinges"])
         assert np.allclose(bp, c["bar_par"], rtol=1e-14) and np.allclose(hp, c["hinge_par"], rtol=1e-14)
+
+
+def test_pillar_collapse_decisions():
+    """pf-pillar-collapse at 90 degrees: the oracle's diffuseSolid matches the
+    reference's, and the oracle takes the reference's decision at the final
+    bisection bounds (holds at the lower, collapses at the upper)."""
+    from minim_gb300 import abi
+    from tests import workloads as W
+    gold = np.load(f"{G.GOLDEN}/pillar.npz")
+    a = list(gold["angles"]).index(90.0)
+    kw = W.pillar_kwargs(90.0, diffuse=True)
+    ora = Oracle(G.params_from("pf", kw), W.pillar_diffuse_init(W.pillar_solid()))
+    tol = 1e-8 * kw["surface_tension"][0] * W.PILLAR["res"] ** 2
+    r = ora.minimise(abi.minimiser("lbfgs", linesearch="none", max_iter=100, tol=tol))
+    assert r.iter == gold["diffuse_iters"][a]
+    assert np.max(np.abs(ora.coords[0::3] - gold["diffused90"])) < 1e-12
+    x0 = W.pillar_fluid(ora.coords)
+    for p, want in ((gold["lo"][a], False), (gold["hi"][a], True)):
+        run = Oracle(G.params_from("pf", W.pillar_kwargs(90.0, pressure=p)), x0)
+        run.minimise(abi.minimiser("lbfgs", linesearch="none", max_iter=5000))
+        assert W.pillar_failed(run.coords) == want, p
