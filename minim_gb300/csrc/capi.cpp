@@ -153,6 +153,15 @@ bool stepped_cfg() {
   }();
   return v;
 }
+// The stepped graph's line-search trials evaluate two consecutive trials of
+// the backtracking sequence per pass unless MINIM_GPU_TRIAL_PAIRS=0.
+bool dual_cfg() {
+  static const bool v = [] {
+    const char* e = std::getenv("MINIM_GPU_TRIAL_PAIRS");
+    return !(e && e[0] == '0');
+  }();
+  return v;
+}
 // L2 prefetch distance of the grid launches' sweeps, in sweep steps
 // (MINIM_GPU_PREFETCH, default 1; 0 disables it).
 int prefetch_cfg() {
@@ -167,19 +176,23 @@ size_t grid_smem(int kk) { return kk == K_LJ ? kLjTileBytes : kStages * (size_t)
 
 // ---- workspace layout --------------------------------------------------------------
 struct WsLayout {
-  size_t x32[2], x64[2], g[2], S, Y, V, total, hstride;
+  size_t x32[2], x64[2], g[2], x32s, gs, S, Y, V, total, hstride;
   int nS, nY;
   bool fp64;
 };
 size_t align256(size_t v) { return (v + 255) & ~(size_t)255; }
-WsLayout ws_layout(size_t n, const minim_gpu_minimiser_params& mp) {
+// dual: the stepped path's spare buffers for two line-search trials per pass
+// (a point, a gradient and one more y slot)
+WsLayout ws_layout(size_t n, const minim_gpu_minimiser_params& mp, bool dual = false) {
   WsLayout L{};
   size_t o = 0;
   auto take = [&](size_t bytes) { size_t r = o; o += align256(bytes); return r; };
   L.fp64 = mp.precision != MINIM_PREC_FP32;
   L.nS = mp.method == MINIM_LBFGS ? mp.m + 1 : (mp.method == MINIM_FIRE ? 1 : 0);
-  L.nY = mp.method == MINIM_LBFGS ? mp.m + 1 : 0;
+  L.nY = mp.method == MINIM_LBFGS ? mp.m + 1 + (dual ? 1 : 0) : 0;
   for (int k = 0; k < 2; k++) L.x32[k] = take(n * 4);
+  L.x32s = dual ? take(n * 4) : (size_t)-1;
+  L.gs = dual ? take(n * 4) : (size_t)-1;
   for (int k = 0; k < 2; k++) L.x64[k] = L.fp64 ? take(n * 8) : (size_t)-1;
   for (int k = 0; k < 2; k++) L.g[k] = take(n * 4);
   L.hstride = (n + 63) & ~(size_t)63;
@@ -198,6 +211,8 @@ void ws_apply(InstDesc& d, char* base, const WsLayout& L) {
     d.X64[k] = L.fp64 ? (double*)(base + L.x64[k]) : nullptr;
     d.G[k] = (float*)(base + L.g[k]);
   }
+  d.X32s = L.x32s != (size_t)-1 ? (float*)(base + L.x32s) : nullptr;
+  d.Gs = L.gs != (size_t)-1 ? (float*)(base + L.gs) : nullptr;
   d.hstride = (int)L.hstride;
   d.Sb = L.nS ? (float*)(base + L.S) : nullptr;
   d.Yb = L.nY ? (float*)(base + L.Y) : nullptr;
@@ -275,7 +290,6 @@ struct minim_gpu_instance_s {
   // single-instance workspace (lazy)
   void* ws = nullptr;
   size_t ws_bytes = 0;
-  void* stepped = nullptr;  // cached graph of the stepped FP32 path
   MinScalars* d_st = nullptr;
 
   void* own(void* p) {
@@ -290,10 +304,6 @@ struct minim_gpu_instance_s {
     return p;
   }
   ~minim_gpu_instance_s() {
-    if (stepped) {
-      cudaStreamSynchronize(dev().s);
-      mg_stepped_free(&stepped);
-    }
     for (void* p : owned) dfree(p);
     dfree(ws);
   }
@@ -434,7 +444,11 @@ void do_minimise(minim_gpu_instance_s* h, const minim_gpu_minimiser_params& mp, 
   check_mp(mp);
   ensure_grid(h);
   const double tol = mp.tol >= 0 ? mp.tol : h->default_tol;
-  WsLayout L = ws_layout(h->n, mp);
+  // the FP32 stage of a large binary PhaseField L-BFGS runs as the stepped graph
+  const bool stepped_ok = stepped_cfg() && h->kk == K_PF1 && mp.method == MINIM_LBFGS &&
+                          mp.precision != MINIM_PREC_FP64 && h->d.fixed == nullptr && h->n >= ((size_t)1 << 18);
+  const bool dual = stepped_ok && dual_cfg();
+  WsLayout L = ws_layout(h->n, mp, dual);
   const size_t need = L.total + align256(sizeof(MinScalars));
   if (need > h->ws_bytes) {
     dfree(h->ws);
@@ -450,6 +464,7 @@ void do_minimise(minim_gpu_instance_s* h, const minim_gpu_minimiser_params& mp, 
   h->d_st = (MinScalars*)((char*)h->ws + L.total);
   d.st = h->d_st;
   MinScalars s = fresh_scalars();
+  s.ybuf2 = dual ? mp.m + 1 : -1;
   CK(cudaMemcpyAsync(h->d_st, &s, sizeof s, cudaMemcpyHostToDevice, D.s));
   CK(cudaMemcpyAsync(h->d_desc, &d, sizeof d, cudaMemcpyHostToDevice, D.s));
   int slice = 64;
@@ -458,9 +473,7 @@ void do_minimise(minim_gpu_instance_s* h, const minim_gpu_minimiser_params& mp, 
   cudaEvent_t ev0, ev1;
   CK(cudaEventCreate(&ev0));
   CK(cudaEventCreate(&ev1));
-  const bool stepped = stepped_cfg() && h->kk == K_PF1 && mp.method == MINIM_LBFGS &&
-                       mp.precision != MINIM_PREC_FP64 && h->d.fixed == nullptr && h->n >= ((size_t)1 << 18) &&
-                       L.total < ((size_t)1 << 34);  // signed 32-bit float4 offsets across the workspace
+  const bool stepped = stepped_ok && L.total < ((size_t)1 << 34);  // signed 32-bit float4 offsets across the workspace
   if (stepped) {
     // iteration 0 (set-up) on the persistent kernel, then the FP32 stage as
     // graph launches until it hands over (precision switch, convergence,
@@ -479,7 +492,7 @@ void do_minimise(minim_gpu_instance_s* h, const minim_gpu_minimiser_params& mp, 
       const int it0 = s.iter;
       double kernels = 0;
       CK(cudaEventRecord(ev0, D.s));
-      CK((cudaError_t)mg_stepped_pf1_run(&h->stepped, h->d_desc, h->d_st, mp.m, h->d.pf.n, D.nsm, 4096, D.s, &kernels));
+      CK((cudaError_t)mg_stepped_pf1_run(h->d_desc, h->d_st, mp.m, h->d.pf.n, D.nsm, 4096, dual ? 1 : 0, D.s, &kernels));
       CK(cudaEventRecord(ev1, D.s));
       CK(cudaMemcpyAsync(&s, h->d_st, sizeof s, cudaMemcpyDeviceToHost, D.s));
       CK(cudaStreamSynchronize(D.s));

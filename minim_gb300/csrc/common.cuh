@@ -164,6 +164,54 @@ __device__ __forceinline__ unsigned long long globaltimer_ns() {
   return t;
 }
 
+// ---- compact-form L-BFGS algebra on one warp -----------------------------------
+// Every lane of the calling warp takes part; lane k < mt holds pair k in age
+// order (oldest first) with sg = s_k.g and yg = y_k.g.  Solves
+//   R u = S^T g,   R^T w = (D + gamma Y^T Y) u - gamma Y^T g,
+// R the upper triangle of S^T Y and D its diagonal, for the coefficients of
+// P = -(gamma g + S w - gamma Y u): the direction the reference's two-loop
+// recursion forms (src/minimisers/Lbfgs.cpp:60-105), in compact form.
+// sy(a, b) = s_a.y_b and yy(a, b) = y_a.y_b in age order.  The triangular
+// solves go column by column: once lane b holds its unknown it is broadcast
+// and every lane still open subtracts its term, so the dependent chain per
+// pair is one multiply and one FMA (FP64 runs at 1/64 of the FP32 rate on
+// this GPU, with a long latency per dependent operation) instead of a row's
+// dot product and a division; 1 / R[k][k] is formed once per lane.
+template <class SYf, class YYf>
+__device__ __forceinline__ void lbfgs_compact_warp(int mt, double gamma, double sg, double yg, SYf sy, YYf yy,
+                                                   double& u_out, double& w_out) {
+  const int lane = (threadIdx.y * blockDim.x + threadIdx.x) & 31;
+  const bool on = lane < mt;
+  const double r = on ? 1.0 / sy(lane, lane) : 0.0;
+  double t = on ? sg : 0.0, u = 0.0;
+  for (int b = mt - 1; b >= 0; b--) {
+    const double ub = __shfl_sync(0xffffffffu, t * r, b);
+    if (lane == b) u = ub;
+    else if (lane < b) t -= sy(lane, b) * ub;
+  }
+  double v = on ? sy(lane, lane) * u - gamma * yg : 0.0;
+  for (int b = 0; b < mt; b++) {
+    const double ub = __shfl_sync(0xffffffffu, u, b);
+    if (on) v += gamma * yy(lane, b) * ub;
+  }
+  double w = 0.0;
+  t = v;
+  for (int b = 0; b < mt; b++) {
+    const double wb = __shfl_sync(0xffffffffu, t * r, b);
+    if (lane == b) w = wb;
+    else if (on && lane > b) t -= sy(b, lane) * wb;
+  }
+  u_out = u;
+  w_out = w;
+}
+
+// slot of pair k (age order) of the m-slot ring whose next slot is c, with
+// mt pairs stored: (c - mt + k) mod m
+__device__ __forceinline__ int ring_slot(int c, int mt, int k, int m) {
+  const int s = c - mt + k;
+  return s < 0 ? s + m : s;
+}
+
 // ---- bulk copies into shared memory (cp.async.bulk + mbarrier) -----------------
 // A stage is a shared buffer with an mbarrier.  One thread announces the
 // bytes the stage will receive (arrive.expect_tx) and issues the copies; the

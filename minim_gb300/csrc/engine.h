@@ -105,6 +105,7 @@ struct MinScalars {
   int stall;         // iterations since the best rms improved (stage 0)
   int nsteps;        // Fire::_nSteps
   int pbuf, ybuf;    // spare history buffers (direction / new y)
+  int ybuf2;         // second spare y slot (stepped path, two trials per pass), or -1
   int exhausted_run; // consecutive line searches that found no Armijo point
   int switch_reason; // why the FP64 stage started: 1 converged in FP32,
                      // 2 line search exhausted twice, 3 stalled near tol
@@ -146,6 +147,10 @@ struct InstDesc {
   float* X32[2];
   double* X64[2];
   float* G[2];
+  // stepped path, two trials per pass: the second trial's point and gradient
+  // (exchanged with X32[1 - xi] / G[1 - gi] when it is accepted), or NULL
+  float* X32s;
+  float* Gs;
   int hstride;     // floats between history buffers (ndof rounded up to 64)
   float* Sb;       // (m + 1) * hstride: ring of directions (s = sigma * S)
   float* Yb;       // (m + 1) * hstride
@@ -194,9 +199,10 @@ MG_DECLARE_LAUNCHERS(pf1)
 // engine_misc.cu: FP64 <-> FP32 vector conversion on a stream
 int mg_convert(const void* src, void* dst, size_t n, int to_float, void* stream);
 // stepped.cu: up to `slice` FP32 L-BFGS iterations (history m) of a binary
-// PhaseField instance as one graph launch (graph cached in *cache); returns
-// a cudaError_t
-int mg_stepped_pf1_run(void** cache, const mg::InstDesc* d, mg::MinScalars* st, int m, const int* grid,
-                       int nsm, int slice, void* stream, double* kernels);
-void mg_stepped_free(void** cache);
+// PhaseField instance as one launch of the graph of its shape (cached per
+// process); dual: the workspace has the spare buffers for two trials per
+// pass.  Returns a cudaError_t.
+int mg_stepped_pf1_run(mg::InstDesc* d, mg::MinScalars* st, int m, const int* grid, int nsm, int slice,
+                       int dual, void* stream, double* kernels);
+void mg_stepped_free_all();
 }

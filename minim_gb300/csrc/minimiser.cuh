@@ -522,46 +522,42 @@ struct Runner {
     }
   }
 
-  // small dense algebra in one thread per block (bitwise the same in all):
+  // small dense algebra on warp 0 of every block (bitwise the same in all):
   // R u = S^T g, R^T w = (D + gamma Y^T Y) u - gamma Y^T g, coefficients of
   // P = -(gamma g + S w - gamma Y u)
   __device__ __noinline__ void direction_algebra(int mt, int c, int kn, bool np) {
     const int m = in.mp.m;
     const long long hs = in.hstride;
-    if (threadIdx.x == 0) {
-      double sg[MINIM_MAXM], yg[MINIM_MAXM], u[MINIM_MAXM], w[MINIM_MAXM];
-      int sl[MINIM_MAXM];
-      for (int k = 0; k < mt; k++) {
-        sl[k] = (c - mt + k + 2 * m) % m;
-        sg[k] = sig[sl[k]] * wout[k];
-        yg[k] = wout[MINIM_MAXM + k];
-      }
-      if (np) {
-        for (int k = 0; k < mt; k++) {
-          SY[sl[k] * MINIM_MAXM + pend] = sig[sl[k]] * wout[2 * MINIM_MAXM + k];
-          YY[sl[k] * MINIM_MAXM + pend] = wout[3 * MINIM_MAXM + k];
-          YY[pend * MINIM_MAXM + sl[k]] = wout[3 * MINIM_MAXM + k];
+    if (threadIdx.x < 32) {
+      const int lane = threadIdx.x;
+      const bool on = lane < mt;
+      const int slk = on ? ring_slot(c, mt, lane, m) : 0;
+      double sg = 0.0, yg = 0.0;
+      if (on) {
+        sg = sig[slk] * wout[lane];
+        yg = wout[MINIM_MAXM + lane];
+        if (np) {
+          SY[slk * MINIM_MAXM + pend] = sig[slk] * wout[2 * MINIM_MAXM + lane];
+          YY[slk * MINIM_MAXM + pend] = wout[3 * MINIM_MAXM + lane];
+          YY[pend * MINIM_MAXM + slk] = wout[3 * MINIM_MAXM + lane];
         }
       }
+      __syncwarp();
       const double gamma = SY[kn * MINIM_MAXM + kn] / YY[kn * MINIM_MAXM + kn];
-      for (int a = mt - 1; a >= 0; a--) {  // R u = S^T g
-        double t = sg[a];
-        for (int b = a + 1; b < mt; b++) t -= SY[sl[a] * MINIM_MAXM + sl[b]] * u[b];
-        u[a] = t / SY[sl[a] * MINIM_MAXM + sl[a]];
+      const double* sy_ = SY;
+      const double* yy_ = YY;
+      double u, w;
+      lbfgs_compact_warp(
+          mt, gamma, sg, yg,
+          [=](int a, int b) { return sy_[ring_slot(c, mt, a, m) * MINIM_MAXM + ring_slot(c, mt, b, m)]; },
+          [=](int a, int b) { return yy_[ring_slot(c, mt, a, m) * MINIM_MAXM + ring_slot(c, mt, b, m)]; }, u, w);
+      if (lane < MINIM_MAXM) {
+        coefS[lane] = on ? (float)(-w * sig[slk]) : 0.f;
+        coefY[lane] = on ? (float)(gamma * u) : 0.f;
+        boff[lane] = on ? (long long)sidx[slk] * hs : 0;
+        boff[MINIM_MAXM + lane] = on ? (long long)yidx[slk] * hs : 0;
       }
-      for (int a = 0; a < mt; a++) {  // R^T w = (D + gamma Y^T Y) u - gamma Y^T g
-        double t = SY[sl[a] * MINIM_MAXM + sl[a]] * u[a] - gamma * yg[a];
-        for (int b = 0; b < mt; b++) t += gamma * YY[sl[a] * MINIM_MAXM + sl[b]] * u[b];
-        for (int b = 0; b < a; b++) t -= SY[sl[b] * MINIM_MAXM + sl[a]] * w[b];
-        w[a] = t / SY[sl[a] * MINIM_MAXM + sl[a]];
-      }
-      for (int k = 0; k < MINIM_MAXM; k++) {
-        coefS[k] = (k < mt) ? (float)(-w[k] * sig[sl[k]]) : 0.f;
-        coefY[k] = (k < mt) ? (float)(gamma * u[k]) : 0.f;
-        boff[k] = (k < mt) ? (long long)sidx[sl[k]] * hs : 0;
-        boff[MINIM_MAXM + k] = (k < mt) ? (long long)yidx[sl[k]] * hs : 0;
-      }
-      wout[MINIM_WIDE - 1] = gamma;
+      if (lane == 0) wout[MINIM_WIDE - 1] = gamma;
     }
     __syncthreads();
   }

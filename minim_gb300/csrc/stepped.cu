@@ -35,8 +35,11 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstddef>
 #include <cstdio>
 #include <cstdlib>
+#include <mutex>
+#include <vector>
 
 #include "kernels.cuh"
 
@@ -48,6 +51,9 @@ struct FlatTeam {
   __device__ __forceinline__ int nthr() const { return gridDim.x * blockDim.x; }
 };
 
+constexpr int kGroup = 16;       // blocks per group of the grouped row sums
+constexpr int kMaxGroups = 128;  // groups per launch (2048 blocks)
+
 // Device control block of the stepped path (one per instance).
 struct StepCtl {
   double t, thr, e0;         // line search: multiplier, Armijo threshold, energy at x
@@ -56,16 +62,32 @@ struct StepCtl {
   int k, exhausted;          // trials so far; the policy's "line search exhausted"
   int iters, slice;          // iterations in this launch, at most `slice`
   int mt;                    // pairs used by this iteration's direction
+  int gmode;                 // two-trial graph: the next trial pass is the gradient at t only
   float fg;                  // -gamma
   float coefS[MINIM_MAXM], coefY[MINIM_MAXM];
   int so[MINIM_MAXM], yo[MINIM_MAXM];  // slot buffers: float4 offsets from the ring bases
   // stencil kernels' span (first block's start, last block's end), split
   // into the gap before, the kernel and the controller work after;
-  // [0] trials, [1] gradient
+  // [0] trials, [1] gradient, [2] direction pass A, [3] direction pass B
   unsigned long long ks, ke;
   unsigned kdone;
-  double gap_pre[2], kdur[2], gap_post[2];
+  unsigned gdone[kMaxGroups];  // grouped row sums: blocks of each group done
+  double gap_pre[4], kdur[4], gap_post[4];
+  double work[4];         // the controllers' scalar work (span_end to phase_mark)
+  unsigned long long tw;  // start of the current controller's scalar work
+  int cur;                // its span slot
+  unsigned acc_hist[11];  // iterations by the trial accepted (10: none)
 };
+
+// adds the last phase kernel's span to slot j of the span records
+__device__ __forceinline__ void span_end(StepCtl* ctl, int j) {
+  const unsigned long long now = globaltimer_ns();
+  ctl->gap_pre[j] += (double)(ctl->ks - ctl->tmark);
+  ctl->kdur[j] += (double)(ctl->ke - ctl->ks);
+  ctl->gap_post[j] += (double)(now - ctl->ke);
+  ctl->tw = now;
+  ctl->cur = j;
+}
 
 // span bookkeeping of a stencil kernel (first block in, last block out)
 __device__ __forceinline__ void span_begin(StepCtl* ctl) {
@@ -90,13 +112,50 @@ __device__ __forceinline__ bool last_block(StepCtl* ctl) {
   return is_last != 0;
 }
 
+// Two-level form of last_block for wide rows: the last block of each group
+// of kGroup blocks sums the group's rows in order into row `group` of part2;
+// the block that completes the last group returns true, with the totals to
+// be summed from the ngroups rows of part2 (the final sum reads ngroups rows
+// instead of one per block, which is what makes a single block's sum of
+// many wide rows slow).
+__device__ inline bool last_block_grouped(StepCtl* ctl, const double* part, double* part2, int K,
+                                          double* wide, double* rowbuf) {
+  __shared__ int flag;
+  const int nb = gridDim.x, g = blockIdx.x / kGroup, g0 = g * kGroup;
+  const int members = min(kGroup, nb - g0), ngroups = (nb + kGroup - 1) / kGroup;
+  __syncthreads();
+  if (threadIdx.x == 0 && threadIdx.y == 0) {
+    __threadfence();
+    flag = atomicAdd(&ctl->gdone[g], 1u) == (unsigned)(members - 1);
+    if (flag) ctl->gdone[g] = 0;
+  }
+  __syncthreads();
+  if (!flag) return false;
+  sum_rows_fixed(part + (size_t)g0 * MINIM_WIDE, members, K, rowbuf, wide);
+  __syncthreads();
+  const int tl = threadIdx.y * blockDim.x + threadIdx.x;
+  for (int k = tl; k < K; k += blockDim.x * blockDim.y) part2[(size_t)g * MINIM_WIDE + k] = rowbuf[k];
+  __syncthreads();
+  if (threadIdx.x == 0 && threadIdx.y == 0) {
+    __threadfence();
+    flag = atomicAdd(&ctl->kdone, 1u) == (unsigned)(ngroups - 1);
+    if (flag) {
+      ctl->ke = globaltimer_ns();
+      ctl->kdone = 0;
+      __threadfence();
+    }
+  }
+  __syncthreads();
+  return flag != 0;
+}
+
 constexpr int kThreads = 256;
 
 // One row of K <= 4 block sums (deterministic: warp butterflies, then warps
 // in order).
 template <int K>
 __device__ void block_row(double (&v)[K], double* row) {
-  __shared__ double red[kThreads / 32][4];
+  __shared__ double red[kThreads / 32][K < 4 ? 4 : K];
   // linear thread index (blocks may be 2-D); the block has whole warps
   const int tl = threadIdx.y * blockDim.x + threadIdx.x;
   const int lane = tl & 31, w = tl >> 5, nw = (blockDim.x * blockDim.y) >> 5;
@@ -113,6 +172,32 @@ __device__ void block_row(double (&v)[K], double* row) {
   }
 }
 
+// The controllers' thread 0 walks the state record, the control block and
+// the descriptor with dependent loads; fetching one word of each of their
+// 128-byte lines from the whole block first (while the partial rows are
+// summed) brings them into L1, so each of those loads is an L1 hit instead of
+// an L2 round trip.  Returns a value that the caller stores to shared memory
+// (so that the loads have completed before thread 0 starts).
+__device__ __forceinline__ unsigned warm_lines(const void* p, int bytes) {
+  const int tl = threadIdx.y * blockDim.x + threadIdx.x, nt = blockDim.x * blockDim.y;
+  const char* c = static_cast<const char*>(p);
+  unsigned v = 0;
+  for (int o = tl * 128; o < bytes; o += nt * 128) {
+    unsigned w;
+    asm volatile("ld.global.ca.u32 %0, [%1];" : "=r"(w) : "l"(c + o));
+    v += w;
+  }
+  return v;
+}
+__device__ __forceinline__ unsigned warm_ctl(const InstDesc* d, const MinScalars* st, const StepCtl* ctl) {
+  return warm_lines(st, (int)sizeof(MinScalars)) + warm_lines(ctl, (int)sizeof(StepCtl)) +
+         warm_lines(d, (int)sizeof(InstDesc));
+}
+__device__ __forceinline__ void warm_done(unsigned w) {
+  __shared__ unsigned sink[32];
+  sink[threadIdx.x & 31] = w;
+}
+
 // controllers, run by the last block of each phase kernel (defined below)
 __device__ void ctl_a(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, const double* part, int nb);
 __device__ void ctl_b(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, const double* part, int nb,
@@ -124,6 +209,9 @@ __device__ void ctl_g(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* c
 __device__ void ctl_lsg(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, const double* part,
                         int nb, cudaGraphConditionalHandle ls, cudaGraphConditionalHandle grad,
                         cudaGraphConditionalHandle outer);
+__device__ void ctl_lsg2(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, const double* part,
+                         int nb, cudaGraphConditionalHandle ls, cudaGraphConditionalHandle grad,
+                         cudaGraphConditionalHandle outer);
 
 // ---- vector and stencil kernels -------------------------------------------------
 
@@ -137,6 +225,7 @@ __device__ void ctl_lsg(const InstDesc* __restrict__ d, MinScalars* st, StepCtl*
 template <int M>
 __global__ void __launch_bounds__(kThreads, 4)
 k_dir_a(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, double* part) {
+  span_begin(ctl);
   constexpr int NG = (M + 7) / 8;
   constexpr int GS = (M + NG - 1) / NG;  // pairs per part
   __shared__ double wide[8 * MINIM_WIDE];
@@ -225,7 +314,12 @@ k_dir_a(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, double* pa
     for (int w = 0; w < (int)(blockDim.x >> 5); w++) sum += wide[w * MINIM_WIDE + k];
     part[(size_t)blockIdx.x * MINIM_WIDE + k] = sum;
   }
-  if (last_block(ctl)) ctl_a(d, st, ctl, part, gridDim.x);
+  {
+    __shared__ double rowbuf[MINIM_WIDE];
+    double* part2 = part + (size_t)gridDim.x * MINIM_WIDE;
+    if (last_block_grouped(ctl, part, part2, MINIM_WIDE, wide, rowbuf))
+      ctl_a(d, st, ctl, part2, (gridDim.x + kGroup - 1) / kGroup);
+  }
 }
 
 // P = -gamma g - S w + gamma Y u with g.P and P.P (M compile-time, unused
@@ -234,6 +328,7 @@ template <int M>
 __global__ void __launch_bounds__(kThreads, 4)
 k_dir_b(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, double* part, cudaGraphConditionalHandle ls,
         cudaGraphConditionalHandle grad, int spec) {
+  span_begin(ctl);
   const int n = d->ndof, nq4 = n >> 2, mt = ctl->mt;
   const float* G = d->G[st->gi];
   float* P = d->Sb + (long long)st->pbuf * d->hstride;
@@ -335,14 +430,74 @@ k_grad(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, double* par
 // division; a quad's four cells are evaluated from 16-byte loads of the quad
 // and of its four neighbour lines plus two scalars at the z ends.  The trial
 // energy is summed per quad in FP32 and per thread with compensation; the
-// gradient variant also writes the point, g and y = g - g_old.
+// gradient variants also write the point, g and y = g - g_old.
 // MODE 0: trial energy; 1: gradient at the accepted point; 2: trial energy
-// with the gradient at the trial point (kept when the trial is accepted)
-template <int MODE>
-__global__ void __launch_bounds__(kThreads, MODE ? 3 : 4)
+// with the gradient at the trial point (kept when the trial is accepted);
+// 3: as 2 for two trials in one pass, at t and at t/2 (the next trial of the
+// backtracking sequence), the second written to the spare buffers.
+
+// x, P of a quad, its two z-end cells and its four neighbour lines
+struct QuadLoads {
+  float4 xc, pc, xym, pym, xyp, pyp, xxm, pxm, xxp, pxp;
+  float xzm, pzm, xzp, pzp;
+};
+struct LineCoef {
+  float fb, Fi, pr, V;
+  bool dx_on, dy_on;
+};
+
+// energy of the quad at x + t P (returned) and, with want_g, its gradient;
+// c4 receives the quad's point
+__device__ __forceinline__ float quad_eval(const QuadLoads& L, float t, const LineCoef& K, bool want_g, float4& c4,
+                                           float4& g4) {
+  auto tr = [t](float4 a, float4 b) {
+    return make_float4(__fadd_rn(a.x, __fmul_rn(t, b.x)), __fadd_rn(a.y, __fmul_rn(t, b.y)),
+                       __fadd_rn(a.z, __fmul_rn(t, b.z)), __fadd_rn(a.w, __fmul_rn(t, b.w)));
+  };
+  c4 = tr(L.xc, L.pc);
+  const float cc[4] = {c4.x, c4.y, c4.z, c4.w};
+  const float zm = __fadd_rn(L.xzm, __fmul_rn(t, L.pzm)), zp = __fadd_rn(L.xzp, __fmul_rn(t, L.pzp));
+  const float4 ym = tr(L.xym, L.pym), yp = tr(L.xyp, L.pyp), xm = tr(L.xxm, L.pxm), xp = tr(L.xxp, L.pxp);
+  const float ymv[4] = {ym.x, ym.y, ym.z, ym.w}, ypv[4] = {yp.x, yp.y, yp.z, yp.w};
+  const float xmv[4] = {xm.x, xm.y, xm.z, xm.w}, xpv[4] = {xp.x, xp.y, xp.z, xp.w};
+  float es = 0.f, g[4];
+#pragma unroll
+  for (int j = 0; j < 4; j++) {
+    const float c = cc[j];
+    const float cm = j == 0 ? zm : cc[j - 1], cp = j == 3 ? zp : cc[j + 1];
+    float gm = c - cm, gp = c - cp;
+    float lap = gm + gp, eg = 0.5f * (gm * gm + gp * gp);
+    if (K.dy_on) {
+      gm = c - ymv[j];
+      gp = c - ypv[j];
+      lap += gm + gp;
+      eg += 0.5f * (gm * gm + gp * gp);
+    }
+    if (K.dx_on) {
+      gm = c - xmv[j];
+      gp = c - xpv[j];
+      lap += gm + gp;
+      eg += 0.5f * (gm * gm + gp * gp);
+    }
+    const float a = (c + 1) * (c - 1);
+    es += K.fb * a * a + K.Fi * eg;
+    if (K.pr != 0.f) es -= K.pr * (0.5f * (c + 1) * K.V);
+    g[j] = 0.f;
+    if (want_g) {
+      g[j] = K.fb * 4 * c * (c * c - 1) + 2 * K.Fi * lap;
+      if (K.pr != 0.f) g[j] -= 0.5f * K.pr * K.V;
+    }
+  }
+  g4 = make_float4(g[0], g[1], g[2], g[3]);
+  return es;
+}
+
+template <int MODE, int MINB = (MODE == 3 ? 2 : (MODE ? 3 : 4))>
+__global__ void __launch_bounds__(kThreads, MINB)
 k_lines(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, double* part, cudaGraphConditionalHandle ls,
         cudaGraphConditionalHandle grad, cudaGraphConditionalHandle outer) {
   constexpr bool WANT_G = MODE != 0;
+  constexpr bool DUAL = MODE == 3;
   span_begin(ctl);
   const PotPF& Pf = d->pf;
   const int nx = Pf.n[0], ny = Pf.n[1], nz = Pf.n[2], nz4 = nz >> 2;
@@ -350,15 +505,26 @@ k_lines(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, double* pa
   const float* X = d->X32[xi];
   const float* Pd = d->Sb + (long long)st->pbuf * d->hstride;
   const float t = (float)ctl->t;
-  const float V = (float)Pf.vol_of_type[1];
-  const float fb = (float)Pf.kappa[0] / 16 * V;
-  const float Fi = 0.25f / (float)Pf.res2 * (float)Pf.kappaP[0] * V;
-  const float pr = (Pf.flags & PF_PRESSURE) ? (float)Pf.pressure[0] : 0.f;
-  const bool dx_on = nx > 1, dy_on = ny > 1;
+  LineCoef K;
+  K.V = (float)Pf.vol_of_type[1];
+  K.fb = (float)Pf.kappa[0] / 16 * K.V;
+  K.Fi = 0.25f / (float)Pf.res2 * (float)Pf.kappaP[0] * K.V;
+  K.pr = (Pf.flags & PF_PRESSURE) ? (float)Pf.pressure[0] : 0.f;
+  K.dx_on = nx > 1;
+  K.dy_on = ny > 1;
   const int zq = threadIdx.x, nl = nx * ny;
   const int z0 = 4 * zq;
   const int izm = z0 == 0 ? nz - 1 : z0 - 1, izp = z0 + 4 == nz ? 0 : z0 + 4;
-  Acc e, gg, py, yy;
+  float* Xa = d->X32[1 - xi];
+  float* Ga = d->G[1 - gi];
+  float* Ya = d->Yb + (long long)st->ybuf * d->hstride;
+  // two-trial pass, or (gmode) the gradient at t alone
+  const bool two = DUAL && ctl->gmode == 0;
+  float* Xb = DUAL ? d->X32s : nullptr;
+  float* Gb = DUAL ? d->Gs : nullptr;
+  float* Yb2 = DUAL ? d->Yb + (long long)st->ybuf2 * d->hstride : nullptr;
+  const float* Go = d->G[gi];
+  Acc e, gg, py, yy, e2, gg2, py2, yy2;
   if (zq < nz4) {
     for (int l = blockIdx.x * blockDim.y + threadIdx.y; l < nl; l += gridDim.x * blockDim.y) {
       const int x = l / ny, y = l - x * ny;
@@ -366,66 +532,50 @@ k_lines(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, double* pa
       const int lxm = (x == 0 ? nx - 1 : x - 1) * ny + y, lxp = (x == nx - 1 ? 0 : x + 1) * ny + y;
       const int q = l * nz4 + zq;
       // every load of the quad first
-      const float4 xc = ld4(X, q), pc = ld4(Pd, q);
-      const float xzm = X[l * nz + izm], pzm = Pd[l * nz + izm];
-      const float xzp = X[l * nz + izp], pzp = Pd[l * nz + izp];
-      const float4 xym = ld4(X, lym * nz4 + zq), pym = ld4(Pd, lym * nz4 + zq);
-      const float4 xyp = ld4(X, lyp * nz4 + zq), pyp = ld4(Pd, lyp * nz4 + zq);
-      const float4 xxm = ld4(X, lxm * nz4 + zq), pxm = ld4(Pd, lxm * nz4 + zq);
-      const float4 xxp = ld4(X, lxp * nz4 + zq), pxp = ld4(Pd, lxp * nz4 + zq);
+      QuadLoads L;
+      L.xc = ld4(X, q);
+      L.pc = ld4(Pd, q);
+      L.xzm = X[l * nz + izm];
+      L.pzm = Pd[l * nz + izm];
+      L.xzp = X[l * nz + izp];
+      L.pzp = Pd[l * nz + izp];
+      L.xym = ld4(X, lym * nz4 + zq);
+      L.pym = ld4(Pd, lym * nz4 + zq);
+      L.xyp = ld4(X, lyp * nz4 + zq);
+      L.pyp = ld4(Pd, lyp * nz4 + zq);
+      L.xxm = ld4(X, lxm * nz4 + zq);
+      L.pxm = ld4(Pd, lxm * nz4 + zq);
+      L.xxp = ld4(X, lxp * nz4 + zq);
+      L.pxp = ld4(Pd, lxp * nz4 + zq);
       float4 go = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (WANT_G) go = ld4(d->G[gi], q);
-      auto tr = [t](float4 a, float4 b) {
-        return make_float4(__fadd_rn(a.x, __fmul_rn(t, b.x)), __fadd_rn(a.y, __fmul_rn(t, b.y)),
-                           __fadd_rn(a.z, __fmul_rn(t, b.z)), __fadd_rn(a.w, __fmul_rn(t, b.w)));
-      };
-      const float4 c4 = tr(xc, pc);
-      const float cc[4] = {c4.x, c4.y, c4.z, c4.w};
-      const float zm = __fadd_rn(xzm, __fmul_rn(t, pzm)), zp = __fadd_rn(xzp, __fmul_rn(t, pzp));
-      const float4 ym = tr(xym, pym), yp = tr(xyp, pyp), xm = tr(xxm, pxm), xp = tr(xxp, pxp);
-      const float ymv[4] = {ym.x, ym.y, ym.z, ym.w}, ypv[4] = {yp.x, yp.y, yp.z, yp.w};
-      const float xmv[4] = {xm.x, xm.y, xm.z, xm.w}, xpv[4] = {xp.x, xp.y, xp.z, xp.w};
-      float es = 0.f, g[4];
-#pragma unroll
-      for (int j = 0; j < 4; j++) {
-        const float c = cc[j];
-        const float cm = j == 0 ? zm : cc[j - 1], cp = j == 3 ? zp : cc[j + 1];
-        float gm = c - cm, gp = c - cp;
-        float lap = gm + gp, eg = 0.5f * (gm * gm + gp * gp);
-        if (dy_on) {
-          gm = c - ymv[j];
-          gp = c - ypv[j];
-          lap += gm + gp;
-          eg += 0.5f * (gm * gm + gp * gp);
-        }
-        if (dx_on) {
-          gm = c - xmv[j];
-          gp = c - xpv[j];
-          lap += gm + gp;
-          eg += 0.5f * (gm * gm + gp * gp);
-        }
-        const float a = (c + 1) * (c - 1);
-        es += fb * a * a + Fi * eg;
-        if (pr != 0.f) es -= pr * (0.5f * (c + 1) * V);
-        if (WANT_G) {
-          g[j] = fb * 4 * c * (c * c - 1) + 2 * Fi * lap;
-          if (pr != 0.f) g[j] -= 0.5f * pr * V;
-        }
-      }
-      e.add(es);
+      if (WANT_G) go = ld4(Go, q);
+      float4 c4, gv;
+      e.add(quad_eval(L, t, K, WANT_G, c4, gv));
       if (WANT_G) {
-        const float4 gv = make_float4(g[0], g[1], g[2], g[3]);
-        st4(d->X32[1 - xi], q, c4);
-        st4(d->G[1 - gi], q, gv);
+        st4(Xa, q, c4);
+        st4(Ga, q, gv);
         gg.add(dot4(gv, gv));
-        const float4 yv = make_float4(g[0] - go.x, g[1] - go.y, g[2] - go.z, g[3] - go.w);
-        st4(d->Yb + (long long)st->ybuf * d->hstride, q, yv);
-        py.add(dot4(pc, yv));
+        const float4 yv = make_float4(gv.x - go.x, gv.y - go.y, gv.z - go.z, gv.w - go.w);
+        st4(Ya, q, yv);
+        py.add(dot4(L.pc, yv));
         yy.add(dot4(yv, yv));
+      }
+      if (DUAL && two) {
+        e2.add(quad_eval(L, 0.5f * t, K, true, c4, gv));
+        st4(Xb, q, c4);
+        st4(Gb, q, gv);
+        gg2.add(dot4(gv, gv));
+        const float4 yv = make_float4(gv.x - go.x, gv.y - go.y, gv.z - go.z, gv.w - go.w);
+        st4(Yb2, q, yv);
+        py2.add(dot4(L.pc, yv));
+        yy2.add(dot4(yv, yv));
       }
     }
   }
-  if (WANT_G) {
+  if (DUAL) {
+    double v[8] = {e.total(), gg.total(), py.total(), yy.total(), e2.total(), gg2.total(), py2.total(), yy2.total()};
+    block_row<8>(v, part + (size_t)blockIdx.x * MINIM_WIDE);
+  } else if (WANT_G) {
     double v[4] = {e.total(), gg.total(), py.total(), yy.total()};
     block_row<4>(v, part + (size_t)blockIdx.x * MINIM_WIDE);
   } else {
@@ -435,7 +585,8 @@ k_lines(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, double* pa
   if (last_block(ctl)) {
     if (MODE == 0) ctl_ls(d, st, ctl, part, gridDim.x, ls);
     else if (MODE == 1) ctl_g(d, st, ctl, part, gridDim.x, outer);
-    else ctl_lsg(d, st, ctl, part, gridDim.x, ls, grad, outer);
+    else if (MODE == 2) ctl_lsg(d, st, ctl, part, gridDim.x, ls, grad, outer);
+    else ctl_lsg2(d, st, ctl, part, gridDim.x, ls, grad, outer);
   }
 }
 
@@ -460,59 +611,77 @@ __global__ void k_begin(const InstDesc* __restrict__ d, const MinScalars* __rest
 __device__ __forceinline__ void phase_time(MinScalars* st, StepCtl* ctl, int ph) {
   st->tphase[ph] += (double)(globaltimer_ns() - ctl->tmark);
 }
-__device__ __forceinline__ void phase_mark(StepCtl* ctl) { ctl->tmark = globaltimer_ns(); }
+__device__ __forceinline__ void phase_mark(StepCtl* ctl) {
+  const unsigned long long now = globaltimer_ns();
+  ctl->work[ctl->cur] += (double)(now - ctl->tw);
+  ctl->tmark = now;
+}
 
 // dirA sums, the compact-form algebra of getDirection, pass-B coefficients
 __device__ void ctl_a(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, const double* part, int nb) {
   __shared__ double wide[8 * MINIM_WIDE];
   __shared__ double wout[MINIM_WIDE];
+  const unsigned warm = warm_ctl(d, st, ctl);
   sum_rows_fixed(part, nb, MINIM_WIDE, wout, wide);
+  warm_done(warm);
   __syncthreads();
-  if (threadIdx.x != 0 || threadIdx.y != 0) return;
-  phase_time(st, ctl, 2);
+  // warp 0: the algebra (lbfgs_compact_warp), lane k on pair k
+  const int lane = threadIdx.y * blockDim.x + threadIdx.x;
+  if (lane >= 32) return;
+  if (lane == 0) {
+    phase_time(st, ctl, 2);
+    span_end(ctl, 2);
+  }
   const int m = d->mp.m, n = d->ndof;
   const long long hs = d->hstride;
   const int ii = st->ii + 1, mt = ii < m ? ii : m, c = ii % m, kn = (c - 1 + m) % m;
   const int pend = st->pend;
   double(*SY)[MINIM_MAXM] = st->SY;
   double(*YY)[MINIM_MAXM] = st->YY;
-  double sg[MINIM_MAXM], yg[MINIM_MAXM], u[MINIM_MAXM], w[MINIM_MAXM];
-  int sl[MINIM_MAXM];
-  for (int k = 0; k < mt; k++) {
-    sl[k] = (c - mt + k + 2 * m) % m;
-    sg[k] = st->sigma[sl[k]] * wout[k];
-    yg[k] = wout[MINIM_MAXM + k];
-  }
-  if (pend >= 0)
-    for (int k = 0; k < mt; k++) {
-      SY[sl[k]][pend] = st->sigma[sl[k]] * wout[2 * MINIM_MAXM + k];
-      YY[sl[k]][pend] = wout[3 * MINIM_MAXM + k];
-      YY[pend][sl[k]] = wout[3 * MINIM_MAXM + k];
+  const bool on = lane < mt;
+  const int slk = on ? ring_slot(c, mt, lane, m) : 0;
+  double sg = 0.0, yg = 0.0;
+  if (on) {
+    sg = st->sigma[slk] * wout[lane];
+    yg = wout[MINIM_MAXM + lane];
+    if (pend >= 0) {
+      SY[slk][pend] = st->sigma[slk] * wout[2 * MINIM_MAXM + lane];
+      YY[slk][pend] = wout[3 * MINIM_MAXM + lane];
+      YY[pend][slk] = wout[3 * MINIM_MAXM + lane];
     }
+  }
+  __threadfence_block();
+  __syncwarp();
+  // the mt x mt blocks of S^T Y and Y^T Y in age order, staged in shared memory
+  double* Rs = wide;
+  double* Ys = wide + MINIM_MAXM * MINIM_MAXM;
+  for (int e = lane; e < mt * mt; e += 32) {
+    const int a = e / mt, b = e - a * mt;
+    const int sa = ring_slot(c, mt, a, m), sb = ring_slot(c, mt, b, m);
+    Rs[a * MINIM_MAXM + b] = SY[sa][sb];
+    Ys[a * MINIM_MAXM + b] = YY[sa][sb];
+  }
+  __syncwarp();
   const double gamma = SY[kn][kn] / YY[kn][kn];
-  for (int a = mt - 1; a >= 0; a--) {  // R u = S^T g
-    double t = sg[a];
-    for (int b = a + 1; b < mt; b++) t -= SY[sl[a]][sl[b]] * u[b];
-    u[a] = t / SY[sl[a]][sl[a]];
+  double u, w;
+  lbfgs_compact_warp(
+      mt, gamma, sg, yg, [=](int a, int b) { return Rs[a * MINIM_MAXM + b]; },
+      [=](int a, int b) { return Ys[a * MINIM_MAXM + b]; }, u, w);
+  if (lane < MINIM_MAXM) {
+    ctl->coefS[lane] = on ? (float)(-w * st->sigma[slk]) : 0.f;
+    ctl->coefY[lane] = on ? (float)(gamma * u) : 0.f;
+    ctl->so[lane] = on ? (int)(((long long)st->sidx[slk] * hs) >> 2) : 0;
+    ctl->yo[lane] = on ? (int)(((long long)st->yidx[slk] * hs) >> 2) : 0;
   }
-  for (int a = 0; a < mt; a++) {  // R^T w = (D + gamma Y^T Y) u - gamma Y^T g
-    double t = SY[sl[a]][sl[a]] * u[a] - gamma * yg[a];
-    for (int b = 0; b < mt; b++) t += gamma * YY[sl[a]][sl[b]] * u[b];
-    for (int b = 0; b < a; b++) t -= SY[sl[b]][sl[a]] * w[b];
-    w[a] = t / SY[sl[a]][sl[a]];
+  __syncwarp();
+  if (lane == 0) {
+    ctl->fg = (float)(-gamma);
+    ctl->mt = mt;
+    st->ii = ii;
+    st->pend = -1;
+    st->abytes += (4.0 * mt + 2.0) * 4.0 * n;
+    phase_mark(ctl);
   }
-  for (int k = 0; k < MINIM_MAXM; k++) {
-    ctl->coefS[k] = (k < mt) ? (float)(-w[k] * st->sigma[sl[k]]) : 0.f;
-    ctl->coefY[k] = (k < mt) ? (float)(gamma * u[k]) : 0.f;
-    ctl->so[k] = (k < mt) ? (int)(((long long)st->sidx[sl[k]] * hs) >> 2) : 0;
-    ctl->yo[k] = (k < mt) ? (int)(((long long)st->yidx[sl[k]] * hs) >> 2) : 0;
-  }
-  ctl->fg = (float)(-gamma);
-  ctl->mt = mt;
-  st->ii = ii;
-  st->pend = -1;
-  st->abytes += (4.0 * mt + 2.0) * 4.0 * n;
-  phase_mark(ctl);
 }
 
 // dirB sums: step cap, descent check, line-search set-up
@@ -520,10 +689,13 @@ __device__ void ctl_b(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* c
                       cudaGraphConditionalHandle ls, cudaGraphConditionalHandle grad, int spec) {
   __shared__ double wide[8 * MINIM_WIDE];
   __shared__ double v[2];
+  const unsigned warm = warm_ctl(d, st, ctl);
   sum_rows_fixed(part, nb, 2, v, wide);
+  warm_done(warm);
   __syncthreads();
   if (threadIdx.x != 0 || threadIdx.y != 0) return;
   phase_time(st, ctl, 2);
+  span_end(ctl, 3);
   double gp = v[0], scale = 1.0;
   if (d->mp.max_step != 0) {
     const double ss = sqrt(v[1]);
@@ -536,7 +708,19 @@ __device__ void ctl_b(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* c
     scale = -scale;
   }
   ctl->t = scale;
-  if (d->mp.linesearch == 0) {
+  if (spec == 2) {
+    // two-trial graph: the first trial pass follows unconditionally; without
+    // a line search it is the gradient at the full step
+    ctl->gmode = d->mp.linesearch == 0 ? 0 : 1;
+    if (d->mp.linesearch == 0) {
+      ctl->thr = -0.5 * gs;
+      ctl->e0 = st->E;
+      ctl->k = 0;
+      ctl->exhausted = 1;
+    } else {
+      ctl->exhausted = 0;
+    }
+  } else if (d->mp.linesearch == 0) {
     ctl->thr = -0.5 * gs;
     ctl->e0 = st->E;
     ctl->k = 0;
@@ -557,16 +741,13 @@ __device__ void ctl_ls(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* 
          cudaGraphConditionalHandle ls) {
   __shared__ double wide[8 * MINIM_WIDE];
   __shared__ double v[1];
+  const unsigned warm = warm_ctl(d, st, ctl);
   sum_rows_fixed(part, nb, 1, v, wide);
+  warm_done(warm);
   __syncthreads();
   if (threadIdx.x != 0 || threadIdx.y != 0) return;
   phase_time(st, ctl, 1);
-  {
-    const unsigned long long now = globaltimer_ns();
-    ctl->gap_pre[0] += (double)(ctl->ks - ctl->tmark);
-    ctl->kdur[0] += (double)(ctl->ke - ctl->ks);
-    ctl->gap_post[0] += (double)(now - ctl->ke);
-  }
+  span_end(ctl, 0);
   st->evals++;
   st->abytes += 8.0 * d->ndof;
   ctl->kernels += 1;
@@ -659,16 +840,13 @@ __device__ void ctl_g(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* c
         cudaGraphConditionalHandle outer) {
   __shared__ double wide[8 * MINIM_WIDE];
   __shared__ double v[4];
+  const unsigned warm = warm_ctl(d, st, ctl);
   sum_rows_fixed(part, nb, 4, v, wide);
+  warm_done(warm);
   __syncthreads();
   if (threadIdx.x != 0 || threadIdx.y != 0) return;
   phase_time(st, ctl, 0);
-  {
-    const unsigned long long now = globaltimer_ns();
-    ctl->gap_pre[1] += (double)(ctl->ks - ctl->tmark);
-    ctl->kdur[1] += (double)(ctl->ke - ctl->ks);
-    ctl->gap_post[1] += (double)(now - ctl->ke);
-  }
+  span_end(ctl, 1);
   st->evals++;
   st->abytes += 24.0 * d->ndof;
   ctl->kernels += 3;
@@ -685,20 +863,18 @@ __device__ void ctl_lsg(const InstDesc* __restrict__ d, MinScalars* st, StepCtl*
                         cudaGraphConditionalHandle outer) {
   __shared__ double wide[8 * MINIM_WIDE];
   __shared__ double v[4];
+  const unsigned warm = warm_ctl(d, st, ctl);
   sum_rows_fixed(part, nb, 4, v, wide);
+  warm_done(warm);
   __syncthreads();
   if (threadIdx.x != 0 || threadIdx.y != 0) return;
   phase_time(st, ctl, 1);
-  {
-    const unsigned long long now = globaltimer_ns();
-    ctl->gap_pre[0] += (double)(ctl->ks - ctl->tmark);
-    ctl->kdur[0] += (double)(ctl->ke - ctl->ks);
-    ctl->gap_post[0] += (double)(now - ctl->ke);
-  }
+  span_end(ctl, 0);
   st->evals++;
   ctl->kernels += 1;
   if (ctl->e0 - v[0] >= ctl->thr) {
     ctl->exhausted = ctl->k >= 8;
+    ctl->acc_hist[ctl->k]++;
     cudaGraphSetConditional(ls, 0u);
     cudaGraphSetConditional(grad, 0u);
     st->evals++;
@@ -711,10 +887,77 @@ __device__ void ctl_lsg(const InstDesc* __restrict__ d, MinScalars* st, StepCtl*
     ctl->thr *= 0.5;
     ctl->k++;
     const bool more = ctl->k < 10;
+    if (!more) ctl->acc_hist[10]++;
     cudaGraphSetConditional(ls, more ? 1u : 0u);
     cudaGraphSetConditional(grad, more ? 0u : 1u);
     phase_mark(ctl);
   }
+}
+
+// Two consecutive trials of the backtracking sequence from one pass (t and
+// t / 2, each with its gradient): the Armijo test of the first, then, if it
+// failed, of the second, as the sequential line search takes them.  When the
+// second is accepted its point, gradient and y (written to the spare
+// buffers) become the next ones by exchanging buffer pointers and slots.
+// After the tenth failed trial (or without a line search) the next pass is
+// the gradient at the step alone (gmode), which completes the iteration.
+__device__ void ctl_lsg2(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, const double* part,
+                         int nb, cudaGraphConditionalHandle ls, cudaGraphConditionalHandle grad,
+                         cudaGraphConditionalHandle outer) {
+  __shared__ double wide[8 * MINIM_WIDE];
+  __shared__ double v[8];
+  const unsigned warm = warm_ctl(d, st, ctl);
+  sum_rows_fixed(part, nb, 8, v, wide);
+  warm_done(warm);
+  __syncthreads();
+  if (threadIdx.x != 0 || threadIdx.y != 0) return;
+  phase_time(st, ctl, 1);
+  span_end(ctl, 0);
+  ctl->kernels += 1;
+  const double n = (double)d->ndof;
+  if (ctl->gmode) {
+    ctl->gmode = 0;
+    st->evals++;
+    st->abytes += 24.0 * n;
+    cudaGraphSetConditional(ls, 0u);
+    commit_grad(d, st, ctl, v, outer);
+    return;
+  }
+  for (int j = 0; j < 2; j++) {
+    st->evals++;
+    if (ctl->e0 - v[4 * j] >= ctl->thr) {
+      ctl->exhausted = ctl->k >= 8;
+      ctl->acc_hist[ctl->k]++;
+      if (j == 1) {
+        InstDesc* dw = const_cast<InstDesc*>(d);
+        float* tx = dw->X32[1 - st->xi];
+        dw->X32[1 - st->xi] = dw->X32s;
+        dw->X32s = tx;
+        float* tg = dw->G[1 - st->gi];
+        dw->G[1 - st->gi] = dw->Gs;
+        dw->Gs = tg;
+        const int ty = st->ybuf;
+        st->ybuf = st->ybuf2;
+        st->ybuf2 = ty;
+      }
+      cudaGraphSetConditional(ls, 0u);
+      st->evals++;
+      st->abytes += 24.0 * n;
+      commit_grad(d, st, ctl, v + 4 * j, outer);
+      return;
+    }
+    st->abytes += 8.0 * n;
+    ctl->t *= 0.5;
+    ctl->thr *= 0.5;
+    ctl->k++;
+    if (ctl->k >= 10) break;
+  }
+  if (ctl->k >= 10) {
+    ctl->acc_hist[10]++;
+    ctl->gmode = 1;
+  }
+  cudaGraphSetConditional(ls, 1u);
+  phase_mark(ctl);
 }
 
 int occupancy(const void* f, int threads) {
@@ -725,14 +968,22 @@ int occupancy(const void* f, int threads) {
 
 }  // namespace
 
-// One instance's stepped graph.
+// A stepped graph and the records its kernels run on.  Graphs are kept per
+// process, one per shape (grid, history length, SM count, iterations per
+// launch, trials per pass): a launch copies the instance's descriptor and
+// state record into the graph's own copies and back afterwards, so a new
+// instance of a shape seen before reuses the graph built for it
+// (instantiating a graph with conditional nodes costs far more than the two
+// small copies).
 struct SteppedGraph {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   StepCtl* ctl = nullptr;
   double* part = nullptr;
-  const MinScalars* st = nullptr;
-  int slice = 0, m = 0;
+  InstDesc* d = nullptr;     // the graph's copy of the descriptor
+  MinScalars* st = nullptr;  // the graph's copy of the state record
+  int n[3] = {0, 0, 0};
+  int m = 0, nsm = 0, slice = 0, dual = 0, spec = 0;
 };
 
 }  // namespace mg
@@ -795,8 +1046,7 @@ bool dir_kernels(int m, const void** a, const void** b) {
   }
 }
 
-int build(SteppedGraph* sg, const InstDesc* d, MinScalars* st, int m, const int* grid, int nsm, int slice,
-          cudaStream_t s) {
+int build(SteppedGraph* sg, int m, const int* grid, int nsm, int slice, int dual, int spec, cudaStream_t s) {
   const void* fa = nullptr;
   const void* fb = nullptr;
   if (!dir_kernels(m, &fa, &fb)) return (int)cudaErrorInvalidValue;
@@ -809,23 +1059,35 @@ int build(SteppedGraph* sg, const InstDesc* d, MinScalars* st, int m, const int*
   const bool use_lines = lines && (nz4 * by) % 32 == 0;
   const dim3 sblock = use_lines ? dim3(nz4, by) : dim3(kThreads);
   // trials that also evaluate the gradient at their point (kept when the
-  // trial is accepted) unless MINIM_GPU_SPECULATIVE=0
-  const char* env = std::getenv("MINIM_GPU_SPECULATIVE");
-  int spec = !(env && env[0] == '0');
-  const void* fe = spec ? (use_lines ? (const void*)k_lines<2> : (const void*)k_grad<true>)
+  // trial is accepted) unless MINIM_GPU_SPECULATIVE=0; two trials per pass
+  // (with the gradient-only pass folded into the same kernel) when the
+  // workspace has the spare buffers
+  const bool two = spec && use_lines && dual;
+  const int bmode = two ? 2 : spec;  // direction pass B's set-up of the trials
+  const void* fe = spec ? (use_lines ? (dual ? (const void*)k_lines<3> : (const void*)k_lines<2>)
+                                     : (const void*)k_grad<true>)
                         : (use_lines ? (const void*)k_lines<0> : (const void*)k_eonly);
   const void* fg = use_lines ? (const void*)k_lines<1> : (const void*)k_grad<false>;
   const int occ_a = occupancy(fa, kThreads), occ_b = occupancy(fb, kThreads);
   const int occ_e = occupancy(fe, (int)(sblock.x * sblock.y)), occ_g = occupancy(fg, (int)(sblock.x * sblock.y));
   if (!occ_a || !occ_b || !occ_e || !occ_g) return (int)cudaErrorInvalidConfiguration;
-  int nb_a = nsm * occ_a, nb_b = nsm * occ_b, nb_e = nsm * occ_e, nb_g = nsm * occ_g;
+  const int nb_a = nsm * occ_a, nb_b = nsm * occ_b, nb_e = nsm * occ_e, nb_g = nsm * occ_g;
   const int nb_max = std::max(std::max(nb_a, nb_b), std::max(nb_e, nb_g));
+  SCK(cudaMallocAsync((void**)&sg->d, sizeof(InstDesc), s));
+  SCK(cudaMallocAsync((void**)&sg->st, sizeof(MinScalars), s));
   SCK(cudaMallocAsync((void**)&sg->ctl, sizeof(StepCtl), s));
-  SCK(cudaMallocAsync((void**)&sg->part, (size_t)nb_max * MINIM_WIDE * sizeof(double), s));
+  if ((nb_a + kGroup - 1) / kGroup > kMaxGroups) return (int)cudaErrorInvalidConfiguration;
+  // rows of every block, then the group rows of the direction pass A
+  SCK(cudaMallocAsync((void**)&sg->part, ((size_t)nb_max + kMaxGroups) * MINIM_WIDE * sizeof(double), s));
   SCK(cudaMemsetAsync(sg->ctl, 0, sizeof(StepCtl), s));
-  sg->st = st;
-  sg->slice = slice;
+  for (int k = 0; k < 3; k++) sg->n[k] = grid[k];
   sg->m = m;
+  sg->nsm = nsm;
+  sg->slice = slice;
+  sg->dual = dual;
+  sg->spec = spec;
+  const InstDesc* d = sg->d;
+  MinScalars* st = sg->st;
   cudaGraph_t g = nullptr;
   SCK(cudaGraphCreate(&g, 0));
   sg->graph = g;
@@ -842,18 +1104,30 @@ int build(SteppedGraph* sg, const InstDesc* d, MinScalars* st, int m, const int*
   SCK(add_while(&n_outer, g, &n_begin, 1, h_outer, &body));
   SCK(cudaGraphConditionalHandleCreate(&h_ls, body, 0, 0));
   cudaGraphConditionalHandle h_grad = 0;
-  if (spec) SCK(cudaGraphConditionalHandleCreate(&h_grad, body, 0, 0));
+  if (spec && !two) SCK(cudaGraphConditionalHandleCreate(&h_grad, body, 0, 0));
   cudaGraphNode_t na, nb, nls, ngr;
   {
     void* args[] = {(void*)&d, (void*)&st, (void*)&ctl, (void*)&part};
     SCK(add_kernel(&na, body, nullptr, 0, fa, nb_a, kThreads, args));
   }
   {
-    void* args[] = {(void*)&d, (void*)&st, (void*)&ctl, (void*)&part, (void*)&h_ls, (void*)&h_grad, (void*)&spec};
+    void* args[] = {(void*)&d, (void*)&st, (void*)&ctl, (void*)&part, (void*)&h_ls, (void*)&h_grad, (void*)&bmode};
     SCK(add_kernel(&nb, body, &na, 1, fb, nb_b, kThreads, args));
   }
   void* args_s[] = {(void*)&d, (void*)&st, (void*)&ctl, (void*)&part, (void*)&h_ls, (void*)&h_grad, (void*)&h_outer};
   cudaGraph_t ls_body;
+  if (two) {
+    // dirA -> dirB -> trial pass -> WHILE(more passes) { trial pass }: the
+    // first pass follows pass B directly; a pass that accepts a trial (or is
+    // the gradient-only pass) ends the iteration
+    cudaGraphNode_t nt;
+    SCK(add_kernel(&nt, body, &nb, 1, fe, nb_e, sblock, args_s));
+    SCK(add_while(&nls, body, &nt, 1, h_ls, &ls_body));
+    cudaGraphNode_t ne;
+    SCK(add_kernel(&ne, ls_body, nullptr, 0, fe, nb_e, sblock, args_s));
+    SCK(cudaGraphInstantiate(&sg->exec, g, 0));
+    return 0;
+  }
   SCK(add_while(&nls, body, &nb, 1, h_ls, &ls_body));
   {
     cudaGraphNode_t ne;
@@ -874,46 +1148,88 @@ int build(SteppedGraph* sg, const InstDesc* d, MinScalars* st, int m, const int*
 
 }  // namespace
 
-// Runs up to `slice` FP32 L-BFGS iterations (history m) of the binary
-// PhaseField instance (device descriptor d, state st) as one graph launch on
-// stream s.  The graph is built on the first call for this state record and
-// kept in *cache.  Adds the kernels executed to *kernels.  Returns a
-// cudaError_t.
-extern "C" int mg_stepped_pf1_run(void** cache, const InstDesc* d, MinScalars* st, int m, const int* grid,
-                                  int nsm, int slice, void* stream, double* kernels) {
-  cudaStream_t s = static_cast<cudaStream_t>(stream);
-  SteppedGraph* sg = static_cast<SteppedGraph*>(*cache);
-  if (sg && (sg->st != st || sg->slice != slice || sg->m != m)) {
-    SCK(cudaStreamSynchronize(s));
-    mg_stepped_free(cache);
-    sg = nullptr;
-  }
-  if (!sg) {
-    sg = new SteppedGraph;
-    *cache = sg;
-    SCK(build(sg, d, st, m, grid, nsm, slice, s));
-  }
-  SCK(cudaGraphLaunch(sg->exec, s));
-  StepCtl c;
-  SCK(cudaMemcpyAsync(&c, sg->ctl, sizeof c, cudaMemcpyDeviceToHost, s));
-  SCK(cudaStreamSynchronize(s));
-  if (kernels) *kernels += c.kernels;
-  if (std::getenv("MINIM_GPU_STEPPED_TIMING"))  // cumulative over this instance's launches
-    std::fprintf(stderr,
-                 "stepped spans (ms): trials gap %.3f kernel %.3f gap %.3f | gradient gap %.3f kernel %.3f "
-                 "gap %.3f\n",
-                 c.gap_pre[0] * 1e-6, c.kdur[0] * 1e-6, c.gap_post[0] * 1e-6, c.gap_pre[1] * 1e-6,
-                 c.kdur[1] * 1e-6, c.gap_post[1] * 1e-6);
-  return 0;
-}
+namespace {
+std::mutex g_graphs_mu;
+std::vector<SteppedGraph*> g_graphs;  // most recently used last
+constexpr size_t kMaxGraphs = 8;
 
-extern "C" void mg_stepped_free(void** cache) {
-  SteppedGraph* sg = static_cast<SteppedGraph*>(*cache);
-  if (!sg) return;
+void free_graph(SteppedGraph* sg) {
   if (sg->exec) cudaGraphExecDestroy(sg->exec);
   if (sg->graph) cudaGraphDestroy(sg->graph);
   if (sg->ctl) cudaFree(sg->ctl);
   if (sg->part) cudaFree(sg->part);
+  if (sg->d) cudaFree(sg->d);
+  if (sg->st) cudaFree(sg->st);
   delete sg;
-  *cache = nullptr;
+}
+}  // namespace
+
+// Runs up to `slice` FP32 L-BFGS iterations (history m) of the binary
+// PhaseField instance (device descriptor d, state st) as one graph launch on
+// stream s, with the graph of this shape (built on first use).  Adds the
+// kernels executed to *kernels.  Returns a cudaError_t.
+extern "C" int mg_stepped_pf1_run(InstDesc* d, MinScalars* st, int m, const int* grid, int nsm, int slice,
+                                  int dual, void* stream, double* kernels) {
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const char* env = std::getenv("MINIM_GPU_SPECULATIVE");
+  const int spec = !(env && env[0] == '0');
+  std::lock_guard<std::mutex> lk(g_graphs_mu);
+  SteppedGraph* sg = nullptr;
+  for (size_t i = 0; i < g_graphs.size(); i++) {
+    SteppedGraph* c = g_graphs[i];
+    if (c->n[0] == grid[0] && c->n[1] == grid[1] && c->n[2] == grid[2] && c->m == m && c->nsm == nsm &&
+        c->slice == slice && c->dual == dual && c->spec == spec) {
+      sg = c;
+      g_graphs.erase(g_graphs.begin() + (long)i);
+      g_graphs.push_back(sg);
+      break;
+    }
+  }
+  if (!sg) {
+    if (g_graphs.size() >= kMaxGraphs) {
+      SCK(cudaDeviceSynchronize());
+      free_graph(g_graphs.front());
+      g_graphs.erase(g_graphs.begin());
+    }
+    sg = new SteppedGraph;
+    const int rc = build(sg, m, grid, nsm, slice, dual, spec, s);
+    if (rc) {
+      cudaStreamSynchronize(s);
+      free_graph(sg);
+      return rc;
+    }
+    g_graphs.push_back(sg);
+  }
+  const bool timing = std::getenv("MINIM_GPU_STEPPED_TIMING") != nullptr;
+  if (timing) {  // span records of this launch only
+    const size_t o = offsetof(StepCtl, gap_pre);
+    SCK(cudaMemsetAsync(reinterpret_cast<char*>(sg->ctl) + o, 0, sizeof(StepCtl) - o, s));
+  }
+  SCK(cudaMemcpyAsync(sg->d, d, sizeof(InstDesc), cudaMemcpyDeviceToDevice, s));
+  SCK(cudaMemcpyAsync(sg->st, st, sizeof(MinScalars), cudaMemcpyDeviceToDevice, s));
+  SCK(cudaGraphLaunch(sg->exec, s));
+  // the accepted trial's buffers may have been exchanged in the copy
+  SCK(cudaMemcpyAsync(d, sg->d, sizeof(InstDesc), cudaMemcpyDeviceToDevice, s));
+  SCK(cudaMemcpyAsync(st, sg->st, sizeof(MinScalars), cudaMemcpyDeviceToDevice, s));
+  StepCtl c;
+  SCK(cudaMemcpyAsync(&c, sg->ctl, sizeof c, cudaMemcpyDeviceToHost, s));
+  SCK(cudaStreamSynchronize(s));
+  if (kernels) *kernels += c.kernels;
+  if (timing) {
+    static const char* name[4] = {"trials", "gradient", "dirA", "dirB"};
+    for (int j = 0; j < 4; j++)
+      std::fprintf(stderr, "stepped spans (ms): %-8s gap %.3f kernel %.3f row sums %.3f scalar work %.3f\n",
+                   name[j], c.gap_pre[j] * 1e-6, c.kdur[j] * 1e-6, c.gap_post[j] * 1e-6, c.work[j] * 1e-6);
+    std::fprintf(stderr, "stepped accepted trial:");
+    for (int k = 0; k < 11; k++) std::fprintf(stderr, " %u", c.acc_hist[k]);
+    std::fprintf(stderr, "\n");
+  }
+  return 0;
+}
+
+// Frees every cached stepped graph (the device must be idle).
+extern "C" void mg_stepped_free_all() {
+  std::lock_guard<std::mutex> lk(g_graphs_mu);
+  for (SteppedGraph* sg : g_graphs) free_graph(sg);
+  g_graphs.clear();
 }

@@ -213,9 +213,11 @@ def test_pf_stepped_max_iter():
     assert r.iter == 20
 
 
-def test_pf_stepped_matches_persistent_path():
-    """Same minimisation with the stepped FP32 stage switched off (separate
-    process): same minimum to the tolerance, similar iteration count."""
+@pytest.mark.parametrize("switch", ["MINIM_GPU_STEPPED", "MINIM_GPU_TRIAL_PAIRS"])
+def test_pf_stepped_matches_persistent_path(switch):
+    """Same minimisation with the stepped FP32 stage switched off, or with
+    one line-search trial per pass instead of two (separate process): same
+    minimum to the tolerance, similar iteration count."""
     import json
     import os
     import subprocess
@@ -234,7 +236,7 @@ def test_pf_stepped_matches_persistent_path():
         "print(json.dumps({'status': r.status, 'iter': r.iter, 'energy': r.energy}))"
     )
     repo = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-    env = dict(os.environ, MINIM_GPU_STEPPED="0")
+    env = dict(os.environ, **{switch: "0"})
     out = subprocess.run([sys.executable, "-c", code], cwd=repo, env=env, capture_output=True, text=True,
                          timeout=300)
     assert out.returncode == 0, out.stderr
@@ -243,6 +245,25 @@ def test_pf_stepped_matches_persistent_path():
     e_init = Oracle(p, x0).energy(x0)
     assert abs(r.energy - q["energy"]) <= 1e-8 * max(abs(r.energy), abs(e_init))
     assert abs(r.iter - q["iter"]) <= 0.2 * q["iter"] + 10
+
+
+def test_pf_stepped_graph_reuse():
+    """Instances of one shape share the cached stepped graph: the same input
+    gives bitwise the same result before and after another instance ran."""
+    grid = (64, 64, 64)
+    p = abi.phase_field(grid, interface_size=1.0, surface_tension=1.0)
+    mp = abi.minimiser("lbfgs", m=10, tol=1e-7)
+    x0, x1 = pf_noise(grid, seed=26, amp=0.05), pf_noise(grid, seed=27, amp=0.05)
+    runs = []
+    for x in (x0, x1, x0):
+        inst = runtime.Instance(p, x)
+        r = inst.minimise(mp)
+        assert r.status == abi.RES_CONVERGED, r.as_dict()
+        runs.append((r.iter, r.evals, r.energy, inst.coords))
+        inst.close()
+    assert runs[0][:3] == runs[2][:3]
+    assert np.array_equal(runs[0][3], runs[2][3])
+    assert runs[1][2] != runs[0][2]
 
 
 def test_pf_ternary_volume_minimise_batch():
