@@ -440,17 +440,18 @@ __device__ inline void sum_rows_fixed(const double* P, int G, int K, double* out
   };
   D4q acc{0.0, 0.0, 0.0, 0.0};
   if (q < nq) {
-    int b = r0;
-    for (; b + 3 * rs < G; b += 4 * rs) {
-      const D4q v0 = ld(b), v1 = ld(b + rs), v2 = ld(b + 2 * rs), v3 = ld(b + 3 * rs);
+    // four rows per step, all loads issued before the adds (rows past G
+    // read as zero), so that up to 4 * rs rows cost one L2 round trip
+    const D4q z{0.0, 0.0, 0.0, 0.0};
+    for (int b = r0; b < G; b += 4 * rs) {
+      const D4q v0 = ld(b);
+      const D4q v1 = b + rs < G ? ld(b + rs) : z;
+      const D4q v2 = b + 2 * rs < G ? ld(b + 2 * rs) : z;
+      const D4q v3 = b + 3 * rs < G ? ld(b + 3 * rs) : z;
       acc.x += v0.x; acc.y += v0.y; acc.z += v0.z; acc.w += v0.w;
       acc.x += v1.x; acc.y += v1.y; acc.z += v1.z; acc.w += v1.w;
       acc.x += v2.x; acc.y += v2.y; acc.z += v2.z; acc.w += v2.w;
       acc.x += v3.x; acc.y += v3.y; acc.z += v3.z; acc.w += v3.w;
-    }
-    for (; b < G; b += rs) {
-      const D4q v = ld(b);
-      acc.x += v.x; acc.y += v.y; acc.z += v.z; acc.w += v.w;
     }
   }
   for (int off = 16; off >= nqp; off >>= 1) {
@@ -466,9 +467,16 @@ __device__ inline void sum_rows_fixed(const double* P, int G, int K, double* out
   }
   __syncthreads();
   for (int k = tl; k < K; k += nt) {
-    double t = 0.0;
-    for (int i = 0; i < nw; i++) t += wide[i * MINIM_WIDE + k];
-    out[k] = t;
+    if (nw <= 8) {  // the warps' sums as a pairwise tree (short FP64 add chain)
+      double t[8];
+#pragma unroll
+      for (int i = 0; i < 8; i++) t[i] = i < nw ? wide[i * MINIM_WIDE + k] : 0.0;
+      out[k] = ((t[0] + t[1]) + (t[2] + t[3])) + ((t[4] + t[5]) + (t[6] + t[7]));
+    } else {
+      double t = 0.0;
+      for (int i = 0; i < nw; i++) t += wide[i * MINIM_WIDE + k];
+      out[k] = t;
+    }
   }
 }
 

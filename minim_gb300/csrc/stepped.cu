@@ -74,6 +74,7 @@ struct StepCtl {
   unsigned gdone[kMaxGroups];  // grouped row sums: blocks of each group done
   double gap_pre[4], kdur[4], gap_post[4];
   double work[4];         // the controllers' scalar work (span_end to phase_mark)
+  int timing;             // record the spans above (MINIM_GPU_STEPPED_TIMING)
   unsigned long long tw;  // start of the current controller's scalar work
   int cur;                // its span slot
   unsigned acc_hist[11];  // iterations by the trial accepted (10: none)
@@ -81,6 +82,7 @@ struct StepCtl {
 
 // adds the last phase kernel's span to slot j of the span records
 __device__ __forceinline__ void span_end(StepCtl* ctl, int j) {
+  if (!ctl->timing) return;
   const unsigned long long now = globaltimer_ns();
   ctl->gap_pre[j] += (double)(ctl->ks - ctl->tmark);
   ctl->kdur[j] += (double)(ctl->ke - ctl->ks);
@@ -527,6 +529,7 @@ k_lines(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, double* pa
   Acc e, gg, py, yy, e2, gg2, py2, yy2;
   if (zq < nz4) {
     for (int l = blockIdx.x * blockDim.y + threadIdx.y; l < nl; l += gridDim.x * blockDim.y) {
+
       const int x = l / ny, y = l - x * ny;
       const int lym = x * ny + (y == 0 ? ny - 1 : y - 1), lyp = x * ny + (y == ny - 1 ? 0 : y + 1);
       const int lxm = (x == 0 ? nx - 1 : x - 1) * ny + y, lxp = (x == nx - 1 ? 0 : x + 1) * ny + y;
@@ -593,8 +596,9 @@ k_lines(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, double* pa
 // ---- controllers (one block) ----------------------------------------------------
 
 __global__ void k_begin(const InstDesc* __restrict__ d, const MinScalars* __restrict__ st, StepCtl* ctl,
-                        int slice, cudaGraphConditionalHandle outer) {
+                        int slice, int timing, cudaGraphConditionalHandle outer) {
   if (threadIdx.x == 0) {
+    ctl->timing = timing;
     ctl->iters = 0;
     ctl->slice = slice;
     ctl->kernels = 1;
@@ -613,7 +617,7 @@ __device__ __forceinline__ void phase_time(MinScalars* st, StepCtl* ctl, int ph)
 }
 __device__ __forceinline__ void phase_mark(StepCtl* ctl) {
   const unsigned long long now = globaltimer_ns();
-  ctl->work[ctl->cur] += (double)(now - ctl->tw);
+  if (ctl->timing) ctl->work[ctl->cur] += (double)(now - ctl->tw);
   ctl->tmark = now;
 }
 
@@ -1088,6 +1092,7 @@ int build(SteppedGraph* sg, int m, const int* grid, int nsm, int slice, int dual
   sg->spec = spec;
   const InstDesc* d = sg->d;
   MinScalars* st = sg->st;
+  int timing = std::getenv("MINIM_GPU_STEPPED_TIMING") != nullptr;
   cudaGraph_t g = nullptr;
   SCK(cudaGraphCreate(&g, 0));
   sg->graph = g;
@@ -1097,7 +1102,7 @@ int build(SteppedGraph* sg, int m, const int* grid, int nsm, int slice, int dual
   double* part = sg->part;
   cudaGraphNode_t n_begin, n_outer;
   {
-    void* args[] = {(void*)&d, (void*)&st, (void*)&ctl, (void*)&sg->slice, (void*)&h_outer};
+    void* args[] = {(void*)&d, (void*)&st, (void*)&ctl, (void*)&sg->slice, (void*)&timing, (void*)&h_outer};
     SCK(add_kernel(&n_begin, g, nullptr, 0, (const void*)k_begin, 1, 32, args));
   }
   cudaGraph_t body;
