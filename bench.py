@@ -38,10 +38,10 @@ METRIC = "converged minimisations/s batched vs plain on GB300 at ΔE/E<1e-8; p50
 # DRAM bytes per algorithmic byte of the PhaseField 192^3 minimisation's
 # FP32 stage (the stepped graph), from one ncu capture of a graph launch
 # running 19 iterations: dram__bytes_read.sum + dram__bytes_write.sum =
-# 23.68 GB against the kernels' own count of 20.77 GB
+# 24.20 GB against the kernels' own count of 21.52 GB
 # (profiles/stepped_graph_pf1_192cubed.md).  Traffic per step = this ratio x
 # the step's algorithmic bytes.
-PF_TRAFFIC_PER_ALGO_BYTE = 23.68 / 20.77
+PF_TRAFFIC_PER_ALGO_BYTE = 24.20 / 21.52
 
 
 def _peaks():
@@ -446,7 +446,7 @@ def run_profile_case(iters):
     r = inst.minimise(mp)
     st = runtime.last_run_stats()
     print(json.dumps({"profile_case": "PhaseField 192^3 Lbfgs m=10", "iterations": iters,
-                      "kernel_ms": st["kernel_ms"], "launches": st["launches"],
+                      "kernel_ms": st["kernel_ms"], "launches": st["launches"], "abytes": st["abytes"],
                       "abytes_per_launch": st["abytes"] / max(st["launches"], 1), "status": r.status}))
 
 
