@@ -63,6 +63,7 @@ struct StepCtl {
   int iters, slice;          // iterations in this launch, at most `slice`
   int mt;                    // pairs used by this iteration's direction
   int gmode;                 // two-trial graph: the next trial pass is the gradient at t only
+  int retry;                 // two-trial graph: the next outer pass only continues the line search
   float fg;                  // -gamma
   float coefS[MINIM_MAXM], coefY[MINIM_MAXM];
   int so[MINIM_MAXM], yo[MINIM_MAXM];  // slot buffers: float4 offsets from the ring bases
@@ -212,8 +213,7 @@ __device__ void ctl_lsg(const InstDesc* __restrict__ d, MinScalars* st, StepCtl*
                         int nb, cudaGraphConditionalHandle ls, cudaGraphConditionalHandle grad,
                         cudaGraphConditionalHandle outer);
 __device__ void ctl_lsg2(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, const double* part,
-                         int nb, cudaGraphConditionalHandle ls, cudaGraphConditionalHandle grad,
-                         cudaGraphConditionalHandle outer);
+                         int nb, cudaGraphConditionalHandle outer);
 
 // ---- vector and stencil kernels -------------------------------------------------
 
@@ -227,6 +227,7 @@ __device__ void ctl_lsg2(const InstDesc* __restrict__ d, MinScalars* st, StepCtl
 template <int M>
 __global__ void __launch_bounds__(kThreads, 4)
 k_dir_a(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, double* part) {
+  if (ctl->retry) return;  // this pass of the loop only continues a line search
   span_begin(ctl);
   constexpr int NG = (M + 7) / 8;
   constexpr int GS = (M + NG - 1) / NG;  // pairs per part
@@ -330,6 +331,7 @@ template <int M>
 __global__ void __launch_bounds__(kThreads, 4)
 k_dir_b(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, double* part, cudaGraphConditionalHandle ls,
         cudaGraphConditionalHandle grad, int spec) {
+  if (ctl->retry) return;  // this pass of the loop only continues a line search
   span_begin(ctl);
   const int n = d->ndof, nq4 = n >> 2, mt = ctl->mt;
   const float* G = d->G[st->gi];
@@ -589,7 +591,7 @@ k_lines(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, double* pa
     if (MODE == 0) ctl_ls(d, st, ctl, part, gridDim.x, ls);
     else if (MODE == 1) ctl_g(d, st, ctl, part, gridDim.x, outer);
     else if (MODE == 2) ctl_lsg(d, st, ctl, part, gridDim.x, ls, grad, outer);
-    else ctl_lsg2(d, st, ctl, part, gridDim.x, ls, grad, outer);
+    else ctl_lsg2(d, st, ctl, part, gridDim.x, outer);
   }
 }
 
@@ -599,6 +601,7 @@ __global__ void k_begin(const InstDesc* __restrict__ d, const MinScalars* __rest
                         int slice, int timing, cudaGraphConditionalHandle outer) {
   if (threadIdx.x == 0) {
     ctl->timing = timing;
+    ctl->retry = 0;
     ctl->iters = 0;
     ctl->slice = slice;
     ctl->kernels = 1;
@@ -905,9 +908,11 @@ __device__ void ctl_lsg(const InstDesc* __restrict__ d, MinScalars* st, StepCtl*
 // buffers) become the next ones by exchanging buffer pointers and slots.
 // After the tenth failed trial (or without a line search) the next pass is
 // the gradient at the step alone (gmode), which completes the iteration.
+// A pass that completes no iteration sets `retry`: the outer loop runs once
+// more with the direction kernels returning at once, so the common pass
+// (one of the two trials accepted) costs one conditional node, not two.
 __device__ void ctl_lsg2(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, const double* part,
-                         int nb, cudaGraphConditionalHandle ls, cudaGraphConditionalHandle grad,
-                         cudaGraphConditionalHandle outer) {
+                         int nb, cudaGraphConditionalHandle outer) {
   __shared__ double wide[8 * MINIM_WIDE];
   __shared__ double v[8];
   const unsigned warm = warm_ctl(d, st, ctl);
@@ -921,9 +926,9 @@ __device__ void ctl_lsg2(const InstDesc* __restrict__ d, MinScalars* st, StepCtl
   const double n = (double)d->ndof;
   if (ctl->gmode) {
     ctl->gmode = 0;
+    ctl->retry = 0;
     st->evals++;
     st->abytes += 24.0 * n;
-    cudaGraphSetConditional(ls, 0u);
     commit_grad(d, st, ctl, v, outer);
     return;
   }
@@ -944,7 +949,7 @@ __device__ void ctl_lsg2(const InstDesc* __restrict__ d, MinScalars* st, StepCtl
         st->ybuf = st->ybuf2;
         st->ybuf2 = ty;
       }
-      cudaGraphSetConditional(ls, 0u);
+      ctl->retry = 0;
       st->evals++;
       st->abytes += 24.0 * n;
       commit_grad(d, st, ctl, v + 4 * j, outer);
@@ -960,7 +965,8 @@ __device__ void ctl_lsg2(const InstDesc* __restrict__ d, MinScalars* st, StepCtl
     ctl->acc_hist[10]++;
     ctl->gmode = 1;
   }
-  cudaGraphSetConditional(ls, 1u);
+  ctl->retry = 1;
+  cudaGraphSetConditional(outer, 1u);
   phase_mark(ctl);
 }
 
@@ -1096,7 +1102,7 @@ int build(SteppedGraph* sg, int m, const int* grid, int nsm, int slice, int dual
   cudaGraph_t g = nullptr;
   SCK(cudaGraphCreate(&g, 0));
   sg->graph = g;
-  cudaGraphConditionalHandle h_outer, h_ls;
+  cudaGraphConditionalHandle h_outer, h_ls = 0;
   SCK(cudaGraphConditionalHandleCreate(&h_outer, g, 1, cudaGraphCondAssignDefault));
   StepCtl* ctl = sg->ctl;
   double* part = sg->part;
@@ -1107,7 +1113,7 @@ int build(SteppedGraph* sg, int m, const int* grid, int nsm, int slice, int dual
   }
   cudaGraph_t body;
   SCK(add_while(&n_outer, g, &n_begin, 1, h_outer, &body));
-  SCK(cudaGraphConditionalHandleCreate(&h_ls, body, 0, 0));
+  if (!two) SCK(cudaGraphConditionalHandleCreate(&h_ls, body, 0, 0));
   cudaGraphConditionalHandle h_grad = 0;
   if (spec && !two) SCK(cudaGraphConditionalHandleCreate(&h_grad, body, 0, 0));
   cudaGraphNode_t na, nb, nls, ngr;
@@ -1122,14 +1128,11 @@ int build(SteppedGraph* sg, int m, const int* grid, int nsm, int slice, int dual
   void* args_s[] = {(void*)&d, (void*)&st, (void*)&ctl, (void*)&part, (void*)&h_ls, (void*)&h_grad, (void*)&h_outer};
   cudaGraph_t ls_body;
   if (two) {
-    // dirA -> dirB -> trial pass -> WHILE(more passes) { trial pass }: the
-    // first pass follows pass B directly; a pass that accepts a trial (or is
-    // the gradient-only pass) ends the iteration
+    // dirA -> dirB -> trial pass: a pass that accepts a trial (or is the
+    // gradient-only pass) ends the iteration; one that does not sets
+    // `retry`, and the next pass of the outer loop skips the direction
     cudaGraphNode_t nt;
     SCK(add_kernel(&nt, body, &nb, 1, fe, nb_e, sblock, args_s));
-    SCK(add_while(&nls, body, &nt, 1, h_ls, &ls_body));
-    cudaGraphNode_t ne;
-    SCK(add_kernel(&ne, ls_body, nullptr, 0, fe, nb_e, sblock, args_s));
     SCK(cudaGraphInstantiate(&sg->exec, g, 0));
     return 0;
   }
