@@ -253,6 +253,16 @@ int minim_gpu_bah_elements(const minim_gpu_bah_params* q, const double* x0, size
                            double* hinge_par);
 int minim_gpu_bah_colouring(const minim_gpu_bah_params* q, const double* x0, size_t ndof,
                             int* nbar_colors, int* nhinge_colors, int* valid);
+/* The BarAndHinge elements an instance evaluates, in its colour order (no
+ * counterpart in the reference; for checking the set-up, which runs on the
+ * device for a triangulation unless MINIM_GPU_BAH_DEVICE_SETUP=0): bars (2
+ * per bar) with {k, l0}, hinges (4 per hinge) with {k, theta0}, at most cap
+ * of each; colour offsets (ncolors + 1 entries, at most 65); on_device = 1
+ * when the device built them.  Elements whose coordinates are all fixed are
+ * not included. */
+int minim_gpu_instance_bah_arrays(minim_gpu_handle h, int cap, int* nbar, int* bars, double* bar_par,
+                                  int* nbar_colors, int* bar_off, int* nhinge, int* hinges,
+                                  double* hinge_par, int* nhinge_colors, int* hinge_off, int* on_device);
 /* kernel_variant: 1 = general PhaseField kernel, 3 = binary kernel without
  * optional terms. */
 int minim_gpu_pf_setup(const minim_gpu_pf_params* q, const double* x0, size_t ndof, double* kappa,

@@ -18,7 +18,7 @@ CUDA = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-CU = ["engine_lj.cu", "engine_pf.cu", "engine_pf1.cu", "engine_bah.cu", "engine_misc.cu", "noalloc.cu", "stepped.cu"]
+CU = ["engine_lj.cu", "engine_pf.cu", "engine_pf1.cu", "engine_bah.cu", "engine_misc.cu", "noalloc.cu", "stepped.cu", "topology.cu"]
 CPP = ["setup.cpp", "capi.cpp"]
 API = ["api_core.cpp", "api_minimisers.cpp", "api_potentials.cpp"]  # source-compatible C++ API
 HEADERS = ["common.cuh", "potentials.cuh", "minimiser.cuh", "kernels.cuh", "engine.h", "setup.h"]

@@ -21,6 +21,7 @@
 #include "engine.h"
 #include "minim_gpu.h"
 #include "setup.h"
+#include "topology.h"
 
 using namespace mg;
 
@@ -162,6 +163,15 @@ bool dual_cfg() {
   }();
   return v;
 }
+// BarAndHinge instances given by a triangulation are set up on the device
+// (topology.cu) unless MINIM_GPU_BAH_DEVICE_SETUP=0.
+bool bah_device_cfg() {
+  static const bool v = [] {
+    const char* e = std::getenv("MINIM_GPU_BAH_DEVICE_SETUP");
+    return !(e && e[0] == '0');
+  }();
+  return v;
+}
 // L2 prefetch distance of the grid launches' sweeps, in sweep steps
 // (MINIM_GPU_PREFETCH, default 1; 0 disables it).
 int prefetch_cfg() {
@@ -275,6 +285,8 @@ struct minim_gpu_instance_s {
   std::vector<void*> owned;
   double default_tol = 1e-6;
   BahHost bah;
+  BahTopoDev bah_topo;   // device-built elements (bah_dev), before filtering and colouring
+  bool bah_dev = false;
   std::vector<unsigned char> fixed;
   size_t pot_bytes = 0;
   // grid-launch resources (lazy)
@@ -312,8 +324,54 @@ struct minim_gpu_instance_s {
 namespace {
 
 void upload_bah_arrays(minim_gpu_instance_s* h) {
-  BahDevArrays A = bah_arrays(h->bah, h->fixed);
   PotBAH& P = h->d.bah;
+  if (h->bah_dev) {
+    BahColouredDev C;
+    const int rc = mg_bah_colour_device(&h->bah_topo, h->fixed.empty() ? nullptr : h->fixed.data(), &C, dev().s);
+    if (rc == MG_TOPO_CUDA) throw ApiError{MINIM_GPU_ERR_CUDA, "BarAndHinge device colouring failed"};
+    if (rc == MG_TOPO_OK) {
+      P.nvert = h->bah.nvert;
+      P.nbar = C.nbar;
+      P.nhinge = C.nhinge;
+      P.bars = (int2*)h->own(C.bars);
+      P.bar_par = (double2*)h->own(C.bpar);
+      P.hinges = (int4*)h->own(C.hinges);
+      P.hinge_par = (double2*)h->own(C.hpar);
+      P.nbar_colors = C.nbar_colors;
+      P.nhinge_colors = C.nhinge_colors;
+      P.bar_color_off = (int*)h->own(C.bar_off);
+      P.hinge_color_off = (int*)h->own(C.hinge_off);
+      P.node_el = (unsigned char*)h->own(C.node_el);
+      P.nforce = (int)h->bah.force.size();
+      P.force = h->own_upload(h->bah.force);
+      P.wall_on = h->bah.wall_on;
+      P.wall_adh = h->bah.wall_adh;
+      P.wall_eps = h->bah.wall_eps;
+      P.wall_sig = h->bah.wall_sig;
+      return;
+    }
+    // more colours than the device colouring handles: continue on the host
+    // from the device-built elements
+    const BahTopoDev& T = h->bah_topo;
+    std::vector<int2> b2(T.nbar);
+    std::vector<int4> h4(T.nhinge);
+    std::vector<double2> bp(T.nbar), hp(T.nhinge);
+    CK(cudaMemcpyAsync(b2.data(), T.bars, b2.size() * sizeof(int2), cudaMemcpyDeviceToHost, dev().s));
+    CK(cudaMemcpyAsync(bp.data(), T.bpar, bp.size() * sizeof(double2), cudaMemcpyDeviceToHost, dev().s));
+    CK(cudaMemcpyAsync(h4.data(), T.hinges, h4.size() * sizeof(int4), cudaMemcpyDeviceToHost, dev().s));
+    CK(cudaMemcpyAsync(hp.data(), T.hpar, hp.size() * sizeof(double2), cudaMemcpyDeviceToHost, dev().s));
+    CK(cudaStreamSynchronize(dev().s));
+    for (size_t i = 0; i < b2.size(); i++) {
+      h->bah.bars.insert(h->bah.bars.end(), {b2[i].x, b2[i].y});
+      h->bah.bpar.insert(h->bah.bpar.end(), {bp[i].x, bp[i].y});
+    }
+    for (size_t i = 0; i < h4.size(); i++) {
+      h->bah.hinges.insert(h->bah.hinges.end(), {h4[i].x, h4[i].y, h4[i].z, h4[i].w});
+      h->bah.hpar.insert(h->bah.hpar.end(), {hp[i].x, hp[i].y});
+    }
+    h->bah_dev = false;
+  }
+  BahDevArrays A = bah_arrays(h->bah, h->fixed);
   P.nvert = h->bah.nvert;
   P.nbar = (int)A.bars.size();
   P.nhinge = (int)A.hinges.size();
@@ -365,7 +423,27 @@ minim_gpu_instance_s* create_instance(int kind, const void* params, const double
       h->d.pf.ff_init = h->own_upload(H.ff_init);
     } else if (kind == MINIM_GPU_BAH) {
       h->kk = K_BAH;
-      h->bah = setup_bah(*(const minim_gpu_bah_params*)params, x0, ndof);
+      const auto* q = (const minim_gpu_bah_params*)params;
+      if (ndof % 3) throw ApiError{MINIM_GPU_ERR_INVALID, "BarAndHinge: coordinates must be 3 per vertex"};
+      bool built = false;
+      if (bah_device_cfg() && q->ntri > 0 && q->nbond == 0 && q->nhinge == 0) {
+        char msg[256] = {0};
+        const int rc = mg_bah_topology_device(q, x0, (int)(ndof / 3), &h->bah_topo, dev().s, msg, (int)sizeof msg);
+        if (rc == MG_TOPO_INVALID) throw ApiError{MINIM_GPU_ERR_INVALID, msg};
+        if (rc == MG_TOPO_CUDA) throw ApiError{MINIM_GPU_ERR_CUDA, "BarAndHinge device set-up failed"};
+        if (rc == MG_TOPO_OK) {
+          h->own(h->bah_topo.bars);
+          h->own(h->bah_topo.bpar);
+          h->own(h->bah_topo.hinges);
+          h->own(h->bah_topo.hpar);
+          h->bah = BahHost{};
+          h->bah.nvert = (int)(ndof / 3);
+          bah_scalars(*q, h->bah);
+          h->bah_dev = true;
+          built = true;
+        }
+      }
+      if (!built) h->bah = setup_bah(*q, x0, ndof);
       upload_bah_arrays(h);
       h->d.GA = (double*)h->own(dalloc(ndof * sizeof(double)));
     } else {
@@ -1103,6 +1181,51 @@ int minim_gpu_bah_colouring(const minim_gpu_bah_params* q, const double* x0, siz
           seen[v] = c;
         }
     *valid = ok;
+  });
+}
+
+int minim_gpu_instance_bah_arrays(minim_gpu_handle h, int cap, int* nbar, int* bars, double* bar_par,
+                                  int* nbar_colors, int* bar_off, int* nhinge, int* hinges, double* hinge_par,
+                                  int* nhinge_colors, int* hinge_off, int* on_device) {
+  return guarded([&] {
+    if (!h || h->kind != MINIM_GPU_BAH) throw ApiError{MINIM_GPU_ERR_INVALID, "not a BarAndHinge instance"};
+    const PotBAH& P = h->d.bah;
+    *nbar = P.nbar;
+    *nhinge = P.nhinge;
+    *nbar_colors = P.nbar_colors;
+    *nhinge_colors = P.nhinge_colors;
+    *on_device = h->bah_dev ? 1 : 0;
+    if (P.nbar > cap || P.nhinge > cap || P.nbar_colors > 64 || P.nhinge_colors > 64) return;
+    Dev& D = need_dev();
+    std::vector<int2> b2(P.nbar);
+    std::vector<int4> h4(P.nhinge);
+    std::vector<double2> bp(P.nbar), hp(P.nhinge);
+    if (P.nbar) {
+      CK(cudaMemcpyAsync(b2.data(), P.bars, b2.size() * sizeof(int2), cudaMemcpyDeviceToHost, D.s));
+      CK(cudaMemcpyAsync(bp.data(), P.bar_par, bp.size() * sizeof(double2), cudaMemcpyDeviceToHost, D.s));
+    }
+    if (P.nhinge) {
+      CK(cudaMemcpyAsync(h4.data(), P.hinges, h4.size() * sizeof(int4), cudaMemcpyDeviceToHost, D.s));
+      CK(cudaMemcpyAsync(hp.data(), P.hinge_par, hp.size() * sizeof(double2), cudaMemcpyDeviceToHost, D.s));
+    }
+    CK(cudaMemcpyAsync(bar_off, P.bar_color_off, (P.nbar_colors + 1) * sizeof(int), cudaMemcpyDeviceToHost, D.s));
+    CK(cudaMemcpyAsync(hinge_off, P.hinge_color_off, (P.nhinge_colors + 1) * sizeof(int), cudaMemcpyDeviceToHost,
+                       D.s));
+    CK(cudaStreamSynchronize(D.s));
+    for (int i = 0; i < P.nbar; i++) {
+      bars[2 * i] = b2[i].x;
+      bars[2 * i + 1] = b2[i].y;
+      bar_par[2 * i] = bp[i].x;
+      bar_par[2 * i + 1] = bp[i].y;
+    }
+    for (int i = 0; i < P.nhinge; i++) {
+      hinges[4 * i] = h4[i].x;
+      hinges[4 * i + 1] = h4[i].y;
+      hinges[4 * i + 2] = h4[i].z;
+      hinges[4 * i + 3] = h4[i].w;
+      hinge_par[2 * i] = hp[i].x;
+      hinge_par[2 * i + 1] = hp[i].y;
+    }
   });
 }
 

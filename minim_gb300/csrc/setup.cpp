@@ -490,6 +490,11 @@ BahHost setup_bah(const minim_gpu_bah_params& q, const double* x, size_t ndof) {
     }
     B.hpar[2 * h + 1] = t0;
   }
+  bah_scalars(q, B);
+  return B;
+}
+
+void bah_scalars(const minim_gpu_bah_params& q, BahHost& B) {
   if (q.n_force > 0) {
     if (q.n_force != 3 && q.n_force != 3 * B.nvert)
       throw SetupError(MINIM_GPU_ERR_INVALID, "BarAndHinge: force must have 3 or 3*nvert entries");
@@ -499,7 +504,6 @@ BahHost setup_bah(const minim_gpu_bah_params& q, const double* x, size_t ndof) {
   B.wall_adh = q.wall_adhesion;
   B.wall_eps = q.wall_epsilon;
   B.wall_sig = q.wall_sigma;
-  return B;
 }
 
 namespace {

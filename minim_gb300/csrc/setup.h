@@ -51,6 +51,8 @@ struct BahHost {
   double wall_eps = 0, wall_sig = 0;
 };
 BahHost setup_bah(const minim_gpu_bah_params& q, const double* x0, size_t ndof);
+// the body force and wall of q into B (B.nvert set)
+void bah_scalars(const minim_gpu_bah_params& q, BahHost& B);
 
 // Element arrays after removing fully fixed elements and sorting by colour.
 struct BahDevArrays {

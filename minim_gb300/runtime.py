@@ -31,7 +31,7 @@ EXPORTS = [
     "minim_gpu_server_create", "minim_gpu_server_submit", "minim_gpu_server_step",
     "minim_gpu_server_poll", "minim_gpu_server_take", "minim_gpu_server_cancel",
     "minim_gpu_server_destroy", "minim_gpu_bah_elements", "minim_gpu_bah_colouring",
-    "minim_gpu_pf_setup", "minim_gpu_lj_minimise_noalloc",
+    "minim_gpu_pf_setup", "minim_gpu_lj_minimise_noalloc", "minim_gpu_instance_bah_arrays",
 ]
 
 
@@ -82,6 +82,8 @@ def load(path=LIB_PATH):
                                    C.c_int),
         "minim_gpu_bah_colouring": ([P, _dp, C.c_size_t, _ip, _ip, _ip], C.c_int),
         "minim_gpu_pf_setup": ([P, _dp, C.c_size_t, _dp, _dp, _ip, _dp, _dp, _ip], C.c_int),
+        "minim_gpu_instance_bah_arrays": ([P, C.c_int, _ip, _ip, _dp, _ip, _ip, _ip, _ip, _dp, _ip, _ip, _ip],
+                                          C.c_int),
         "minim_gpu_lj_minimise_noalloc": ([P, C.c_void_p, C.c_size_t, C.POINTER(abi.MinimiserParams),
                                            C.POINTER(abi.Result), C.c_void_p], C.c_int),
     }
@@ -183,6 +185,30 @@ class Instance:
         a = _vec(v).copy()
         _check(_lib.minim_gpu_apply_constraints(self.h, a.ctypes.data_as(_dp)))
         return a
+
+    def bah_arrays(self):
+        """The BarAndHinge elements this instance evaluates, in colour order:
+        bars (k, 2), bar_par (k, 2) = {k, l0}, hinges (k, 4), hinge_par (k, 2)
+        = {k, theta0}, the colour offsets and whether the device built them."""
+        lib = load()
+        cnt = [C.c_int() for _ in range(5)]
+        _check(lib.minim_gpu_instance_bah_arrays(self.h, 0, C.byref(cnt[0]), None, None, C.byref(cnt[1]), None,
+                                                 C.byref(cnt[2]), None, None, C.byref(cnt[3]), None,
+                                                 C.byref(cnt[4])))
+        nb, nh = cnt[0].value, cnt[2].value
+        cap = max(nb, nh, 1)
+        bars, bp = np.zeros(2 * cap, np.int32), np.zeros(2 * cap)
+        hinges, hp = np.zeros(4 * cap, np.int32), np.zeros(2 * cap)
+        boff, hoff = np.zeros(65, np.int32), np.zeros(65, np.int32)
+        ncb, nch, dev = C.c_int(), C.c_int(), C.c_int()
+        _check(lib.minim_gpu_instance_bah_arrays(
+            self.h, cap, C.byref(cnt[0]), bars.ctypes.data_as(_ip), bp.ctypes.data_as(_dp), C.byref(ncb),
+            boff.ctypes.data_as(_ip), C.byref(cnt[2]), hinges.ctypes.data_as(_ip), hp.ctypes.data_as(_dp),
+            C.byref(nch), hoff.ctypes.data_as(_ip), C.byref(dev)))
+        return {"bars": bars[:2 * nb].reshape(-1, 2), "bar_par": bp[:2 * nb].reshape(-1, 2),
+                "hinges": hinges[:4 * nh].reshape(-1, 4), "hinge_par": hp[:2 * nh].reshape(-1, 2),
+                "bar_off": boff[:ncb.value + 1].copy(), "hinge_off": hoff[:nch.value + 1].copy(),
+                "on_device": bool(dev.value)}
 
     def minimise(self, mp):
         r = abi.Result()
