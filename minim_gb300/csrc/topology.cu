@@ -10,10 +10,9 @@
 // order.  Hinges are the pairs of triangles (t1 < t2) that share exactly two
 // vertices, sorted by (t1, t2).  Both orders come from bucketing by the
 // lower index (count, scan, scatter) and sorting each small bucket, so no
-// global sort is needed.  The colouring is speculative first-fit: every
-// uncoloured element takes the lowest colour none of its coloured neighbours
-// has; of neighbours that pick the same colour in a round the lowest index
-// keeps it; the rest retry.  Every step is deterministic.
+// global sort is needed.  The colouring is the greedy pass in element order
+// (on the host, one 64-bit mask per vertex), after which the device orders
+// the elements by colour.  Every step is deterministic.
 //
 // Triangulations outside what this builder handles (out-of-range or repeated
 // vertices in a triangle, more than 4 triangles on an edge, a vertex on more
@@ -21,8 +20,11 @@
 // which then uses the host builder (setup.cpp).
 #include <cuda_runtime.h>
 
+#include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -459,68 +461,6 @@ __global__ void k_compact(const void* __restrict__ el, const double2* __restrict
   par_out[kpos[e]] = par[e];
 }
 
-template <int PER>
-__global__ void k_incidence_count(const void* __restrict__ el, int ne, int* __restrict__ cnt) {
-  const int e = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= ne) return;
-  int v[PER];
-  nodes_of<PER>(el, e, v);
-  for (int k = 0; k < PER; k++) atomicAdd(&cnt[v[k]], 1);
-}
-
-template <int PER>
-__global__ void k_incidence_fill(const void* __restrict__ el, int ne, const int* __restrict__ off,
-                                 int* __restrict__ cur, int* __restrict__ inc) {
-  const int e = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= ne) return;
-  int v[PER];
-  nodes_of<PER>(el, e, v);
-  for (int k = 0; k < PER; k++) inc[off[v[k]] + atomicAdd(&cur[v[k]], 1)] = e;
-}
-
-// a round of speculative first-fit: the lowest colour no coloured neighbour has
-template <int PER>
-__global__ void k_tentative(const void* __restrict__ el, int ne, const int* __restrict__ col,
-                            const unsigned long long* __restrict__ vmask, int* __restrict__ tent, int* flags) {
-  const int e = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= ne) return;
-  if (col[e] >= 0) {
-    tent[e] = -1;
-    return;
-  }
-  int v[PER];
-  nodes_of<PER>(el, e, v);
-  unsigned long long forb = 0;
-  for (int k = 0; k < PER; k++) forb |= vmask[v[k]];
-  if (forb == ~0ull) {
-    atomicOr(flags, F_COLOURS);
-    tent[e] = -1;
-    return;
-  }
-  tent[e] = __ffsll((long long)~forb) - 1;
-}
-
-// keep the tentative colour unless a lower-indexed neighbour picked the same
-template <int PER>
-__global__ void k_commit(const void* __restrict__ el, int ne, const int* __restrict__ tent,
-                         const int* __restrict__ off, const int* __restrict__ inc, int* __restrict__ col,
-                         unsigned long long* __restrict__ vmask, int* __restrict__ ncommit) {
-  const int e = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= ne) return;
-  const int c = tent[e];
-  if (c < 0) return;
-  int v[PER];
-  nodes_of<PER>(el, e, v);
-  for (int k = 0; k < PER; k++)
-    for (int i = off[v[k]]; i < off[v[k] + 1]; i++) {
-      const int f = inc[i];
-      if (f < e && tent[f] == c) return;
-    }
-  col[e] = c;
-  for (int k = 0; k < PER; k++) atomicOr(&vmask[v[k]], 1ull << c);
-  atomicAdd(ncommit, 1);
-}
-
 // colour order: per block of 1024 elements, counts per colour
 __global__ void __launch_bounds__(1024) k_colour_hist(const int* __restrict__ col, int ne, int* __restrict__ bc) {
   __shared__ int h[64];
@@ -651,6 +591,20 @@ struct Scratch {
   }
 };
 
+// MINIM_GPU_BAH_SETUP_TIMING: host wall time of the set-up's phases (each
+// phase ends at a synchronising read) printed to stderr
+struct PhaseClock {
+  bool on = std::getenv("MINIM_GPU_BAH_SETUP_TIMING") != nullptr;
+  std::chrono::steady_clock::time_point t = std::chrono::steady_clock::now();
+  void mark(const char* what) {
+    if (!on) return;
+    const auto now = std::chrono::steady_clock::now();
+    std::fprintf(stderr, "bah set-up %-22s %8.3f ms\n", what,
+                 std::chrono::duration<double, std::milli>(now - t).count());
+    t = now;
+  }
+};
+
 void set_err(char* err, int len, const char* msg) {
   if (err && len > 0) std::snprintf(err, (size_t)len, "%s", msg);
 }
@@ -665,48 +619,40 @@ int colour_elements(Scratch& S, const void* el, const double2* par, int ne, int 
   int* kpos = S.alloc<int>((size_t)ne + 1);
   if (S.err == cudaSuccess && ne) k_keep<PER><<<nblk(ne), kT, 0, S.s>>>(el, ne, d_fixed, keep);
   S.scan(keep, kpos, ne);
+  PhaseClock clk;
   const int nk = S.read(kpos + ne);
+  clk.mark(PER == 2 ? "bars kept" : "hinges kept");
   void* ek = S.alloc<char>((size_t)nk * esz);
   double2* pk = S.alloc<double2>(nk);
   if (S.err == cudaSuccess && ne) k_compact<PER><<<nblk(ne), kT, 0, S.s>>>(el, par, ne, keep, kpos, ek, pk);
-  // vertex -> element incidence
-  int* icnt = S.zeros<int>(nvert);
-  int* ioff = S.alloc<int>((size_t)nvert + 1);
-  int* icur = S.zeros<int>(nvert);
-  int* inc = S.alloc<int>((size_t)nk * PER);
-  if (S.err == cudaSuccess && nk) k_incidence_count<PER><<<nblk(nk), kT, 0, S.s>>>(ek, nk, icnt);
-  S.scan(icnt, ioff, nvert);
-  if (S.err == cudaSuccess && nk) k_incidence_fill<PER><<<nblk(nk), kT, 0, S.s>>>(ek, nk, ioff, icur, inc);
-  // colouring rounds
-  int* col = S.alloc<int>(nk);
-  int* tent = S.alloc<int>(nk);
-  unsigned long long* vmask = S.zeros<unsigned long long>(nvert);
-  int* ncommit = S.zeros<int>(1);
-  if (S.err == cudaSuccess && nk) S.err = cudaMemsetAsync(col, 0xff, (size_t)nk * sizeof(int), S.s);
-  // every round colours at least the lowest-indexed uncoloured element of
-  // each conflict, unless the colours ran out (flagged)
-  int done = 0;
-  while (done < nk && S.err == cudaSuccess) {
-    k_tentative<PER><<<nblk(nk), kT, 0, S.s>>>(ek, nk, col, vmask, tent, flags);
-    k_commit<PER><<<nblk(nk), kT, 0, S.s>>>(ek, nk, tent, ioff, inc, col, vmask, ncommit);
-    S.err = cudaGetLastError();
-    const int now = S.read(ncommit);
-    if (S.err != cudaSuccess) break;
-    if (now == done) return 1;
-    done = now;
-  }
-  // number of colours: one past the largest
+  // greedy colouring in element order on the host (one 64-bit mask of used
+  // colours per vertex): a sequential pass whose colour count the parallel
+  // schemes tried here did not reach on meshes (a 100k-vertex sheet: 8 bar
+  // and 19 hinge colours against 6 and 13), and every colour costs the
+  // gradient scatter one barrier
+  std::vector<char> he((size_t)nk * esz);
+  if (S.err == cudaSuccess && nk) S.err = cudaMemcpyAsync(he.data(), ek, he.size(), cudaMemcpyDeviceToHost, S.s);
+  if (S.err == cudaSuccess) S.err = cudaStreamSynchronize(S.s);
+  std::vector<int> hc(nk);
+  std::vector<unsigned long long> used(nvert, 0ull);
   int ncol = 0;
-  if (nk && S.err == cudaSuccess) {
-    std::vector<int> hc(nk);
-    S.err = cudaMemcpyAsync(hc.data(), col, (size_t)nk * sizeof(int), cudaMemcpyDeviceToHost, S.s);
-    if (S.err == cudaSuccess) S.err = cudaStreamSynchronize(S.s);
-    for (int c : hc) ncol = c + 1 > ncol ? c + 1 : ncol;
+  for (int e = 0; e < nk && S.err == cudaSuccess; e++) {
+    const int* v = reinterpret_cast<const int*>(he.data() + (size_t)e * esz);
+    unsigned long long forb = 0;
+    for (int k = 0; k < PER; k++) forb |= used[v[k]];
+    if (forb == ~0ull) return 1;  // more than 64 colours: the host builder's multi-word greedy
+    int c = 0;
+    while (forb & (1ull << c)) c++;
+    hc[e] = c;
+    ncol = c + 1 > ncol ? c + 1 : ncol;
+    for (int k = 0; k < PER; k++) used[v[k]] |= 1ull << c;
   }
-  // order by colour, element order within a colour
+  clk.mark(PER == 2 ? "bars coloured" : "hinges coloured");
+  int* col = S.upload(hc.data(), (size_t)nk);
+  // order by colour (element order within a colour)
   const int nbk = nblk(nk, 1024);
   int* bc = S.alloc<int>((size_t)(nbk ? nbk : 1) * 64);
-  int* off = S.alloc<int>((size_t)ncol + 1);
+  int* off = S.alloc<int>(65);
   int* perm = S.alloc<int>(nk);
   void* eo = S.alloc<char>((size_t)nk * esz);
   double2* po = S.alloc<double2>(nk);
@@ -719,6 +665,9 @@ int colour_elements(Scratch& S, const void* el, const double2* par, int ne, int 
   } else if (S.err == cudaSuccess) {
     S.err = cudaMemsetAsync(off, 0, sizeof(int), S.s);
   }
+  if (clk.on && S.err == cudaSuccess) S.err = cudaStreamSynchronize(S.s);
+  clk.mark(PER == 2 ? "bars ordered" : "hinges ordered");
+  if (clk.on) std::fprintf(stderr, "bah set-up %s: %d colours\n", PER == 2 ? "bars" : "hinges", ncol);
   S.keep(eo);
   S.keep(po);
   S.keep(off);
@@ -771,7 +720,9 @@ extern "C" int mg_bah_topology_device(const minim_gpu_bah_params* q, const doubl
     S.err = cudaGetLastError();
   }
   S.scan(nbv, boff, nvert);
+  PhaseClock clk;
   const int nb = S.read(boff + nvert);
+  clk.mark("bonds counted");
   if (S.err != cudaSuccess) return MG_TOPO_CUDA;
   if (S.read(flags)) return MG_TOPO_HOST;
   int2* bab = S.alloc<int2>(nb);
@@ -792,6 +743,7 @@ extern "C" int mg_bah_topology_device(const minim_gpu_bah_params* q, const doubl
   }
   S.scan(pc, poff, nb);
   const int np = S.read(poff + nb);
+  clk.mark("bonds written");
   if (S.err != cudaSuccess) return MG_TOPO_CUDA;
   if (S.read(flags)) return MG_TOPO_HOST;
   int2* pairs = S.alloc<int2>(np);
@@ -814,6 +766,7 @@ extern "C" int mg_bah_topology_device(const minim_gpu_bah_params* q, const doubl
   }
   S.scan(hc, hoff, ntri);
   const int nh = S.read(hoff + ntri);
+  clk.mark("hinges counted");
   if (S.err != cudaSuccess) return MG_TOPO_CUDA;
   // per-element arrays of the wrong length are the caller's error
   auto wrong = [&](int n, int want, const char* what) {
@@ -860,6 +813,7 @@ extern "C" int mg_bah_topology_device(const minim_gpu_bah_params* q, const doubl
     S.err = cudaGetLastError();
   }
   const int fl = S.read(flags);
+  clk.mark("hinges and parameters");
   if (S.err != cudaSuccess) return MG_TOPO_CUDA;
   if (fl & F_NOBOND) {
     set_err(err, errlen, "The hingeList should contain the index of the bond.");
