@@ -525,7 +525,9 @@ void do_minimise(minim_gpu_instance_s* h, const minim_gpu_minimiser_params& mp, 
   // the FP32 stage of a large binary PhaseField L-BFGS runs as the stepped graph
   const bool stepped_ok = stepped_cfg() && h->kk == K_PF1 && mp.method == MINIM_LBFGS &&
                           mp.precision != MINIM_PREC_FP64 && h->d.fixed == nullptr && h->n >= ((size_t)1 << 18);
-  const bool dual = stepped_ok && dual_cfg();
+  // two trials per pass; its graph sets up the line search in the first
+  // pass's controller, which has no step cap (Lbfgs::setMaxStep)
+  const bool dual = stepped_ok && dual_cfg() && mp.max_step == 0;
   WsLayout L = ws_layout(h->n, mp, dual);
   const size_t need = L.total + align256(sizeof(MinScalars));
   if (need > h->ws_bytes) {

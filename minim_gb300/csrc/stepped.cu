@@ -64,6 +64,7 @@ struct StepCtl {
   int mt;                    // pairs used by this iteration's direction
   int gmode;                 // two-trial graph: the next trial pass is the gradient at t only
   int retry;                 // two-trial graph: the next outer pass only continues the line search
+  int fresh;                 // two-trial graph: the next trial pass is the first of a new direction
   float fg;                  // -gamma
   float coefS[MINIM_MAXM], coefY[MINIM_MAXM];
   int so[MINIM_MAXM], yo[MINIM_MAXM];  // slot buffers: float4 offsets from the ring bases
@@ -368,8 +369,10 @@ k_dir_b(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, double* pa
       q = axpy4(cY[k], yv[k], q);
     }
     st4(P, i, q);
-    d1.add(dot4(q, g));
-    d2.add(dot4(q, q));
+    if (spec != 2) {
+      d1.add(dot4(q, g));
+      d2.add(dot4(q, q));
+    }
   }
   for (int i = 4 * nq4 + t0; i < n; i += nt) {
     const float g = G[i];
@@ -383,6 +386,9 @@ k_dir_b(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, double* pa
     d1.add(q * g);
     d2.add(q * q);
   }
+  // two-trial graph: g.P is summed by the first trial pass, whose
+  // controller does the set-up below, so this kernel ends here
+  if (spec == 2) return;
   double v[2] = {d1.total(), d2.total()};
   block_row<2>(v, part + (size_t)blockIdx.x * MINIM_WIDE);
   if (last_block(ctl)) ctl_b(d, st, ctl, part, gridDim.x, ls, grad, spec);
@@ -528,7 +534,7 @@ k_lines(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, double* pa
   float* Gb = DUAL ? d->Gs : nullptr;
   float* Yb2 = DUAL ? d->Yb + (long long)st->ybuf2 * d->hstride : nullptr;
   const float* Go = d->G[gi];
-  Acc e, gg, py, yy, e2, gg2, py2, yy2;
+  Acc e, gg, py, yy, e2, gg2, py2, yy2, gpa;
   if (zq < nz4) {
     for (int l = blockIdx.x * blockDim.y + threadIdx.y; l < nl; l += gridDim.x * blockDim.y) {
 
@@ -555,6 +561,7 @@ k_lines(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, double* pa
       float4 go = make_float4(0.f, 0.f, 0.f, 0.f);
       if (WANT_G) go = ld4(Go, q);
       float4 c4, gv;
+      if (DUAL) gpa.add(dot4(go, L.pc));  // g.P for the first pass of a direction
       e.add(quad_eval(L, t, K, WANT_G, c4, gv));
       if (WANT_G) {
         st4(Xa, q, c4);
@@ -578,8 +585,9 @@ k_lines(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, double* pa
     }
   }
   if (DUAL) {
-    double v[8] = {e.total(), gg.total(), py.total(), yy.total(), e2.total(), gg2.total(), py2.total(), yy2.total()};
-    block_row<8>(v, part + (size_t)blockIdx.x * MINIM_WIDE);
+    double v[9] = {e.total(),   gg.total(),  py.total(),  yy.total(), e2.total(),
+                   gg2.total(), py2.total(), yy2.total(), gpa.total()};
+    block_row<9>(v, part + (size_t)blockIdx.x * MINIM_WIDE);
   } else if (WANT_G) {
     double v[4] = {e.total(), gg.total(), py.total(), yy.total()};
     block_row<4>(v, part + (size_t)blockIdx.x * MINIM_WIDE);
@@ -682,6 +690,12 @@ __device__ void ctl_a(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* c
   }
   __syncwarp();
   if (lane == 0) {
+    // the two-trial graph's first pass tries the unit step along P at once
+    // and checks that P is a descent direction afterwards (fresh); the other
+    // graph's pass-B controller overwrites these
+    ctl->t = 1.0;
+    ctl->gmode = d->mp.linesearch == 0 ? 0 : 1;
+    ctl->fresh = 1;
     ctl->fg = (float)(-gamma);
     ctl->mt = mt;
     st->ii = ii;
@@ -914,9 +928,9 @@ __device__ void ctl_lsg(const InstDesc* __restrict__ d, MinScalars* st, StepCtl*
 __device__ void ctl_lsg2(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, const double* part,
                          int nb, cudaGraphConditionalHandle outer) {
   __shared__ double wide[8 * MINIM_WIDE];
-  __shared__ double v[8];
+  __shared__ double v[9];
   const unsigned warm = warm_ctl(d, st, ctl);
-  sum_rows_fixed(part, nb, 8, v, wide);
+  sum_rows_fixed(part, nb, 9, v, wide);
   warm_done(warm);
   __syncthreads();
   if (threadIdx.x != 0 || threadIdx.y != 0) return;
@@ -924,6 +938,24 @@ __device__ void ctl_lsg2(const InstDesc* __restrict__ d, MinScalars* st, StepCtl
   span_end(ctl, 0);
   ctl->kernels += 1;
   const double n = (double)d->ndof;
+  if (ctl->fresh) {
+    // the set-up of the line search (the other graph's ctl_b, without a step
+    // cap): when g.P > 0 the direction is reversed, and this pass, made at
+    // +P, is discarded and made again at -P
+    ctl->fresh = 0;
+    const double gp = v[8];
+    ctl->e0 = st->E;
+    ctl->k = 0;
+    ctl->exhausted = ctl->gmode ? 0 : 1;
+    ctl->thr = -0.5 * (gp > 0 ? -gp : gp);
+    if (gp > 0) {
+      ctl->t = -1.0;
+      ctl->retry = 1;
+      cudaGraphSetConditional(outer, 1u);
+      phase_mark(ctl);
+      return;
+    }
+  }
   if (ctl->gmode) {
     ctl->gmode = 0;
     ctl->retry = 0;

@@ -247,6 +247,39 @@ def test_pf_stepped_matches_persistent_path(switch):
     assert abs(r.iter - q["iter"]) <= 0.2 * q["iter"] + 10
 
 
+@pytest.mark.parametrize("extra", [{"max_step": 50.0}, {"linesearch": "none"}])
+def test_pf_stepped_options_match_persistent_path(extra):
+    """A step cap (the one-trial graph with pass B's set-up) and no line
+    search (the two-trial graph's gradient-only passes) against the
+    persistent kernel (separate process)."""
+    import json
+    import os
+    import subprocess
+    import sys
+    grid = (64, 64, 64)
+    x0 = pf_noise(grid, seed=28, amp=0.05)
+    p = abi.phase_field(grid, interface_size=1.0, surface_tension=1.0)
+    kw = dict(m=10, tol=1e-7, max_iter=20000, **extra)
+    r = runtime.Instance(p, x0).minimise(abi.minimiser("lbfgs", **kw))
+    code = (
+        "import json, sys; sys.path.insert(0, '.');"
+        "from minim_gb300 import abi, runtime; from tests.workloads import pf_noise;"
+        "g = (64, 64, 64); x0 = pf_noise(g, seed=28, amp=0.05);"
+        "i = runtime.Instance(abi.phase_field(g, interface_size=1.0, surface_tension=1.0), x0);"
+        f"r = i.minimise(abi.minimiser('lbfgs', **{kw!r}));"
+        "print(json.dumps({'status': r.status, 'iter': r.iter, 'energy': r.energy}))"
+    )
+    repo = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    out = subprocess.run([sys.executable, "-c", code], cwd=repo, env=dict(os.environ, MINIM_GPU_STEPPED="0"),
+                         capture_output=True, text=True, timeout=300)
+    assert out.returncode == 0, out.stderr
+    q = json.loads(out.stdout.strip().splitlines()[-1])
+    assert r.status == q["status"] == abi.RES_CONVERGED, (r.as_dict(), q)
+    e_init = Oracle(p, x0).energy(x0)
+    assert abs(r.energy - q["energy"]) <= 1e-8 * max(abs(r.energy), abs(e_init))
+    assert abs(r.iter - q["iter"]) <= 0.2 * q["iter"] + 10
+
+
 def test_pf_stepped_graph_reuse():
     """Instances of one shape share the cached stepped graph: the same input
     gives bitwise the same result before and after another instance ran."""
