@@ -176,30 +176,53 @@ __device__ void block_row(double (&v)[K], double* row) {
   }
 }
 
-// The controllers' thread 0 walks the state record, the control block and
-// the descriptor with dependent loads; fetching one word of each of their
-// 128-byte lines from the whole block first (while the partial rows are
-// summed) brings them into L1, so each of those loads is an L1 hit instead of
-// an L2 round trip.  Returns a value that the caller stores to shared memory
-// (so that the loads have completed before thread 0 starts).
-__device__ __forceinline__ unsigned warm_lines(const void* p, int bytes) {
+// The controllers mirror the state record and the control block in shared
+// memory: every thread of the block loads a few words (issued before the
+// partial rows are summed, so both wait on one memory round trip), thread 0
+// (warp 0 for pass A) runs the scalar logic on the copies, and every thread
+// writes them back.  Thread 0 working on global memory directly made one L2
+// round trip per dependent access (its own stores evict the lines it reads).
+struct Mirror {
+  MinScalars st;
+  StepCtl ctl;
+};
+constexpr int kMirrorWords = (int)(sizeof(Mirror) / 8);
+static_assert(sizeof(MinScalars) % 8 == 0 && sizeof(StepCtl) % 8 == 0, "mirror copies 8-byte words");
+constexpr int kMirrorRegs = 6;  // words per thread held in registers (blocks of >= 128 threads)
+struct MirrorRegs {
+  unsigned long long w[kMirrorRegs];
+};
+__device__ __forceinline__ const unsigned long long* mirror_src(const MinScalars* st, const StepCtl* ctl, int i) {
+  constexpr int ns = (int)(sizeof(MinScalars) / 8);
+  return i < ns ? reinterpret_cast<const unsigned long long*>(st) + i
+                : reinterpret_cast<const unsigned long long*>(ctl) + (i - ns);
+}
+__device__ __forceinline__ MirrorRegs mirror_load(const MinScalars* st, const StepCtl* ctl) {
   const int tl = threadIdx.y * blockDim.x + threadIdx.x, nt = blockDim.x * blockDim.y;
-  const char* c = static_cast<const char*>(p);
-  unsigned v = 0;
-  for (int o = tl * 128; o < bytes; o += nt * 128) {
-    unsigned w;
-    asm volatile("ld.global.ca.u32 %0, [%1];" : "=r"(w) : "l"(c + o));
-    v += w;
+  MirrorRegs r;
+#pragma unroll
+  for (int k = 0; k < kMirrorRegs; k++) {
+    const int i = tl + k * nt;
+    r.w[k] = i < kMirrorWords ? __ldcg(mirror_src(st, ctl, i)) : 0ull;
   }
-  return v;
+  return r;
 }
-__device__ __forceinline__ unsigned warm_ctl(const InstDesc* d, const MinScalars* st, const StepCtl* ctl) {
-  return warm_lines(st, (int)sizeof(MinScalars)) + warm_lines(ctl, (int)sizeof(StepCtl)) +
-         warm_lines(d, (int)sizeof(InstDesc));
+__device__ __forceinline__ void mirror_store(Mirror* m, const MirrorRegs& r, const MinScalars* st,
+                                             const StepCtl* ctl) {
+  const int tl = threadIdx.y * blockDim.x + threadIdx.x, nt = blockDim.x * blockDim.y;
+#pragma unroll
+  for (int k = 0; k < kMirrorRegs; k++) {
+    const int i = tl + k * nt;
+    if (i < kMirrorWords) reinterpret_cast<unsigned long long*>(m)[i] = r.w[k];
+  }
+  // words past the register batch (small blocks only)
+  for (int i = tl + kMirrorRegs * nt; i < kMirrorWords; i += nt)
+    reinterpret_cast<unsigned long long*>(m)[i] = __ldcg(mirror_src(st, ctl, i));
 }
-__device__ __forceinline__ void warm_done(unsigned w) {
-  __shared__ unsigned sink[32];
-  sink[threadIdx.x & 31] = w;
+__device__ __forceinline__ void mirror_out(const Mirror* m, MinScalars* st, StepCtl* ctl) {
+  const int tl = threadIdx.y * blockDim.x + threadIdx.x, nt = blockDim.x * blockDim.y;
+  for (int i = tl; i < kMirrorWords; i += nt)
+    *const_cast<unsigned long long*>(mirror_src(st, ctl, i)) = reinterpret_cast<const unsigned long long*>(m)[i];
 }
 
 // controllers, run by the last block of each phase kernel (defined below)
@@ -633,60 +656,90 @@ __device__ __forceinline__ void phase_mark(StepCtl* ctl) {
 }
 
 // dirA sums, the compact-form algebra of getDirection, pass-B coefficients
-__device__ void ctl_a(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, const double* part, int nb) {
+__device__ void ctl_a(const InstDesc* __restrict__ d, MinScalars* st_g, StepCtl* ctl_g, const double* part, int nb) {
   __shared__ double wide[8 * MINIM_WIDE];
   __shared__ double wout[MINIM_WIDE];
-  const unsigned warm = warm_ctl(d, st, ctl);
+  __shared__ Mirror mir;
+  const MirrorRegs mr = mirror_load(st_g, ctl_g);
   sum_rows_fixed(part, nb, MINIM_WIDE, wout, wide);
-  warm_done(warm);
+  mirror_store(&mir, mr, st_g, ctl_g);
   __syncthreads();
+  MinScalars* st = &mir.st;
+  StepCtl* ctl = &mir.ctl;
   // warp 0: the algebra (lbfgs_compact_warp), lane k on pair k
   const int lane = threadIdx.y * blockDim.x + threadIdx.x;
-  if (lane >= 32) return;
+  if (lane < 32) [&] {
   if (lane == 0) {
     phase_time(st, ctl, 2);
     span_end(ctl, 2);
   }
   const int m = d->mp.m, n = d->ndof;
   const long long hs = d->hstride;
-  const int ii = st->ii + 1, mt = ii < m ? ii : m, c = ii % m, kn = (c - 1 + m) % m;
+  const int ii = st->ii + 1, mt = ii < m ? ii : m, c = ii % m;
   const int pend = st->pend;
   double(*SY)[MINIM_MAXM] = st->SY;
   double(*YY)[MINIM_MAXM] = st->YY;
   const bool on = lane < mt;
   const int slk = on ? ring_slot(c, mt, lane, m) : 0;
-  double sg = 0.0, yg = 0.0;
-  if (on) {
-    sg = st->sigma[slk] * wout[lane];
-    yg = wout[MINIM_MAXM + lane];
-    if (pend >= 0) {
-      SY[slk][pend] = st->sigma[slk] * wout[2 * MINIM_MAXM + lane];
-      YY[slk][pend] = wout[3 * MINIM_MAXM + lane];
-      YY[pend][slk] = wout[3 * MINIM_MAXM + lane];
-    }
-  }
-  __threadfence_block();
-  __syncwarp();
-  // the mt x mt blocks of S^T Y and Y^T Y in age order, staged in shared memory
+  // the mt x mt blocks of S^T Y and Y^T Y in age order, staged in shared
+  // memory from the state record; the newest pair's column (pend, the last
+  // in age order) is then set from this pass's sums and written back, so
+  // nothing is read back from global memory after being written.  Every
+  // lane issues all its loads (up to 8 entries of each, its pair's scalars)
+  // before using any: one memory round trip instead of one per entry.
   double* Rs = wide;
   double* Ys = wide + MINIM_MAXM * MINIM_MAXM;
-  for (int e = lane; e < mt * mt; e += 32) {
-    const int a = e / mt, b = e - a * mt;
-    const int sa = ring_slot(c, mt, a, m), sb = ring_slot(c, mt, b, m);
-    Rs[a * MINIM_MAXM + b] = SY[sa][sb];
-    Ys[a * MINIM_MAXM + b] = YY[sa][sb];
+  double rv[8], yv[8];
+  const int ne = mt * mt;
+#pragma unroll
+  for (int j = 0; j < 8; j++) {
+    const int e = lane + 32 * j;
+    rv[j] = 0.0;
+    yv[j] = 0.0;
+    if (e < ne) {
+      const int a = e / mt, b = e - a * mt;
+      const int sa = ring_slot(c, mt, a, m), sb = ring_slot(c, mt, b, m);
+      rv[j] = SY[sa][sb];
+      yv[j] = YY[sa][sb];
+    }
+  }
+  const double sig = on ? st->sigma[slk] : 0.0;
+  const int sid = on ? st->sidx[slk] : 0, yid = on ? st->yidx[slk] : 0;
+#pragma unroll
+  for (int j = 0; j < 8; j++) {
+    const int e = lane + 32 * j;
+    if (e < ne) {
+      const int a = e / mt, b = e - a * mt;
+      Rs[a * MINIM_MAXM + b] = rv[j];
+      Ys[a * MINIM_MAXM + b] = yv[j];
+    }
   }
   __syncwarp();
-  const double gamma = SY[kn][kn] / YY[kn][kn];
+  double sg = 0.0, yg = 0.0;
+  if (on) {
+    sg = sig * wout[lane];
+    yg = wout[MINIM_MAXM + lane];
+    if (pend >= 0) {  // pend == kn: age index mt - 1
+      const double syn = sig * wout[2 * MINIM_MAXM + lane], yyn = wout[3 * MINIM_MAXM + lane];
+      Rs[lane * MINIM_MAXM + mt - 1] = syn;
+      Ys[lane * MINIM_MAXM + mt - 1] = yyn;
+      Ys[(mt - 1) * MINIM_MAXM + lane] = yyn;
+      SY[slk][pend] = syn;
+      YY[slk][pend] = yyn;
+      YY[pend][slk] = yyn;
+    }
+  }
+  __syncwarp();
+  const double gamma = Rs[(mt - 1) * (MINIM_MAXM + 1)] / Ys[(mt - 1) * (MINIM_MAXM + 1)];
   double u, w;
   lbfgs_compact_warp(
       mt, gamma, sg, yg, [=](int a, int b) { return Rs[a * MINIM_MAXM + b]; },
       [=](int a, int b) { return Ys[a * MINIM_MAXM + b]; }, u, w);
   if (lane < MINIM_MAXM) {
-    ctl->coefS[lane] = on ? (float)(-w * st->sigma[slk]) : 0.f;
+    ctl->coefS[lane] = on ? (float)(-w * sig) : 0.f;
     ctl->coefY[lane] = on ? (float)(gamma * u) : 0.f;
-    ctl->so[lane] = on ? (int)(((long long)st->sidx[slk] * hs) >> 2) : 0;
-    ctl->yo[lane] = on ? (int)(((long long)st->yidx[slk] * hs) >> 2) : 0;
+    ctl->so[lane] = on ? (int)(((long long)sid * hs) >> 2) : 0;
+    ctl->yo[lane] = on ? (int)(((long long)yid * hs) >> 2) : 0;
   }
   __syncwarp();
   if (lane == 0) {
@@ -703,18 +756,24 @@ __device__ void ctl_a(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* c
     st->abytes += (4.0 * mt + 2.0) * 4.0 * n;
     phase_mark(ctl);
   }
+  }();
+  __syncthreads();
+  mirror_out(&mir, st_g, ctl_g);
 }
 
 // dirB sums: step cap, descent check, line-search set-up
-__device__ void ctl_b(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, const double* part, int nb,
+__device__ void ctl_b(const InstDesc* __restrict__ d, MinScalars* st_g, StepCtl* ctl_g, const double* part, int nb,
                       cudaGraphConditionalHandle ls, cudaGraphConditionalHandle grad, int spec) {
   __shared__ double wide[8 * MINIM_WIDE];
   __shared__ double v[2];
-  const unsigned warm = warm_ctl(d, st, ctl);
+  __shared__ Mirror mir;
+  const MirrorRegs mr = mirror_load(st_g, ctl_g);
   sum_rows_fixed(part, nb, 2, v, wide);
-  warm_done(warm);
+  mirror_store(&mir, mr, st_g, ctl_g);
   __syncthreads();
-  if (threadIdx.x != 0 || threadIdx.y != 0) return;
+  MinScalars* st = &mir.st;
+  StepCtl* ctl = &mir.ctl;
+  if (threadIdx.x == 0 && threadIdx.y == 0) [&] {
   phase_time(st, ctl, 2);
   span_end(ctl, 3);
   double gp = v[0], scale = 1.0;
@@ -754,19 +813,25 @@ __device__ void ctl_b(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* c
     if (spec) cudaGraphSetConditional(grad, 1u);
   }
   phase_mark(ctl);
+  }();
+  __syncthreads();
+  mirror_out(&mir, st_g, ctl_g);
 }
 
 // one line-search trial: Armijo test, or halve the step (10 trials at most;
 // after the last failure the halved step is taken unevaluated)
-__device__ void ctl_ls(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, const double* part, int nb,
+__device__ void ctl_ls(const InstDesc* __restrict__ d, MinScalars* st_g, StepCtl* ctl_g, const double* part, int nb,
          cudaGraphConditionalHandle ls) {
   __shared__ double wide[8 * MINIM_WIDE];
   __shared__ double v[1];
-  const unsigned warm = warm_ctl(d, st, ctl);
+  __shared__ Mirror mir;
+  const MirrorRegs mr = mirror_load(st_g, ctl_g);
   sum_rows_fixed(part, nb, 1, v, wide);
-  warm_done(warm);
+  mirror_store(&mir, mr, st_g, ctl_g);
   __syncthreads();
-  if (threadIdx.x != 0 || threadIdx.y != 0) return;
+  MinScalars* st = &mir.st;
+  StepCtl* ctl = &mir.ctl;
+  if (threadIdx.x == 0 && threadIdx.y == 0) [&] {
   phase_time(st, ctl, 1);
   span_end(ctl, 0);
   st->evals++;
@@ -783,6 +848,9 @@ __device__ void ctl_ls(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* 
   }
   cudaGraphSetConditional(ls, more ? 1u : 0u);
   phase_mark(ctl);
+  }();
+  __syncthreads();
+  mirror_out(&mir, st_g, ctl_g);
 }
 
 // The pair update of Lbfgs::iteration with the sums {E, g.g, P.y, y.y} of
@@ -857,21 +925,27 @@ __device__ void commit_grad(const InstDesc* __restrict__ d, MinScalars* st, Step
 
 // gradient sums: the pair update of Lbfgs::iteration, then the end-of-
 // iteration decision (continue here, or hand over to the persistent kernel)
-__device__ void ctl_g(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, const double* part, int nb,
+__device__ void ctl_g(const InstDesc* __restrict__ d, MinScalars* st_g, StepCtl* ctl_g, const double* part, int nb,
         cudaGraphConditionalHandle outer) {
   __shared__ double wide[8 * MINIM_WIDE];
   __shared__ double v[4];
-  const unsigned warm = warm_ctl(d, st, ctl);
+  __shared__ Mirror mir;
+  const MirrorRegs mr = mirror_load(st_g, ctl_g);
   sum_rows_fixed(part, nb, 4, v, wide);
-  warm_done(warm);
+  mirror_store(&mir, mr, st_g, ctl_g);
   __syncthreads();
-  if (threadIdx.x != 0 || threadIdx.y != 0) return;
+  MinScalars* st = &mir.st;
+  StepCtl* ctl = &mir.ctl;
+  if (threadIdx.x == 0 && threadIdx.y == 0) [&] {
   phase_time(st, ctl, 0);
   span_end(ctl, 1);
   st->evals++;
   st->abytes += 24.0 * d->ndof;
   ctl->kernels += 3;
   commit_grad(d, st, ctl, v, outer);
+  }();
+  __syncthreads();
+  mirror_out(&mir, st_g, ctl_g);
 }
 
 // A line-search trial that also evaluated the gradient at its point (x, g
@@ -879,16 +953,19 @@ __device__ void ctl_g(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* c
 // gradient is the accepted point's and the iteration completes here; when
 // it fails the step is halved (10 trials at most, after which the halved
 // step is taken unevaluated and the gradient kernel runs).
-__device__ void ctl_lsg(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, const double* part,
+__device__ void ctl_lsg(const InstDesc* __restrict__ d, MinScalars* st_g, StepCtl* ctl_g, const double* part,
                         int nb, cudaGraphConditionalHandle ls, cudaGraphConditionalHandle grad,
                         cudaGraphConditionalHandle outer) {
   __shared__ double wide[8 * MINIM_WIDE];
   __shared__ double v[4];
-  const unsigned warm = warm_ctl(d, st, ctl);
+  __shared__ Mirror mir;
+  const MirrorRegs mr = mirror_load(st_g, ctl_g);
   sum_rows_fixed(part, nb, 4, v, wide);
-  warm_done(warm);
+  mirror_store(&mir, mr, st_g, ctl_g);
   __syncthreads();
-  if (threadIdx.x != 0 || threadIdx.y != 0) return;
+  MinScalars* st = &mir.st;
+  StepCtl* ctl = &mir.ctl;
+  if (threadIdx.x == 0 && threadIdx.y == 0) [&] {
   phase_time(st, ctl, 1);
   span_end(ctl, 0);
   st->evals++;
@@ -913,6 +990,9 @@ __device__ void ctl_lsg(const InstDesc* __restrict__ d, MinScalars* st, StepCtl*
     cudaGraphSetConditional(grad, more ? 0u : 1u);
     phase_mark(ctl);
   }
+  }();
+  __syncthreads();
+  mirror_out(&mir, st_g, ctl_g);
 }
 
 // Two consecutive trials of the backtracking sequence from one pass (t and
@@ -925,15 +1005,18 @@ __device__ void ctl_lsg(const InstDesc* __restrict__ d, MinScalars* st, StepCtl*
 // A pass that completes no iteration sets `retry`: the outer loop runs once
 // more with the direction kernels returning at once, so the common pass
 // (one of the two trials accepted) costs one conditional node, not two.
-__device__ void ctl_lsg2(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, const double* part,
+__device__ void ctl_lsg2(const InstDesc* __restrict__ d, MinScalars* st_g, StepCtl* ctl_g, const double* part,
                          int nb, cudaGraphConditionalHandle outer) {
   __shared__ double wide[8 * MINIM_WIDE];
   __shared__ double v[9];
-  const unsigned warm = warm_ctl(d, st, ctl);
+  __shared__ Mirror mir;
+  const MirrorRegs mr = mirror_load(st_g, ctl_g);
   sum_rows_fixed(part, nb, 9, v, wide);
-  warm_done(warm);
+  mirror_store(&mir, mr, st_g, ctl_g);
   __syncthreads();
-  if (threadIdx.x != 0 || threadIdx.y != 0) return;
+  MinScalars* st = &mir.st;
+  StepCtl* ctl = &mir.ctl;
+  if (threadIdx.x == 0 && threadIdx.y == 0) [&] {
   phase_time(st, ctl, 1);
   span_end(ctl, 0);
   ctl->kernels += 1;
@@ -1000,6 +1083,9 @@ __device__ void ctl_lsg2(const InstDesc* __restrict__ d, MinScalars* st, StepCtl
   ctl->retry = 1;
   cudaGraphSetConditional(outer, 1u);
   phase_mark(ctl);
+  }();
+  __syncthreads();
+  mirror_out(&mir, st_g, ctl_g);
 }
 
 int occupancy(const void* f, int threads) {
