@@ -377,7 +377,10 @@ k_dir_b(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, double* pa
   }
   Acc d1, d2;
   const int t0 = blockIdx.x * blockDim.x + threadIdx.x, nt = gridDim.x * blockDim.x;
-  for (int i = t0; i < nq4; i += nt) {
+  // the sweep runs from the end of the vectors down: pass A swept upwards,
+  // so the vectors' last ~100 MB it read are still in L2
+  for (int r = t0; r < nq4; r += nt) {
+    const int i = nq4 - 1 - r;
     const float4 g = ld4(G, i);
     float4 sv[M], yv[M];
 #pragma unroll
@@ -566,21 +569,24 @@ k_lines(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, double* pa
       const int lxm = (x == 0 ? nx - 1 : x - 1) * ny + y, lxp = (x == nx - 1 ? 0 : x + 1) * ny + y;
       const int q = l * nz4 + zq;
       // every load of the quad first
+      auto load_quad = [&](QuadLoads& L) {
+        L.xc = ld4(X, q);
+        L.pc = ld4(Pd, q);
+        L.xzm = X[l * nz + izm];
+        L.pzm = Pd[l * nz + izm];
+        L.xzp = X[l * nz + izp];
+        L.pzp = Pd[l * nz + izp];
+        L.xym = ld4(X, lym * nz4 + zq);
+        L.pym = ld4(Pd, lym * nz4 + zq);
+        L.xyp = ld4(X, lyp * nz4 + zq);
+        L.pyp = ld4(Pd, lyp * nz4 + zq);
+        L.xxm = ld4(X, lxm * nz4 + zq);
+        L.pxm = ld4(Pd, lxm * nz4 + zq);
+        L.xxp = ld4(X, lxp * nz4 + zq);
+        L.pxp = ld4(Pd, lxp * nz4 + zq);
+      };
       QuadLoads L;
-      L.xc = ld4(X, q);
-      L.pc = ld4(Pd, q);
-      L.xzm = X[l * nz + izm];
-      L.pzm = Pd[l * nz + izm];
-      L.xzp = X[l * nz + izp];
-      L.pzp = Pd[l * nz + izp];
-      L.xym = ld4(X, lym * nz4 + zq);
-      L.pym = ld4(Pd, lym * nz4 + zq);
-      L.xyp = ld4(X, lyp * nz4 + zq);
-      L.pyp = ld4(Pd, lyp * nz4 + zq);
-      L.xxm = ld4(X, lxm * nz4 + zq);
-      L.pxm = ld4(Pd, lxm * nz4 + zq);
-      L.xxp = ld4(X, lxp * nz4 + zq);
-      L.pxp = ld4(Pd, lxp * nz4 + zq);
+      load_quad(L);
       float4 go = make_float4(0.f, 0.f, 0.f, 0.f);
       if (WANT_G) go = ld4(Go, q);
       float4 c4, gv;
