@@ -450,6 +450,22 @@ def run_profile_case(iters):
                       "abytes_per_launch": st["abytes"] / max(st["launches"], 1), "status": r.status}))
 
 
+def run_profile_lj(iters):
+    """One batch launch of 304 Lennard-Jones clusters (N=300, Fire(0.1), FP32
+    coordinates, `iters` iterations each) for profiler captures of the batched
+    kernel."""
+    from minim_gb300 import abi, runtime
+    from tests.workloads import lj_cluster
+    insts = [runtime.Instance(abi.lj(), lj_cluster(300, seed=i)) for i in range(304)]
+    b = runtime.Batch()
+    for a in insts:
+        b.add(a, abi.minimiser("fire", dt_max=0.1, tol=1e-12, max_iter=iters, precision="fp32"))
+    b.run(threads=256)
+    st = runtime.last_run_stats()
+    print(json.dumps({"profile_case": "304 LJ clusters N=300 Fire(0.1) fp32", "iterations": st["iterations"],
+                      "kernel_ms": st["kernel_ms"], "launches": st["launches"]}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -468,9 +484,14 @@ def main():
                     help="iterations of a full minimisation (the GPU run of the same algorithm needs 981-987)")
     ap.add_argument("--profile", type=int, default=0,
                     help="run one short minimisation of N iterations (profiler capture) and exit")
+    ap.add_argument("--profile-lj", type=int, default=0,
+                    help="run one batch of 304 LJ clusters for N iterations (profiler capture) and exit")
     args = ap.parse_args()
     if args.profile:
         run_profile_case(args.profile)
+        return
+    if args.profile_lj:
+        run_profile_lj(args.profile_lj)
         return
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
