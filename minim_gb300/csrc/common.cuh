@@ -366,6 +366,32 @@ struct StageRing {
 // ---------------------------------------------------------------------------
 // Team = one CTA
 // ---------------------------------------------------------------------------
+// Sum of two compensated FP32 partial sums (s, c): TwoSum of the running
+// sums, errors added (the combination Acc::add uses).  Symmetric in its
+// arguments, so both lanes of a butterfly exchange get the same result.
+__device__ __forceinline__ void pair_add(float& s, float& c, float s2, float c2) {
+  const float t = __fadd_rn(s, s2);
+  const float bp = __fsub_rn(t, s);
+  const float err = __fadd_rn(__fsub_rn(s, __fsub_rn(t, bp)), __fsub_rn(s2, bp));
+  c = __fadd_rn(__fadd_rn(c, c2), err);
+  s = t;
+}
+__device__ __forceinline__ void warp_pair_sum(float& s, float& c) {
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    const float s2 = __shfl_xor_sync(0xffffffffu, s, off), c2 = __shfl_xor_sync(0xffffffffu, c, off);
+    pair_add(s, c, s2, c2);
+  }
+}
+// A double as such a pair (exact for the sum of an Acc's two floats)
+__device__ __forceinline__ void to_pair(double v, float& s, float& c) {
+  s = (float)v;
+  c = (float)(v - (double)s);
+}
+struct NoPost {
+  __device__ void operator()(double*) const {}
+};
+
 struct CtaTeam {
   // thread index and count come from special registers, never from memory
   __device__ __forceinline__ int tid() const { return threadIdx.x; }
@@ -396,6 +422,43 @@ struct CtaTeam {
     __syncthreads();
 #pragma unroll
     for (int k = 0; k < K; k++) v[k] = red[32 * MINIM_MAXRED + k];
+    __syncthreads();
+  }
+
+  // The team sums of K compensated FP32 partials (s[k], c[k]) with FP32
+  // butterflies inside the warps; warp 0 alone forms the FP64 totals over the
+  // warps (fixed order), and its thread 0 runs post(totals) to append D
+  // derived values (e.g. square roots), so that no other warp issues an FP64
+  // instruction.  out[0..K+D) receives totals and derived values.
+  template <int K, int D = 0, class Post = NoPost>
+  __device__ void reduce_pairs(float (&s)[K], float (&c)[K], double (&out)[K + D], Post post = Post{}) {
+    static_assert(K + D <= MINIM_MAXRED, "too many values");
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    float* rf = reinterpret_cast<float*>(red);  // [warp][2K] floats, before the totals
+    double* tot = red + 32 * MINIM_MAXRED;
+#pragma unroll
+    for (int k = 0; k < K; k++) warp_pair_sum(s[k], c[k]);
+    if (lane == 0) {
+#pragma unroll
+      for (int k = 0; k < K; k++) {
+        rf[w * 2 * MINIM_MAXRED + 2 * k] = s[k];
+        rf[w * 2 * MINIM_MAXRED + 2 * k + 1] = c[k];
+      }
+    }
+    __syncthreads();
+    if (threadIdx.x < 32) {
+      if (lane < K) {
+        double t = 0.0;
+        for (int i = 0; i < nw; i++)
+          t += (double)rf[i * 2 * MINIM_MAXRED + 2 * lane] + (double)rf[i * 2 * MINIM_MAXRED + 2 * lane + 1];
+        tot[lane] = t;
+      }
+      __syncwarp();
+      if (lane == 0) post(tot);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < K + D; k++) out[k] = tot[k];
     __syncthreads();
   }
 
@@ -577,6 +640,40 @@ struct GridTeam {
     arrive_release(K, red + 32 * MINIM_MAXRED);
 #pragma unroll
     for (int k = 0; k < K; k++) v[k] = red[32 * MINIM_MAXRED + k];
+    __syncthreads();
+  }
+
+  // As CtaTeam::reduce_pairs: the block's sums from FP32 butterflies and warp
+  // 0, the grid's from every block's partial row (fixed order), then post in
+  // thread 0 of every block (all blocks hold the same totals).
+  template <int K, int D = 0, class Post = NoPost>
+  __device__ void reduce_pairs(float (&s)[K], float (&c)[K], double (&out)[K + D], Post post = Post{}) {
+    static_assert(K + D <= MINIM_MAXRED, "too many values");
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    float* rf = reinterpret_cast<float*>(red);
+    double* tot = red + 32 * MINIM_MAXRED;
+#pragma unroll
+    for (int k = 0; k < K; k++) warp_pair_sum(s[k], c[k]);
+    if (lane == 0) {
+#pragma unroll
+      for (int k = 0; k < K; k++) {
+        rf[w * 2 * MINIM_MAXRED + 2 * k] = s[k];
+        rf[w * 2 * MINIM_MAXRED + 2 * k + 1] = c[k];
+      }
+    }
+    __syncthreads();
+    double* P = partials + (size_t)buf * gridDim.x * MINIM_WIDE;
+    if (threadIdx.x < K) {
+      double t = 0.0;
+      for (int i = 0; i < nw; i++)
+        t += (double)rf[i * 2 * MINIM_MAXRED + 2 * threadIdx.x] + (double)rf[i * 2 * MINIM_MAXRED + 2 * threadIdx.x + 1];
+      P[blockIdx.x * MINIM_WIDE + threadIdx.x] = t;
+    }
+    arrive_release(K, tot);
+    if (threadIdx.x == 0) post(tot);
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < K + D; k++) out[k] = tot[k];
     __syncthreads();
   }
 

@@ -93,6 +93,14 @@ struct StoreEmit64 {
   }
 };
 
+// Work counters and phase timers are only read from thread 0 (which stores
+// the state): only thread 0 updates them, so the other threads issue no FP64
+// instruction for them (FP64 runs at 1/64 of the FP32 rate on GB300).
+#define MG_ACCT(ctr, expr)            \
+  do {                                \
+    if (threadIdx.x == 0) (ctr) += (expr); \
+  } while (0)
+
 template <class Team, int KIND>
 struct Runner {
   Team& tm;
@@ -103,6 +111,7 @@ struct Runner {
   int n, status, initd, iter, ii, stage, xi, gi, evals, fp64_iters, stall, nsteps, pbuf, ybuf;
   int exhausted_run, switch_reason, pend, cool, resume, resume_exhausted;
   double E, gg, best_rms, dt, a, dtmax, gnorm;
+  double rms_v, gnorm_v;  // sqrt(gg / n) and sqrt(gg) of the current gradient
   double abytes, pairs32, pairs64;
   double tph[3];
   // shared arrays (one copy per block; written by thread 0 between barriers)
@@ -133,13 +142,15 @@ struct Runner {
   // one potential evaluation: coordinates read (plus the direction for a
   // trial point), gradient written; pair count for Lennard-Jones
   __device__ void count_eval(bool trial, bool want_g) {
+    if (threadIdx.x != 0) return;
     double b = xbytes() + (trial ? 4.0 : 0.0) + (want_g ? 4.0 : 0.0);
     if constexpr (KIND == K_LJ) {
       const double np = in.lj.np;
       const double pairs = want_g ? np * (np - 1) : 0.5 * np * (np - 1);
-      if (stage) pairs64 += pairs; else pairs32 += pairs;
+      if (stage) MG_ACCT(pairs64, pairs);
+      else MG_ACCT(pairs32, pairs);
     }
-    abytes += b * n;
+    MG_ACCT(abytes, b * n);
   }
 
   // ---- potential dispatch -------------------------------------------------------
@@ -201,19 +212,43 @@ struct Runner {
         }
       }
     }
-    double v[4] = {ep, em.gg.total(), em.py.total(), em.yy.total()};
-    tm.reduce(v);
-    E = v[0];
-    gg = v[1];
-    py = v[2];
-    yyv = v[3];
+    if (stage == 0) {
+      // FP32 partials summed as FP32 pairs; the square roots of the gradient
+      // norm once per team (warp 0), not in every thread
+      float ps[4], pc[4];
+      to_pair(ep, ps[0], pc[0]);
+      ps[1] = em.gg.s; pc[1] = em.gg.c;
+      ps[2] = em.py.s; pc[2] = em.py.c;
+      ps[3] = em.yy.s; pc[3] = em.yy.c;
+      const double nd = (double)n;
+      double v[6];
+      tm.template reduce_pairs<4, 2>(ps, pc, v, [nd](double* o) {
+        o[4] = sqrt(o[1] / nd);
+        o[5] = sqrt(o[1]);
+      });
+      E = v[0];
+      gg = v[1];
+      py = v[2];
+      yyv = v[3];
+      rms_v = v[4];
+      gnorm_v = v[5];
+    } else {
+      double v[4] = {ep, em.gg.total(), em.py.total(), em.yy.total()};
+      tm.reduce(v);
+      E = v[0];
+      gg = v[1];
+      py = v[2];
+      yyv = v[3];
+      rms_v = sqrt(gg / n);
+      gnorm_v = sqrt(gg);
+    }
     evals++;
     count_eval(P != nullptr, true);
-    if (write_x) abytes += xbytes() * n;
-    if (want_y) abytes += 8.0 * n;
+    if (write_x) MG_ACCT(abytes, xbytes() * n);
+    if (want_y) MG_ACCT(abytes, 8.0 * n);
     gi = 1 - gi;
     if (write_x) xi = 1 - xi;
-    tph[0] += (double)(globaltimer_ns() - t_start);
+    MG_ACCT(tph[0], (double)(globaltimer_ns() - t_start));
   }
 
   __device__ double energy_at(double t, const float* P) {
@@ -228,10 +263,16 @@ struct Runner {
       ep = pot_eval<double>(cv, nullptr, ne, true, false);
     }
     double v[1] = {ep};
-    tm.reduce(v);
+    if (stage == 0) {
+      float ps[1], pc[1];
+      to_pair(ep, ps[0], pc[0]);
+      tm.template reduce_pairs<1>(ps, pc, v);
+    } else {
+      tm.reduce(v);
+    }
     evals++;
     count_eval(P != nullptr, false);
-    tph[1] += (double)(globaltimer_ns() - t_start);
+    MG_ACCT(tph[1], (double)(globaltimer_ns() - t_start));
     return v[0];
   }
 
@@ -241,8 +282,9 @@ struct Runner {
     Acc d;
     for (int i = tm.tid(); i < n4(); i += tm.nthr()) d.add(dot4(ld4(G, i), ld4(P, i)));
     for (int i = 4 * n4() + tm.tid(); i < n; i += tm.nthr()) d.add(G[i] * P[i]);
-    double v[1] = {d.total()};
-    tm.reduce(v);
+    float ps[1] = {d.s}, pc[1] = {d.c};
+    double v[1];
+    tm.template reduce_pairs<1>(ps, pc, v);
     return v[0];
   }
 
@@ -312,8 +354,8 @@ struct Runner {
       }
       for (int i = 4 * n4() + tm.tid(); i < n; i += tm.nthr()) P[i] = -G[i];
       tm.sync();
-      abytes += 8.0 * n;
-      const double gn = sqrt(gg);
+      MG_ACCT(abytes, 8.0 * n);
+      const double gn = gnorm_v;
       const double scale = gn > 0 ? in.mp.init_step / gn : 1.0;
       gp = -gg * scale;
       return scale;
@@ -321,7 +363,7 @@ struct Runner {
     const int mt = ii < m ? ii : m;
     const int c = ii % m;
     const int kn = (c - 1 + m) % m;  // newest slot
-    abytes += (4.0 * mt + 2.0) * 4.0 * n;
+    MG_ACCT(abytes, (4.0 * mt + 2.0) * 4.0 * n);
     const bool np = pend >= 0;
     const bool staged = stage_chunk(2 + 2 * mt) > 0;
     if (staged) pass_a_staged(G, mt, c, np);
@@ -329,10 +371,14 @@ struct Runner {
     if (!tm.ok()) return 1.0;
     direction_algebra(mt, c, kn, np);
     pend = -1;
+    Acc pv[2];
+    if (staged && stage_chunk(1 + 2 * mt) > 0) pass_b_staged(G, P, mt, pv);
+    else pass_b_plain(G, P, mt, pv);
     double v[2];
-    if (staged && stage_chunk(1 + 2 * mt) > 0) pass_b_staged(G, P, mt, v);
-    else pass_b_plain(G, P, mt, v);
-    tm.reduce(v);
+    {
+      float ps[2] = {pv[0].s, pv[1].s}, pc[2] = {pv[0].c, pv[1].c};
+      tm.template reduce_pairs<2>(ps, pc, v);
+    }
     gp = v[0];
     double scale = 1.0;
     if (in.mp.max_step != 0) {
@@ -564,7 +610,7 @@ struct Runner {
 
   // pass B: P = -(gamma g + S w - gamma Y u), with g.P and P.P; the slot
   // buffers and coefficients are read from shared memory (broadcast)
-  __device__ __noinline__ void pass_b_plain(const float* G, float* P, int mt, double (&v)[2]) {
+  __device__ __noinline__ void pass_b_plain(const float* G, float* P, int mt, Acc (&v)[2]) {
     const int nn = n, nq4 = n >> 2, t0 = tm.tid(), nt = tm.nthr(), pd = in.pf_dist * nt;
     const float fg = (float)(-wout[MINIM_WIDE - 1]);
     // slot buffers as 32-bit float4 offsets from the ring bases (the host
@@ -616,13 +662,13 @@ struct Runner {
       d1.add(q * g);
       d2.add(q * q);
     }
-    v[0] = d1.total();
-    v[1] = d2.total();
+    v[0] = d1;
+    v[1] = d2;
   }
 
   // pass B through shared memory: g, S_0..S_mt-1, Y_0..Y_mt-1 arrive chunk by
   // chunk; P is written straight to global memory
-  __device__ __noinline__ void pass_b_staged(const float* G, float* P, int mt, double (&v)[2]) {
+  __device__ __noinline__ void pass_b_staged(const float* G, float* P, int mt, Acc (&v)[2]) {
     if constexpr (Team::kGrid) {
       const int nv = 1 + 2 * mt;
       auto vec = [&](int k) -> const float* {
@@ -663,8 +709,8 @@ struct Runner {
         rg.release(vec);
       }
       ring_done(rg);
-      v[0] = d1.total();
-      v[1] = d2.total();
+      v[0] = d1;
+      v[1] = d2;
     }
   }
 
@@ -680,7 +726,7 @@ struct Runner {
     double gp;
     const unsigned long long t_dir = globaltimer_ns();
     double scale = lbfgs_direction(gp);
-    tph[2] += (double)(globaltimer_ns() - t_dir);
+    MG_ACCT(tph[2], (double)(globaltimer_ns() - t_dir));
     float* P = Sbuf(pbuf);
     if (has_constraints()) gp = scale * constrain_dir(P);
     double gs = gp;
@@ -716,7 +762,7 @@ struct Runner {
     if (iter == 0) {
       dt = dtmax;
       grad_eval(0.0, nullptr, false, false, py, yyv);
-      gnorm = sqrt(gg);
+      gnorm = gnorm_v;
     }
     const float* G = in.G[gi];
     float* Vv = in.V;
@@ -732,15 +778,23 @@ struct Runner {
       d1.add(v * G[i]);
       d2.add(v * v);
     }
-    double r[2] = {d1.total(), d2.total()};
-    tm.reduce(r);
-    abytes += 8.0 * n;
+    // v.g and v.v as FP32 pairs; |v| and the FIRE mixing factor a |v| / |g|
+    // + dt once per team (thread 0 of warp 0)
+    double r[4];
+    {
+      float ps[2] = {d1.s, d2.s}, pc[2] = {d1.c, d2.c};
+      const double a_ = a, gn_ = gnorm, dt_ = dt;
+      tm.template reduce_pairs<2, 2>(ps, pc, r, [a_, gn_, dt_](double* o) {
+        o[2] = sqrt(o[1]);
+        o[3] = a_ * o[2] / gn_ + dt_;
+      });
+    }
+    MG_ACCT(abytes, 8.0 * n);
     const double p = -r[0];
     double c1, c2;
     if (p > 0) {
-      const double vnorm = sqrt(r[1]);
       c1 = 1 - a;
-      c2 = a * vnorm / gnorm + dt;
+      c2 = r[3];
       nsteps++;
     } else {
       c1 = 0.0;
@@ -779,20 +833,21 @@ struct Runner {
       P[i] = s;
       dg.add(G[i] * s);
     }
-    abytes += 16.0 * n;
+    MG_ACCT(abytes, 16.0 * n);
     double gs;
     if (has_constraints()) {
       gs = constrain_dir(P);
     } else {
-      double v[1] = {dg.total()};
-      tm.reduce(v);
+      float ps[1] = {dg.s}, pc[1] = {dg.c};
+      double v[1];
+      tm.template reduce_pairs<1>(ps, pc, v);
       gs = v[0];
     }
     double t = 1.0;
     if (in.mp.linesearch == 0) t = linesearch(P, 1.0, gs, exhausted);
     if (!tm.ok()) return;
     grad_eval(t, P, true, false, py, yyv);
-    gnorm = sqrt(gg);
+    gnorm = gnorm_v;
   }
 
   // ---- gradient descent -------------------------------------------------------------
@@ -817,7 +872,7 @@ struct Runner {
     }
     xi = 1 - xi;
     tm.sync();
-    abytes += (2.0 * xbytes() + 4.0) * n;
+    MG_ACCT(abytes, (2.0 * xbytes() + 4.0) * n);
   }
 
   // ---- precision stages -------------------------------------------------------------
@@ -826,7 +881,7 @@ struct Runner {
     double* X64 = in.X64[xi];
     for (int i = tm.tid(); i < n; i += tm.nthr()) X64[i] = (double)X[i];
     tm.sync();
-    abytes += 12.0 * n;
+    MG_ACCT(abytes, 12.0 * n);
     stage = 1;
   }
   __device__ void to_fp32() {
@@ -834,7 +889,7 @@ struct Runner {
     float* X = in.X32[xi];
     for (int i = tm.tid(); i < n; i += tm.nthr()) X[i] = (float)X64[i];
     tm.sync();
-    abytes += 12.0 * n;
+    MG_ACCT(abytes, 12.0 * n);
     stage = 0;
   }
   // the current gradient (and energy) again at the current point, in the
@@ -842,10 +897,10 @@ struct Runner {
   __device__ void reeval() {
     double py, yyv;
     grad_eval(0.0, nullptr, false, false, py, yyv);
-    if (in.mp.method == 1) gnorm = sqrt(gg);
+    if (in.mp.method == 1) gnorm = gnorm_v;
   }
 
-  __device__ double rms() const { return sqrt(gg / n); }
+  __device__ double rms() const { return rms_v; }
 
   // ---- driver -------------------------------------------------------------------------
   __device__ void load(const MinScalars& s) {
@@ -855,6 +910,8 @@ struct Runner {
     exhausted_run = s.exhausted_run; switch_reason = s.switch_reason; pend = s.pend; cool = s.cool;
     resume = s.resume; resume_exhausted = s.resume_exhausted;
     dt = s.dt; a = s.a; dtmax = s.dtmax; gnorm = s.gnorm;
+    rms_v = sqrt(gg / n);
+    gnorm_v = sqrt(gg);
     abytes = s.abytes; pairs32 = s.pairs32; pairs64 = s.pairs64;
     tph[0] = s.tphase[0]; tph[1] = s.tphase[1]; tph[2] = s.tphase[2];
     for (int k = threadIdx.x; k < MINIM_MAXM * MINIM_MAXM; k += blockDim.x) {
@@ -1001,7 +1058,7 @@ struct Runner {
         if (dtmax == 0) {
           double py, yyv;
           grad_eval(0.0, nullptr, false, false, py, yyv);
-          const double gn = sqrt(gg);
+          const double gn = gnorm_v;
           dtmax = (gn != 0) ? 0.1 / sqrt(gn) : 1.0;
         }
       }
