@@ -161,9 +161,9 @@ struct Runner {
         // batched path: each pair once, when positions and forces of all
         // particles fit the tile buffer
         const int ntp = ((in.lj.np + 31) >> 5) + (((in.lj.np + 31) >> 5) & 1);
-        if (want_g && (size_t)32 * ntp * 7 * sizeof(T) <= (size_t)lj_tile * sizeof(D4) &&
-            (blockDim.x & 31) == 0)
-          return lj_eval_sym<T>(tm, in.lj, cv, xw, &em, want_e, smem_pot);
+        const bool fits = (size_t)32 * ntp * 7 * sizeof(T) <= (size_t)lj_tile * sizeof(D4) && (blockDim.x & 31) == 0;
+        if (fits && want_g) return lj_eval_sym<T>(tm, in.lj, cv, xw, &em, want_e, smem_pot);
+        if (fits && want_e && !xw) return lj_energy_sym<T>(tm, in.lj, cv, smem_pot);
       }
       return lj_eval<T>(tm, in.lj, cv, xw, &em, want_e, want_g, smem_pot, lj_tile);
     } else if constexpr (KIND == K_PF) {

@@ -195,6 +195,78 @@ __device__ __noinline__ double lj_eval(Team& tm, const PotLJ& P, CView<T> cv, T*
   return 4.0 * P.eps * ((e4[0].total() + e4[1].total()) + (e4[2].total() + e4[3].total()));
 }
 
+// Energy only, for one CTA (the batched path's line-search trials): each
+// unordered pair once, 32x32 tile pairs (I <= J) dealt to the warps in turn
+// -- no forces, so no rounds and no barriers, and every warp gets the same
+// number of pairs whatever N (a thread per particle over j > i leaves the
+// first threads with N pairs and the last with none).  Diagonal tiles count
+// every pair twice at half weight; pairs with padding particles are skipped.
+template <typename T>
+__device__ __noinline__ double lj_energy_sym(CtaTeam& tm, const PotLJ& P, CView<T> cv, void* smem) {
+  using L = LjC<T>;
+  using C = typename L::C;
+  const int N = P.np, nd = P.ndim;
+  const int nt = (N + 31) >> 5;
+  CV3<C>* sx = reinterpret_cast<CV3<C>*>(smem);
+  const C s6 = L::from((T)P.s6);
+  const C zero = L::from((T)0);
+  const C half = L::from((T)0.5);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int j = threadIdx.x; j < 32 * nt; j += blockDim.x) {
+    CV3<C> v;
+    if (j < N) {
+      v.x = L::from(cv(nd * j));
+      v.y = L::from(cv(nd * j + 1));
+      v.z = (nd == 3) ? L::from(cv(nd * j + 2)) : zero;
+    } else {
+      v.x = L::from((T)(1e6 * (double)(j + 1)));
+      v.y = zero;
+      v.z = zero;
+    }
+    sx[j] = v;
+  }
+  __syncthreads();
+  LjAcc<C> e;
+  const int npairs = nt * (nt + 1) / 2;
+  for (int p = w; p < npairs; p += nw) {
+    // (I, J), I <= J, row by row of the upper triangle
+    int I = 0, rem = p;
+    while (rem >= nt - I) {
+      rem -= nt - I;
+      I++;
+    }
+    const int J = I + rem;
+    const int i = 32 * I + lane;
+    const CV3<C> a = sx[i];
+    C ee = zero;
+    if (I == J) {
+#pragma unroll 4
+      for (int s = 1; s < 32; s++) {
+        const int j = 32 * I + ((lane + s) & 31);
+        const CV3<C> b = sx[j];
+        const C dx = a.x - b.x, dy = a.y - b.y, dz = a.z - b.z;
+        C lj6, lj12, f;
+        lj_pair(dx, dy, dz, s6, lj6, lj12, f);
+        if (j < N) ee = ee + (lj12 - lj6);
+      }
+      if (i < N) e.add(ee * half);
+    } else {
+#pragma unroll 4
+      for (int s = 0; s < 32; s++) {
+        const int j = 32 * J + ((lane + s) & 31);
+        const CV3<C> b = sx[j];
+        const C dx = a.x - b.x, dy = a.y - b.y, dz = a.z - b.z;
+        C lj6, lj12, f;
+        lj_pair(dx, dy, dz, s6, lj6, lj12, f);
+        if (j < N) ee = ee + (lj12 - lj6);
+      }
+      if (i < N) e.add(ee);
+    }
+  }
+  __syncthreads();
+  return 4.0 * P.eps * e.total();
+}
+
 // Symmetric all-pairs evaluation for one CTA (the batched path): each
 // unordered pair is computed once.  Particles are grouped in tiles of 32;
 // tile pairs are scheduled round-robin (circle method) so that within a
