@@ -834,10 +834,10 @@ struct Runner {
       dg.add(G[i] * s);
     }
     MG_ACCT(abytes, 16.0 * n);
-    double gs;
+    double gs = 0.0;
     if (has_constraints()) {
       gs = constrain_dir(P);
-    } else {
+    } else if (in.mp.linesearch == 0) {  // g.P only for the line search
       float ps[1] = {dg.s}, pc[1] = {dg.c};
       double v[1];
       tm.template reduce_pairs<1>(ps, pc, v);
