@@ -486,41 +486,44 @@ struct LineCoef {
 // c4 receives the quad's point
 __device__ __forceinline__ float quad_eval(const QuadLoads& L, float t, const LineCoef& K, bool want_g, float4& c4,
                                            float4& g4) {
+  // trial point x + t P with one rounding (fused multiply-add)
   auto tr = [t](float4 a, float4 b) {
-    return make_float4(__fadd_rn(a.x, __fmul_rn(t, b.x)), __fadd_rn(a.y, __fmul_rn(t, b.y)),
-                       __fadd_rn(a.z, __fmul_rn(t, b.z)), __fadd_rn(a.w, __fmul_rn(t, b.w)));
+    return make_float4(fmaf(t, b.x, a.x), fmaf(t, b.y, a.y), fmaf(t, b.z, a.z), fmaf(t, b.w, a.w));
   };
   c4 = tr(L.xc, L.pc);
   const float cc[4] = {c4.x, c4.y, c4.z, c4.w};
-  const float zm = __fadd_rn(L.xzm, __fmul_rn(t, L.pzm)), zp = __fadd_rn(L.xzp, __fmul_rn(t, L.pzp));
+  const float zm = fmaf(t, L.pzm, L.xzm), zp = fmaf(t, L.pzp, L.xzp);
   const float4 ym = tr(L.xym, L.pym), yp = tr(L.xyp, L.pyp), xm = tr(L.xxm, L.pxm), xp = tr(L.xxp, L.pxp);
   const float ymv[4] = {ym.x, ym.y, ym.z, ym.w}, ypv[4] = {yp.x, yp.y, yp.z, yp.w};
   const float xmv[4] = {xm.x, xm.y, xm.z, xm.w}, xpv[4] = {xp.x, xp.y, xp.z, xp.w};
+  const float fih = 0.5f * K.Fi, fi2 = 2.f * K.Fi, fb4 = 4.f * K.fb;
   float es = 0.f, g[4];
 #pragma unroll
   for (int j = 0; j < 4; j++) {
     const float c = cc[j];
     const float cm = j == 0 ? zm : cc[j - 1], cp = j == 3 ? zp : cc[j + 1];
+    // differences to the neighbours: their sum (the Laplacian) and their
+    // squares (the gradient energy), per direction
     float gm = c - cm, gp = c - cp;
-    float lap = gm + gp, eg = 0.5f * (gm * gm + gp * gp);
+    float lap = gm + gp, s2 = fmaf(gm, gm, gp * gp);
     if (K.dy_on) {
       gm = c - ymv[j];
       gp = c - ypv[j];
       lap += gm + gp;
-      eg += 0.5f * (gm * gm + gp * gp);
+      s2 = fmaf(gm, gm, fmaf(gp, gp, s2));
     }
     if (K.dx_on) {
       gm = c - xmv[j];
       gp = c - xpv[j];
       lap += gm + gp;
-      eg += 0.5f * (gm * gm + gp * gp);
+      s2 = fmaf(gm, gm, fmaf(gp, gp, s2));
     }
-    const float a = (c + 1) * (c - 1);
-    es += K.fb * a * a + K.Fi * eg;
+    const float a = fmaf(c, c, -1.f);  // (c + 1)(c - 1)
+    es = fmaf(K.fb * a, a, fmaf(fih, s2, es));
     if (K.pr != 0.f) es -= K.pr * (0.5f * (c + 1) * K.V);
     g[j] = 0.f;
     if (want_g) {
-      g[j] = K.fb * 4 * c * (c * c - 1) + 2 * K.Fi * lap;
+      g[j] = fmaf(fb4 * c, a, fi2 * lap);
       if (K.pr != 0.f) g[j] -= 0.5f * K.pr * K.V;
     }
   }
