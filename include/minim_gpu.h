@@ -11,6 +11,7 @@
  *   minim_gpu_instance_create   State::State(pot, coords)       src/State.cpp:12-26
  *                               + Potential::init/initLocal     src/potentials/LjNd.cpp:12-26,
  *                                 src/potentials/PhaseField.cpp:137-235,
+ *                                 src/potentials/PhaseFieldUnstructured.cpp:114-308,
  *                                 src/potentials/BarAndHinge.cpp:16-248
  *   minim_gpu_energy_gradient   State::energy/gradient/energyGradient
  *                                                               src/State.cpp:134-192
@@ -59,7 +60,11 @@ enum {
 };
 
 /* ---- potential kinds ---------------------------------------------------- */
-enum { MINIM_GPU_LJ = 0, MINIM_GPU_PF = 1, MINIM_GPU_BAH = 2 };
+/* MINIM_GPU_PFU is PhaseFieldUnstructured (include/potentials/
+ * PhaseFieldUnstructured.h), the element form of the same model: it takes a
+ * minim_gpu_pf_params with that class's meaning (fixed volume as an energy
+ * penalty, DENSITY_FIXED as the Nth fluid computed from the others). */
+enum { MINIM_GPU_LJ = 0, MINIM_GPU_PF = 1, MINIM_GPU_BAH = 2, MINIM_GPU_PFU = 3 };
 
 /* LjNd(nDim, sigma, epsilon): include/potentials/LjNd.h:22-24 */
 typedef struct {
@@ -83,7 +88,7 @@ typedef struct {
   int density_constraint;       /* MINIM_PF_DENSITY_* (default hard) */
   double density_const;         /* default 1 */
   int volume_fixed;             /* setVolumeFixed / setVolume */
-  double vol_const;             /* default 0.01 (only the energy diagnostic uses it) */
+  double vol_const;             /* default 0.01 (PF: unused; PFU: the volume penalty's strength) */
   const double* volume;         /* nfluid target volumes, or NULL = initial volumes */
   const double* pressure;       /* nfluid, or NULL (= 0) */
   const char* solid;            /* ngrid (0/1), or NULL (= no solid) */

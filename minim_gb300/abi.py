@@ -14,8 +14,8 @@ OK, ERR_INVALID, ERR_RUNTIME, ERR_CUDA, ERR_OOM, ERR_NO_DEVICE, ERR_BUSY = range
 RES_CONVERGED, RES_MAXITER, RES_NAN, RES_TIMEOUT, RES_CANCELLED, RES_RUNNING, RES_REJECTED = range(7)
 RES_NAMES = {0: "converged", 1: "maxiter", 2: "nan", 3: "timeout", 4: "cancelled",
              5: "running", 6: "rejected"}
-# potential kinds
-LJ, PF, BAH = 0, 1, 2
+# potential kinds (PFU: PhaseFieldUnstructured, the element form of PhaseField)
+LJ, PF, BAH, PFU = 0, 1, 2, 3
 # PhaseField density constraints
 DENSITY = {"hard": 0, "gradient": 0, "soft": 1, "energy penalty": 1, "none": 2, "fixed": 3}
 # minimisers, line searches, precision
@@ -176,6 +176,15 @@ def phase_field(grid, nfluid=1, resolution=1.0, interface_size=None, surface_ten
     arr("fix_fluid", fix_fluid, _u8, ptr_type=C.c_void_p)
     arr("confinement", confinement, _f64)
     return Params(PF, s, keep)
+
+
+def phase_field_unstructured(grid, **kw):
+    """PhaseFieldUnstructured with the reference's setter names and defaults
+    (the same keywords as :func:`phase_field`; ``vol_const`` is the fixed
+    volume's penalty strength)."""
+    p = phase_field(grid, **kw)
+    p.kind = PFU
+    return p
 
 
 def bar_and_hinge(triangulation=None, bonds=None, hinges=None, modulus=1.0, poisson_ratio=0.3,

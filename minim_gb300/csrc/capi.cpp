@@ -411,8 +411,8 @@ minim_gpu_instance_s* create_instance(int kind, const void* params, const double
       h->d.lj.np = (int)(ndof / q->ndim);
       h->d.lj.s6 = std::pow(q->sigma, 6);
       h->d.lj.eps = q->epsilon;
-    } else if (kind == MINIM_GPU_PF) {
-      PfHost H = setup_pf(*(const minim_gpu_pf_params*)params, x0, ndof);
+    } else if (kind == MINIM_GPU_PF || kind == MINIM_GPU_PFU) {
+      PfHost H = setup_pf(*(const minim_gpu_pf_params*)params, x0, ndof, kind == MINIM_GPU_PFU);
       h->kk = H.kernel_kind;
       h->default_tol = H.default_tol;
       h->d.pf = H.pot;

@@ -34,6 +34,11 @@ enum PfFlags : unsigned {
   PF_CONFINE = 1u << 7,
   PF_NODE_KAPPA = 1u << 8, // per-node kappa / kappaP arrays
   PF_FIXFLUID = 1u << 9,
+  // PhaseFieldUnstructured (element form): pressure on fixed fluids too, the
+  // soft density over the first three fluids, no node terms on solid nodes
+  PF_UNSTR = 1u << 10,
+  PF_UVOL = 1u << 11,      // fixed volume as an energy penalty (vol_target, vol_coef)
+  PF_NALL = 1u << 12,      // DENSITY_FIXED: the last fluid is 1 minus the others
 };
 
 struct PotPF {
@@ -60,6 +65,8 @@ struct PotPF {
   double fmag[MINIM_MAXF];
   double fnorm[MINIM_MAXF][3];
   double total_volume2;       // sum nodeVol^2 (PF_VOLUME)
+  double vol_target[MINIM_MAXF];  // PF_UVOL: target volumes
+  double vol_coef;            // PF_UVOL: volConst * sigmaMean / res^4
   int pf_dist;                // L2 prefetch distance of the stencil sweep (0 = none)
 };
 

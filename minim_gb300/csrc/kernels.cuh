@@ -89,7 +89,11 @@ __device__ void eval_op(Runner<Team, KIND>& R, Team& tm, const InstDesc& in, con
 template <class Team, int KIND>
 __device__ void constrain_op(Team& tm, const InstDesc& in, const EvalIO& io) {
   double* v = io.v;
-  if (in.fixed)
+  // PhaseFieldUnstructured::init replaces the constraint list, so fixed
+  // degrees of freedom set on the state come after its own constraints
+  bool fixed_last = false;
+  if constexpr (KIND == K_PF) fixed_last = (in.pf.flags & PF_UNSTR) != 0;
+  if (in.fixed && !fixed_last)
     for (int i = tm.tid(); i < in.ndof; i += tm.nthr())
       if (in.fixed[i]) v[i] = 0.0;
   if constexpr (KIND == K_PF) {
@@ -101,6 +105,11 @@ __device__ void constrain_op(Team& tm, const InstDesc& in, const EvalIO& io) {
       tm.sync();
       pf_volume_project<double>(tm, in.pf, v);
     }
+  }
+  if (in.fixed && fixed_last) {
+    tm.sync();
+    for (int i = tm.tid(); i < in.ndof; i += tm.nthr())
+      if (in.fixed[i]) v[i] = 0.0;
   }
 }
 

@@ -290,7 +290,11 @@ struct Runner {
 
   // State::applyConstraints on the direction P, then returns g.P
   __device__ double constrain_dir(float* P) {
-    if (in.fixed) {
+    // the element form (PhaseFieldUnstructured) applies fixed degrees of
+    // freedom after its own constraints
+    bool fixed_last = false;
+    if constexpr (KIND == K_PF) fixed_last = (in.pf.flags & PF_UNSTR) != 0;
+    if (in.fixed && !fixed_last) {
       for (int i = tm.tid(); i < n; i += tm.nthr())
         if (in.fixed[i]) P[i] = 0.f;
     }
@@ -303,6 +307,11 @@ struct Runner {
         tm.sync();
         pf_volume_project<float>(tm, in.pf, P);
       }
+    }
+    if (in.fixed && fixed_last) {
+      tm.sync();
+      for (int i = tm.tid(); i < n; i += tm.nthr())
+        if (in.fixed[i]) P[i] = 0.f;
     }
     tm.sync();
     return dot_gP(P);

@@ -392,6 +392,13 @@ __device__ __noinline__ double lj_eval_sym(CtaTeam& tm, const PotLJ& P, CView<T>
 // 580-612).  Each node computes its own bulk and gradient terms and collects
 // the contributions that the reference scatters into it from its two
 // neighbours in every direction, so every DOF is written exactly once.
+//
+// With PF_UNSTR the same sweep evaluates PhaseFieldUnstructured's energy
+// elements (src/potentials/PhaseFieldUnstructured.cpp:158-236, 518-692):
+// solid nodes carry no elements, pressure acts on fixed fluids too, the soft
+// density element reads the first three fluids; PF_NALL is its
+// fluidEnergyAll (DENSITY_FIXED) and PF_UVOL its blockEnergyGradient volume
+// penalty (lines 280-308), whose volumes are summed over the team first.
 // ===========================================================================
 __device__ __forceinline__ int pf_type1(const PotPF& P, int node) {  // type + 1
   return P.aux ? (int)(P.aux[node] & 15u) : 1;
@@ -408,6 +415,32 @@ __device__ __noinline__ double pf_eval(Team& tm, const PotPF& P, CView<T> cv, T*
   const unsigned fl = P.flags;
   const T res2 = (T)P.res2;
   EAcc<T> e;
+  // PF_UVOL: volume differences at these coordinates, every thread
+  double dvol[NFMAX];
+#pragma unroll
+  for (int f = 0; f < NFMAX; f++) dvol[f] = 0.0;
+  if (fl & PF_UVOL) {
+    for (int iG = tm.tid(); iG < ng; iG += tm.nthr()) {
+      const double V = P.vol_of_type[pf_type1(P, iG)];
+#pragma unroll
+      for (int f = 0; f < NFMAX; f++) {
+        if (f < nf) {
+          const double cf = (double)cv(iG * nf + f);
+          dvol[f] += (nf == 1) ? 0.5 * (cf + 1) * V : cf * V;
+        }
+      }
+    }
+    tm.reduce(dvol);
+#pragma unroll
+    for (int f = 0; f < NFMAX; f++) {
+      if (f < nf) {
+        dvol[f] -= P.vol_target[f];
+        if (want_e && tm.tid() == 0) e.add((T)(P.vol_coef * dvol[f] * dvol[f]));
+      }
+    }
+  }
+  const bool unstr = (fl & PF_UNSTR) != 0;
+  const bool nall = (fl & PF_NALL) != 0;
   for (int iG = tm.tid(); iG < ng; iG += tm.nthr()) {
     const int z = iG % nz, y = (iG / nz) % ny, x = iG / (ny * nz);
     int nb[6];
@@ -435,11 +468,57 @@ __device__ __noinline__ double pf_eval(Team& tm, const PotPF& P, CView<T> cv, T*
         g[f] = 0;
       }
     }
-    T rd = -1;  // soft density: sum c - 1
+    // solid nodes carry no elements in the element form
+    const bool node_terms = !(unstr && solid_i);
+    T rd = -1;  // soft density: sum c - 1 (element form: the first three fluids)
     if (fl & PF_SOFT) {
+      if (unstr) {
+        rd = c[0] + c[1] + c[2] - 1;
+      } else {
 #pragma unroll
-      for (int f = 0; f < NFMAX; f++)
-        if (f < nf) rd += c[f];
+        for (int f = 0; f < NFMAX; f++)
+          if (f < nf) rd += c[f];
+      }
+    }
+    // PF_NALL: the last fluid's term (fluidEnergyAll), whose gradient every
+    // other fluid receives with the opposite sign.  Its local indices are all
+    // distinct, so a solid neighbour (replaced by the node itself) enters as
+    // a zero difference, and its factor has no 1/res^2.
+    T gnall = 0;
+    if (nall && node_terms) {
+      T cN[7];
+#pragma unroll
+      for (int k = 0; k < 7; k++) cN[k] = 1;
+#pragma unroll
+      for (int f = 0; f < NFMAX - 1; f++) {
+        if (f < nf - 1) {
+          cN[0] -= c[f];
+#pragma unroll
+          for (int k = 0; k < 6; k++) cN[k + 1] -= cv((((mask_i >> k) & 1u) ? iG : nb[k]) * nf + f);
+        }
+      }
+      const T bN = (T)0.5 * (T)P.kappa[nf - 1] * V;
+      const T gfN = (T)0.5 * (T)P.kappaP[nf - 1] * V;
+      const T a = cN[0] * (cN[0] - 1);
+      if (want_e) e.add(bN * a * a);
+      gnall = bN * 2 * cN[0] * (cN[0] - 1) * (2 * cN[0] - 1);
+      T eg = 0;
+#pragma unroll
+      for (int d = 0; d < 3; d++) {
+        const T gm = cN[0] - cN[1 + 2 * d], gp = cN[0] - cN[2 + 2 * d];
+        eg += (T)0.5 * (gm * gm + gp * gp);
+        gnall += gfN * (gm + gp);
+        // the elements of the non-solid neighbours, whose slot toward this
+        // node holds this node
+#pragma unroll
+        for (int sd = 0; sd < 2; sd++) {
+          const int k = 2 * d + sd;
+          if ((mask_i >> k) & 1u) continue;
+          const T Vj = (T)P.vol_of_type[aux_nb[k] & 15u];
+          gnall -= (T)0.5 * (T)P.kappaP[nf - 1] * Vj * (cN[1 + k] - cN[0]);
+        }
+      }
+      if (want_e) e.add(gfN * eg);
     }
     bool force_e_done = false;  // energy-only semantics of forceEnergy
 #pragma unroll
@@ -450,8 +529,11 @@ __device__ __noinline__ double pf_eval(Team& tm, const PotPF& P, CView<T> cv, T*
       const T kap = (fl & PF_NODE_KAPPA) ? (T)P.kappa_node[dof] : (T)P.kappa[f];
       const T kP = (fl & PF_NODE_KAPPA) ? (T)P.kappaP_node[dof] : (T)P.kappaP[f];
       T gv = 0;
-      // bulk
-      if (nf == 1) {
+      if (nall) gv -= gnall;
+      // bulk (with PF_NALL the last fluid has none of its own)
+      if (nall && f == nf - 1) {
+        // nothing: its concentration is 1 minus the others'
+      } else if (nf == 1) {
         const T fac = kap / 16 * V;
         const T a = (cc + 1) * (cc - 1);
         if (want_e) e.add(fac * a * a);
@@ -466,9 +548,10 @@ __device__ __noinline__ double pf_eval(Team& tm, const PotPF& P, CView<T> cv, T*
       const T coefk = ((nf == 1) ? (T)0.25 : (T)0.5) / res2;
       const T Fi = coefk * kP * V;
       T eg = 0;
+      const bool own_grad = !(nall && f == nf - 1);
 #pragma unroll
       for (int d = 0; d < 3; d++) {
-        if (P.n[d] == 1) continue;
+        if (P.n[d] == 1 || !own_grad) continue;
         const int im = nb[2 * d], ip = nb[2 * d + 1];
         const T cm = cv(im * nf + f), cp = cv(ip * nf + f);
         const bool sm = (mask_i >> (2 * d)) & 1u, sp = (mask_i >> (2 * d + 1)) & 1u;
@@ -511,8 +594,8 @@ __device__ __noinline__ double pf_eval(Team& tm, const PotPF& P, CView<T> cv, T*
           gv += w * (cc * cc - 1);
         }
       }
-      // pressure
-      if ((fl & PF_PRESSURE) && P.pressure[f] != 0 && !((P.fix_mask >> f) & 1u)) {
+      // pressure (the element form has it on fixed fluids too)
+      if ((fl & PF_PRESSURE) && P.pressure[f] != 0 && node_terms && (unstr || !((P.fix_mask >> f) & 1u))) {
         const T pr = (T)P.pressure[f];
         if (nf == 1) {
           if (want_e) e.add(-pr * ((T)0.5 * (cc + 1) * V));
@@ -523,7 +606,7 @@ __device__ __noinline__ double pf_eval(Team& tm, const PotPF& P, CView<T> cv, T*
         }
       }
       // soft density
-      if ((fl & PF_SOFT) && nf > 1) {
+      if ((fl & PF_SOFT) && nf > 1 && node_terms && (!unstr || f < 3)) {
         const T sc = (T)P.soft_coef;
         if (want_e && f == 0) e.add(sc * rd * rd);
         gv += 2 * sc * rd;
@@ -543,13 +626,19 @@ __device__ __noinline__ double pf_eval(Team& tm, const PotPF& P, CView<T> cv, T*
         }
       }
       // diffuse-solid confinement
-      if ((fl & PF_CONFINE) && P.confine_coef[f] != 0) {
+      if ((fl & PF_CONFINE) && P.confine_coef[f] != 0 && node_terms) {
         const T c0 = (T)P.ff_init[dof];
         if ((c0 - (T)0.5) * (cc - (T)0.5) < 0) {
           const T coef = (T)P.confine_coef[f];
           if (want_e) e.add(coef * (cc - (T)0.5) * (cc - (T)0.5));
           gv += coef * 2 * (cc - (T)0.5);
         }
+      }
+      // element form's fixed volume: the penalty's force on interface nodes
+      if (fl & PF_UVOL) {
+        T w = 4 * cc * (1 - cc);
+        if (w < 0) w = 0;
+        gv += (T)(P.vol_coef * dvol[f]) * V * w;
       }
       g[f] = gv;
     }

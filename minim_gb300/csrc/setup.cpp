@@ -2,6 +2,8 @@
 //
 //   PhaseField   PhaseField::init / assignFluidCoefficients / initLocal /
 //                getType           src/potentials/PhaseField.cpp:78-235, 903-995
+//   PhaseFieldUnstructured::init / checkArraySizes
+//                                  src/potentials/PhaseFieldUnstructured.cpp:71-256, 929-954
 //   BarAndHinge  BarAndHinge::init / computeBondList / computeHingeList /
 //                computeRigidities / computeLength0 / computeTheta0
 //                                  src/potentials/BarAndHinge.cpp:16-248
@@ -59,7 +61,7 @@ int node_type(const std::vector<char>& solid, const int* n, int x, int y, int z)
 }
 }  // namespace
 
-PfHost setup_pf(const minim_gpu_pf_params& q, const double* x0, size_t ndof) {
+PfHost setup_pf(const minim_gpu_pf_params& q, const double* x0, size_t ndof, bool unstr) {
   PfHost H;
   PotPF& P = H.pot;
   for (int d = 0; d < 3; d++) {
@@ -85,7 +87,11 @@ PfHost setup_pf(const minim_gpu_pf_params& q, const double* x0, size_t ndof) {
   std::vector<double> st_in = (q.n_surface_tension > 0)
                                   ? std::vector<double>(q.surface_tension, q.surface_tension + q.n_surface_tension)
                                   : std::vector<double>{1.0};
-  const int nkgrid = ((int)st_in.size() == ng * nparams) ? ng : 1;
+  // PhaseFieldUnstructured has no per-node surface tensions and wants one
+  // interface width per fluid (checkArraySizes)
+  const int nkgrid = (!unstr && (int)st_in.size() == ng * nparams) ? ng : 1;
+  if (unstr && q.n_interface_size != 0 && q.n_interface_size != nf)
+    throw SetupError(MINIM_GPU_ERR_INVALID, "PhaseFieldUnstructured: Invalid size interfaceSize array.");
   const int nst = nkgrid * nparams;
   std::vector<double> st(nst);
   if (st_in.size() == 1) std::fill(st.begin(), st.end(), st_in[0]);
@@ -249,15 +255,38 @@ PfHost setup_pf(const minim_gpu_pf_params& q, const double* x0, size_t ndof) {
       else H.wet.clear();
     }
   }
-  if (q.volume_fixed) {
+  if (unstr) {
+    // element form: the fixed volume is an energy penalty on the volumes
+    // sum c * nodeVol (targets default to the initial ones), and
+    // DENSITY_FIXED evaluates the last fluid as 1 minus the others
+    flags |= PF_UNSTR;
+    if (nf == 2 && q.density_constraint == MINIM_PF_DENSITY_SOFT)
+      throw SetupError(MINIM_GPU_ERR_INVALID,
+                       "PhaseFieldUnstructured: the soft density constraint needs at least three fluids");
+    if (q.density_constraint == MINIM_PF_DENSITY_FIXED) flags |= PF_NALL;
+    if (q.volume_fixed) {
+      flags |= PF_UVOL;
+      for (int f = 0; f < nf; f++) {
+        double v = 0;
+        if (q.volume) {
+          v = q.volume[f];
+        } else {
+          for (int i = 0; i < ng; i++) v += x0[f + (size_t)nf * i] * H.node_vol[i];
+        }
+        P.vol_target[f] = v;
+      }
+      P.vol_coef = q.vol_const * st_mean / std::pow(q.resolution, 4);
+    }
+  } else if (q.volume_fixed) {
     flags |= PF_VOLUME;
     double tv = 0;
     for (int i = 0; i < ng; i++) tv += H.node_vol[i] * H.node_vol[i];
     P.total_volume2 = tv;
   }
   P.flags = flags;
+  // PF_UNSTR alone changes nothing for one fluid without the optional terms
   const unsigned general = PF_SOLID | PF_CONTACT | PF_SOFT | PF_HARD | PF_VOLUME | PF_FORCE |
-                           PF_CONFINE | PF_NODE_KAPPA | PF_FIXFLUID;
+                           PF_CONFINE | PF_NODE_KAPPA | PF_FIXFLUID | PF_UVOL | PF_NALL;
   H.kernel_kind = (nf == 1 && !(flags & general)) ? K_PF1 : K_PF;
   (void)kPi;
   return H;

@@ -29,7 +29,8 @@ struct PfHost {
   std::vector<double> surface_area;
   std::vector<double> kappa, kappaP;  // as the reference stores them
 };
-PfHost setup_pf(const minim_gpu_pf_params& q, const double* x0, size_t ndof);
+// unstr: PhaseFieldUnstructured semantics (src/potentials/PhaseFieldUnstructured.cpp)
+PfHost setup_pf(const minim_gpu_pf_params& q, const double* x0, size_t ndof, bool unstr = false);
 
 // BarAndHinge topology in the reference's order (computeBondList /
 // computeHingeList), built with hash maps in O(T log T) instead of O(T^2).

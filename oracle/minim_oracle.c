@@ -60,6 +60,10 @@ typedef struct {
   double* fmag;      /* nfluid */
   double* fnorm;     /* nfluid*3 */
   int any_force;
+  /* PhaseFieldUnstructured (element form, src/potentials/PhaseFieldUnstructured.cpp) */
+  int unstr;
+  double vol_const;
+  double* volume;    /* nfluid target volumes (PFU with a fixed volume) */
 } pf_t;
 
 typedef struct {
@@ -180,9 +184,10 @@ static void* xcalloc(size_t n, size_t sz) {
 /* PhaseField::init + assignFluidCoefficients + initLocal
  * (src/potentials/PhaseField.cpp:78-235; 1 rank so procSizes == gridSize and
  * no halo). */
-static int pf_setup(oracle_inst* o, const minim_gpu_pf_params* q, const double* x0) {
+static int pf_setup(oracle_inst* o, const minim_gpu_pf_params* q, const double* x0, int unstr) {
   pf_t* p = &o->pf;
   memset(p, 0, sizeof *p);
+  p->unstr = unstr;
   for (int d = 0; d < 3; d++) p->n[d] = q->grid[d];
   p->nfluid = q->nfluid;
   p->ngrid = q->grid[0] * q->grid[1] * q->grid[2];
@@ -196,8 +201,13 @@ static int pf_setup(oracle_inst* o, const minim_gpu_pf_params* q, const double* 
   int nst = q->n_surface_tension > 0 ? q->n_surface_tension : 1;
   const double one = 1.0;
   const double* st_in = q->n_surface_tension > 0 ? q->surface_tension : &one;
-  int nkgrid = (nst == ng * nparams) ? ng : 1;
+  /* PhaseFieldUnstructured has no per-node surface tensions
+   * (PhaseFieldUnstructured.cpp:71-86), and checkArraySizes (lines 929-933) wants
+   * one interface width per fluid */
+  int nkgrid = (!unstr && nst == ng * nparams) ? ng : 1;
   int nstt = nkgrid * nparams;
+  if (unstr && q->n_interface_size != 0 && q->n_interface_size != nf)
+    return set_err(MINIM_GPU_ERR_INVALID, "PhaseFieldUnstructured: Invalid size interfaceSize array.");
   double* st = xcalloc(nstt, sizeof(double));
   if (nst == 1) {
     for (int i = 0; i < nstt; i++) st[i] = st_in[0];
@@ -318,7 +328,251 @@ static int pf_setup(oracle_inst* o, const minim_gpu_pf_params* q, const double* 
     p->ff_init = xcalloc(o->ndof, sizeof(double));
     memcpy(p->ff_init, x0, o->ndof * sizeof(double));
   }
+  if (unstr) {
+    /* the soft density element reads the node's first three fluids
+     * (PhaseFieldUnstructured.cpp:631-642); with two it would read past them */
+    if (nf == 2 && p->density == D_SOFT)
+      return set_err(MINIM_GPU_ERR_INVALID,
+                     "PhaseFieldUnstructured: the soft density constraint needs at least three fluids");
+    p->vol_const = q->vol_const;
+    if (p->volume_fixed) {
+      p->volume = xcalloc(nf, sizeof(double));
+      if (q->volume) {
+        memcpy(p->volume, q->volume, nf * sizeof(double));
+      } else {
+        /* initial volumes, lines 148-156: sum of c * nodeVol (also for one
+         * fluid, whose penalty then measures 0.5 (c + 1) * nodeVol) */
+        for (int i = 0; i < ng; i++)
+          for (int f = 0; f < nf; f++) p->volume[f] += x0[f + nf * i] * p->node_vol[i];
+      }
+    }
+  }
   return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* PhaseFieldUnstructured: src/potentials/PhaseFieldUnstructured.cpp         */
+/* ------------------------------------------------------------------------ */
+/* phaseGradient for one fluid, lines 311-396: idof[0] is the node, idof[1..6]
+ * its x-, y-, z-, z+, y+, x+ neighbours; a neighbour whose index equals the
+ * node's (a solid neighbour, or a dimension of size 1) drops that side. */
+static void pfu_phase_gradient(const double* c, const int* idof, double factor, double* e, double* g) {
+  static const int side[3][2] = {{1, 6}, {2, 5}, {3, 4}};
+  double c1 = c[idof[0]];
+  double grad2 = 0;
+  for (int d = 0; d < 3; d++) {
+    int im = idof[side[d][0]], ip = idof[side[d][1]];
+    if (im != idof[0] && ip != idof[0]) {
+      double gm = c1 - c[im], gp = c1 - c[ip];
+      if (e) grad2 += 0.5 * (pow(gm, 2) + pow(gp, 2));
+      if (g) {
+        g[idof[0]] += factor * (gm + gp);
+        g[im] -= factor * gm;
+        g[ip] -= factor * gp;
+      }
+    } else if (ip != idof[0]) {
+      double gp = c1 - c[ip];
+      if (e) grad2 += pow(gp, 2);
+      if (g) {
+        g[idof[0]] += factor * 2 * gp;
+        g[ip] -= factor * 2 * gp;
+      }
+    } else if (im != idof[0]) {
+      double gm = c1 - c[im];
+      if (e) grad2 += pow(gm, 2);
+      if (g) {
+        g[idof[0]] += factor * 2 * gm;
+        g[im] -= factor * 2 * gm;
+      }
+    }
+  }
+  if (e) *e += factor * grad2;
+}
+
+/* fluidEnergy, lines 518-538 */
+static void pfu_fluid(const pf_t* p, const double* c, const int* idof, double V, int f, double* e, double* g) {
+  int nf = p->nfluid;
+  double cc = c[idof[0]];
+  if (nf == 1) {
+    double fac = p->kappa[0] / 16 * V;
+    if (e) *e += fac * pow(cc + 1, 2) * pow(cc - 1, 2);
+    if (g) g[idof[0]] += fac * 4 * cc * (cc * cc - 1);
+  } else {
+    double fac = 0.5 * p->kappa[f] * V;
+    if (e) *e += fac * pow(cc, 2) * pow(cc - 1, 2);
+    if (g) g[idof[0]] += fac * 2 * cc * (cc - 1) * (2 * cc - 1);
+  }
+  double fac = (nf == 1) ? 0.25 * p->kappaP[0] * V : 0.5 * p->kappaP[f] * V;
+  fac = fac / pow(p->res, 2);
+  pfu_phase_gradient(c, idof, fac, e, g);
+}
+
+/* fluidEnergyAll (DENSITY_FIXED), lines 541-586: the last fluid's
+ * concentration is 1 minus the others'.  Its gradient term runs over the
+ * local indices 0..6, which are all distinct, so a solid neighbour (whose
+ * index is the node's own) enters as a zero difference on the two-sided
+ * form, and its factor is not divided by res^2 -- both as in the reference. */
+static void pfu_fluid_all(const pf_t* p, const double* c, const int* idof, double V, double* e, double* g) {
+  static const int iota7[7] = {0, 1, 2, 3, 4, 5, 6};
+  int nf = p->nfluid;
+  double cN[7], gN[7] = {0, 0, 0, 0, 0, 0, 0};
+  for (int i = 0; i < 7; i++) cN[i] = 1;
+  for (int f = 0; f < nf - 1; f++)
+    for (int i = 0; i < 7; i++) cN[i] -= c[idof[i] + f];
+  double bN = 0.5 * p->kappa[nf - 1] * V;
+  double gfN = 0.5 * p->kappaP[nf - 1] * V;
+  if (e) *e += bN * pow(cN[0], 2) * pow(cN[0] - 1, 2);
+  if (g) {
+    gN[0] += bN * 2 * cN[0] * (cN[0] - 1) * (2 * cN[0] - 1);
+    pfu_phase_gradient(cN, iota7, gfN, e, gN);
+  } else {
+    pfu_phase_gradient(cN, iota7, gfN, e, NULL);
+  }
+  for (int f = 0; f < nf - 1; f++) {
+    int id[7];
+    for (int i = 0; i < 7; i++) id[i] = idof[i] + f;
+    double cc = c[id[0]];
+    double bf = 0.5 * p->kappa[f] * V;
+    if (e) *e += bf * pow(cc, 2) * pow(cc - 1, 2);
+    if (g) g[id[0]] += bf * 2 * cc * (cc - 1) * (2 * cc - 1);
+    double gf = 0.5 * p->kappaP[f] * V;
+    gf = gf / pow(p->res, 2);
+    pfu_phase_gradient(c, id, gf, e, g);
+    if (g)
+      for (int i = 0; i < 7; i++) g[id[i]] -= gN[i];
+  }
+}
+
+/* The energy elements of PhaseFieldUnstructured::init (lines 158-236) in
+ * their order, evaluated as State's elementEG does (src/State.cpp:58-79),
+ * then blockEnergyGradient (lines 280-308). */
+static void pfu_eg(const oracle_inst* o, const double* c, double* e, double* g) {
+  const pf_t* p = &o->pf;
+  int nf = p->nfluid, ng = p->ngrid;
+  double res2 = pow(p->res, 2);
+  for (int iG = 0; iG < ng; iG++) {
+    if (p->solid[iG]) continue;
+    int z = iG % p->n[2], y = (iG / p->n[2]) % p->n[1], x = iG / (p->n[1] * p->n[2]);
+    int nodes[7] = {iG, pf_idx(p, x - 1, y, z), pf_idx(p, x, y - 1, z), pf_idx(p, x, y, z - 1),
+                    pf_idx(p, x, y, z + 1), pf_idx(p, x, y + 1, z), pf_idx(p, x + 1, y, z)};
+    for (int k = 1; k < 7; k++)
+      if (p->solid[nodes[k]]) nodes[k] = iG;
+    double V = p->node_vol[iG];
+    if (p->density == D_FIXED) {
+      int idof[7];
+      for (int k = 0; k < 7; k++) idof[k] = nodes[k] * nf;
+      pfu_fluid_all(p, c, idof, V, e, g);
+    } else {
+      for (int f = 0; f < nf; f++) {
+        int idof[7];
+        for (int k = 0; k < 7; k++) idof[k] = nodes[k] * nf + f;
+        pfu_fluid(p, c, idof, V, f, e, g);
+      }
+    }
+    /* pressureEnergy, lines 613-628 (every fluid with a pressure) */
+    for (int f = 0; f < nf; f++) {
+      if (p->pressure[f] == 0) continue;
+      int iD = iG * nf + f;
+      if (nf == 1) {
+        double vol = 0.5 * (c[iD] + 1) * V;
+        if (e) *e -= p->pressure[f] * vol;
+        if (g) g[iD] -= 0.5 * p->pressure[f] * V;
+      } else {
+        double vol = c[iD] * V;
+        if (e) *e -= p->pressure[f] * vol;
+        if (g) g[iD] -= p->pressure[f] * V;
+      }
+    }
+    /* densityConstraintEnergy, lines 631-642: the first three fluids */
+    if (nf > 1 && p->density == D_SOFT) {
+      double coef = p->density_const * p->st_mean * res2;
+      int i0 = iG * nf;
+      double rd = c[i0] + c[i0 + 1] + c[i0 + 2] - 1;
+      if (e) *e += coef * pow(rd, 2);
+      if (g) {
+        g[i0] += 2 * coef * rd;
+        g[i0 + 1] += 2 * coef * rd;
+        g[i0 + 2] += 2 * coef * rd;
+      }
+    }
+    /* surfaceEnergy, lines 645-654 (binary fluids only) */
+    if (p->surf_area[iG] > 0 && p->ncontact > 0 && p->contact[iG] != 90 && nf == 1) {
+      double w = 1 / sqrt(2.0) * cos(p->contact[iG] * 3.1415926536 / 180);
+      double phi = c[iG];
+      if (e) *e += w * (pow(phi, 3) / 3 - phi - 2.0 / 3) * p->surf_area[iG];
+      if (g) g[iG] += w * (pow(phi, 2) - 1) * p->surf_area[iG];
+    }
+    /* forceEnergy, lines 657-676 */
+    if (p->any_force) {
+      double co[3] = {x - (p->n[0] - 1) / 2.0, y - (p->n[1] - 1) / 2.0, z - (p->n[2] - 1) / 2.0};
+      for (int f = 0; f < nf; f++) {
+        if (!(p->fmag[f] > 0)) continue;
+        const double* fn = p->fnorm + 3 * f;
+        double h = -(co[0] * fn[0] + co[1] * fn[1] + co[2] * fn[2]) * p->res;
+        int iD = iG * nf + f;
+        double cc = (nf == 1) ? 0.5 * (1 + c[iD]) : c[iD];
+        if (cc < 0.01) continue;
+        if (e) *e += cc * V * p->fmag[f] * h;
+        if (g) g[iD] += (nf == 1) ? 0.5 * V * p->fmag[f] * h : V * p->fmag[f] * h;
+      }
+    }
+    /* ffConfinementEnergy, lines 679-692 */
+    for (int f = 0; f < nf; f++) {
+      if (p->confine[f] == 0) continue;
+      int iD = iG * nf + f;
+      double coef = p->confine[f] * p->st_mean * res2;
+      double cc = c[iD], c0 = p->ff_init[iD];
+      if ((c0 - 0.5) * (cc - 0.5) < 0) {
+        if (e) *e += coef * pow(cc - 0.5, 2);
+        if (g) g[iD] += coef * 2 * (cc - 0.5);
+      }
+    }
+  }
+  /* blockEnergyGradient: the fixed volume as an energy penalty whose
+   * gradient acts on interface nodes only */
+  if (p->volume_fixed) {
+    double vf[64] = {0};
+    for (int i = 0; i < ng * nf; i++) {
+      double V = p->node_vol[i / nf];
+      if (nf == 1) vf[0] += 0.5 * (c[i] + 1) * V;
+      else vf[i % nf] += c[i] * V;
+    }
+    double coef = p->vol_const * p->st_mean / pow(p->res, 4);
+    for (int f = 0; f < nf; f++) {
+      double dv = vf[f] - p->volume[f];
+      if (e) *e += coef * pow(dv, 2);
+      if (!g) continue;
+      for (int iG = 0; iG < ng; iG++) {
+        int iD = iG * nf + f;
+        double w = 4 * c[iD] * (1 - c[iD]);
+        if (w < 0) w = 0;
+        g[iD] += coef * dv * p->node_vol[iG] * w;
+      }
+    }
+  }
+}
+
+/* The constraints PhaseFieldUnstructured::init sets (lines 239-256): the hard
+ * density normal (1,..,1) over the variable fluids of every node, through
+ * Potential::applyConstraints (src/Potential.cpp:102-115), then the fixed
+ * fluids. */
+static void pfu_constraints(const oracle_inst* o, double* v) {
+  const pf_t* p = &o->pf;
+  int nf = p->nfluid, ng = p->ngrid;
+  int var[64], nvar = 0;
+  for (int f = 0; f < nf; f++)
+    if (!p->fix_fluid[f] && nvar < 64) var[nvar++] = f;
+  if (nf > 1 && p->density == D_HARD) {
+    for (int i = 0; i < ng; i++) {
+      double nsq = 0, gn = 0;
+      for (int k = 0; k < nvar; k++) nsq += 1.0;
+      for (int k = 0; k < nvar; k++) gn += v[i * nf + var[k]];
+      for (int k = 0; k < nvar; k++) v[i * nf + var[k]] -= gn * 1.0 / nsq;
+    }
+  }
+  for (int f = 0; f < nf; f++)
+    if (p->fix_fluid[f])
+      for (int i = 0; i < ng; i++) v[i * nf + f] = 0;
 }
 
 /* phaseGradient, src/potentials/PhaseField.cpp:238-288 */
@@ -870,6 +1124,15 @@ static void bah_eg(const oracle_inst* o, const double* x, double* e, double* g) 
 /* Potential::applyConstraints (src/Potential.cpp:102-115)                   */
 /* ------------------------------------------------------------------------ */
 static void apply_constraints(const oracle_inst* o, double* v) {
+  if (o->kind == MINIM_GPU_PFU) {
+    /* init replaces the constraint list (PhaseFieldUnstructured.cpp:240), so
+     * fixed degrees of freedom set on the state come after its own */
+    pfu_constraints(o, v);
+    if (o->fixed)
+      for (size_t i = 0; i < o->ndof; i++)
+        if (o->fixed[i]) v[i] = 0;
+    return;
+  }
   if (o->fixed)
     for (size_t i = 0; i < o->ndof; i++)
       if (o->fixed[i]) v[i] = 0;
@@ -879,6 +1142,7 @@ static void apply_constraints(const oracle_inst* o, double* v) {
 static void raw_eg(const oracle_inst* o, const double* x, double* e, double* g) {
   if (o->kind == MINIM_GPU_LJ) lj_eg(o, x, e, g);
   else if (o->kind == MINIM_GPU_PF) pf_eg(o, x, e, g);
+  else if (o->kind == MINIM_GPU_PFU) pfu_eg(o, x, e, g);
   else bah_eg(o, x, e, g);
 }
 
@@ -1127,7 +1391,7 @@ void oracle_destroy(oracle_inst* o) {
   pf_t* p = &o->pf;
   free(p->kappa); free(p->kappaP); free(p->node_vol); free(p->surf_area); free(p->solid);
   free(p->contact); free(p->pressure); free(p->fix_fluid); free(p->confine); free(p->ff_init);
-  free(p->fmag); free(p->fnorm);
+  free(p->fmag); free(p->fnorm); free(p->volume);
   bah_t* b = &o->bah;
   free(b->bars); free(b->bpar); free(b->hinges); free(b->hpar); free(b->node_el); free(b->force);
   free(o);
@@ -1156,8 +1420,8 @@ int oracle_create(int kind, const void* params, const double* x0, size_t ndof,
     o->eps = q->epsilon;
     if (q->ndim < 1 || q->ndim > 3 || ndof % q->ndim)
       rc = set_err(MINIM_GPU_ERR_INVALID, "LjNd: Length of coords must be a multiple of the number of dimensions.");
-  } else if (kind == MINIM_GPU_PF) {
-    rc = pf_setup(o, params, x0);
+  } else if (kind == MINIM_GPU_PF || kind == MINIM_GPU_PFU) {
+    rc = pf_setup(o, params, x0, kind == MINIM_GPU_PFU);
   } else if (kind == MINIM_GPU_BAH) {
     rc = bah_setup(o, params, x0);
   } else {
@@ -1195,7 +1459,8 @@ int oracle_bah_elements(const oracle_inst* o, int* nbar, const int** bars, const
 
 int oracle_pf_internals(const oracle_inst* o, const double** kappa, const double** kappaP,
                         const double** node_vol, const double** surface_area, int* nk) {
-  if (o->kind != MINIM_GPU_PF) return set_err(MINIM_GPU_ERR_INVALID, "not a PhaseField instance");
+  if (o->kind != MINIM_GPU_PF && o->kind != MINIM_GPU_PFU)
+    return set_err(MINIM_GPU_ERR_INVALID, "not a PhaseField instance");
   *kappa = o->pf.kappa;
   *kappaP = o->pf.kappaP;
   *node_vol = o->pf.node_vol;

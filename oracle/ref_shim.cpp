@@ -1,5 +1,5 @@
 // ref_shim.cpp -- extern "C" driver over the reference minim library's own
-// public C++ API (State, Potential subclasses, Lbfgs/Fire/GradDescent).
+// public C++ API (State, Potential subclasses, Lbfgs/Fire/GradDescent/Anneal).
 //
 // Test infrastructure only: it is linked against the reference sources
 // compiled unmodified by oracle/Makefile into oracle/_ref/, and is used to
@@ -79,6 +79,37 @@ std::unique_ptr<State> build(int kind, const void* params, const double* x0, siz
     if (p->confinement) pf.setConfinement(vec_of(p->confinement, p->nfluid));
     if (!fix.empty()) pf.setConstraints(fix);
     return std::make_unique<State>(pf, x);
+  }
+  if (kind == MINIM_GPU_PFU) {
+    auto p = static_cast<const minim_gpu_pf_params*>(params);
+    PhaseFieldUnstructured pf;
+    pf.setNFluid(p->nfluid);
+    pf.setGridSize({p->grid[0], p->grid[1], p->grid[2]});
+    pf.setResolution(p->resolution);
+    if (p->n_interface_size > 0) pf.setInterfaceSize(vec_of(p->interface_size, p->n_interface_size));
+    if (p->n_surface_tension > 0) pf.setSurfaceTension(vec_of(p->surface_tension, p->n_surface_tension));
+    pf.densityConstraint = p->density_constraint;
+    pf.densityConst = p->density_const;
+    int ngrid = p->grid[0] * p->grid[1] * p->grid[2];
+    if (p->volume_fixed) {
+      if (p->volume) pf.setVolume(vec_of(p->volume, p->nfluid), p->vol_const);
+      else pf.setVolumeFixed(true, p->vol_const);
+    }
+    if (p->pressure) pf.setPressure(vec_of(p->pressure, p->nfluid));
+    if (p->solid) pf.setSolid(vec_of(p->solid, ngrid));
+    if (p->n_contact_angle > 0) pf.setContactAngle(vec_of(p->contact_angle, p->n_contact_angle));
+    if (p->force) {
+      pf.force = vector<vector<double>>(p->nfluid, vector<double>(3));
+      for (int f = 0; f < p->nfluid; f++)
+        for (int d = 0; d < 3; d++) pf.force[f][d] = p->force[3 * f + d];
+    }
+    if (p->fix_fluid) pf.fixFluid = vec_of(p->fix_fluid, p->nfluid);
+    if (p->confinement) pf.setConfinement(vec_of(p->confinement, p->nfluid));
+    // init() replaces the potential's constraint list, so fixed degrees of
+    // freedom are added to the state's own copy afterwards
+    auto st = std::make_unique<State>(pf, x);
+    if (!fix.empty()) st->pot->setConstraints(fix);
+    return st;
   }
   if (kind == MINIM_GPU_BAH) {
     auto p = static_cast<const minim_gpu_bah_params*>(params);
@@ -276,6 +307,18 @@ int ref_bah_elements(void* h, int cap, int* nbar, int* bars, double* bar_par,
 int ref_pf_internals(void* h, double* kappa, double* kappaP, double* node_vol,
                      double* surface_area, int* nk) {
   auto rs = static_cast<RefState*>(h);
+  if (rs->kind == MINIM_GPU_PFU) {
+    // nodeVol is per degree of freedom after initLocal; no surfaceArea member
+    auto& pf = static_cast<PhaseFieldUnstructured&>(*rs->state->pot);
+    *nk = (int)pf.kappa.size();
+    std::memcpy(kappa, pf.kappa.data(), pf.kappa.size() * sizeof(double));
+    std::memcpy(kappaP, pf.kappaP.data(), pf.kappaP.size() * sizeof(double));
+    for (int i = 0; i < pf.nGrid; i++) {
+      node_vol[i] = pf.nodeVol[(size_t)i * pf.nFluid];
+      surface_area[i] = 0;
+    }
+    return 0;
+  }
   auto& pf = static_cast<PhaseField&>(*rs->state->pot);
   *nk = (int)pf.kappa.size();
   std::memcpy(kappa, pf.kappa.data(), pf.kappa.size() * sizeof(double));

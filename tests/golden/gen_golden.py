@@ -9,7 +9,8 @@ minim_gb300.abi.*), the inputs and the reference's outputs:
   *_min                  : Minimiser::minimise results (final x, energy, iter)
   pf_setup               : kappa, kappaP, nodeVol, surfaceArea
   bah_setup              : element lists (bars, hinges) with their parameters
-Usage: python tests/golden/gen_golden.py
+  pfu_eg / pfu_min       : the same for PhaseFieldUnstructured
+Usage: python tests/golden/gen_golden.py [lj] [pf] [bah] [pfu]   (default: all)
 """
 import json
 import os
@@ -30,11 +31,11 @@ def params_from(kind, kw):
     kw = dict(kw)
     if kind == "lj":
         return abi.lj(**kw)
-    if kind == "pf":
+    if kind in ("pf", "pfu"):
         for k in ("solid", "fix_fluid"):
             if k in kw and kw[k] is not None:
                 kw[k] = np.asarray(kw[k], np.uint8)
-        return abi.phase_field(**kw)
+        return abi.phase_field(**kw) if kind == "pf" else abi.phase_field_unstructured(**kw)
     if kind == "bah":
         return abi.bar_and_hinge(**kw)
     raise ValueError(kind)
@@ -88,9 +89,20 @@ def save(fname, cases):
     np.savez_compressed(os.path.join(HERE, fname), **out)
 
 
-def main():
-    s2 = np.sqrt(2.0)
-    # ---- Lennard-Jones ------------------------------------------------------------
+def main(parts):
+    parts = set(parts) or {"lj", "pf", "bah", "pfu"}
+    if "lj" in parts:
+        gen_lj()
+    if "pf" in parts:
+        gen_pf()
+    if "bah" in parts:
+        gen_bah()
+    if "pfu" in parts:
+        gen_pfu()
+    print("wrote fixtures to", HERE)
+
+
+def gen_lj():
     lj = [eg_case("pair_kat", "lj", {}, [0, 0, 0, 2, 0, 0])]
     for n, nd, sig, eps in [(13, 3, 1.0, 1.0), (40, 3, 1.1, 0.7), (25, 2, 1.0, 1.0)]:
         x = lj_cluster(n, seed=n, ndim=nd)
@@ -110,7 +122,8 @@ def main():
                         {"method": "lbfgs", "m": 5, "tol": 1e-6}))
     save("lj_min.npz", ljm)
 
-    # ---- PhaseField -----------------------------------------------------------------
+
+def gen_pf():
     pf = []
     pf.append(eg_case("binary_3d", "pf", {"grid": [6, 5, 4]}, pf_noise((6, 5, 4), seed=2, amp=0.5)))
     pf.append(eg_case("binary_res2_pressure", "pf", {"grid": [5, 6, 7], "resolution": 2.0, "pressure": [1.5]},
@@ -150,7 +163,9 @@ def main():
                    "kappa": k, "kappaP": kp, "node_vol": nv, "surface_area": sa})
     save("pf_setup.npz", ps)
 
-    # ---- BarAndHinge -----------------------------------------------------------------
+
+def gen_bah():
+    s2 = np.sqrt(2.0)
     x2 = np.array([-1, 0, 1, 0, -s2, 0, 0, s2, 0, 1, 0, 1.0])
     tri2 = [[0, 1, 2], [1, 3, 2]]
     bah = [eg_case("two_triangles", "bah", {"triangulation": tri2, "rigidity": [100, 1]}, x2,
@@ -179,8 +194,62 @@ def main():
     bm.append(min_case("sheet6_relax", "bah", {"triangulation": tris, "rigidity": [1, 0.01]}, flat,
                        {"method": "lbfgs", "tol": 1e-7}, coords=pert))
     save("bah_min.npz", bm)
-    print("wrote fixtures to", HERE)
+
+
+def gen_pfu():
+    """PhaseFieldUnstructured: every element type, both fixed-volume forms,
+    all four density constraints (soft with three and four fluids), at
+    points away from the initial state (so the volume penalty acts)."""
+    solid = np.zeros((9, 8, 5), np.uint8)
+    solid[3:5, 2:4, 1:3] = 1
+    solid[:, 0, :] = 1
+    walls = np.zeros((12, 10, 1), np.uint8)
+    walls[:, 0, :] = 1
+    ca = Rng(14).uniform(solid.size) * 120 + 30
+
+    def case(name, kw, x0, seed, fixed=None):
+        x = np.asarray(x0, float) + 0.05 * Rng(seed + 50).normal(len(x0))
+        return eg_case(name, "pfu", kw, x0, x=x, fixed=fixed, seed=seed)
+
+    pfu = [case("binary_3d", {"grid": [6, 5, 4]}, pf_noise((6, 5, 4), seed=12, amp=0.5), 12),
+           case("binary_solid_contact_force_volume",
+                {"grid": [9, 8, 5], "solid": solid.ravel(), "contact_angle": ca, "force": [0.1, -0.3, 0.2],
+                 "pressure": [0.4], "volume_fixed": True, "vol_const": 0.5},
+                pf_noise((9, 8, 5), seed=14, amp=0.9), 14, fixed=[3, 50, 51]),
+           case("binary_2d_target_volume_res2",
+                {"grid": [10, 8, 1], "resolution": 2.0, "volume_fixed": True, "volume": [120.0],
+                 "vol_const": 0.2, "confinement": [1.5]}, pf_noise((10, 8, 1), seed=15, amp=0.9), 15)]
+    for dens in ["hard", "soft", "none", "fixed"]:
+        pfu.append(case(f"ternary_{dens}",
+                        {"grid": [12, 10, 1], "nfluid": 3, "solid": walls.ravel(), "volume_fixed": True,
+                         "density_constraint": dens, "surface_tension": [1.0, 0.8, 1.2],
+                         "pressure": [0, 0.3, 0], "force": [[0, -1, 0], [0.2, 0, 0], [0, 0, 0]],
+                         "confinement": [0, 1.0, 0]}, pf_simplex((12, 10, 1), 3, seed=16), 16))
+    for dens in ["soft", "fixed"]:
+        pfu.append(case(f"four_fluids_{dens}",
+                        {"grid": [5, 4, 3], "nfluid": 4, "density_constraint": dens,
+                         "solid": solid[:5, :4, :3].ravel(), "pressure": [0.1, 0, 0.2, 0.3]},
+                        pf_simplex((5, 4, 3), 4, seed=17), 17))
+    pfu.append(case("binary_fluids_fixfluid_pressure",
+                    {"grid": [6, 5, 3], "nfluid": 2, "fix_fluid": [1, 0], "pressure": [0.5, 0.25]},
+                    pf_simplex((6, 5, 3), 2, seed=18), 18, fixed=[4, 9]))
+    save("pfu_eg.npz", pfu)
+    pfum = [min_case("binary_8cubed", "pfu", {"grid": [8, 8, 8]}, pf_noise((8, 8, 8), seed=31),
+                     {"method": "lbfgs", "m": 10, "tol": 1e-7}),
+            min_case("binary_drop_volume_16", "pfu", {"grid": [16, 16, 1], "volume_fixed": True, "vol_const": 0.1},
+                     pfu_drop(16), {"method": "lbfgs", "tol": 1e-7, "max_iter": 20000}),
+            min_case("ternary_fixed_walls", "pfu",
+                     {"grid": [12, 10, 1], "nfluid": 3, "solid": walls.ravel(), "density_constraint": "fixed"},
+                     pf_simplex((12, 10, 1), 3, seed=33), {"method": "lbfgs", "tol": 1e-7, "max_iter": 20000})]
+    save("pfu_min.npz", pfum)
+
+
+def pfu_drop(n):
+    """A binary disc of radius 5 on an n x n grid (tanh profile)."""
+    X, Y = np.meshgrid(np.arange(n), np.arange(n), indexing="ij")
+    d = np.sqrt((X - (n - 1) / 2) ** 2 + (Y - (n - 1) / 2) ** 2)
+    return np.tanh((5 - d) / np.sqrt(2)).ravel()
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:])

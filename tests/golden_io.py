@@ -27,4 +27,4 @@ def load(fname):
 
 
 def case_ids(cases):
-    return [c["name"] for c in cases]
+    return [f'{c["kind"]}-{c["name"]}' for c in cases]

@@ -8,8 +8,8 @@ import pytest
 from oracle.oracle import Oracle
 from tests import golden_io as G
 
-EG = G.load("lj_eg.npz") + G.load("pf_eg.npz") + G.load("bah_eg.npz")
-MIN = G.load("lj_min.npz") + G.load("pf_min.npz") + G.load("bah_min.npz")
+EG = G.load("lj_eg.npz") + G.load("pf_eg.npz") + G.load("bah_eg.npz") + G.load("pfu_eg.npz")
+MIN = G.load("lj_min.npz") + G.load("pf_min.npz") + G.load("bah_min.npz") + G.load("pfu_min.npz")
 
 
 @pytest.mark.parametrize("c", EG, ids=G.case_ids(EG))
