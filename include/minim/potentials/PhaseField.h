@@ -70,7 +70,7 @@ class PhaseField : public NewPotential<PhaseField> {
 
   int nGrid = 1;
 
- private:
+ protected:
   minim_gpu_pf_params deviceParams(std::vector<double>& st, std::vector<double>& iw,
                                    std::vector<double>& ca, std::vector<double>& fo,
                                    std::vector<char>& fx, std::vector<double>& cf,

@@ -21,7 +21,8 @@
  *                               Potential::setConstraints(iFix) src/Potential.cpp:80-84
  *   minim_gpu_apply_constraints State::applyConstraints         src/State.cpp:321-323
  *   minim_gpu_minimise          Minimiser::minimise(state)      src/Minimiser.cpp:27-38
- *                               with Lbfgs/Fire/GradDescent     src/minimisers/{Lbfgs,Fire,GradDescent}.cpp
+ *                               with Lbfgs/Fire/GradDescent/Anneal
+ *                                                               src/minimisers/{Lbfgs,Fire,GradDescent,Anneal}.cpp
  *   minim_gpu_batch_*           (no counterpart: many States minimised together)
  *   minim_gpu_server_*          (no counterpart: continuous batching of requests)
  */
@@ -122,7 +123,7 @@ typedef struct {
 } minim_gpu_bah_params;
 
 /* ---- minimisers ---------------------------------------------------------- */
-enum { MINIM_LBFGS = 0, MINIM_FIRE = 1, MINIM_GD = 2 };
+enum { MINIM_LBFGS = 0, MINIM_FIRE = 1, MINIM_GD = 2, MINIM_ANNEAL = 3 };
 enum { MINIM_LS_BACKTRACKING = 0, MINIM_LS_NONE = 1 };
 /* Precision of the coordinates while minimising.  MIXED runs FP32
  * coordinates/gradients with FP64 reductions, then switches to FP64
@@ -140,7 +141,22 @@ typedef struct {
   double init_step;  /* Lbfgs::setInitStep (default 1) */
   double dt_max;     /* Fire dtMax (0 = estimate 0.1/sqrt|g| at start) */
   double alpha;      /* GradDescent::setAlpha (default 0.1) */
-  int precision;     /* MINIM_PREC_* */
+  int precision;     /* MINIM_PREC_* (Anneal always runs FP64 coordinates) */
+  /* Anneal(tempInit, displacement), include/minimisers/Anneal.h:9-44.  Each
+   * iteration moves every coordinate by displacement * U(-1, 1) from the
+   * last accepted state and accepts by the Metropolis rule at
+   * T = temp_init / (1 + cooling_rate * iter), or T = temp_schedule[iter]
+   * (clamped to the last entry) when a schedule is given -- a
+   * setCoolingSchedule function tabulated by the caller.  The random numbers
+   * are a counter-based hash of (seed, iter, index): the same seed gives the
+   * same run (the reference seeds rand() with time(0) + rank). */
+  double temp_init;         /* default 1 */
+  double displacement;      /* default 0.1 */
+  double cooling_rate;      /* setCoolingRate (default 1) */
+  int max_rejections;       /* setMaxRejections (default 0: runs max_iter + 1 iterations) */
+  int n_temp_schedule;      /* 0, or entries of temp_schedule */
+  const double* temp_schedule;  /* read during the call that uses it (batch: batch_add copies it) */
+  uint64_t seed;
 } minim_gpu_minimiser_params;
 
 typedef struct {
@@ -149,7 +165,7 @@ typedef struct {
   int fp64_iters;       /* iterations run with FP64 coordinates */
   int evals;            /* potential evaluations (energy-only and energy+gradient) */
   double energy;        /* energy at the returned coordinates */
-  double rms;           /* sqrt(g.g/ndof) at the returned coordinates */
+  double rms;           /* sqrt(g.g/ndof) at the returned coordinates (Anneal: 0, no gradient) */
   double dt_max;        /* Fire: the dtMax used (estimated when 0 was passed) */
   double latency_ms;    /* serving: submit -> completion wall time */
 } minim_gpu_result;

@@ -19,7 +19,7 @@ LJ, PF, BAH, PFU = 0, 1, 2, 3
 # PhaseField density constraints
 DENSITY = {"hard": 0, "gradient": 0, "soft": 1, "energy penalty": 1, "none": 2, "fixed": 3}
 # minimisers, line searches, precision
-LBFGS, FIRE, GD = 0, 1, 2
+LBFGS, FIRE, GD, ANNEAL = 0, 1, 2, 3
 LS_BACKTRACKING, LS_NONE = 0, 1
 PREC_MIXED, PREC_FP64, PREC_FP32 = 0, 1, 2
 
@@ -68,6 +68,9 @@ class MinimiserParams(C.Structure):
         ("tol", C.c_double), ("m", C.c_int), ("max_step", C.c_double),
         ("init_step", C.c_double), ("dt_max", C.c_double), ("alpha", C.c_double),
         ("precision", C.c_int),
+        ("temp_init", C.c_double), ("displacement", C.c_double), ("cooling_rate", C.c_double),
+        ("max_rejections", C.c_int), ("n_temp_schedule", C.c_int), ("temp_schedule", _dp),
+        ("seed", C.c_uint64),
     ]
 
 
@@ -232,14 +235,18 @@ def bar_and_hinge(triangulation=None, bonds=None, hinges=None, modulus=1.0, pois
     return Params(BAH, s, keep)
 
 
-_METHODS = {"lbfgs": LBFGS, "fire": FIRE, "gd": GD, "graddescent": GD}
+_METHODS = {"lbfgs": LBFGS, "fire": FIRE, "gd": GD, "graddescent": GD, "anneal": ANNEAL}
 
 
 def minimiser(method="lbfgs", linesearch=None, max_iter=100000, tol=-1.0, m=5, max_step=0.0,
-              init_step=1.0, dt_max=0.0, alpha=0.1, precision="mixed"):
+              init_step=1.0, dt_max=0.0, alpha=0.1, precision="mixed", temp_init=1.0,
+              displacement=0.1, cooling_rate=1.0, max_rejections=0, temp_schedule=None, seed=0):
     """Minimiser parameters with the reference defaults.  ``linesearch`` None
     takes the reference default: backtracking, except Fire with an explicit
-    dtMax (the ``Fire(dtMax)`` constructor) which uses none."""
+    dtMax (the ``Fire(dtMax)`` constructor) which uses none.  Anneal takes
+    ``temp_init``, ``displacement`` (its constructor's arguments),
+    ``cooling_rate``, ``max_rejections``, an optional tabulated
+    ``temp_schedule`` and the random ``seed``."""
     meth = _METHODS[method.lower()] if isinstance(method, str) else int(method)
     if linesearch is None:
         ls = LS_NONE if (meth == FIRE and dt_max != 0) else LS_BACKTRACKING
@@ -248,4 +255,11 @@ def minimiser(method="lbfgs", linesearch=None, max_iter=100000, tol=-1.0, m=5, m
             if isinstance(linesearch, str) else int(linesearch)
     prec = {"mixed": PREC_MIXED, "fp64": PREC_FP64, "fp32": PREC_FP32}[precision] \
         if isinstance(precision, str) else int(precision)
-    return MinimiserParams(meth, ls, max_iter, tol, m, max_step, init_step, dt_max, alpha, prec)
+    mp = MinimiserParams(meth, ls, max_iter, tol, m, max_step, init_step, dt_max, alpha, prec,
+                         temp_init, displacement, cooling_rate, max_rejections, 0, None, seed)
+    if temp_schedule is not None:
+        ts = _f64(temp_schedule)
+        mp._keep = ts
+        mp.n_temp_schedule = ts.size
+        mp.temp_schedule = ts.ctypes.data_as(_dp)
+    return mp

@@ -1,4 +1,4 @@
-// api_minimisers.cpp -- Lbfgs, Fire and GradDescent of the C++ API.
+// api_minimisers.cpp -- Lbfgs, Fire, GradDescent and Anneal of the C++ API.
 //
 // deviceParams() describes the algorithm to the GPU engine (the path taken
 // by minimise() for device potentials).  iteration() is the host loop used
@@ -6,8 +6,10 @@
 //   Lbfgs        src/minimisers/Lbfgs.cpp:34-133
 //   Fire         src/minimisers/Fire.cpp:11-90
 //   GradDescent  src/minimisers/GradDescent.cpp:11-46
+//   Anneal       src/minimisers/Anneal.cpp:9-95
 //   line search  src/minimisers/linesearch.cpp:8-30
 #include <cmath>
+#include <ctime>
 
 #include "minim.h"
 
@@ -229,5 +231,101 @@ void GradDescent::iteration(State& state) {
 bool GradDescent::checkConvergence(const State& state) {
   return std::sqrt(state.comm->dotProduct(_g, _g) / state.ndof) < state.convergence;
 }
+
+// ---- Anneal ------------------------------------------------------------------------
+namespace {
+// the engine's random numbers (SplitMix64's output mix, Steele, Lea and Flood
+// 2014, on a counter of (iteration, index) keyed by the seed)
+uint64_t mix64(uint64_t z) {
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ULL;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebULL;
+  return z ^ (z >> 31);
+}
+double anneal_unit(uint64_t seed, int iter, uint32_t idx) {
+  const uint64_t h = mix64(seed ^ mix64(((uint64_t)(uint32_t)iter << 32) | idx));
+  return (double)(h >> 11) * (1.0 / 9007199254740992.0);
+}
+uint64_t seed_of(uint64_t seed) { return seed ? seed : (uint64_t)std::time(nullptr) + (uint64_t)mpi.rank; }
+}  // namespace
+
+Anneal& Anneal::setDisplacement(double d) {
+  displacement = d;
+  return *this;
+}
+Anneal& Anneal::setTempInit(double t) {
+  tempInit = t;
+  return *this;
+}
+Anneal& Anneal::setCoolingRate(double r) {
+  coolingRate = r;
+  return *this;
+}
+Anneal& Anneal::setCoolingSchedule(std::function<double(int)> f) {
+  coolingSchedule = f;
+  return *this;
+}
+Anneal& Anneal::setMaxIter(int m) {
+  Minimiser::setMaxIter(m);
+  return *this;
+}
+Anneal& Anneal::setMaxRejections(int m) {
+  maxRejections = m;
+  return *this;
+}
+Anneal& Anneal::setSeed(uint64_t s) {
+  seed = s;
+  return *this;
+}
+
+bool Anneal::deviceParams(const State&, minim_gpu_minimiser_params* p) const {
+  p->method = MINIM_ANNEAL;
+  p->temp_init = tempInit;
+  p->displacement = displacement;
+  p->cooling_rate = coolingRate;
+  p->max_rejections = maxRejections;
+  p->seed = seed_of(seed);
+  _table.clear();
+  if (coolingSchedule) {
+    const int n = (int)std::min<long long>((long long)maxIter + 1, 1LL << 24);
+    _table.resize(n);
+    for (int i = 0; i < n; i++) _table[i] = coolingSchedule(i);
+    p->n_temp_schedule = n;
+    p->temp_schedule = _table.data();
+  }
+  return true;
+}
+
+void Anneal::init(State& state) {
+  _sinceAccepted = 0;
+  _currentState = state.blockCoords();
+  _currentE = state.energy();
+  _seed = seed_of(seed);
+}
+
+void Anneal::iteration(State& state) {
+  _temp = coolingSchedule ? coolingSchedule(iter) : tempInit / (1 + coolingRate * iter);
+  vector<double> next(_currentState.size());
+  for (size_t i = 0; i < next.size(); i++) {
+    const double r = 2 * anneal_unit(_seed, iter, (uint32_t)i) - 1;
+    next[i] = _currentState[i] + r * displacement;
+  }
+  state.blockCoords(next);
+  const double e = state.energy();
+  if (acceptMetropolis(e)) {
+    _currentState = state.blockCoords();
+    _currentE = e;
+    _sinceAccepted = 0;
+  } else {
+    _sinceAccepted++;
+  }
+  if (checkConvergence(state) || iter == maxIter) state.blockCoords(_currentState);
+}
+
+bool Anneal::acceptMetropolis(double energy) {
+  const double u = anneal_unit(_seed, iter, (uint32_t)_currentState.size());
+  return energy < _currentE || u < std::exp((_currentE - energy) / _temp);
+}
+
+bool Anneal::checkConvergence(const State&) { return maxRejections > 0 && _sinceAccepted >= maxRejections; }
 
 }  // namespace minim

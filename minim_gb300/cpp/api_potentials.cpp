@@ -225,6 +225,17 @@ minim_gpu_handle PhaseField::createDevice(const vector<double>& coords) const {
   return h;
 }
 
+// PhaseFieldUnstructured (src/potentials/PhaseFieldUnstructured.cpp): the
+// same description, created as the element-form kind.
+minim_gpu_handle PhaseFieldUnstructured::createDevice(const vector<double>& coords) const {
+  std::vector<double> st, iw, ca, fo, cf, pr, vol;
+  std::vector<char> fx;
+  minim_gpu_pf_params p = deviceParams(st, iw, ca, fo, fx, cf, pr, vol);
+  minim_gpu_handle h = nullptr;
+  throw_gpu(minim_gpu_instance_create(MINIM_GPU_PFU, &p, coords.data(), coords.size(), &h));
+  return h;
+}
+
 // diffuseSolid (src/potentials/PhaseField.cpp:998-1035): relax a solid mask
 // into a smooth field with a confinement potential, L-BFGS without line
 // search for at most 100 iterations (optionally twice).

@@ -189,6 +189,8 @@ struct WsLayout {
   size_t x32[2], x64[2], g[2], x32s, gs, S, Y, V, total, hstride;
   int nS, nY;
   bool fp64;
+  size_t sched;  // Anneal's tabulated temperatures
+  int nsched;
 };
 size_t align256(size_t v) { return (v + 255) & ~(size_t)255; }
 // dual: the stepped path's spare buffers for two line-search trials per pass
@@ -197,7 +199,7 @@ WsLayout ws_layout(size_t n, const minim_gpu_minimiser_params& mp, bool dual = f
   WsLayout L{};
   size_t o = 0;
   auto take = [&](size_t bytes) { size_t r = o; o += align256(bytes); return r; };
-  L.fp64 = mp.precision != MINIM_PREC_FP32;
+  L.fp64 = mp.precision != MINIM_PREC_FP32 || mp.method == MINIM_ANNEAL;
   L.nS = mp.method == MINIM_LBFGS ? mp.m + 1 : (mp.method == MINIM_FIRE ? 1 : 0);
   L.nY = mp.method == MINIM_LBFGS ? mp.m + 1 + (dual ? 1 : 0) : 0;
   for (int k = 0; k < 2; k++) L.x32[k] = take(n * 4);
@@ -212,6 +214,8 @@ WsLayout ws_layout(size_t n, const minim_gpu_minimiser_params& mp, bool dual = f
   L.S = L.nS ? take((size_t)L.nS * L.hstride * 4) : (size_t)-1;
   L.Y = L.nY ? take((size_t)L.nY * L.hstride * 4) : (size_t)-1;
   L.V = mp.method == MINIM_FIRE ? take(n * 4) : (size_t)-1;
+  L.nsched = (mp.method == MINIM_ANNEAL && mp.n_temp_schedule > 0) ? mp.n_temp_schedule : 0;
+  L.sched = L.nsched ? take((size_t)L.nsched * 8) : (size_t)-1;
   L.total = o;
   return L;
 }
@@ -228,9 +232,24 @@ void ws_apply(InstDesc& d, char* base, const WsLayout& L) {
   d.Yb = L.nY ? (float*)(base + L.Y) : nullptr;
   d.V = L.V != (size_t)-1 ? (float*)(base + L.V) : nullptr;
 }
+// after ws_apply and to_mp: Anneal's temperature table into the workspace
+void ws_sched(InstDesc& d, char* base, const WsLayout& L, const std::vector<double>& sched, cudaStream_t s) {
+  d.mp.ntsched = 0;
+  d.mp.tsched = nullptr;
+  if (!L.nsched || sched.empty()) return;
+  CK(cudaMemcpyAsync(base + L.sched, sched.data(), (size_t)L.nsched * 8, cudaMemcpyHostToDevice, s));
+  d.mp.tsched = (const double*)(base + L.sched);
+  d.mp.ntsched = L.nsched;
+}
+std::vector<double> sched_of(const minim_gpu_minimiser_params& mp) {
+  if (mp.method != MINIM_ANNEAL || mp.n_temp_schedule <= 0) return {};
+  return std::vector<double>(mp.temp_schedule, mp.temp_schedule + mp.n_temp_schedule);
+}
 
 void check_mp(const minim_gpu_minimiser_params& mp) {
-  if (mp.method < 0 || mp.method > 2) throw ApiError{MINIM_GPU_ERR_INVALID, "unknown minimiser method"};
+  if (mp.method < 0 || mp.method > 3) throw ApiError{MINIM_GPU_ERR_INVALID, "unknown minimiser method"};
+  if (mp.method == MINIM_ANNEAL && (mp.n_temp_schedule < 0 || (mp.n_temp_schedule > 0 && !mp.temp_schedule)))
+    throw ApiError{MINIM_GPU_ERR_INVALID, "Anneal: invalid temperature schedule"};
   if (mp.linesearch != MINIM_LS_BACKTRACKING && mp.linesearch != MINIM_LS_NONE)
     throw ApiError{MINIM_GPU_ERR_INVALID, "Invalid line search method."};
   if (mp.method == MINIM_LBFGS && (mp.m < 1 || mp.m > MINIM_MAXM))
@@ -250,6 +269,14 @@ MinParams to_mp(const minim_gpu_minimiser_params& q, double tol) {
   p.init_step = q.init_step;
   p.dt_max = q.dt_max;
   p.alpha = q.alpha;
+  if (q.method == MINIM_ANNEAL) {
+    p.precision = MINIM_PREC_FP64;  // the Metropolis test compares FP64 energies
+    p.temp_init = q.temp_init;
+    p.displacement = q.displacement;
+    p.cooling_rate = q.cooling_rate;
+    p.max_rej = q.max_rejections;
+    p.seed = q.seed;
+  }
   return p;
 }
 
@@ -538,6 +565,7 @@ void do_minimise(minim_gpu_instance_s* h, const minim_gpu_minimiser_params& mp, 
   InstDesc d = h->d;
   ws_apply(d, (char*)h->ws, L);
   d.mp = to_mp(mp, tol);
+  ws_sched(d, (char*)h->ws, L, sched_of(mp), D.s);
   d.stage_bytes = grid_stage_bytes(h->kk);
   d.pf_dist = prefetch_cfg();
   d.pf.pf_dist = d.pf_dist;
@@ -643,6 +671,7 @@ int guarded(F&& f) {
 struct minim_gpu_batch_s {
   std::vector<minim_gpu_handle> inst;
   std::vector<minim_gpu_minimiser_params> mp;
+  std::vector<std::vector<double>> sched;  // Anneal schedules, copied at batch_add
 };
 
 namespace {
@@ -738,6 +767,7 @@ struct Request {
   uint64_t id = 0;
   minim_gpu_instance_s* inst = nullptr;
   minim_gpu_minimiser_params mp{};
+  std::vector<double> sched;  // Anneal schedule, copied at submit
   double tol = 0;
   int state = 0;  // 0 queued, 1 resident, 2 done
   int slot = -1;
@@ -805,6 +835,9 @@ void minim_gpu_default_minimiser(int method, minim_gpu_minimiser_params* p) {
   p->dt_max = 0;
   p->alpha = 0.1;
   p->precision = MINIM_PREC_MIXED;
+  p->temp_init = 1;
+  p->displacement = 0.1;
+  p->cooling_rate = 1;
 }
 
 void minim_gpu_default_pf(minim_gpu_pf_params* p) {
@@ -910,6 +943,7 @@ int minim_gpu_batch_add(minim_gpu_batch b, minim_gpu_handle h, const minim_gpu_m
     check_mp(*mp);
     b->inst.push_back(h);
     b->mp.push_back(*mp);
+    b->sched.push_back(sched_of(*mp));
   });
 }
 
@@ -935,6 +969,7 @@ int minim_gpu_batch_run(minim_gpu_batch b, int threads, minim_gpu_result* result
       ws_apply(d, arena + off[i], L[i]);
       const double tol = b->mp[i].tol >= 0 ? b->mp[i].tol : b->inst[i]->default_tol;
       d.mp = to_mp(b->mp[i], tol);
+      ws_sched(d, arena + off[i], L[i], b->sched[i], D.s);
       d.st = d_st + i;
       descs[i] = d;
       kks[i] = b->inst[i]->kk;
@@ -998,6 +1033,7 @@ int minim_gpu_server_submit(minim_gpu_server s, int kind, const void* params, co
     r.id = s->next_id++;
     r.inst = create_instance(kind, params, x0, ndof);
     r.mp = *mp;
+    r.sched = sched_of(*mp);
     r.tol = mp->tol >= 0 ? mp->tol : r.inst->default_tol;
     r.bytes = ws_layout(ndof, *mp).total;
     r.t_submit = now_ms();
@@ -1039,6 +1075,7 @@ int minim_gpu_server_step(minim_gpu_server s, int* n_resident, int* n_queued) {
       InstDesc d = r.inst->d;
       ws_apply(d, (char*)r.ws, L);
       d.mp = to_mp(r.mp, r.tol);
+      ws_sched(d, (char*)r.ws, L, r.sched, D.s);
       d.st = s->d_st + free_slot;
       s->descs[free_slot] = d;
       admitted.push_back(free_slot);

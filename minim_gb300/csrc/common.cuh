@@ -392,6 +392,20 @@ struct NoPost {
   __device__ void operator()(double*) const {}
 };
 
+// Anneal's random numbers: SplitMix64's output mix (Steele, Lea and Flood
+// 2014) applied twice to a counter of (iteration, coordinate index), keyed by
+// the seed; the top 53 bits give u in [0, 1).  Stateless, so every thread
+// draws its own coordinates' numbers in any order.
+__device__ __forceinline__ unsigned long long mix64(unsigned long long z) {
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ULL;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebULL;
+  return z ^ (z >> 31);
+}
+__device__ __forceinline__ double anneal_unit(unsigned long long seed, int iter, unsigned idx) {
+  const unsigned long long h = mix64(seed ^ mix64(((unsigned long long)(unsigned)iter << 32) | idx));
+  return (double)(h >> 11) * (1.0 / 9007199254740992.0);
+}
+
 struct CtaTeam {
   // thread index and count come from special registers, never from memory
   __device__ __forceinline__ int tid() const { return threadIdx.x; }

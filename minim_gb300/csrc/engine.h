@@ -88,13 +88,19 @@ struct PotBAH {
 
 // ---- minimiser ------------------------------------------------------------------
 struct MinParams {
-  int method;       // 0 lbfgs, 1 fire, 2 gd
+  int method;       // 0 lbfgs, 1 fire, 2 gd, 3 anneal
   int linesearch;   // 0 backtracking, 1 none
   int max_iter;
   int m;
   int precision;    // 0 mixed, 1 fp64, 2 fp32
   double tol;
   double max_step, init_step, dt_max, alpha;
+  // Anneal
+  double temp_init, displacement, cooling_rate;
+  int max_rej;
+  int ntsched;               // entries of tsched (0: temp_init / (1 + cooling_rate * iter))
+  const double* tsched;      // device copy of the tabulated schedule
+  unsigned long long seed;
 };
 
 enum RunStatus { ST_CONVERGED = 0, ST_MAXITER = 1, ST_NAN = 2, ST_TIMEOUT = 3,
@@ -110,7 +116,7 @@ struct MinScalars {
   int evals;
   int fp64_iters;
   int stall;         // iterations since the best rms improved (stage 0)
-  int nsteps;        // Fire::_nSteps
+  int nsteps;        // Fire::_nSteps; Anneal::_sinceAccepted
   int pbuf, ybuf;    // spare history buffers (direction / new y)
   int ybuf2;         // second spare y slot (stepped path, two trials per pass), or -1
   int exhausted_run; // consecutive line searches that found no Armijo point

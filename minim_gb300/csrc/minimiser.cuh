@@ -884,6 +884,50 @@ struct Runner {
     MG_ACCT(abytes, (2.0 * xbytes() + 4.0) * n);
   }
 
+  // ---- simulated annealing -------------------------------------------------------------
+  // Anneal::iteration / acceptMetropolis (src/minimisers/Anneal.cpp:53-88):
+  // every coordinate moves by displacement * U(-1, 1) from the last accepted
+  // state (X64[xi]) into X64[1 - xi], the energy there decides by the
+  // Metropolis rule, and an accepted point becomes current by swapping the
+  // two buffers.  FP64 coordinates throughout.
+  __device__ void anneal_iteration() {
+    const MinParams& mp = in.mp;
+    const double T = mp.ntsched > 0 ? mp.tsched[iter < mp.ntsched ? iter : mp.ntsched - 1]
+                                    : mp.temp_init / (1 + mp.cooling_rate * iter);
+    const double* Xc = in.X64[xi];
+    double* Xn = in.X64[1 - xi];
+    for (int i = tm.tid(); i < n; i += tm.nthr()) {
+      const double r = 2 * anneal_unit(mp.seed, iter, (unsigned)i) - 1;
+      Xn[i] = __dadd_rn(Xc[i], __dmul_rn(r, mp.displacement));
+    }
+    tm.sync();
+    const unsigned long long t_start = globaltimer_ns();
+    FusedEmit ne{nullptr, nullptr, nullptr, nullptr, nullptr};
+    CView<double> cv{Xn, nullptr, 0.0};
+    double v[1] = {pot_eval<double>(cv, nullptr, ne, true, false)};
+    tm.reduce(v);
+    evals++;
+    count_eval(false, false);
+    MG_ACCT(tph[1], (double)(globaltimer_ns() - t_start));
+    MG_ACCT(abytes, 16.0 * n);  // the displacement pass: read x, write x'
+    const double En = v[0];
+    const double u = anneal_unit(mp.seed, iter, (unsigned)n);
+    if (En < E || u < exp((E - En) / T)) {
+      xi = 1 - xi;
+      E = En;
+      nsteps = 0;
+    } else {
+      nsteps++;
+    }
+  }
+  // Anneal::checkConvergence (lines 91-94), then the loop's iter++
+  __device__ bool anneal_post() {
+    fp64_iters++;
+    if (in.mp.max_rej > 0 && nsteps >= in.mp.max_rej) { status = ST_CONVERGED; return true; }
+    iter++;
+    return false;
+  }
+
   // ---- precision stages -------------------------------------------------------------
   __device__ void to_fp64() {
     const float* X = in.X32[xi];
@@ -1059,6 +1103,11 @@ struct Runner {
         pbuf = mp.m; ybuf = mp.m;
         pend = -1;
         __syncthreads();
+      } else if (mp.method == 3) {
+        // Anneal::init: the current state and its energy
+        nsteps = 0;
+        gg = 0.0;
+        E = energy_at(0.0, nullptr);
       } else if (mp.method == 1) {
         for (int i = tm.tid(); i < n; i += tm.nthr()) in.V[i] = 0.f;
         tm.sync();
@@ -1086,6 +1135,12 @@ struct Runner {
     for (int s = 0; s < slice && !done; s++) {
       if (iter > mp.max_iter) { status = ST_MAXITER; break; }
       bool exhausted = false;
+      if (mp.method == 3) {
+        anneal_iteration();
+        if (!tm.ok()) { status = ST_TIMEOUT; break; }
+        done = anneal_post();
+        continue;
+      }
       if (mp.method == 0) lbfgs_iteration(exhausted);
       else if (mp.method == 1) fire_iteration(exhausted);
       else gd_iteration(exhausted);

@@ -14,6 +14,7 @@
 #include <math.h>
 #include <stdarg.h>
 #include <stdio.h>
+#include <stdint.h>
 #include <stdlib.h>
 #include <string.h>
 
@@ -1212,7 +1213,96 @@ static double linesearch(oracle_inst* o, double* step, double de0, double* tmp) 
 /* Minimiser::minimise loop (src/Minimiser.cpp:27-38) with Lbfgs
  * (src/minimisers/Lbfgs.cpp:34-133), Fire (src/minimisers/Fire.cpp:27-90)
  * and GradDescent (src/minimisers/GradDescent.cpp:22-46). */
+/* ------------------------------------------------------------------------ */
+/* Anneal: src/minimisers/Anneal.cpp:45-95                                   */
+/* ------------------------------------------------------------------------ */
+/* The device engine's random numbers: SplitMix64's output mix (Steele, Lea
+ * and Flood 2014) applied twice to a counter made of the iteration and the
+ * coordinate index, keyed by the seed; 53 bits give u in [0, 1). */
+static uint64_t mix64(uint64_t z) {
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ULL;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebULL;
+  return z ^ (z >> 31);
+}
+static double anneal_unit(uint64_t seed, int iter, uint32_t idx) {
+  uint64_t h = mix64(seed ^ mix64(((uint64_t)(uint32_t)iter << 32) | idx));
+  return (double)(h >> 11) * (1.0 / 9007199254740992.0);
+}
+
+/* one random number: counter mode (the device engine's) or the C library's
+ * rand() in the reference's call order (to pin this restatement to the
+ * reference library itself) */
+typedef struct {
+  int libc;
+  uint64_t seed;
+} anneal_rng;
+static double anneal_draw(const anneal_rng* r, int iter, uint32_t idx) {
+  if (r->libc) return (double)rand() / RAND_MAX;
+  return anneal_unit(r->seed, iter, idx);
+}
+
+static int anneal_run(oracle_inst* o, const minim_gpu_minimiser_params* mp, const anneal_rng* rng,
+                      minim_gpu_result* res) {
+  size_t n = o->ndof;
+  int maxIter = mp->max_iter;
+  double* cur = xcalloc(n, sizeof(double));
+  o->evals = 0;
+  /* init: _sinceAccepted = 0, _currentState, _currentE */
+  memcpy(cur, o->x, n * sizeof(double));
+  double curE = st_energy(o, o->x);
+  int since = 0, iter;
+  for (iter = 0; iter <= maxIter; iter++) {
+    double T;
+    if (mp->n_temp_schedule > 0) {
+      int k = iter < mp->n_temp_schedule ? iter : mp->n_temp_schedule - 1;
+      T = mp->temp_schedule[k];
+    } else {
+      T = mp->temp_init / (1 + mp->cooling_rate * iter);
+    }
+    for (size_t j = 0; j < n; j++) {
+      double random = 2 * anneal_draw(rng, iter, (uint32_t)j) - 1;
+      o->x[j] = cur[j] + random * mp->displacement;
+    }
+    double e = st_energy(o, o->x);
+    /* acceptMetropolis: the random number is drawn before the comparison */
+    double u = anneal_draw(rng, iter, (uint32_t)n);
+    int accept = (e < curE) ? 1 : (u < exp((curE - e) / T));
+    if (accept) {
+      memcpy(cur, o->x, n * sizeof(double));
+      curE = e;
+      since = 0;
+    } else {
+      since++;
+    }
+    int conv = (mp->max_rejections > 0) && (since >= mp->max_rejections);
+    if (conv || iter == maxIter) memcpy(o->x, cur, n * sizeof(double));
+    if (conv) break;
+  }
+  free(cur);
+  if (res) {
+    memset(res, 0, sizeof *res);
+    res->iter = iter;
+    res->status = iter <= maxIter ? MINIM_RES_CONVERGED : MINIM_RES_MAXITER;
+    res->fp64_iters = iter <= maxIter ? iter + 1 : maxIter + 1;
+    res->evals = (int)o->evals;
+    res->energy = curE;
+    res->rms = 0; /* no gradient */
+  }
+  return 0;
+}
+
+int oracle_anneal_libc(oracle_inst* o, const minim_gpu_minimiser_params* mp, unsigned seed,
+                       minim_gpu_result* res) {
+  anneal_rng r = {1, 0};
+  srand(seed);
+  return anneal_run(o, mp, &r, res);
+}
+
 int oracle_minimise(oracle_inst* o, const minim_gpu_minimiser_params* mp, minim_gpu_result* res) {
+  if (mp->method == MINIM_ANNEAL) {
+    anneal_rng r = {0, mp->seed};
+    return anneal_run(o, mp, &r, res);
+  }
   size_t n = o->ndof;
   double tol = mp->tol >= 0 ? mp->tol : o->tol_default;
   int ls = mp->linesearch == MINIM_LS_BACKTRACKING;

@@ -2,10 +2,10 @@
  * minim_oracle.h -- CPU checker for the GPU engine (test infrastructure).
  *
  * A plain-C, FP64 restatement of the reference minim library's hot path:
- * LjNd / PhaseField / BarAndHinge energy and gradient, the generic and
- * PhaseField constraints, and the Lbfgs / Fire / GradDescent iterations with
- * the backtracking line search.  Only tests, the smoke check and the CPU
- * baseline leg of bench.py use it.  It is pinned against the reference's own
+ * LjNd / PhaseField / PhaseFieldUnstructured / BarAndHinge energy and
+ * gradient, the generic and PhaseField constraints, and the Lbfgs / Fire /
+ * GradDescent / Anneal iterations with the backtracking line search.  Only
+ * tests, the smoke check and the CPU baseline leg of bench.py use it.  It is pinned against the reference's own
  * unit-test constants and against fixtures produced by the reference library
  * itself (tests/golden/).
  */
@@ -39,6 +39,10 @@ int oracle_get_coords(const oracle_inst* o, double* x);
 int oracle_energy_gradient(oracle_inst* o, const double* x, double* e, double* g);
 int oracle_apply_constraints(oracle_inst* o, double* v);
 int oracle_minimise(oracle_inst* o, const minim_gpu_minimiser_params* mp, minim_gpu_result* res);
+/* Anneal with the C library's rand() after srand(seed), drawn in the
+ * reference's order (to compare with the reference library itself). */
+int oracle_anneal_libc(oracle_inst* o, const minim_gpu_minimiser_params* mp, unsigned seed,
+                       minim_gpu_result* res);
 /* BarAndHinge bars (2 nodes + {k,l0}) and hinges (4 nodes + {k,theta0}) in
  * the reference's element order. */
 int oracle_bah_elements(const oracle_inst* o, int* nbar, const int** bars, const double** bar_par,

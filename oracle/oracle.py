@@ -57,6 +57,8 @@ def _load_oracle():
         lib.oracle_pf_internals.argtypes = [C.c_void_p, C.POINTER(_dp), C.POINTER(_dp),
                                             C.POINTER(_dp), C.POINTER(_dp), _ip]
         lib.oracle_set_threads.argtypes = [C.c_void_p, C.c_int]
+        lib.oracle_anneal_libc.argtypes = [C.c_void_p, C.POINTER(abi.MinimiserParams), C.c_uint,
+                                           C.POINTER(abi.Result)]
         _lib = lib
     return _lib
 
@@ -168,6 +170,16 @@ class Oracle(_Base):
 
     def _error(self):
         return self._lib.oracle_last_error().decode()
+
+    def anneal_libc(self, mp):
+        """Anneal drawing its random numbers from the C library's rand()
+        after srand(mp.seed), in the reference's order: the same run as the
+        reference library's with the same seed."""
+        r = abi.Result()
+        rc = self._lib.oracle_anneal_libc(self.h, C.byref(mp), C.c_uint(mp.seed & 0xFFFFFFFF), C.byref(r))
+        if rc != 0:
+            raise RuntimeError(self._error())
+        return r
 
     @property
     def default_tol(self):

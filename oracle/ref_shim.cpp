@@ -11,6 +11,7 @@
 #include "minim_gpu.h"
 
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <stdexcept>
@@ -251,14 +252,33 @@ int ref_minimise(void* h, const minim_gpu_minimiser_params* mp, minim_gpu_result
       min.setLinesearch(ls);
       min.minimise(s);
       iter = min.iter;
+    } else if (mp->method == MINIM_ANNEAL) {
+      // Minimiser::minimise (src/Minimiser.cpp:27-38) spelled out, so that
+      // rand() can be seeded after Anneal::init (which seeds it from the
+      // clock): srand(seed), then the reference's own iterations
+      Anneal min(mp->temp_init, mp->displacement);
+      min.setCoolingRate(mp->cooling_rate).setMaxRejections(mp->max_rejections).setMaxIter(mp->max_iter);
+      if (mp->n_temp_schedule > 0) {
+        vector<double> tab(mp->temp_schedule, mp->temp_schedule + mp->n_temp_schedule);
+        min.setCoolingSchedule([tab](int i) { return tab[i < (int)tab.size() ? i : (int)tab.size() - 1]; });
+      }
+      min.init(s);
+      srand((unsigned)mp->seed);
+      for (min.iter = 0; min.iter <= min.maxIter; min.iter++) {
+        min.iteration(s);
+        if (min.checkConvergence(s)) break;
+      }
+      iter = min.iter;
     } else {
       throw std::invalid_argument("ref_shim: unknown minimiser");
     }
     if (res) {
       std::memset(res, 0, sizeof(*res));
-      auto g = s.gradient();
       double gg = 0;
-      for (double v : g) gg += v * v;
+      if (mp->method != MINIM_ANNEAL) {
+        auto g = s.gradient();
+        for (double v : g) gg += v * v;
+      }
       res->rms = std::sqrt(gg / s.ndof);
       res->energy = s.energy();
       res->iter = iter;

@@ -1,7 +1,8 @@
 // The reference library's unit tests, restated against the source-compatible
 // C++ API (include/minim/minim.h): same calls, same expected values.
 //   test/unit/State_test.cpp, Fire_test.cpp, Potential_test.cpp,
-//   BarAndHinge_test.cpp, PhaseField_test.cpp, Lbfgs_test.cpp
+//   BarAndHinge_test.cpp, PhaseField_test.cpp, PhaseFieldUnstructured_test.cpp,
+//   Lbfgs_test.cpp; examples/toy2d (Anneal)
 // Usage: api_test host   (host potentials only; no GPU needed)
 //        api_test all    (also the GPU-evaluated built-in potentials)
 #include <cmath>
@@ -37,7 +38,34 @@ class Toy2d : public NewPotential<Toy2d> {
   std::vector<double> gradient(const std::vector<double>& c) const override { return 2 * c; }
 };
 
+class Quartic2d : public NewPotential<Quartic2d> {  // examples/toy2d
+ public:
+  double energy(const std::vector<double>& c) const override {
+    return c[0] * c[0] + c[1] * c[1] + c[0] * c[0] * c[0] * c[0] + c[1] * c[1] * c[1] * c[1];
+  }
+  std::vector<double> gradient(const std::vector<double>& c) const override {
+    return {2 * c[0] + 4 * c[0] * c[0] * c[0], 2 * c[1] + 4 * c[1] * c[1] * c[1]};
+  }
+};
+
 static void host_tests() {
+  {  // examples/toy2d with Anneal (a fixed seed makes the run repeatable)
+    Quartic2d pot;
+    Vector out[2];
+    int iters[2];
+    for (int k = 0; k < 2; k++) {
+      State state = pot.newState({1, 4});
+      Anneal min = Anneal(1, 0.1).setMaxIter(20000).setSeed(42);
+      out[k] = min.minimise(state);
+      iters[k] = min.iter;
+    }
+    CHECK(out[0] == out[1] && iters[0] == 20001);
+    CHECK(vec::norm(out[0]) < 0.1);
+    State state = pot.newState({1, 4});
+    Anneal m2 = Anneal(1, 0.1).setMaxRejections(30).setSeed(3);
+    m2.minimise(state);
+    CHECK(m2.iter < 100000 && state.energy() < 17);
+  }
   {  // Fire_test TestStep
     Vector coords = {1, 4}, g = {2, 8};
     Toy2d pot;
@@ -181,6 +209,35 @@ static void device_tests() {
     int calls = 0;
     m2.minimise(s2, [&calls](int, State&) { calls++; });
     CHECK(calls > 0 && std::fabs(s2.energy() - (-6.0)) < 1e-6);
+  }
+  {  // PhaseFieldUnstructured_test TestPressureConstraint / TestVolumeConstraint
+    PhaseFieldUnstructured pot;
+    pot.setGridSize({6, 1, 1}).setSolid({1, 0, 0, 0, 0, 1}).setPressure({10});
+    auto sp = pot.newState({1, 1, 1, 1, 1, 1});
+    CHECK(sp.pot->potentialType() == Potential::UNSTRUCTURED);
+    CHECK(feq(sp.energy(), -30));
+    CHECK(near(sp.gradient(), {0, -2.5, -5, -5, -2.5, 0}));
+    PhaseFieldUnstructured pv;
+    pv.setGridSize({6, 1, 1});
+    pv.setSolid({1, 0, 0, 0, 0, 1});
+    pv.setVolumeFixed(true, 1);
+    State s1(pv, {1, 1, 1, 1, 1, 1});
+    CHECK(std::fabs(s1.energy()) < 1e-12);
+    pv.setVolume({1}, 100);
+    State s2(pv, {1, 1, 1, 1, 1, 1});
+    CHECK(feq(s2.energy(), 100 * 4));
+    CHECK(near(s2.gradient(), {0, 0, 0, 0, 0, 0}));
+  }
+  {  // Anneal on the GPU equals the host loop (same random numbers, device energies)
+    Lj3d potential;
+    Vector x0 = {0, 0, 0, 2, 0, 0, 1, 1, 0, 5, 1, 1};
+    State a(potential, x0), b(potential, x0);
+    Anneal ma = Anneal(0.2, 0.05).setMaxIter(2000).setSeed(9);
+    Anneal mb = Anneal(0.2, 0.05).setMaxIter(2000).setSeed(9);
+    auto xa = ma.minimise(a);
+    auto xb = mb.minimise(b, [](int, State&) {});
+    CHECK(ma.iter == mb.iter && near(xa, xb, 1e-12));
+    CHECK(a.energy() < State(potential, x0).energy());
   }
   {  // diffuseSolid produces a smooth field between 0 and 1
     std::vector<char> solid(16 * 16, 0);

@@ -10,7 +10,9 @@ minim_gb300.abi.*), the inputs and the reference's outputs:
   pf_setup               : kappa, kappaP, nodeVol, surfaceArea
   bah_setup              : element lists (bars, hinges) with their parameters
   pfu_eg / pfu_min       : the same for PhaseFieldUnstructured
-Usage: python tests/golden/gen_golden.py [lj] [pf] [bah] [pfu]   (default: all)
+  anneal_min             : Anneal runs with rand() seeded by srand(seed) after
+                           Anneal::init (the reference seeds it from the clock)
+Usage: python tests/golden/gen_golden.py [lj] [pf] [bah] [pfu] [anneal]   (default: all)
 """
 import json
 import os
@@ -90,7 +92,7 @@ def save(fname, cases):
 
 
 def main(parts):
-    parts = set(parts) or {"lj", "pf", "bah", "pfu"}
+    parts = set(parts) or {"lj", "pf", "bah", "pfu", "anneal"}
     if "lj" in parts:
         gen_lj()
     if "pf" in parts:
@@ -99,6 +101,8 @@ def main(parts):
         gen_bah()
     if "pfu" in parts:
         gen_pfu()
+    if "anneal" in parts:
+        gen_anneal()
     print("wrote fixtures to", HERE)
 
 
@@ -242,6 +246,35 @@ def gen_pfu():
                      {"grid": [12, 10, 1], "nfluid": 3, "solid": walls.ravel(), "density_constraint": "fixed"},
                      pf_simplex((12, 10, 1), 3, seed=33), {"method": "lbfgs", "tol": 1e-7, "max_iter": 20000})]
     save("pfu_min.npz", pfum)
+
+
+def gen_anneal():
+    """Anneal (src/minimisers/Anneal.cpp) on each potential kind: cooling by
+    rate and by a tabulated schedule, stopping on max_iter and on
+    max_rejections."""
+    flat, tris, pert = sheet(4, seed=71)
+    cases = [
+        ("lj13_maxiter", "lj", {}, lj_cluster(13, seed=5),
+         {"temp_init": 0.5, "displacement": 0.02, "max_iter": 3000, "seed": 11}),
+        ("lj13_max_rejections", "lj", {}, lj_cluster(13, seed=5),
+         {"temp_init": 0.1, "displacement": 0.05, "max_rejections": 50, "seed": 12}),
+        ("lj38_cooling_rate", "lj", {}, lj_cluster(38, seed=2),
+         {"temp_init": 2.0, "displacement": 0.01, "cooling_rate": 0.01, "max_iter": 2000, "seed": 13}),
+        ("lj13_schedule", "lj", {}, lj_cluster(13, seed=5),
+         {"temp_init": 1.0, "displacement": 0.02, "max_iter": 500, "seed": 14,
+          "temp_schedule": np.linspace(1, 0.001, 300).tolist()}),
+        ("pf_binary_6cubed", "pf", {"grid": [6, 6, 6]}, pf_noise((6, 6, 6), seed=3),
+         {"temp_init": 0.01, "displacement": 0.01, "max_iter": 500, "seed": 15}),
+        ("pfu_ternary", "pfu", {"grid": [6, 5, 1], "nfluid": 3}, pf_simplex((6, 5, 1), 3, seed=4),
+         {"temp_init": 0.05, "displacement": 0.01, "max_iter": 400, "seed": 16}),
+        ("bah_sheet4", "bah", {"triangulation": tris, "rigidity": [1, 0.01]}, pert,
+         {"temp_init": 1e-3, "displacement": 1e-3, "max_iter": 800, "seed": 17}),
+    ]
+    out = []
+    for name, kind, kw, x0, akw in cases:
+        mkw = dict(akw, method="anneal")
+        out.append(min_case(name, kind, kw, x0, mkw))
+    save("anneal_min.npz", out)
 
 
 def pfu_drop(n):
