@@ -529,7 +529,7 @@ __device__ __noinline__ double pf_eval(Team& tm, const PotPF& P, CView<T> cv, T*
       const T kap = (fl & PF_NODE_KAPPA) ? (T)P.kappa_node[dof] : (T)P.kappa[f];
       const T kP = (fl & PF_NODE_KAPPA) ? (T)P.kappaP_node[dof] : (T)P.kappaP[f];
       T gv = 0;
-      if (nall) gv -= gnall;
+      if (nall && f < nf - 1) gv -= gnall;
       // bulk (with PF_NALL the last fluid has none of its own)
       if (nall && f == nf - 1) {
         // nothing: its concentration is 1 minus the others'
@@ -620,7 +620,9 @@ __device__ __noinline__ double pf_eval(Team& tm, const PotPF& P, CView<T> cv, T*
           const T h = -(co0 * (T)P.fnorm[f][0] + co1 * (T)P.fnorm[f][1] + co2 * (T)P.fnorm[f][2]) *
                       (T)P.res;
           const T epc = V * (T)P.fmag[f] * h;
-          if (want_e && !force_e_done) e.add(cf * epc);
+          // PhaseField::forceEnergy returns after the first fluid when no
+          // gradient is asked for; the element form counts every fluid
+          if (want_e && (unstr || !force_e_done)) e.add(cf * epc);
           force_e_done = true;
           gv += (nf == 1) ? (T)0.5 * epc : epc;
         }
