@@ -14,6 +14,10 @@ N ~ U{13..400}, half FIRE (dtMax 0.1, no line search) and half L-BFGS
 (m = 5) to RMS < 1e-6, run by the persistent batch kernels, against the same
 instances minimised one at a time with the whole GPU (a sample).
 
+Also reported (key "rows"): Anneal on a batch of LJ clusters and
+PhaseFieldUnstructured on a batch of three-fluid grids, each against the CPU
+oracle on a sample.
+
 --impl reference times the CPU restatement of the reference algorithm
 (oracle/, or the reference library itself when it was built on this host)
 on a bounded sample of the same workload.
@@ -208,6 +212,8 @@ def run_gpu(args):
         out.update(run_mixed(args))
     if args.serve > 0:
         out.update(run_serving(args))
+    if args.rows:
+        out["rows"] = run_rows(args)
     if not args.no_cpu:
         out["cpu_baseline"] = cpu_baseline(results[-1].iter, budget_s=args.cpu_budget)
     return out
@@ -291,6 +297,79 @@ def run_mixed(args):
                             "instances": len(items), "converged": int(conv), "kernel_ms": st["kernel_ms"],
                             "workload": f"{npf} 2-D ternary PhaseField grids (64^2/128^2, fixed volume) + "
                                         f"{nbah} BarAndHinge sheets (1k-4.2k vertices), Lbfgs RMS<1e-7"}}
+
+
+def run_rows(args):
+    """The minimiser and potential beyond the headline path, each as one
+    batch launch with the FP64 oracle timed on a sample of the same instances
+    (one host thread, as the reference runs them):
+      anneal: `args.anneal` Lennard-Jones clusters of 38 particles, Anneal
+              (T0 0.3, displacement 0.02, rate 1) for 2000 iterations each,
+              FP64 coordinates -- annealing iterations (one energy evaluation
+              each) per second;
+      pfu:    `args.pfu` PhaseFieldUnstructured 2-D three-fluid grids (64^2,
+              DENSITY fixed: the last fluid from the others), Lbfgs to RMS
+              < 1e-7 -- converged minimisations per second."""
+    from minim_gb300 import abi, runtime
+    from oracle.oracle import Oracle
+    from tests.workloads import lj_cluster, pf_simplex
+    rows = {}
+    iters = 2000
+
+    def anneal_mp(i):
+        return abi.minimiser("anneal", temp_init=0.3, displacement=0.02, max_iter=iters - 1, seed=1 + i)
+
+    if args.anneal > 0:
+        b = runtime.Batch()
+        xs = [lj_cluster(38, seed=9000 + i) for i in range(args.anneal)]
+        insts = []
+        for i, x in enumerate(xs):
+            inst = runtime.Instance(abi.lj(), x)
+            b.add(inst, anneal_mp(i))
+            insts.append(inst)
+        res = b.run()
+        st = runtime.last_run_stats()
+        gpu_it = sum(r.iter for r in res)
+        gpu_rate = gpu_it / (st["kernel_ms"] / 1e3)
+        t0, cpu_it, k = time.perf_counter(), 0, 0
+        same = True
+        while k < len(xs) and (k < 2 or time.perf_counter() - t0 < args.cpu_budget / 4):
+            o = Oracle(abi.lj(), xs[k])
+            ro = o.minimise(anneal_mp(k))
+            cpu_it += ro.iter
+            same &= (ro.iter == res[k].iter and abs(ro.energy - res[k].energy) <= 1e-12 * abs(ro.energy))
+            k += 1
+        cpu_rate = cpu_it / (time.perf_counter() - t0)
+        rows["anneal"] = {"value": gpu_rate, "unit": "annealing iterations/s", "instances": len(xs),
+                          "kernel_ms": st["kernel_ms"], "pairs_per_s": gpu_rate * 38 * 37 / 2,
+                          "cpu_oracle": {"value": cpu_rate, "cores": 1, "sample": f"{k} clusters"},
+                          "speedup_vs_cpu": gpu_rate / cpu_rate, "sample_runs_match_oracle": bool(same),
+                          "workload": f"{len(xs)} LJ38 clusters, Anneal T0=0.3 d=0.02, {iters} iterations, FP64"}
+    if args.pfu > 0:
+        grid = (64, 64, 1)
+        p = abi.phase_field_unstructured(grid, nfluid=3, density_constraint="fixed")
+        mp = abi.minimiser("lbfgs", tol=1e-7, max_iter=20000)
+        xs = [pf_simplex(grid, 3, seed=9500 + i) for i in range(args.pfu)]
+        b = runtime.Batch()
+        for x in xs:
+            b.add(runtime.Instance(p, x), mp)
+        res = b.run()
+        st = runtime.last_run_stats()
+        conv = sum(r.status == abi.RES_CONVERGED for r in res)
+        gpu_rate = conv / (st["kernel_ms"] / 1e3)
+        t0, k, cpu_conv = time.perf_counter(), 0, 0
+        while k < len(xs) and (k < 1 or time.perf_counter() - t0 < args.cpu_budget / 4):
+            ro = Oracle(p, xs[k]).minimise(mp)
+            cpu_conv += ro.status == abi.RES_CONVERGED
+            k += 1
+        cpu_rate = cpu_conv / (time.perf_counter() - t0)
+        rows["pfu"] = {"value": gpu_rate, "unit": "converged minimisations/s", "instances": len(xs),
+                       "converged": int(conv), "kernel_ms": st["kernel_ms"],
+                       "cpu_oracle": {"value": cpu_rate, "cores": 1, "sample": f"{k} grids"},
+                       "speedup_vs_cpu": gpu_rate / cpu_rate if cpu_rate > 0 else None,
+                       "workload": f"{len(xs)} PhaseFieldUnstructured 64^2 three-fluid grids, DENSITY fixed, "
+                                   "Lbfgs RMS<1e-7"}
+    return rows
 
 
 def serving_requests(count, rate, seed=7):
@@ -479,6 +558,9 @@ def main():
     ap.add_argument("--mixed", type=int, default=96, help="instances in the mixed PF/BAH batch (0 = skip)")
     ap.add_argument("--serve-rate", type=float, default=2000.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--rows", type=int, default=1, help="1: also time Anneal and PhaseFieldUnstructured")
+    ap.add_argument("--anneal", type=int, default=1024, help="LJ clusters in the Anneal batch")
+    ap.add_argument("--pfu", type=int, default=64, help="grids in the PhaseFieldUnstructured batch")
     ap.add_argument("--cpu-budget", type=float, default=20.0)
     ap.add_argument("--ref-iters-hint", type=int, default=985,
                     help="iterations of a full minimisation (the GPU run of the same algorithm needs 981-987)")
