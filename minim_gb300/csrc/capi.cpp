@@ -129,6 +129,9 @@ Kern kern(int kk) {
 }
 const size_t kLjTileBytes = 1024 * 32;  // 1024 particles of 4 doubles
 size_t pot_smem(int kk) { return kk == K_LJ ? kLjTileBytes : 0; }
+// dynamic shared memory that leaves room for one batch CTA per SM (more than
+// half of an SM's 228 KB)
+const size_t kSpreadSmem = 120 * 1024;
 // Grid launches of the grid-sized potentials can stream the minimiser's
 // vector passes through a ring of kStages shared-memory stages of
 // MINIM_GPU_STAGE_KB kilobytes each (at most 50; 4 x 22.5 KB keeps two
@@ -718,28 +721,43 @@ void run_batch(std::vector<InstDesc>& descs, const std::vector<int>& kks, MinSca
   CK(cudaEventCreate(&ready));
   CK(cudaEventCreate(&t_end));
   CK(cudaEventRecord(ready, D.s));
-  int i0 = 0;
-  std::vector<cudaEvent_t> done;
-  while (i0 < n) {
+  // Every group's launch configuration first: the occupancy query loads a
+  // kernel that has not run yet in this process, and loading one while
+  // another kernel runs waits for it (lazy module loading), which would
+  // serialise the kinds' launches.
+  struct Launch {
+    int kk, i0, i1, thr, blocks;
+    size_t smem;
+  };
+  std::vector<Launch> launches;
+  for (int i0 = 0; i0 < n;) {
     const int kk = kks[order[i0]];
     int i1 = i0;
     while (i1 < n && kks[order[i1]] == kk) i1++;
     std::vector<InstDesc> grp(sorted.begin() + i0, sorted.begin() + i1);
     const int thr = threads > 0 ? threads : default_threads(kk, grp);
-    const size_t smem = pot_smem(kk);
+    // When every instance can have an SM to itself, the grid-sized kinds
+    // (FP64-pipe and bandwidth bound in one CTA) take enough shared memory
+    // that no two CTAs share an SM: otherwise the block scheduler may pair
+    // CTAs of these launches on one SM while other SMs idle.
+    const size_t smem = (kk != K_LJ && n <= D.nsm) ? kSpreadSmem : pot_smem(kk);
     int per_sm = 0;
     CK((cudaError_t)kern(kk).occ(0, thr, smem, &per_sm));
     if (per_sm < 1) throw ApiError{MINIM_GPU_ERR_CUDA, "batch kernel does not fit on an SM"};
-    const int blocks = std::min(i1 - i0, D.nsm * per_sm);
-    cudaStream_t ks = D.ks[kk];
+    launches.push_back({kk, i0, i1, thr, std::min(i1 - i0, D.nsm * per_sm), smem});
+    i0 = i1;
+  }
+  std::vector<cudaEvent_t> done;
+  for (const Launch& L : launches) {
+    cudaStream_t ks = D.ks[L.kk];
     CK(cudaStreamWaitEvent(ks, ready, 0));
-    CK((cudaError_t)kern(kk).batch(d_descs + i0, i1 - i0, d_counters + kk, slice, thr, blocks, smem, ks));
+    CK((cudaError_t)kern(L.kk).batch(d_descs + L.i0, L.i1 - L.i0, d_counters + L.kk, slice, L.thr, L.blocks,
+                                     L.smem, ks));
     g_launches++;
     cudaEvent_t ev;
     CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
     CK(cudaEventRecord(ev, ks));
     done.push_back(ev);
-    i0 = i1;
   }
   for (auto ev : done) {
     CK(cudaStreamWaitEvent(D.s, ev, 0));

@@ -160,9 +160,18 @@ grid_kernel(const InstDesc* __restrict__ inst, int op, const EvalIO* io, int sli
       done = smem;                                                                                \
     }                                                                                             \
   }                                                                                               \
+  static void mg_batch_smem_##NAME(size_t smem) {                                                 \
+    static size_t done = 0;                                                                       \
+    if (smem > done) {                                                                            \
+      cudaFuncSetAttribute((const void*)mg::batch_kernel<KIND>,                                   \
+                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);               \
+      done = smem;                                                                                \
+    }                                                                                             \
+  }                                                                                               \
   extern "C" int mg_launch_batch_##NAME(const mg::InstDesc* d_insts, int ninst, int* d_counter,   \
                                         int slice_iters, int threads, int blocks, size_t smem,    \
                                         void* stream) {                                           \
+    mg_batch_smem_##NAME(smem);                                                                   \
     const int tile = (int)(smem / sizeof(mg::D4));                                                \
     mg::batch_kernel<KIND><<<blocks, threads, smem, (cudaStream_t)stream>>>(                     \
         d_insts, ninst, d_counter, slice_iters, tile);                                            \
@@ -181,6 +190,7 @@ grid_kernel(const InstDesc* __restrict__ inst, int op, const EvalIO* io, int sli
   }                                                                                               \
   extern "C" int mg_occupancy_##NAME(int grid, int threads, size_t smem, int* blocks_per_sm) {    \
     if (grid) mg_grid_smem_##NAME(smem);                                                          \
+    else mg_batch_smem_##NAME(smem);                                                              \
     return grid ? (int)cudaOccupancyMaxActiveBlocksPerMultiprocessor(                             \
                       blocks_per_sm, mg::grid_kernel<KIND>, threads, smem)                        \
                 : (int)cudaOccupancyMaxActiveBlocksPerMultiprocessor(                             \
