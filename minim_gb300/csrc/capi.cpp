@@ -129,9 +129,6 @@ Kern kern(int kk) {
 }
 const size_t kLjTileBytes = 1024 * 32;  // 1024 particles of 4 doubles
 size_t pot_smem(int kk) { return kk == K_LJ ? kLjTileBytes : 0; }
-// dynamic shared memory that leaves room for one batch CTA per SM (more than
-// half of an SM's 228 KB)
-const size_t kSpreadSmem = 120 * 1024;
 // Grid launches of the grid-sized potentials can stream the minimiser's
 // vector passes through a ring of kStages shared-memory stages of
 // MINIM_GPU_STAGE_KB kilobytes each (at most 50; 4 x 22.5 KB keeps two
@@ -679,13 +676,17 @@ struct minim_gpu_batch_s {
 
 namespace {
 
+// The grid-sized kinds run 512 threads per CTA (one CTA per SM at 128
+// registers a thread): sixteen warps to hide the stencil's and the element
+// gathers' memory and FP64 latency.  The choice depends on the kind alone,
+// so an instance's result does not depend on the rest of the batch.
 int default_threads(int kk, const std::vector<InstDesc>& ds) {
   if (kk == K_LJ) {
     int nmax = 0;
     for (auto& d : ds) nmax = std::max(nmax, d.lj.np);
     return nmax <= 96 ? 64 : (nmax <= 192 ? 128 : 256);
   }
-  return 256;
+  return 512;
 }
 
 double cost_of(const InstDesc& d, int kk) {
@@ -736,11 +737,7 @@ void run_batch(std::vector<InstDesc>& descs, const std::vector<int>& kks, MinSca
     while (i1 < n && kks[order[i1]] == kk) i1++;
     std::vector<InstDesc> grp(sorted.begin() + i0, sorted.begin() + i1);
     const int thr = threads > 0 ? threads : default_threads(kk, grp);
-    // When every instance can have an SM to itself, the grid-sized kinds
-    // (FP64-pipe and bandwidth bound in one CTA) take enough shared memory
-    // that no two CTAs share an SM: otherwise the block scheduler may pair
-    // CTAs of these launches on one SM while other SMs idle.
-    const size_t smem = (kk != K_LJ && n <= D.nsm) ? kSpreadSmem : pot_smem(kk);
+    const size_t smem = pot_smem(kk);
     int per_sm = 0;
     CK((cudaError_t)kern(kk).occ(0, thr, smem, &per_sm));
     if (per_sm < 1) throw ApiError{MINIM_GPU_ERR_CUDA, "batch kernel does not fit on an SM"};

@@ -11,6 +11,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <type_traits>
+
 #include "engine.h"
 
 #define MINIM_MAXRED 8    // values reduced together in one team reduction
@@ -134,6 +136,41 @@ __device__ __forceinline__ DF df_rcp(DF b) {
   const DF r = DF{1.f, 0.f} - b * DF{y, 0.f};  // residual 1 - b y
   return DF{y, 0.f} + DF{y, 0.f} * r;
 }
+// Double-float as a number type (the same operations, with operators), for
+// code written once for float / double / double-float arithmetic.  Division
+// goes through the refined reciprocal; comparisons use the sign of the
+// normalised difference.
+struct DFn {
+  float hi, lo;
+  DFn() = default;
+  __device__ __forceinline__ DFn(DF a) : hi(a.hi), lo(a.lo) {}
+  __device__ __forceinline__ DFn(float a) : hi(a), lo(0.f) {}
+  __device__ __forceinline__ DFn(int a) : hi((float)a), lo(0.f) {}  // |a| < 2^24
+  __device__ __forceinline__ DFn(double a) {
+    const DF d = df_from(a);
+    hi = d.hi;
+    lo = d.lo;
+  }
+  __device__ __forceinline__ DF df() const { return DF{hi, lo}; }
+  __device__ __forceinline__ explicit operator double() const { return (double)hi + (double)lo; }
+  __device__ __forceinline__ explicit operator float() const { return __fadd_rn(hi, lo); }
+};
+__device__ __forceinline__ DFn operator+(DFn a, DFn b) { return DFn(a.df() + b.df()); }
+__device__ __forceinline__ DFn operator-(DFn a, DFn b) { return DFn(a.df() - b.df()); }
+__device__ __forceinline__ DFn operator-(DFn a) { return DFn(DF{-a.hi, -a.lo}); }
+__device__ __forceinline__ DFn operator*(DFn a, DFn b) { return DFn(a.df() * b.df()); }
+__device__ __forceinline__ DF df_rcp(DF b);
+__device__ __forceinline__ DFn operator/(DFn a, DFn b) { return DFn(a.df() * df_rcp(b.df())); }
+__device__ __forceinline__ DFn& operator+=(DFn& a, DFn b) { return a = a + b; }
+__device__ __forceinline__ DFn& operator-=(DFn& a, DFn b) { return a = a - b; }
+__device__ __forceinline__ DFn& operator*=(DFn& a, DFn b) { return a = a * b; }
+__device__ __forceinline__ bool operator<(DFn a, DFn b) { return (a - b).hi < 0.f; }
+__device__ __forceinline__ bool operator>(DFn a, DFn b) { return (a - b).hi > 0.f; }
+__device__ __forceinline__ bool operator<=(DFn a, DFn b) { return (a - b).hi <= 0.f; }
+__device__ __forceinline__ bool operator>=(DFn a, DFn b) { return (a - b).hi >= 0.f; }
+__device__ __forceinline__ bool operator==(DFn a, DFn b) { return (a - b).hi == 0.f; }
+__device__ __forceinline__ bool operator!=(DFn a, DFn b) { return (a - b).hi != 0.f; }
+
 __device__ __forceinline__ DF df_shfl(DF a, int src) {
   return DF{__shfl_sync(0xffffffffu, a.hi, src), __shfl_sync(0xffffffffu, a.lo, src)};
 }
@@ -411,7 +448,7 @@ struct CtaTeam {
   __device__ __forceinline__ int tid() const { return threadIdx.x; }
   __device__ __forceinline__ int nthr() const { return blockDim.x; }
   double* red;  // shared scratch, >= (32 + 1) * MINIM_MAXRED doubles
-  double* wide; // shared scratch, >= (8 + 1) * MINIM_WIDE doubles
+  double* wide; // shared scratch, one row of MINIM_WIDE doubles per warp
   static constexpr bool kGrid = false;
   __device__ __forceinline__ void sync() { __syncthreads(); }
   __device__ __forceinline__ bool ok() const { return true; }

@@ -15,7 +15,7 @@ namespace mg {
 
 struct SharedScalars {
   double red[(32 + 1) * MINIM_MAXRED];
-  double wide[8 * MINIM_WIDE];
+  double wide[16 * MINIM_WIDE];  // one row per warp (up to 512 threads)
   double wout[MINIM_WIDE];
   double SY[MINIM_MAXM * MINIM_MAXM], YY[MINIM_MAXM * MINIM_MAXM];
   float coefS[MINIM_MAXM], coefY[MINIM_MAXM];
@@ -47,8 +47,10 @@ __device__ void setup_runner(Runner<Team, KIND>& R, SharedScalars& S, const Inst
   R.sq = 0u;
 }
 
+// (512, 1) caps registers at 128 as (256, 2) does; 512-thread blocks run the
+// grid-sized kinds when every instance has an SM to itself
 template <int KIND>
-__global__ void __launch_bounds__(256, 2)
+__global__ void __launch_bounds__(512, 1)
 batch_kernel(const InstDesc* __restrict__ insts, int ninst, int* counter, int slice, int lj_tile) {
   __shared__ SharedScalars S;
   __shared__ __align__(16) InstDesc s_in;
@@ -74,7 +76,7 @@ __device__ void eval_op(Runner<Team, KIND>& R, Team& tm, const InstDesc& in, con
   CView<double> cv{io.x, nullptr, 0.0};
   StoreEmit64 em{io.g, in.fixed};
   const bool want_g = io.g != nullptr;
-  const double ep = R.template pot_eval<double>(cv, nullptr, em, true, want_g);
+  const double ep = R.template pot_eval<double, false>(cv, nullptr, em, true, want_g);
   if constexpr (KIND == K_PF) {
     if (want_g && (in.pf.flags & PF_VOLUME)) {
       tm.sync();

@@ -154,7 +154,10 @@ struct Runner {
   }
 
   // ---- potential dispatch -------------------------------------------------------
-  template <typename T, class Emit>
+  // kFast: the FP64-coordinate evaluations of the minimiser may use
+  // double-float arithmetic (general PhaseField); the API evaluation and
+  // Anneal's Metropolis energies use FP64 throughout.
+  template <typename T, bool kFast = true, class Emit>
   __device__ double pot_eval(CView<T> cv, T* xw, Emit& em, bool want_e, bool want_g) {
     if constexpr (KIND == K_LJ) {
       if constexpr (!Team::kGrid) {
@@ -167,6 +170,10 @@ struct Runner {
       }
       return lj_eval<T>(tm, in.lj, cv, xw, &em, want_e, want_g, smem_pot, lj_tile);
     } else if constexpr (KIND == K_PF) {
+      if constexpr (kFast && std::is_same_v<T, double>) {
+        // the FP32 coordinate buffers are free while the coordinates are FP64
+        if (in.mp.method != 3) return pf_eval_df(tm, in.pf, cv, xw, &em, want_e, want_g, in.X32[0], in.X32[1]);
+      }
       return pf_eval<T>(tm, in.pf, cv, xw, &em, want_e, want_g);
     } else if constexpr (KIND == K_PF1) {
       if ((in.pf.n[2] & 3) == 0) return pf1_eval_quad<T>(tm, in.pf, cv, xw, &em, want_e, want_g);
@@ -904,7 +911,7 @@ struct Runner {
     const unsigned long long t_start = globaltimer_ns();
     FusedEmit ne{nullptr, nullptr, nullptr, nullptr, nullptr};
     CView<double> cv{Xn, nullptr, 0.0};
-    double v[1] = {pot_eval<double>(cv, nullptr, ne, true, false)};
+    double v[1] = {pot_eval<double, false>(cv, nullptr, ne, true, false)};
     tm.reduce(v);
     evals++;
     count_eval(false, false);

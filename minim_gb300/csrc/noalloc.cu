@@ -165,6 +165,13 @@ extern "C" int minim_gpu_lj_minimise_noalloc(const minim_gpu_lj_params* p, doubl
   if (e == cudaSuccess) {
     const int lj_tile = 1024;
     const size_t smem = (size_t)lj_tile * sizeof(D4);
+    // static plus dynamic shared memory is above the 48 KB default
+    static const cudaError_t opt_in = cudaFuncSetAttribute(
+        (const void*)noalloc_lj_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (opt_in != cudaSuccess) {
+      mg_set_last_error(cudaGetErrorString(opt_in));
+      return MINIM_GPU_ERR_CUDA;
+    }
     noalloc_lj_kernel<<<1, 256, smem, st>>>(d, 0x7fffffff, lj_tile);
     e = cudaGetLastError();
   }

@@ -39,6 +39,11 @@ template <> struct EAcc<double> {
   __device__ __forceinline__ void add(double v) { d += v; }
   __device__ __forceinline__ double total() const { return d; }
 };
+template <> struct EAcc<DFn> {
+  DFn s = DFn(0);
+  __device__ __forceinline__ void add(DFn v) { s += v; }
+  __device__ __forceinline__ double total() const { return (double)s; }
+};
 
 struct NoEmit {
   template <typename T>
@@ -404,17 +409,26 @@ __device__ __forceinline__ int pf_type1(const PotPF& P, int node) {  // type + 1
   return P.aux ? (int)(P.aux[node] & 15u) : 1;
 }
 
-template <typename T, class Team, class Emit>
-__device__ __noinline__ double pf_eval(Team& tm, const PotPF& P, CView<T> cv, T* xw, Emit* emp,
-                                       bool want_e, bool want_g) {
+template <typename T, typename A, class Src, class Team, class Emit>
+__device__ __forceinline__ double pf_eval_impl(Team& tm, const PotPF& P, const Src& src, CView<T> cv, T* xw,
+                                               Emit* emp, bool want_e, bool want_g) {
   constexpr int NFMAX = MINIM_MAXF;
   Emit emit = *emp;
   const int nf = P.nfluid;
   const int nx = P.n[0], ny = P.n[1], nz = P.n[2];
   const int ng = P.ngrid;
   const unsigned fl = P.flags;
-  const T res2 = (T)P.res2;
-  EAcc<T> e;
+  const A res2 = (A)P.res2;
+  EAcc<A> e;
+  // the parameters in the arithmetic type, converted once
+  A volA[9], kapA[NFMAX], kPA[NFMAX];
+#pragma unroll
+  for (int t = 0; t < 9; t++) volA[t] = (A)P.vol_of_type[t];
+#pragma unroll
+  for (int f = 0; f < NFMAX; f++) {
+    kapA[f] = (A)P.kappa[f];
+    kPA[f] = (A)P.kappaP[f];
+  }
   // PF_UVOL: volume differences at these coordinates, every thread
   double dvol[NFMAX];
 #pragma unroll
@@ -435,7 +449,7 @@ __device__ __noinline__ double pf_eval(Team& tm, const PotPF& P, CView<T> cv, T*
     for (int f = 0; f < NFMAX; f++) {
       if (f < nf) {
         dvol[f] -= P.vol_target[f];
-        if (want_e && tm.tid() == 0) e.add((T)(P.vol_coef * dvol[f] * dvol[f]));
+        if (want_e && tm.tid() == 0) e.add((A)(P.vol_coef * dvol[f] * dvol[f]));
       }
     }
   }
@@ -454,23 +468,23 @@ __device__ __noinline__ double pf_eval(Team& tm, const PotPF& P, CView<T> cv, T*
     const int t1 = (int)(aux_i & 15u);
     const bool solid_i = (t1 == 0);
     const unsigned mask_i = aux_i >> 4;
-    const T V = (T)P.vol_of_type[t1];
+    const A V = volA[t1];
     unsigned aux_nb[6];
 #pragma unroll
     for (int k = 0; k < 6; k++) aux_nb[k] = P.aux ? P.aux[nb[k]] : 1u;
 
-    T c[NFMAX], g[NFMAX];
+    A c[NFMAX], g[NFMAX];
 #pragma unroll
     for (int f = 0; f < NFMAX; f++) {
       if (f < nf) {
-        c[f] = cv(iG * nf + f);
-        if (xw) xw[iG * nf + f] = c[f];
+        c[f] = src(iG * nf + f);
+        if (xw) xw[iG * nf + f] = cv(iG * nf + f);
         g[f] = 0;
       }
     }
     // solid nodes carry no elements in the element form
     const bool node_terms = !(unstr && solid_i);
-    T rd = -1;  // soft density: sum c - 1 (element form: the first three fluids)
+    A rd = -1;  // soft density: sum c - 1 (element form: the first three fluids)
     if (fl & PF_SOFT) {
       if (unstr) {
         rd = c[0] + c[1] + c[2] - 1;
@@ -484,9 +498,9 @@ __device__ __noinline__ double pf_eval(Team& tm, const PotPF& P, CView<T> cv, T*
     // other fluid receives with the opposite sign.  Its local indices are all
     // distinct, so a solid neighbour (replaced by the node itself) enters as
     // a zero difference, and its factor has no 1/res^2.
-    T gnall = 0;
+    A gnall = 0;
     if (nall && node_terms) {
-      T cN[7];
+      A cN[7];
 #pragma unroll
       for (int k = 0; k < 7; k++) cN[k] = 1;
 #pragma unroll
@@ -494,28 +508,28 @@ __device__ __noinline__ double pf_eval(Team& tm, const PotPF& P, CView<T> cv, T*
         if (f < nf - 1) {
           cN[0] -= c[f];
 #pragma unroll
-          for (int k = 0; k < 6; k++) cN[k + 1] -= cv((((mask_i >> k) & 1u) ? iG : nb[k]) * nf + f);
+          for (int k = 0; k < 6; k++) cN[k + 1] -= src((((mask_i >> k) & 1u) ? iG : nb[k]) * nf + f);
         }
       }
-      const T bN = (T)0.5 * (T)P.kappa[nf - 1] * V;
-      const T gfN = (T)0.5 * (T)P.kappaP[nf - 1] * V;
-      const T a = cN[0] * (cN[0] - 1);
+      const A bN = (A)0.5 * kapA[nf - 1] * V;
+      const A gfN = (A)0.5 * kPA[nf - 1] * V;
+      const A a = cN[0] * (cN[0] - 1);
       if (want_e) e.add(bN * a * a);
       gnall = bN * 2 * cN[0] * (cN[0] - 1) * (2 * cN[0] - 1);
-      T eg = 0;
+      A eg = 0;
 #pragma unroll
       for (int d = 0; d < 3; d++) {
-        const T gm = cN[0] - cN[1 + 2 * d], gp = cN[0] - cN[2 + 2 * d];
-        eg += (T)0.5 * (gm * gm + gp * gp);
+        const A gm = cN[0] - cN[1 + 2 * d], gp = cN[0] - cN[2 + 2 * d];
+        eg += (A)0.5 * (gm * gm + gp * gp);
         gnall += gfN * (gm + gp);
         // the elements of the non-solid neighbours, whose slot toward this
         // node holds this node
 #pragma unroll
         for (int sd = 0; sd < 2; sd++) {
           const int k = 2 * d + sd;
-          if ((mask_i >> k) & 1u) continue;
-          const T Vj = (T)P.vol_of_type[aux_nb[k] & 15u];
-          gnall -= (T)0.5 * (T)P.kappaP[nf - 1] * Vj * (cN[1 + k] - cN[0]);
+          if (((mask_i >> k) & 1u) || !want_g) continue;
+          const A Vj = volA[aux_nb[k] & 15u];
+          gnall -= (A)0.5 * kPA[nf - 1] * Vj * (cN[1 + k] - cN[0]);
         }
       }
       if (want_e) e.add(gfN * eg);
@@ -525,39 +539,39 @@ __device__ __noinline__ double pf_eval(Team& tm, const PotPF& P, CView<T> cv, T*
     for (int f = 0; f < NFMAX; f++) {
       if (f >= nf) break;
       const int dof = iG * nf + f;
-      const T cc = c[f];
-      const T kap = (fl & PF_NODE_KAPPA) ? (T)P.kappa_node[dof] : (T)P.kappa[f];
-      const T kP = (fl & PF_NODE_KAPPA) ? (T)P.kappaP_node[dof] : (T)P.kappaP[f];
-      T gv = 0;
+      const A cc = c[f];
+      const A kap = (fl & PF_NODE_KAPPA) ? (A)P.kappa_node[dof] : kapA[f];
+      const A kP = (fl & PF_NODE_KAPPA) ? (A)P.kappaP_node[dof] : kPA[f];
+      A gv = 0;
       if (nall && f < nf - 1) gv -= gnall;
       // bulk (with PF_NALL the last fluid has none of its own)
       if (nall && f == nf - 1) {
         // nothing: its concentration is 1 minus the others'
       } else if (nf == 1) {
-        const T fac = kap / 16 * V;
-        const T a = (cc + 1) * (cc - 1);
+        const A fac = kap / 16 * V;
+        const A a = (cc + 1) * (cc - 1);
         if (want_e) e.add(fac * a * a);
         gv += fac * 4 * cc * (cc * cc - 1);
       } else {
-        const T fac = (T)0.5 * kap * V;
-        const T a = cc * (cc - 1);
+        const A fac = (A)0.5 * kap * V;
+        const A a = cc * (cc - 1);
         if (want_e) e.add(fac * a * a);
         gv += fac * 2 * cc * (cc - 1) * (2 * cc - 1);
       }
       // gradient energy
-      const T coefk = ((nf == 1) ? (T)0.25 : (T)0.5) / res2;
-      const T Fi = coefk * kP * V;
-      T eg = 0;
+      const A coefk = ((nf == 1) ? (A)0.25 : (A)0.5) / res2;
+      const A Fi = coefk * kP * V;
+      A eg = 0;
       const bool own_grad = !(nall && f == nf - 1);
 #pragma unroll
       for (int d = 0; d < 3; d++) {
         if (P.n[d] == 1 || !own_grad) continue;
         const int im = nb[2 * d], ip = nb[2 * d + 1];
-        const T cm = cv(im * nf + f), cp = cv(ip * nf + f);
+        const A cm = src(im * nf + f), cp = src(ip * nf + f);
         const bool sm = (mask_i >> (2 * d)) & 1u, sp = (mask_i >> (2 * d + 1)) & 1u;
-        const T gm = cc - cm, gp = cc - cp;
+        const A gm = cc - cm, gp = cc - cp;
         if (!sm && !sp) {
-          eg += (T)0.5 * (gm * gm + gp * gp);
+          eg += (A)0.5 * (gm * gm + gp * gp);
           gv += Fi * (gm + gp);
         } else if (!sp) {
           eg += gp * gp;
@@ -566,40 +580,40 @@ __device__ __noinline__ double pf_eval(Team& tm, const PotPF& P, CView<T> cv, T*
           eg += gm * gm;
           gv += Fi * 2 * gm;
         }
-        if (!solid_i) {
+        if (!solid_i && want_g) {  // gradient only: energy-only sweeps skip the gathers
           if (!sp) {  // term of node p whose minus neighbour is this node
             const unsigned ap = aux_nb[2 * d + 1];
-            const T Vp = (T)P.vol_of_type[ap & 15u];
-            const T kPp = (fl & PF_NODE_KAPPA) ? (T)P.kappaP_node[ip * nf + f] : kP;
-            const T Fp = coefk * kPp * Vp;
+            const A Vp = volA[ap & 15u];
+            const A kPp = (fl & PF_NODE_KAPPA) ? (A)P.kappaP_node[ip * nf + f] : kP;
+            const A Fp = coefk * kPp * Vp;
             const bool pp_solid = ((ap >> 4) >> (2 * d + 1)) & 1u;
-            gv -= (pp_solid ? (T)2 : (T)1) * Fp * (cp - cc);
+            gv -= (pp_solid ? (A)2 : (A)1) * Fp * (cp - cc);
           }
           if (!sm) {  // term of node m whose plus neighbour is this node
             const unsigned am = aux_nb[2 * d];
-            const T Vm = (T)P.vol_of_type[am & 15u];
-            const T kPm = (fl & PF_NODE_KAPPA) ? (T)P.kappaP_node[im * nf + f] : kP;
-            const T Fm = coefk * kPm * Vm;
+            const A Vm = volA[am & 15u];
+            const A kPm = (fl & PF_NODE_KAPPA) ? (A)P.kappaP_node[im * nf + f] : kP;
+            const A Fm = coefk * kPm * Vm;
             const bool mm_solid = ((am >> 4) >> (2 * d)) & 1u;
-            gv -= (mm_solid ? (T)2 : (T)1) * Fm * (cm - cc);
+            gv -= (mm_solid ? (A)2 : (A)1) * Fm * (cm - cc);
           }
         }
       }
       if (want_e) e.add(Fi * eg);
       // surface (binary only)
       if ((fl & PF_CONTACT) && nf == 1) {
-        const T w = (T)P.wet[iG];
+        const A w = (A)P.wet[iG];
         if (w != 0) {
-          if (want_e) e.add(w * (cc * cc * cc / 3 - cc - (T)(2.0 / 3)));
+          if (want_e) e.add(w * (cc * cc * cc / 3 - cc - (A)(2.0 / 3)));
           gv += w * (cc * cc - 1);
         }
       }
       // pressure (the element form has it on fixed fluids too)
       if ((fl & PF_PRESSURE) && P.pressure[f] != 0 && node_terms && (unstr || !((P.fix_mask >> f) & 1u))) {
-        const T pr = (T)P.pressure[f];
+        const A pr = (A)P.pressure[f];
         if (nf == 1) {
-          if (want_e) e.add(-pr * ((T)0.5 * (cc + 1) * V));
-          gv -= (T)0.5 * pr * V;
+          if (want_e) e.add(-pr * ((A)0.5 * (cc + 1) * V));
+          gv -= (A)0.5 * pr * V;
         } else {
           if (want_e) e.add(-pr * (cc * V));
           gv -= pr * V;
@@ -607,40 +621,40 @@ __device__ __noinline__ double pf_eval(Team& tm, const PotPF& P, CView<T> cv, T*
       }
       // soft density
       if ((fl & PF_SOFT) && nf > 1 && node_terms && (!unstr || f < 3)) {
-        const T sc = (T)P.soft_coef;
+        const A sc = (A)P.soft_coef;
         if (want_e && f == 0) e.add(sc * rd * rd);
         gv += 2 * sc * rd;
       }
       // body force
       if ((fl & PF_FORCE) && !solid_i && P.fmag[f] != 0) {
-        const T cf = (nf == 1) ? (T)0.5 * (1 + cc) : cc;
-        if (cf >= (T)0.01) {
-          const T co0 = (T)(x - (nx - 1) / 2.0), co1 = (T)(y - (ny - 1) / 2.0),
-                  co2 = (T)(z - (nz - 1) / 2.0);
-          const T h = -(co0 * (T)P.fnorm[f][0] + co1 * (T)P.fnorm[f][1] + co2 * (T)P.fnorm[f][2]) *
-                      (T)P.res;
-          const T epc = V * (T)P.fmag[f] * h;
+        const A cf = (nf == 1) ? (A)0.5 * (1 + cc) : cc;
+        if (cf >= (A)0.01) {
+          const A co0 = (A)(x - (nx - 1) / 2.0), co1 = (A)(y - (ny - 1) / 2.0),
+                  co2 = (A)(z - (nz - 1) / 2.0);
+          const A h = -(co0 * (A)P.fnorm[f][0] + co1 * (A)P.fnorm[f][1] + co2 * (A)P.fnorm[f][2]) *
+                      (A)P.res;
+          const A epc = V * (A)P.fmag[f] * h;
           // PhaseField::forceEnergy returns after the first fluid when no
           // gradient is asked for; the element form counts every fluid
           if (want_e && (unstr || !force_e_done)) e.add(cf * epc);
           force_e_done = true;
-          gv += (nf == 1) ? (T)0.5 * epc : epc;
+          gv += (nf == 1) ? (A)0.5 * epc : epc;
         }
       }
       // diffuse-solid confinement
       if ((fl & PF_CONFINE) && P.confine_coef[f] != 0 && node_terms) {
-        const T c0 = (T)P.ff_init[dof];
-        if ((c0 - (T)0.5) * (cc - (T)0.5) < 0) {
-          const T coef = (T)P.confine_coef[f];
-          if (want_e) e.add(coef * (cc - (T)0.5) * (cc - (T)0.5));
-          gv += coef * 2 * (cc - (T)0.5);
+        const A c0 = (A)P.ff_init[dof];
+        if ((c0 - (A)0.5) * (cc - (A)0.5) < 0) {
+          const A coef = (A)P.confine_coef[f];
+          if (want_e) e.add(coef * (cc - (A)0.5) * (cc - (A)0.5));
+          gv += coef * 2 * (cc - (A)0.5);
         }
       }
       // element form's fixed volume: the penalty's force on interface nodes
       if (fl & PF_UVOL) {
-        T w = 4 * cc * (1 - cc);
+        A w = 4 * cc * (1 - cc);
         if (w < 0) w = 0;
-        gv += (T)(P.vol_coef * dvol[f]) * V * w;
+        gv += (A)(P.vol_coef * dvol[f]) * V * w;
       }
       g[f] = gv;
     }
@@ -652,11 +666,11 @@ __device__ __noinline__ double pf_eval(Team& tm, const PotPF& P, CView<T> cv, T*
           if (f < nf && ((P.fix_mask >> f) & 1u)) g[f] = 0;
       }
       if ((fl & PF_HARD) && nf > 1) {
-        T comp = 0;
+        A comp = 0;
 #pragma unroll
         for (int f = 0; f < NFMAX; f++)
           if (f < nf && !((P.fix_mask >> f) & 1u)) comp += g[f];
-        comp *= (T)1 / (T)P.nvar;
+        comp *= (A)1 / (A)P.nvar;
 #pragma unroll
         for (int f = 0; f < NFMAX; f++)
           if (f < nf && !((P.fix_mask >> f) & 1u)) g[f] -= comp;
@@ -668,6 +682,45 @@ __device__ __noinline__ double pf_eval(Team& tm, const PotPF& P, CView<T> cv, T*
   }
   *emp = emit;
   return e.total();
+}
+
+
+template <typename T>
+struct CvSrc {
+  CView<T> cv;
+  __device__ __forceinline__ T operator()(int i) const { return cv(i); }
+};
+struct DfSrc {
+  const float* hi;
+  const float* lo;
+  __device__ __forceinline__ DFn operator()(int i) const { return DFn(DF{hi[i], lo[i]}); }
+};
+
+template <typename T, class Team, class Emit>
+__device__ __noinline__ double pf_eval(Team& tm, const PotPF& P, CView<T> cv, T* xw, Emit* emp,
+                                       bool want_e, bool want_g) {
+  return pf_eval_impl<T, T>(tm, P, CvSrc<T>{cv}, cv, xw, emp, want_e, want_g);
+}
+
+// The FP64-coordinate evaluation in double-float arithmetic (about 48 bits;
+// FP64 runs at 1/64 of the FP32 rate on GB300): the field at the evaluated
+// point is split once into hi/lo float arrays (two FP32 scratch vectors of
+// ndof), then the same sweep runs on DFn.  The caller's next team-wide
+// reduction orders this evaluation's reads of the scratch before the next
+// one's writes.
+template <class Team, class Emit>
+__device__ __noinline__ double pf_eval_df(Team& tm, const PotPF& P, CView<double> cv, double* xw, Emit* emp,
+                                          bool want_e, bool want_g, float* hi, float* lo) {
+  const int n = P.ngrid * P.nfluid;
+  for (int i = tm.tid(); i < n; i += tm.nthr()) {
+    const double v = cv(i);
+    if (xw) xw[i] = v;
+    const DF d = df_from(v);
+    hi[i] = d.hi;
+    lo[i] = d.lo;
+  }
+  tm.sync();
+  return pf_eval_impl<double, DFn>(tm, P, DfSrc{hi, lo}, cv, (double*)nullptr, emp, want_e, want_g);
 }
 
 // Four consecutive values of a coordinate view (aligned: element 4*i4).
@@ -905,8 +958,67 @@ __device__ void pf_local_constrain(Team& tm, const PotPF& P, T* v) {
 // Fixed-volume projection (specialisedConstraints lines 614-658):
 // per variable fluid, remove the component along the (density-orthogonal)
 // node-volume vector.  One reduction over the grid.
+//
+// FP32 vectors (the minimiser's gradients and directions): every per-element
+// operation in FP32, the dot products as compensated FP32 pairs reduced with
+// FP64 totals in one warp -- the FP64 form below spent the FP64 pipe (1/64 of
+// the FP32 rate on GB300) on two divisions per element and was the busiest
+// unit of a ternary grid's iteration.
+template <class Team>
+__device__ void pf_volume_project_f32(Team& tm, const PotPF& P, float* v) {
+  const int nf = P.nfluid;
+  const bool hard = (P.flags & PF_HARD) != 0;
+  const float inv_nvar = 1.f / (float)P.nvar;
+  float vf[9];
+#pragma unroll
+  for (int t = 0; t < 9; t++) vf[t] = (float)P.vol_of_type[t];
+  Acc part[MINIM_MAXF];
+  for (int iG = tm.tid(); iG < P.ngrid; iG += tm.nthr()) {
+    const float V = vf[pf_type1(P, iG)];
+    const float* w = v + (size_t)iG * nf;
+    float sv = 0.f;
+    if (hard)
+      for (int f = 0; f < nf; f++)
+        if (!((P.fix_mask >> f) & 1u)) sv += w[f];
+#pragma unroll
+    for (int f = 0; f < MINIM_MAXF; f++) {
+      if (f < nf && !((P.fix_mask >> f) & 1u))
+        part[f].add((w[f] - (hard ? sv * inv_nvar : 0.f)) * V);
+    }
+  }
+  float ps[MINIM_MAXF], pc[MINIM_MAXF];
+  double tot[MINIM_MAXF];
+#pragma unroll
+  for (int f = 0; f < MINIM_MAXF; f++) {
+    ps[f] = part[f].s;
+    pc[f] = part[f].c;
+  }
+  tm.template reduce_pairs<MINIM_MAXF>(ps, pc, tot);
+  float comp[MINIM_MAXF], csum = 0.f;
+#pragma unroll
+  for (int f = 0; f < MINIM_MAXF; f++) {
+    comp[f] = (f < nf && !((P.fix_mask >> f) & 1u)) ? (float)(tot[f] / P.total_volume2) : 0.f;
+    csum += comp[f];
+  }
+  for (int iG = tm.tid(); iG < P.ngrid; iG += tm.nthr()) {
+    const float V = vf[pf_type1(P, iG)];
+    float* w = v + (size_t)iG * nf;
+    for (int f = 0; f < nf; f++) {
+      if ((P.fix_mask >> f) & 1u) continue;
+      float d = comp[f] * V;
+      if (hard) d -= csum * V * inv_nvar;
+      w[f] -= d;
+    }
+  }
+  tm.sync();
+}
+
 template <typename T, class Team>
 __device__ void pf_volume_project(Team& tm, const PotPF& P, T* v) {
+  if constexpr (std::is_same_v<T, float>) {
+    pf_volume_project_f32(tm, P, v);
+    return;
+  }
   const int nf = P.nfluid;
   const bool hard = (P.flags & PF_HARD) != 0;
   double part[MINIM_MAXF];
