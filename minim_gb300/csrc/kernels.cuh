@@ -13,9 +13,11 @@
 
 namespace mg {
 
+// WR: rows of the wide-reduction scratch, one per warp of the block
+template <int WR = 8>
 struct SharedScalars {
   double red[(32 + 1) * MINIM_MAXRED];
-  double wide[16 * MINIM_WIDE];  // one row per warp (up to 512 threads)
+  double wide[WR * MINIM_WIDE];
   double wout[MINIM_WIDE];
   double SY[MINIM_MAXM * MINIM_MAXM], YY[MINIM_MAXM * MINIM_MAXM];
   float coefS[MINIM_MAXM], coefY[MINIM_MAXM];
@@ -34,8 +36,8 @@ __device__ __forceinline__ void copy_desc(InstDesc* dst, const InstDesc* src) {
   for (int i = threadIdx.x; i < nw; i += blockDim.x) d[i] = s[i];
 }
 
-template <class Team, int KIND>
-__device__ void setup_runner(Runner<Team, KIND>& R, SharedScalars& S, const InstDesc& in) {
+template <class Team, int KIND, class SS>
+__device__ void setup_runner(Runner<Team, KIND>& R, SS& S, const InstDesc& in) {
   R.n = in.ndof;
   R.rho = S.rho; R.sig = S.sig; R.yy = S.yy; R.alpha = S.alpha;
   R.sidx = S.sidx; R.yidx = S.yidx;
@@ -47,12 +49,12 @@ __device__ void setup_runner(Runner<Team, KIND>& R, SharedScalars& S, const Inst
   R.sq = 0u;
 }
 
-// (512, 1) caps registers at 128 as (256, 2) does; 512-thread blocks run the
-// grid-sized kinds when every instance has an SM to itself
+// The grid-sized kinds run 512-thread blocks (one per SM at 128 registers a
+// thread); Lennard-Jones keeps up to 256 threads and two or more blocks per SM.
 template <int KIND>
-__global__ void __launch_bounds__(512, 1)
+__global__ void __launch_bounds__(KIND == K_LJ ? 256 : 512, KIND == K_LJ ? 2 : 1)
 batch_kernel(const InstDesc* __restrict__ insts, int ninst, int* counter, int slice, int lj_tile) {
-  __shared__ SharedScalars S;
+  __shared__ SharedScalars<KIND == K_LJ ? 8 : 16> S;
   __shared__ __align__(16) InstDesc s_in;
   extern __shared__ __align__(16) unsigned char dyn[];
   for (;;) {
@@ -119,7 +121,7 @@ template <int KIND>
 __global__ void __launch_bounds__(256, 2)
 grid_kernel(const InstDesc* __restrict__ inst, int op, const EvalIO* io, int slice,
             GridSyncState* bar, double* partials, int lj_tile) {
-  __shared__ SharedScalars S;
+  __shared__ SharedScalars<> S;
   __shared__ __align__(16) InstDesc s_in;
   extern __shared__ __align__(16) unsigned char dyn[];
   copy_desc(&s_in, inst);

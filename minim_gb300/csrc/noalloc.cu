@@ -49,7 +49,7 @@ size_t up256(size_t v) { return (v + 255) & ~(size_t)255; }
 namespace mg {
 
 __global__ void __launch_bounds__(256, 2) noalloc_lj_kernel(InstDesc d, int slice, int lj_tile) {
-  __shared__ SharedScalars S;
+  __shared__ SharedScalars<> S;
   __shared__ __align__(16) InstDesc s_in;
   extern __shared__ __align__(16) unsigned char dyn[];
   if (threadIdx.x == 0) s_in = d;
