@@ -529,6 +529,21 @@ def run_profile_case(iters):
                       "abytes_per_launch": st["abytes"] / max(st["launches"], 1), "status": r.status}))
 
 
+def run_profile_pf(iters, precision):
+    """One batch launch of one 2-D 128^2 three-fluid PhaseField grid (hard
+    density, fixed volumes), L-BFGS for `iters` iterations at `precision`:
+    the instance kind that bounds the mixed PF/BAH batch (profiler capture)."""
+    from minim_gb300 import abi, runtime
+    from tests.workloads import pf_simplex
+    g = (128, 128, 1)
+    inst = runtime.Instance(abi.phase_field(g, nfluid=3, volume_fixed=True), pf_simplex(g, 3, seed=5001))
+    b = runtime.Batch()
+    b.add(inst, abi.minimiser("lbfgs", tol=1e-7, max_iter=iters, precision=precision))
+    r = b.run()[0]
+    st = runtime.last_run_stats()
+    print(json.dumps({"iter": r.iter, "evals": r.evals, "kernel_ms": st["kernel_ms"], "precision": precision}))
+
+
 def run_profile_lj(iters):
     """One batch launch of 304 Lennard-Jones clusters (N=300, Fire(0.1), FP32
     coordinates, `iters` iterations each) for profiler captures of the batched
@@ -568,7 +583,13 @@ def main():
                     help="run one short minimisation of N iterations (profiler capture) and exit")
     ap.add_argument("--profile-lj", type=int, default=0,
                     help="run one batch of 304 LJ clusters for N iterations (profiler capture) and exit")
+    ap.add_argument("--profile-pf", type=int, default=0,
+                    help="run one 128^2 three-fluid PhaseField grid for N iterations (profiler capture) and exit")
+    ap.add_argument("--profile-prec", default="fp64", help="coordinate precision of --profile-pf")
     args = ap.parse_args()
+    if args.profile_pf:
+        run_profile_pf(args.profile_pf, args.profile_prec)
+        return
     if args.profile:
         run_profile_case(args.profile)
         return
