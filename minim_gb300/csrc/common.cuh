@@ -136,6 +136,23 @@ __device__ __forceinline__ DF df_rcp(DF b) {
   const DF r = DF{1.f, 0.f} - b * DF{y, 0.f};  // residual 1 - b y
   return DF{y, 0.f} + DF{y, 0.f} * r;
 }
+// Split of a double into double-float by its bits (integer and FP32
+// instructions only; the FP64 conversions it replaces run at the FP64 rate):
+// hi is x with its mantissa cut to 24 bits, lo the remainder (29 bits) to
+// FP32 rounding, about 47 bits in all.  Magnitudes outside [2^-70, 2^127)
+// (and zero) take the converting split.
+__device__ __forceinline__ DF df_split_bits(double x) {
+  const long long b = __double_as_longlong(x);
+  const int e = (int)((b >> 52) & 0x7ff);
+  if (e < 1023 - 70 || e > 1023 + 126) return df_from(x);
+  const unsigned long long m = (unsigned long long)b & 0xFFFFFFFFFFFFFULL;
+  const unsigned sign = (unsigned)((unsigned long long)b >> 63) << 31;
+  const float hi = __int_as_float((int)(sign | ((unsigned)(e - 1023 + 127) << 23) | (unsigned)(m >> 29)));
+  const float scale = __int_as_float((int)((unsigned)(e - 1075 + 127) << 23));  // 2^(e - 1075)
+  const float lo = __fmul_rn(__uint2float_rn((unsigned)(m & 0x1FFFFFFFULL)), scale);
+  return DF{hi, sign ? -lo : lo};
+}
+
 // Double-float as a number type (the same operations, with operators), for
 // code written once for float / double / double-float arithmetic.  Division
 // goes through the refined reciprocal; comparisons use the sign of the

@@ -702,22 +702,34 @@ __device__ __noinline__ double pf_eval(Team& tm, const PotPF& P, CView<T> cv, T*
   return pf_eval_impl<T, T>(tm, P, CvSrc<T>{cv}, cv, xw, emp, want_e, want_g);
 }
 
-// The FP64-coordinate evaluation in double-float arithmetic (about 48 bits;
+// The FP64-coordinate evaluation in double-float arithmetic (about 47 bits;
 // FP64 runs at 1/64 of the FP32 rate on GB300): the field at the evaluated
 // point is split once into hi/lo float arrays (two FP32 scratch vectors of
-// ndof), then the same sweep runs on DFn.  The caller's next team-wide
+// ndof) -- by bits, and a line-search trial point formed in double-float --
+// then the same sweep runs on DFn.  The caller's next team-wide
 // reduction orders this evaluation's reads of the scratch before the next
 // one's writes.
 template <class Team, class Emit>
 __device__ __noinline__ double pf_eval_df(Team& tm, const PotPF& P, CView<double> cv, double* xw, Emit* emp,
                                           bool want_e, bool want_g, float* hi, float* lo) {
   const int n = P.ngrid * P.nfluid;
-  for (int i = tm.tid(); i < n; i += tm.nthr()) {
-    const double v = cv(i);
-    if (xw) xw[i] = v;
-    const DF d = df_from(v);
-    hi[i] = d.hi;
-    lo[i] = d.lo;
+  if (xw || !cv.p) {
+    // the point is stored (or is the stored one): split the FP64 value
+    for (int i = tm.tid(); i < n; i += tm.nthr()) {
+      const double v = cv(i);
+      if (xw) xw[i] = v;
+      const DF d = df_split_bits(v);
+      hi[i] = d.hi;
+      lo[i] = d.lo;
+    }
+  } else {
+    // a line-search trial x + t p, formed in double-float
+    const DFn t = DFn(cv.t);
+    for (int i = tm.tid(); i < n; i += tm.nthr()) {
+      const DFn d = DFn(df_split_bits(cv.x[i])) + t * DFn(cv.p[i]);
+      hi[i] = d.hi;
+      lo[i] = d.lo;
+    }
   }
   tm.sync();
   return pf_eval_impl<double, DFn>(tm, P, DfSrc{hi, lo}, cv, (double*)nullptr, emp, want_e, want_g);
