@@ -126,7 +126,7 @@ def lj_batch_setup(count=4096):
 
 
 def run_gpu(args):
-    import torch  # noqa: F401  (device plumbing only)
+    import torch  # device plumbing only (pinned host buffers)
     from minim_gb300 import abi, runtime
     from oracle.oracle import Oracle
 
@@ -169,14 +169,18 @@ def run_gpu(args):
     rms_chk = float(np.sqrt(np.mean(g_chk ** 2)))
     del insts
 
-    # end to end through the C ABI with host buffers: H2D of x0, minimise,
-    # D2H of the result, every step
+    # end to end through the C ABI with host buffers: H2D of x0 from pinned
+    # host memory (instance creation), minimise, D2H of the result into pinned
+    # host memory, every step
+    x_pin = torch.empty(x0.size, dtype=torch.float64, pin_memory=True)
+    x_pin.numpy()[:] = x0
+    out_pin = torch.empty(x0.size, dtype=torch.float64, pin_memory=True)
     e2e_times = []
     for _ in range(args.steps):
         ta = time.perf_counter()
-        inst = runtime.Instance(p, x0)
+        inst = runtime.Instance(p, x_pin.numpy())
         inst.minimise(mp)
-        _ = inst.coords
+        inst.get_coords(out_pin.numpy())
         e2e_times.append(time.perf_counter() - ta)
         inst.close()
     e2e_value = args.steps / sum(e2e_times)

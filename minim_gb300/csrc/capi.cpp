@@ -1290,8 +1290,17 @@ int minim_gpu_pf_setup(const minim_gpu_pf_params* q, const double* x0, size_t nd
     *nk = (int)H.kappa.size();
     if (kappa) std::memcpy(kappa, H.kappa.data(), H.kappa.size() * sizeof(double));
     if (kappaP) std::memcpy(kappaP, H.kappaP.data(), H.kappaP.size() * sizeof(double));
-    if (node_vol) std::memcpy(node_vol, H.node_vol.data(), H.node_vol.size() * sizeof(double));
-    if (surface_area) std::memcpy(surface_area, H.surface_area.data(), H.surface_area.size() * sizeof(double));
+    // empty per-node arrays: no solid, every node bulk
+    const size_t ng = (size_t)H.pot.ngrid;
+    const double r3 = std::pow(q->resolution, 3);
+    if (node_vol) {
+      if (H.node_vol.empty()) std::fill(node_vol, node_vol + ng, r3);
+      else std::memcpy(node_vol, H.node_vol.data(), ng * sizeof(double));
+    }
+    if (surface_area) {
+      if (H.surface_area.empty()) std::fill(surface_area, surface_area + ng, 0.0);
+      else std::memcpy(surface_area, H.surface_area.data(), ng * sizeof(double));
+    }
     if (kernel_variant) *kernel_variant = H.kernel_kind;
   });
 }

@@ -201,16 +201,22 @@ PfHost setup_pf(const minim_gpu_pf_params& q, const double* x0, size_t ndof, boo
   P.vol_of_type[0] = 0.0;
   P.vol_of_type[1] = 1.0 * r3;
   for (int t = 1; t <= 7; t++) P.vol_of_type[t + 1] = (t / 8.0) * r3;
+  // without solid nodes every node is bulk (nodeVol = res^3, surfaceArea =
+  // 0) and the per-node arrays stay empty: nothing per node is built on the
+  // host for such grids (a 192^3 grid would fill 113 MB here per instance)
   bool any_solid = false;
-  std::vector<char> solid(ng, 0);
-  if (q.solid)
+  std::vector<char> solid;
+  if (q.solid) {
+    solid.assign(ng, 0);
     for (int i = 0; i < ng; i++) {
       solid[i] = q.solid[i] != 0;
       any_solid |= solid[i] != 0;
     }
-  H.node_vol.assign(ng, r3);
-  H.surface_area.assign(ng, 0.0);
+  }
+  auto node_vol = [&](int i) { return H.node_vol.empty() ? r3 : H.node_vol[i]; };
   if (any_solid) {
+    H.node_vol.assign(ng, r3);
+    H.surface_area.assign(ng, 0.0);
     flags |= PF_SOLID;
     H.aux.resize(ng);
     const int* n = P.n;
@@ -242,7 +248,7 @@ PfHost setup_pf(const minim_gpu_pf_params& q, const double* x0, size_t ndof, boo
   if (q.n_contact_angle > 0) {
     if (q.n_contact_angle != ng * nf)
       throw SetupError(MINIM_GPU_ERR_INVALID, "PhaseField: Invalid size of contactAngle array.");
-    if (nf == 1) {
+    if (nf == 1 && !H.surface_area.empty()) {
       H.wet.assign(ng, 0.0);
       bool any = false;
       for (int i = 0; i < ng; i++) {
@@ -271,7 +277,7 @@ PfHost setup_pf(const minim_gpu_pf_params& q, const double* x0, size_t ndof, boo
         if (q.volume) {
           v = q.volume[f];
         } else {
-          for (int i = 0; i < ng; i++) v += x0[f + (size_t)nf * i] * H.node_vol[i];
+          for (int i = 0; i < ng; i++) v += x0[f + (size_t)nf * i] * node_vol(i);
         }
         P.vol_target[f] = v;
       }
@@ -280,7 +286,7 @@ PfHost setup_pf(const minim_gpu_pf_params& q, const double* x0, size_t ndof, boo
   } else if (q.volume_fixed) {
     flags |= PF_VOLUME;
     double tv = 0;
-    for (int i = 0; i < ng; i++) tv += H.node_vol[i] * H.node_vol[i];
+    for (int i = 0; i < ng; i++) tv += node_vol(i) * node_vol(i);
     P.total_volume2 = tv;
   }
   P.flags = flags;

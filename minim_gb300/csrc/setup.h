@@ -25,8 +25,8 @@ struct PfHost {
   std::vector<double> wet;          // empty without wetting
   std::vector<double> kappa_node, kappaP_node;
   std::vector<double> ff_init;
-  std::vector<double> node_vol;     // per node (diagnostics / tests)
-  std::vector<double> surface_area;
+  std::vector<double> node_vol;     // per node (diagnostics / tests); empty
+  std::vector<double> surface_area; // without solid nodes (all bulk)
   std::vector<double> kappa, kappaP;  // as the reference stores them
 };
 // unstr: PhaseFieldUnstructured semantics (src/potentials/PhaseFieldUnstructured.cpp)

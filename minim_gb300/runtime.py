@@ -153,7 +153,14 @@ class Instance:
 
     @property
     def coords(self):
-        x = np.zeros(self.ndof)
+        return self.get_coords()
+
+    def get_coords(self, out=None):
+        """The coordinates into `out` (a contiguous float64 array of ndof, e.g.
+        a view of pinned host memory) or a new array."""
+        x = np.zeros(self.ndof) if out is None else out
+        if x.dtype != np.float64 or not x.flags.c_contiguous or x.size != self.ndof:
+            raise ValueError("out must be a contiguous float64 array of ndof values")
         _check(_lib.minim_gpu_instance_get_coords(self.h, x.ctypes.data_as(_dp)))
         return x
 
