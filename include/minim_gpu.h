@@ -284,9 +284,9 @@ int minim_gpu_bah_colouring(const minim_gpu_bah_params* q, const double* x0, siz
 int minim_gpu_instance_bah_arrays(minim_gpu_handle h, int cap, int* nbar, int* bars, double* bar_par,
                                   int* nbar_colors, int* bar_off, int* nhinge, int* hinges,
                                   double* hinge_par, int* nhinge_colors, int* hinge_off, int* on_device);
-/* kernel_variant: 1 = general PhaseField kernel, 3 = binary kernel without
- * optional terms. */
-int minim_gpu_pf_setup(const minim_gpu_pf_params* q, const double* x0, size_t ndof, double* kappa,
+/* kind: MINIM_GPU_PF or MINIM_GPU_PFU.  kernel_variant: 1 = general
+ * PhaseField kernel, 3 = binary kernel without optional terms. */
+int minim_gpu_pf_setup(int kind, const minim_gpu_pf_params* q, const double* x0, size_t ndof, double* kappa,
                        double* kappaP, int* nk, double* node_vol, double* surface_area,
                        int* kernel_variant);
 

@@ -1283,10 +1283,11 @@ int minim_gpu_instance_bah_arrays(minim_gpu_handle h, int cap, int* nbar, int* b
   });
 }
 
-int minim_gpu_pf_setup(const minim_gpu_pf_params* q, const double* x0, size_t ndof, double* kappa,
+int minim_gpu_pf_setup(int kind, const minim_gpu_pf_params* q, const double* x0, size_t ndof, double* kappa,
                        double* kappaP, int* nk, double* node_vol, double* surface_area, int* kernel_variant) {
   return guarded([&] {
-    PfHost H = setup_pf(*q, x0, ndof);
+    if (kind != MINIM_GPU_PF && kind != MINIM_GPU_PFU) throw ApiError{MINIM_GPU_ERR_INVALID, "not a phase-field kind"};
+    PfHost H = setup_pf(*q, x0, ndof, kind == MINIM_GPU_PFU);
     *nk = (int)H.kappa.size();
     if (kappa) std::memcpy(kappa, H.kappa.data(), H.kappa.size() * sizeof(double));
     if (kappaP) std::memcpy(kappaP, H.kappaP.data(), H.kappaP.size() * sizeof(double));

@@ -81,7 +81,7 @@ def load(path=LIB_PATH):
         "minim_gpu_bah_elements": ([P, _dp, C.c_size_t, C.c_int, _ip, _ip, _dp, _ip, _ip, _dp],
                                    C.c_int),
         "minim_gpu_bah_colouring": ([P, _dp, C.c_size_t, _ip, _ip, _ip], C.c_int),
-        "minim_gpu_pf_setup": ([P, _dp, C.c_size_t, _dp, _dp, _ip, _dp, _dp, _ip], C.c_int),
+        "minim_gpu_pf_setup": ([C.c_int, P, _dp, C.c_size_t, _dp, _dp, _ip, _dp, _dp, _ip], C.c_int),
         "minim_gpu_instance_bah_arrays": ([P, C.c_int, _ip, _ip, _dp, _ip, _ip, _ip, _ip, _dp, _ip, _ip, _ip],
                                           C.c_int),
         "minim_gpu_lj_minimise_noalloc": ([P, C.c_void_p, C.c_size_t, C.POINTER(abi.MinimiserParams),
@@ -342,7 +342,7 @@ def pf_setup(params, x0):
     nv = np.zeros(ng)
     sa = np.zeros(ng)
     nk, var = C.c_int(), C.c_int()
-    _check(lib.minim_gpu_pf_setup(params.ptr(), x.ctypes.data_as(_dp), x.size, k.ctypes.data_as(_dp),
+    _check(lib.minim_gpu_pf_setup(params.kind, params.ptr(), x.ctypes.data_as(_dp), x.size, k.ctypes.data_as(_dp),
                                   kp.ctypes.data_as(_dp), C.byref(nk), nv.ctypes.data_as(_dp),
                                   sa.ctypes.data_as(_dp), C.byref(var)))
     return {"kappa": k[: nk.value], "kappaP": kp[: nk.value], "node_vol": nv, "surface_area": sa,

@@ -112,3 +112,34 @@ def test_no_gpu_fails_loudly():
     with pytest.raises(runtime.MinimGpuError) as e:
         runtime.Instance(abi.lj(), [0, 0, 0, 2, 0, 0])
     assert e.value.code == abi.ERR_NO_DEVICE
+
+
+def test_default_minimiser_and_python_mirror_agree():
+    """minim_gpu_default_minimiser (the reference's constructor defaults, and
+    Anneal's) against abi.minimiser, field by field."""
+    import ctypes as C
+    lib = runtime.load()
+    for method, name in ((abi.LBFGS, "lbfgs"), (abi.FIRE, "fire"), (abi.GD, "gd"), (abi.ANNEAL, "anneal")):
+        c = abi.MinimiserParams()
+        lib.minim_gpu_default_minimiser(method, C.byref(c))
+        py = abi.minimiser(name)
+        for f, _ in abi.MinimiserParams._fields_:
+            if f == "temp_schedule":
+                assert not getattr(c, f) and not getattr(py, f)
+                continue
+            assert getattr(c, f) == getattr(py, f), (name, f)
+
+
+def test_pfu_setup_errors():
+    """PhaseFieldUnstructured's own argument checks (checkArraySizes, and the
+    soft density element's three fluids)."""
+    with pytest.raises(runtime.MinimGpuError):
+        runtime.pf_setup(abi.phase_field_unstructured([4, 4, 1], nfluid=2, density_constraint="soft"),
+                         np.full(32, 0.5))
+    with pytest.raises(runtime.MinimGpuError):
+        runtime.pf_setup(abi.phase_field_unstructured([4, 4, 1], surface_tension=np.ones(16)), np.zeros(16))
+    with pytest.raises(runtime.MinimGpuError):
+        runtime.pf_setup(abi.phase_field_unstructured([4, 4, 1], nfluid=3, interface_size=[1.0, 1.0]),
+                         np.full(48, 1 / 3))
+    info = runtime.pf_setup(abi.phase_field_unstructured([6, 5, 4]), np.zeros(120))
+    assert info["kernel_variant"] == 3  # binary, no optional term: the PhaseField fast path
