@@ -155,8 +155,8 @@ struct Runner {
 
   // ---- potential dispatch -------------------------------------------------------
   // kFast: the FP64-coordinate evaluations of the minimiser may use
-  // double-float arithmetic (general PhaseField); the API evaluation and
-  // Anneal's Metropolis energies use FP64 throughout.
+  // double-float arithmetic (general PhaseField, BarAndHinge); the API
+  // evaluation and Anneal's Metropolis energies use FP64 throughout.
   template <typename T, bool kFast = true, class Emit>
   __device__ double pot_eval(CView<T> cv, T* xw, Emit& em, bool want_e, bool want_g) {
     if constexpr (KIND == K_LJ) {
@@ -179,6 +179,10 @@ struct Runner {
       if ((in.pf.n[2] & 3) == 0) return pf1_eval_quad<T>(tm, in.pf, cv, xw, &em, want_e, want_g);
       return pf1_eval<T>(tm, in.pf, cv, xw, &em, want_e, want_g);
     } else {
+      if constexpr (kFast && std::is_same_v<T, double>) {
+        if (in.mp.method != 3)
+          return bah_eval_df(tm, in.bah, cv, xw, in.GA, &em, want_e, want_g, in.X32[0], in.X32[1]);
+      }
       return bah_eval<T>(tm, in.bah, cv, xw, in.GA, &em, want_e, want_g);
     }
   }

@@ -1094,9 +1094,38 @@ template <>
 __device__ __forceinline__ float bah_sqrt<float>(float a) { return sqrtf(a); }
 template <>
 __device__ __forceinline__ double bah_sqrt<double>(double a) { return sqrt(a); }
+// double-float square root: the FP32 root refined by one Newton step
+template <>
+__device__ __forceinline__ DFn bah_sqrt<DFn>(DFn a) {
+  if (a.hi <= 0.f) return DFn(0);
+  const float y = sqrtf(a.hi);
+  const float p = __fmul_rn(y, y);
+  const float ep = __fmaf_rn(y, y, -p);
+  // residual a - y^2, then y + r / (2 y)
+  const float r = __fadd_rn(__fsub_rn(__fsub_rn(a.hi, p), ep), a.lo);
+  return DFn(df_fast2sum(y, __fdividef(r, 2.f * y)));
+}
 
-template <typename T>
-__device__ __forceinline__ void bah_bar(const PotBAH& P, const CView<T>& cv, int b, T& e, T* gl, T* gr,
+// The wrapped dihedral difference of bending(): theta from the atan2 form
+// (2 pi - theta when n1.b3 < 0), then fmod(theta - theta0 + pi, 2 pi) - pi.
+// The double-float evaluation takes the angle and its wrap in FP64 from the
+// two double-float arguments.
+template <typename A>
+__device__ __forceinline__ A bah_dtheta(A y, A x, bool neg, double theta0) {
+  const A twopi = (A)(2.0 * 3.14159265358979323846);
+  const A pi = (A)3.14159265358979323846;
+  A th = bah_atan2<A>(y, x);
+  if (neg) th = twopi - th;
+  A dth = th - (A)theta0;
+  return bah_fmod<A>(dth + pi, twopi) - pi;
+}
+template <>
+__device__ __forceinline__ DFn bah_dtheta<DFn>(DFn y, DFn x, bool neg, double theta0) {
+  return DFn(bah_dtheta<double>((double)y, (double)x, neg, theta0));
+}
+
+template <typename T, class Src>
+__device__ __forceinline__ void bah_bar(const PotBAH& P, const Src& cv, int b, T& e, T* gl, T* gr,
                                         bool want_g) {
   const int2 nd = P.bars[b];
   const double2 pr = P.bar_par[b];
@@ -1114,8 +1143,8 @@ __device__ __forceinline__ void bah_bar(const PotBAH& P, const CView<T>& cv, int
   }
 }
 
-template <typename T>
-__device__ __forceinline__ void bah_hinge(const PotBAH& P, const CView<T>& cv, int h, T& e, T (*gq)[3],
+template <typename T, class Src>
+__device__ __forceinline__ void bah_hinge(const PotBAH& P, const Src& cv, int h, T& e, T (*gq)[3],
                                           bool want_g) {
   const int4 nd = P.hinges[h];
   const double2 pr = P.hinge_par[h];
@@ -1137,12 +1166,7 @@ __device__ __forceinline__ void bah_hinge(const PotBAH& P, const CView<T>& cv, i
   const T n1n2 = n1[0] * n2[0] + n1[1] * n2[1] + n1[2] * n2[2];
   const T n1b3 = n1[0] * b3[0] + n1[1] * b3[1] + n1[2] * b3[2];
   // acos(n1.n2/|n1||n2|) = atan2(|n1 x n2|, n1.n2) and |n1 x n2| = |b2| |n1.b3|
-  const T twopi = (T)(2.0 * 3.14159265358979323846);
-  const T pi = (T)3.14159265358979323846;
-  T th = bah_atan2<T>(b2m * (n1b3 >= 0 ? n1b3 : -n1b3), n1n2);
-  if (n1b3 < 0) th = twopi - th;
-  T dth = th - (T)pr.y;
-  dth = bah_fmod<T>(dth + pi, twopi) - pi;
+  const T dth = bah_dtheta<T>(b2m * (n1b3 >= 0 ? n1b3 : -n1b3), n1n2, n1b3 < 0, pr.y);
   const T k = (T)pr.x;
   e = (T)0.5 * k * dth * dth;
   if (want_g) {
@@ -1163,8 +1187,8 @@ __device__ __forceinline__ void bah_hinge(const PotBAH& P, const CView<T>& cv, i
 
 // Per-vertex external force and substrate wall (lines 359-387); returns the
 // energy and the z-gradient of vertex v.
-template <typename T>
-__device__ __forceinline__ void bah_vertex(const PotBAH& P, const CView<T>& cv, int v, T& e, T& gz) {
+template <typename T, class Src>
+__device__ __forceinline__ void bah_vertex(const PotBAH& P, const Src& cv, int v, T& e, T& gz) {
   e = 0; gz = 0;
   if (!P.node_el[v]) return;
   double fz = 0;
@@ -1191,30 +1215,47 @@ __device__ __forceinline__ void bah_vertex(const PotBAH& P, const CView<T>& cv, 
   }
 }
 
-template <typename T, class Team, class Emit>
-__device__ __noinline__ double bah_eval(Team& tm, const PotBAH& P, CView<T> cv, T* xw, double* GA,
-                                        Emit* emp, bool want_e, bool want_g) {
+// Gradient accumulators of the colour scatter: FP64, or double-float pairs in
+// the same 8 bytes per DOF
+struct GaF64 {
+  double* g;
+  template <typename A>
+  __device__ __forceinline__ void set(int j, A v) { g[j] = (double)v; }
+  template <typename A>
+  __device__ __forceinline__ void add(int j, A v) { g[j] += (double)v; }
+  __device__ __forceinline__ double get(int j) const { return g[j]; }
+};
+struct GaDF {
+  DF* g;
+  __device__ __forceinline__ void set(int j, DFn v) { g[j] = v.df(); }
+  __device__ __forceinline__ void add(int j, DFn v) { g[j] = (DFn(g[j]) + v).df(); }
+  __device__ __forceinline__ DFn get(int j) const { return DFn(g[j]); }
+};
+
+template <typename T, typename A, class Src, class Ga, class Team, class Emit>
+__device__ __forceinline__ double bah_eval_impl(Team& tm, const PotBAH& P, const Src& src, CView<T> cv, T* xw,
+                                                Ga ga, Emit* emp, bool want_e, bool want_g) {
   Emit emit = *emp;
-  EAcc<T> e;
+  EAcc<A> e;
   const int nv = P.nvert;
   for (int v = tm.tid(); v < nv; v += tm.nthr()) {
     if (xw) {
       xw[3 * v] = cv(3 * v); xw[3 * v + 1] = cv(3 * v + 1); xw[3 * v + 2] = cv(3 * v + 2);
     }
-    T ev, gz;
-    bah_vertex<T>(P, cv, v, ev, gz);
+    A ev, gz;
+    bah_vertex<A>(P, src, v, ev, gz);
     if (want_e) e.add(ev);
     if (want_g) {
-      GA[3 * v] = 0.0; GA[3 * v + 1] = 0.0; GA[3 * v + 2] = (double)gz;
+      ga.set(3 * v, A(0)); ga.set(3 * v + 1, A(0)); ga.set(3 * v + 2, gz);
     }
   }
   if (!want_g) {
     for (int b = tm.tid(); b < P.nbar; b += tm.nthr()) {
-      T eb; bah_bar<T>(P, cv, b, eb, nullptr, nullptr, false);
+      A eb; bah_bar<A>(P, src, b, eb, (A*)nullptr, (A*)nullptr, false);
       e.add(eb);
     }
     for (int h = tm.tid(); h < P.nhinge; h += tm.nthr()) {
-      T eh; bah_hinge<T>(P, cv, h, eh, nullptr, false);
+      A eh; bah_hinge<A>(P, src, h, eh, (A(*)[3])nullptr, false);
       e.add(eh);
     }
     *emp = emit;
@@ -1224,14 +1265,14 @@ __device__ __noinline__ double bah_eval(Team& tm, const PotBAH& P, CView<T> cv, 
   for (int c = 0; c < P.nbar_colors; c++) {
     const int b0 = P.bar_color_off[c], b1 = P.bar_color_off[c + 1];
     for (int b = b0 + tm.tid(); b < b1; b += tm.nthr()) {
-      T eb, gl[3], gr[3];
-      bah_bar<T>(P, cv, b, eb, gl, gr, true);
+      A eb, gl[3], gr[3];
+      bah_bar<A>(P, src, b, eb, gl, gr, true);
       if (want_e) e.add(eb);
       const int2 nd = P.bars[b];
 #pragma unroll
       for (int d = 0; d < 3; d++) {
-        GA[3 * nd.x + d] += (double)gl[d];
-        GA[3 * nd.y + d] += (double)gr[d];
+        ga.add(3 * nd.x + d, gl[d]);
+        ga.add(3 * nd.y + d, gr[d]);
       }
     }
     tm.sync();
@@ -1239,21 +1280,57 @@ __device__ __noinline__ double bah_eval(Team& tm, const PotBAH& P, CView<T> cv, 
   for (int c = 0; c < P.nhinge_colors; c++) {
     const int h0 = P.hinge_color_off[c], h1 = P.hinge_color_off[c + 1];
     for (int h = h0 + tm.tid(); h < h1; h += tm.nthr()) {
-      T eh, gq[4][3];
-      bah_hinge<T>(P, cv, h, eh, gq, true);
+      A eh, gq[4][3];
+      bah_hinge<A>(P, src, h, eh, gq, true);
       if (want_e) e.add(eh);
       const int4 nd = P.hinges[h];
       const int vs[4] = {nd.x, nd.y, nd.z, nd.w};
 #pragma unroll
       for (int q = 0; q < 4; q++)
 #pragma unroll
-        for (int d = 0; d < 3; d++) GA[3 * vs[q] + d] += (double)gq[q][d];
+        for (int d = 0; d < 3; d++) ga.add(3 * vs[q] + d, gq[q][d]);
     }
     tm.sync();
   }
-  for (int i = tm.tid(); i < 3 * nv; i += tm.nthr()) emit(i, (T)GA[i]);
+  for (int i = tm.tid(); i < 3 * nv; i += tm.nthr()) emit(i, (A)ga.get(i));
   *emp = emit;
   return e.total();
+}
+
+
+template <typename T, class Team, class Emit>
+__device__ __noinline__ double bah_eval(Team& tm, const PotBAH& P, CView<T> cv, T* xw, double* GA,
+                                        Emit* emp, bool want_e, bool want_g) {
+  return bah_eval_impl<T, T>(tm, P, CvSrc<T>{cv}, cv, xw, GaF64{GA}, emp, want_e, want_g);
+}
+
+// The FP64-coordinate evaluation in double-float (as pf_eval_df): the
+// coordinates split once into the hi/lo scratch, bars and hinges in
+// double-float (the dihedral angle and its wrap in FP64), the colour scatter
+// into double-float pairs held in the FP64 accumulator's memory.
+template <class Team, class Emit>
+__device__ __noinline__ double bah_eval_df(Team& tm, const PotBAH& P, CView<double> cv, double* xw, double* GA,
+                                           Emit* emp, bool want_e, bool want_g, float* hi, float* lo) {
+  const int n = 3 * P.nvert;
+  if (xw || !cv.p) {
+    for (int i = tm.tid(); i < n; i += tm.nthr()) {
+      const double v = cv(i);
+      if (xw) xw[i] = v;
+      const DF d = df_split_bits(v);
+      hi[i] = d.hi;
+      lo[i] = d.lo;
+    }
+  } else {
+    const DFn t = DFn(cv.t);
+    for (int i = tm.tid(); i < n; i += tm.nthr()) {
+      const DFn d = DFn(df_split_bits(cv.x[i])) + t * DFn(cv.p[i]);
+      hi[i] = d.hi;
+      lo[i] = d.lo;
+    }
+  }
+  tm.sync();
+  return bah_eval_impl<double, DFn>(tm, P, DfSrc{hi, lo}, cv, (double*)nullptr,
+                                    GaDF{reinterpret_cast<DF*>(GA)}, emp, want_e, want_g);
 }
 
 }  // namespace mg
