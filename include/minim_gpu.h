@@ -290,6 +290,34 @@ int minim_gpu_pf_setup(int kind, const minim_gpu_pf_params* q, const double* x0,
                        double* kappaP, int* nk, double* node_vol, double* surface_area,
                        int* kernel_variant);
 
+/* ---- kernel checks (no counterpart in the reference) ----------------------
+ * One energy (and gradient) evaluation by the potential kernels that a
+ * minimisation runs in a given stage, at the point x + t p, so that those
+ * kernels can be checked one evaluation at a time against an FP64
+ * evaluation of the same point (the reference's State::energyGradient,
+ * src/State.cpp:134-192, is FP64 throughout).  path:
+ *   MINIM_EVAL_FP32_GRID   FP32 coordinates, the single-instance kernels (whole GPU)
+ *   MINIM_EVAL_FP32_CTA    FP32 coordinates, the batch kernels (one CTA per instance)
+ *   MINIM_EVAL_FP64S_GRID  FP64 coordinates with the FP64 stage's arithmetic
+ *                          (double-float where the minimiser uses it), whole GPU
+ *   MINIM_EVAL_FP64S_CTA   the same on one CTA
+ *   MINIM_EVAL_LINES       the line stencil of the stepped L-BFGS graph (binary
+ *                          PhaseField without optional terms, nz % 4 == 0): two
+ *                          trials in one pass, at t and at t/2
+ * x (ndof) is rounded to FP32 on the FP32 paths; p (ndof, or NULL for the
+ * point x itself) is rounded to FP32, as the minimiser's directions are.
+ * The FP32 paths form the point as x32 + fl(t32 * p32) (the line stencil as
+ * one fused multiply-add), the FP64 paths as x + t * p.  g receives the
+ * gradient as the minimiser stores it (FP32 values, constraints applied);
+ * g == NULL runs the energy-only evaluation (the line-search trial kernels).
+ * For MINIM_EVAL_LINES, e and g (if given) hold two evaluations, at t then at
+ * t/2 (2 and 2 * ndof entries), and xt (optional, 2 * ndof) receives the two
+ * points as the stencil formed them; on the other paths xt must be NULL. */
+enum { MINIM_EVAL_FP32_GRID = 0, MINIM_EVAL_FP32_CTA = 1, MINIM_EVAL_FP64S_GRID = 2,
+       MINIM_EVAL_FP64S_CTA = 3, MINIM_EVAL_LINES = 4 };
+int minim_gpu_eval_kernel(minim_gpu_handle h, int path, const double* x, const double* p, double t,
+                          double* e, double* g, double* xt);
+
 /* ---- allocation-free minimisation (no counterpart in the reference) ------
  * Minimises one Lennard-Jones cluster (LjNd energy, the given minimiser) in
  * one CTA without allocating any memory: for callers that cannot call the

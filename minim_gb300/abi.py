@@ -22,6 +22,8 @@ DENSITY = {"hard": 0, "gradient": 0, "soft": 1, "energy penalty": 1, "none": 2, 
 LBFGS, FIRE, GD, ANNEAL = 0, 1, 2, 3
 LS_BACKTRACKING, LS_NONE = 0, 1
 PREC_MIXED, PREC_FP64, PREC_FP32 = 0, 1, 2
+# minim_gpu_eval_kernel paths: the kernels of a minimiser stage
+EVAL_FP32_GRID, EVAL_FP32_CTA, EVAL_FP64S_GRID, EVAL_FP64S_CTA, EVAL_LINES = range(5)
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int)

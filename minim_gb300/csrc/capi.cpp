@@ -118,13 +118,14 @@ struct Kern {
   int (*batch)(const InstDesc*, int, int*, int, int, int, size_t, void*);
   int (*grid)(const InstDesc*, int, const EvalIO*, int, GridSyncState*, double*, int, int, size_t, void*);
   int (*occ)(int, int, size_t, int*);
+  int (*cta_eval)(const InstDesc*, const EvalIO*, int, size_t, void*);
 };
 Kern kern(int kk) {
   switch (kk) {
-    case K_LJ: return {mg_launch_batch_lj, mg_launch_grid_lj, mg_occupancy_lj};
-    case K_PF: return {mg_launch_batch_pf, mg_launch_grid_pf, mg_occupancy_pf};
-    case K_BAH: return {mg_launch_batch_bah, mg_launch_grid_bah, mg_occupancy_bah};
-    default: return {mg_launch_batch_pf1, mg_launch_grid_pf1, mg_occupancy_pf1};
+    case K_LJ: return {mg_launch_batch_lj, mg_launch_grid_lj, mg_occupancy_lj, mg_launch_cta_eval_lj};
+    case K_PF: return {mg_launch_batch_pf, mg_launch_grid_pf, mg_occupancy_pf, mg_launch_cta_eval_pf};
+    case K_BAH: return {mg_launch_batch_bah, mg_launch_grid_bah, mg_occupancy_bah, mg_launch_cta_eval_bah};
+    default: return {mg_launch_batch_pf1, mg_launch_grid_pf1, mg_occupancy_pf1, mg_launch_cta_eval_pf1};
   }
 }
 const size_t kLjTileBytes = 1024 * 32;  // 1024 particles of 4 doubles
@@ -544,6 +545,130 @@ void do_eval(minim_gpu_instance_s* h, const double* x, double* e, double* g) {
   if (e) *e = ev;
 }
 
+int default_threads(int kk, const std::vector<InstDesc>& ds);
+
+// One evaluation by a minimiser stage's own potential kernels (the checks of
+// minim_gpu_eval_kernel).  Temporary buffers come from the caching pool.
+void do_eval_kernel(minim_gpu_instance_s* h, int path, const double* x, const double* p, double t, double* e,
+                    double* g, double* xt) {
+  Dev& D = need_dev();
+  if (path < MINIM_EVAL_FP32_GRID || path > MINIM_EVAL_LINES || !x)
+    throw ApiError{MINIM_GPU_ERR_INVALID, "minim_gpu_eval_kernel: invalid path or null coordinates"};
+  if (xt && path != MINIM_EVAL_LINES)
+    throw ApiError{MINIM_GPU_ERR_INVALID, "minim_gpu_eval_kernel: xt is only returned by the line stencil"};
+  const bool lines = path == MINIM_EVAL_LINES;
+  if (lines && h->kk != K_PF1)
+    throw ApiError{MINIM_GPU_ERR_INVALID, "minim_gpu_eval_kernel: the line stencil runs binary PhaseField "
+                                          "instances without optional terms only"};
+  ensure_grid(h);
+  const size_t n = h->n, vb = align256(n * sizeof(float));
+  // x32, p32, g32, two scratch vectors, and the line stencil's Xa Ga Ya Xb Gb Yb Go
+  const int nvec = lines ? 12 : 5;
+  const int max_rows = 16 * D.nsm;
+  char* buf = (char*)dalloc(nvec * vb + (size_t)max_rows * MINIM_WIDE * sizeof(double));
+  auto vec = [&](int k) { return (float*)(buf + (size_t)k * vb); };
+  float* x32 = vec(0);
+  float* p32 = p ? vec(1) : nullptr;
+  float* g32 = g ? vec(2) : nullptr;
+  try {
+    CK(cudaMemcpyAsync(h->d_tmp, x, n * sizeof(double), cudaMemcpyHostToDevice, D.s));
+    CK((cudaError_t)mg_convert(h->d_tmp, x32, n, 1, D.s));
+    std::vector<float> ph;
+    if (p) {
+      ph.resize(n);
+      for (size_t i = 0; i < n; i++) ph[i] = (float)p[i];
+      CK(cudaMemcpyAsync(p32, ph.data(), n * sizeof(float), cudaMemcpyHostToDevice, D.s));
+    }
+    double ev[2] = {0.0, 0.0};
+    std::vector<float> gh;
+    if (lines) {
+      // trials of a direction: both gradients are written, so a zero
+      // direction stands in for p == NULL
+      if (!p32) {
+        p32 = vec(1);
+        CK(cudaMemsetAsync(p32, 0, n * sizeof(float), D.s));
+      }
+      float* Go = vec(11);
+      CK(cudaMemsetAsync(Go, 0, n * sizeof(float), D.s));
+      CK(cudaMemcpyAsync(h->d_desc, &h->d, sizeof(InstDesc), cudaMemcpyHostToDevice, D.s));
+      double* part = (double*)(buf + nvec * vb);
+      int rows = 0;
+      const int mode = g ? 3 : 0;
+      CK((cudaError_t)mg_stepped_lines_probe(h->d_desc, h->d.pf.n, mode, x32, p32, Go, (float)t, vec(5), vec(6),
+                                             vec(7), vec(8), vec(9), vec(10), part, max_rows, D.nsm, &rows, D.s));
+      g_launches++;
+      std::vector<double> hp((size_t)rows * MINIM_WIDE);
+      CK(cudaMemcpyAsync(hp.data(), part, hp.size() * sizeof(double), cudaMemcpyDeviceToHost, D.s));
+      if (g || xt) gh.resize(4 * n);
+      if (g) {
+        CK(cudaMemcpyAsync(gh.data(), vec(6), n * sizeof(float), cudaMemcpyDeviceToHost, D.s));
+        CK(cudaMemcpyAsync(gh.data() + n, vec(9), n * sizeof(float), cudaMemcpyDeviceToHost, D.s));
+      }
+      if (xt && g) {
+        CK(cudaMemcpyAsync(gh.data() + 2 * n, vec(5), n * sizeof(float), cudaMemcpyDeviceToHost, D.s));
+        CK(cudaMemcpyAsync(gh.data() + 3 * n, vec(8), n * sizeof(float), cudaMemcpyDeviceToHost, D.s));
+      }
+      CK(cudaStreamSynchronize(D.s));
+      // rows: {E, g.g, P.y, y.y, E2, ...} (mode 3) or {E} (mode 0), summed in block order
+      for (int r = 0; r < rows; r++) {
+        ev[0] += hp[(size_t)r * MINIM_WIDE];
+        if (mode == 3) ev[1] += hp[(size_t)r * MINIM_WIDE + 4];
+      }
+      if (e) {
+        e[0] = ev[0];
+        if (mode == 3) e[1] = ev[1];
+      }
+      if (g)
+        for (size_t i = 0; i < 2 * n; i++) g[i] = gh[i];
+      if (xt) {
+        if (!g) throw ApiError{MINIM_GPU_ERR_INVALID, "minim_gpu_eval_kernel: the energy-only pass forms no point"};
+        for (size_t i = 0; i < 2 * n; i++) xt[i] = gh[2 * n + i];
+      }
+      dfree(buf);
+      return;
+    }
+    InstDesc d = h->d;
+    d.X32[0] = vec(3);  // scratch of the double-float sweeps
+    d.X32[1] = vec(4);
+    d.mp = MinParams{};
+    d.mp.method = MINIM_LBFGS;
+    EvalIO io{};
+    io.x = h->d_tmp;
+    io.e = h->d_e;
+    io.stage = (path == MINIM_EVAL_FP64S_GRID || path == MINIM_EVAL_FP64S_CTA) ? 1 : 0;
+    io.t32 = (float)t;
+    io.t64 = t;
+    io.x32 = x32;
+    io.p = p32;
+    io.g32 = g32;
+    CK(cudaMemcpyAsync(h->d_desc, &d, sizeof d, cudaMemcpyHostToDevice, D.s));
+    CK(cudaMemcpyAsync(h->d_io, &io, sizeof io, cudaMemcpyHostToDevice, D.s));
+    if (path == MINIM_EVAL_FP32_GRID || path == MINIM_EVAL_FP64S_GRID) {
+      launch_grid(h, OP_EVAL_STAGE, 0);
+    } else {
+      const int thr = default_threads(h->kk, std::vector<InstDesc>{h->d});
+      CK((cudaError_t)kern(h->kk).cta_eval(h->d_desc, h->d_io, thr, pot_smem(h->kk), D.s));
+      g_launches++;
+    }
+    CK(cudaMemcpyAsync(&ev[0], h->d_e, sizeof(double), cudaMemcpyDeviceToHost, D.s));
+    if (g) {
+      gh.resize(n);
+      CK(cudaMemcpyAsync(gh.data(), g32, n * sizeof(float), cudaMemcpyDeviceToHost, D.s));
+    }
+    CK(cudaStreamSynchronize(D.s));
+    if ((path == MINIM_EVAL_FP32_GRID || path == MINIM_EVAL_FP64S_GRID) && grid_error(h))
+      throw ApiError{MINIM_GPU_ERR_RUNTIME, "device barrier timed out"};
+    if (e) e[0] = ev[0];
+    if (g)
+      for (size_t i = 0; i < n; i++) g[i] = gh[i];
+  } catch (...) {
+    cudaStreamSynchronize(D.s);
+    dfree(buf);
+    throw;
+  }
+  dfree(buf);
+}
+
 void do_minimise(minim_gpu_instance_s* h, const minim_gpu_minimiser_params& mp, minim_gpu_result* res) {
   Dev& D = need_dev();
   check_mp(mp);
@@ -925,6 +1050,14 @@ int minim_gpu_instance_set_fixed(minim_gpu_handle h, const int* idof, size_t n) 
 
 int minim_gpu_energy_gradient(minim_gpu_handle h, const double* x, double* e, double* g) {
   return guarded([&] { do_eval(h, x, e, g); });
+}
+
+int minim_gpu_eval_kernel(minim_gpu_handle h, int path, const double* x, const double* p, double t, double* e,
+                          double* g, double* xt) {
+  return guarded([&] {
+    if (!h) throw ApiError{MINIM_GPU_ERR_INVALID, "null handle"};
+    do_eval_kernel(h, path, x, p, t, e, g, xt);
+  });
 }
 
 int minim_gpu_apply_constraints(minim_gpu_handle h, double* v) {

@@ -16,7 +16,6 @@
 #include "engine.h"
 
 #define MINIM_MAXRED 8    // values reduced together in one team reduction
-#define MINIM_WIDE 64     // values reduced together in one wide reduction
 #define MINIM_NSTAGE 4    // shared-memory stages of a staged vector pass
 
 namespace mg {

@@ -12,6 +12,7 @@
 
 #define MINIM_MAXM 16
 #define MINIM_MAXF 4
+#define MINIM_WIDE 64  // values reduced together in one wide reduction (row width of partial sums)
 
 namespace mg {
 
@@ -184,13 +185,23 @@ struct GridSyncState {
 };
 
 // ---- kernel entry points (engine.cu) ---------------------------------------------
-enum Op { OP_MINIMISE = 0, OP_EVAL = 1, OP_CONSTRAIN = 2 };
+enum Op { OP_MINIMISE = 0, OP_EVAL = 1, OP_CONSTRAIN = 2, OP_EVAL_STAGE = 3 };
 
 struct EvalIO {      // OP_EVAL / OP_CONSTRAIN on one instance, FP64 in/out
   const double* x;   // coordinates (device), ndof
   double* g;         // gradient out (device) or NULL
   double* e;         // energy out (device, 1 double) or NULL
   double* v;         // OP_CONSTRAIN: vector constrained in place
+  // OP_EVAL_STAGE (and the one-CTA evaluation kernel): one evaluation by a
+  // minimiser stage's own potential kernels at x + t p, the gradient stored
+  // as the minimiser stores it (FP32, constrained) into g32, or an
+  // energy-only evaluation when g32 is NULL
+  int stage;         // 0: FP32 coordinates x32; 1: FP64 coordinates x (FP64-stage arithmetic)
+  float t32;
+  double t64;
+  const float* x32;
+  const float* p;    // direction (FP32 in both stages), or NULL
+  float* g32;
 };
 
 }  // namespace mg
@@ -204,7 +215,9 @@ extern "C" {
   int mg_launch_grid_##NAME(const mg::InstDesc* d_inst, int op, const mg::EvalIO* d_io,           \
                             int slice_iters, mg::GridSyncState* d_bar, double* d_partials,       \
                             int threads, int blocks, size_t smem, void* stream);                 \
-  int mg_occupancy_##NAME(int grid, int threads, size_t smem, int* blocks_per_sm);
+  int mg_occupancy_##NAME(int grid, int threads, size_t smem, int* blocks_per_sm);              \
+  int mg_launch_cta_eval_##NAME(const mg::InstDesc* d_inst, const mg::EvalIO* d_io, int threads,  \
+                                size_t smem, void* stream);
 MG_DECLARE_LAUNCHERS(lj)
 MG_DECLARE_LAUNCHERS(pf)
 MG_DECLARE_LAUNCHERS(bah)
@@ -218,4 +231,8 @@ int mg_convert(const void* src, void* dst, size_t n, int to_float, void* stream)
 int mg_stepped_pf1_run(mg::InstDesc* d, mg::MinScalars* st, int m, const int* grid, int nsm, int slice,
                        int dual, void* stream, double* kernels);
 void mg_stepped_free_all();
+// stepped.cu: one line-stencil pass outside the graph (kernel checks)
+int mg_stepped_lines_probe(const mg::InstDesc* d, const int* grid, int mode, const float* X, const float* P,
+                           const float* Go, float t, float* Xa, float* Ga, float* Ya, float* Xb, float* Gb,
+                           float* Yb, double* part, int max_rows, int nsm, int* rows, void* stream);
 }

@@ -90,6 +90,54 @@ __device__ void eval_op(Runner<Team, KIND>& R, Team& tm, const InstDesc& in, con
   if (io.e && tm.block0() && threadIdx.x == 0) *io.e = v[0];
 }
 
+// One evaluation by a minimiser stage's potential kernels (the arithmetic
+// and the reduction of grad_eval / energy_at) at x + t p, for checking them
+// against an FP64 evaluation.
+template <class Team, int KIND>
+__device__ void eval_stage_op(Runner<Team, KIND>& R, Team& tm, const InstDesc& in, const EvalIO& io) {
+  const bool want_g = io.g32 != nullptr;
+  FusedEmit em{io.g32, nullptr, nullptr, nullptr, in.fixed};
+  double ep;
+  if (io.stage == 0) {
+    CView<float> cv{io.x32, io.p, io.t32};
+    ep = R.template pot_eval<float>(cv, nullptr, em, true, want_g);
+  } else {
+    CView<double> cv{io.x, io.p, io.t64};
+    ep = R.template pot_eval<double>(cv, nullptr, em, true, want_g);
+  }
+  if constexpr (KIND == K_PF) {
+    if (want_g && (in.pf.flags & PF_VOLUME)) {
+      tm.sync();
+      pf_volume_project<float>(tm, in.pf, io.g32);
+    }
+  }
+  double v[1] = {ep};
+  if (io.stage == 0) {
+    float ps[1], pc[1];
+    to_pair(ep, ps[0], pc[0]);
+    tm.template reduce_pairs<1>(ps, pc, v);
+  } else {
+    tm.reduce(v);
+  }
+  if (io.e && tm.block0() && threadIdx.x == 0) *io.e = v[0];
+}
+
+// eval_stage_op on one CTA: the batch kernels' team (Lennard-Jones clusters
+// take the symmetric tile path there)
+template <int KIND>
+__global__ void __launch_bounds__(KIND == K_LJ ? 256 : 512, KIND == K_LJ ? 2 : 1)
+cta_eval_kernel(const InstDesc* __restrict__ inst, const EvalIO* io, int lj_tile) {
+  __shared__ SharedScalars<KIND == K_LJ ? 8 : 16> S;
+  __shared__ __align__(16) InstDesc s_in;
+  extern __shared__ __align__(16) unsigned char dyn[];
+  copy_desc(&s_in, inst);
+  __syncthreads();
+  CtaTeam tm{S.red, S.wide};
+  Runner<CtaTeam, KIND> R{tm, s_in, dyn, lj_tile};
+  setup_runner(R, S, s_in);
+  eval_stage_op(R, tm, s_in, *io);
+}
+
 template <class Team, int KIND>
 __device__ void constrain_op(Team& tm, const InstDesc& in, const EvalIO& io) {
   double* v = io.v;
@@ -145,6 +193,8 @@ grid_kernel(const InstDesc* __restrict__ inst, int op, const EvalIO* io, int sli
     R.store(*s_in.st);
   } else if (op == OP_EVAL) {
     eval_op(R, tm, s_in, *io);
+  } else if (op == OP_EVAL_STAGE) {
+    eval_stage_op(R, tm, s_in, *io);
   } else {
     constrain_op<GridTeam, KIND>(tm, s_in, *io);
   }
@@ -191,6 +241,15 @@ grid_kernel(const InstDesc* __restrict__ inst, int op, const EvalIO* io, int sli
                     (void*)&d_bar,  (void*)&d_partials, (void*)&tile};                            \
     return (int)cudaLaunchCooperativeKernel((const void*)mg::grid_kernel<KIND>, dim3(blocks),     \
                                             dim3(threads), args, smem, (cudaStream_t)stream);     \
+  }                                                                                               \
+  extern "C" int mg_launch_cta_eval_##NAME(const mg::InstDesc* d_inst, const mg::EvalIO* d_io,     \
+                                           int threads, size_t smem, void* stream) {              \
+    const int tile = (int)(smem / sizeof(mg::D4));                                                \
+    const cudaError_t a = cudaFuncSetAttribute((const void*)mg::cta_eval_kernel<KIND>,            \
+                                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
+    if (a != cudaSuccess) return (int)a;                                                          \
+    mg::cta_eval_kernel<KIND><<<1, threads, smem, (cudaStream_t)stream>>>(d_inst, d_io, tile);    \
+    return (int)cudaGetLastError();                                                               \
   }                                                                                               \
   extern "C" int mg_occupancy_##NAME(int grid, int threads, size_t smem, int* blocks_per_sm) {    \
     if (grid) mg_grid_smem_##NAME(smem);                                                          \

@@ -18,7 +18,8 @@
 //     caller must serialise them;
 //   * the host does not know the array's device address; it is looked up
 //     with cudaGetSymbolAddress on the first call on each device (with that
-//     device current), so that first call is the one to make before any
+//     device current), together with the kernel's per-device opt-in to its
+//     shared-memory size, so that first call is the one to make before any
 //     stream capture;
 //   * the state record at the start of the array is reset on every call; the
 //     kernel writes every vector before reading it.
@@ -41,6 +42,9 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 std::mutex g_setup_mu;
 void* g_scratch_addr[128];
 bool g_scratch_ready[128];
+// the kernel's opt-in to more than 48 KB of shared memory is a per-device
+// function attribute: set once on each device, with the address lookup
+bool g_smem_ready[128];
 
 size_t up256(size_t v) { return (v + 255) & ~(size_t)255; }
 
@@ -101,9 +105,21 @@ extern "C" int minim_gpu_lj_minimise_noalloc(const minim_gpu_lj_params* p, doubl
     mg_set_last_error("minim_gpu_lj_minimise_noalloc: the kernels are built for sm_103a");
     return MINIM_GPU_ERR_NO_DEVICE;
   }
+  const int lj_tile = 1024;
+  const size_t smem = (size_t)lj_tile * sizeof(D4);
   unsigned char* base = nullptr;
   {
     std::lock_guard<std::mutex> lk(g_setup_mu);
+    if (!g_smem_ready[dev]) {
+      // static plus dynamic shared memory is above the 48 KB default
+      const cudaError_t e = cudaFuncSetAttribute((const void*)noalloc_lj_kernel,
+                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) {
+        mg_set_last_error(cudaGetErrorString(e));
+        return MINIM_GPU_ERR_CUDA;
+      }
+      g_smem_ready[dev] = true;
+    }
     if (!g_scratch_ready[dev]) {
       void* a = nullptr;
       const cudaError_t e = cudaGetSymbolAddress(&a, g_noalloc_scratch);
@@ -163,15 +179,6 @@ extern "C" int minim_gpu_lj_minimise_noalloc(const minim_gpu_lj_params* p, doubl
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   cudaError_t e = cudaMemcpyAsync(d.st, &s, sizeof s, cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) {
-    const int lj_tile = 1024;
-    const size_t smem = (size_t)lj_tile * sizeof(D4);
-    // static plus dynamic shared memory is above the 48 KB default
-    static const cudaError_t opt_in = cudaFuncSetAttribute(
-        (const void*)noalloc_lj_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (opt_in != cudaSuccess) {
-      mg_set_last_error(cudaGetErrorString(opt_in));
-      return MINIM_GPU_ERR_CUDA;
-    }
     noalloc_lj_kernel<<<1, 256, smem, st>>>(d, 0x7fffffff, lj_tile);
     e = cudaGetLastError();
   }

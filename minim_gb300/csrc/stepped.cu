@@ -531,19 +531,40 @@ __device__ __forceinline__ float quad_eval(const QuadLoads& L, float t, const Li
   return es;
 }
 
-template <int MODE, int MINB = (MODE == 3 ? 2 : (MODE ? 3 : 4))>
-__global__ void __launch_bounds__(kThreads, MINB)
-k_lines(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, double* part, cudaGraphConditionalHandle ls,
-        cudaGraphConditionalHandle grad, cudaGraphConditionalHandle outer) {
+// Pointers and trial multiplier of one line-stencil pass.  The first trial
+// (at t) writes its point, gradient and y = g - g_old to Xa, Ga, Ya; with
+// `two` the second (at t/2) writes to Xb, Gb, Yb.
+struct LinesIO {
+  const float* X;
+  const float* P;
+  const float* Go;
+  float* Xa;
+  float* Ga;
+  float* Ya;
+  float* Xb;
+  float* Gb;
+  float* Yb;
+  float t;
+  bool two;
+};
+// per-thread compensated sums of one pass: energy, g.g, P.y, y.y of each
+// trial and g_old.P
+struct LinesAcc {
+  Acc e, gg, py, yy, e2, gg2, py2, yy2, gpa;
+};
+
+constexpr int lines_min_blocks(int mode) { return mode == 3 ? 2 : (mode ? 3 : 4); }
+
+// The sweep of a line-stencil pass over every line of the grid (blocks of
+// (nz/4) x lines threads, lines dealt round-robin to the blocks).
+template <int MODE>
+__device__ __forceinline__ void lines_sweep(const PotPF& Pf, const LinesIO& io, LinesAcc& a) {
   constexpr bool WANT_G = MODE != 0;
   constexpr bool DUAL = MODE == 3;
-  span_begin(ctl);
-  const PotPF& Pf = d->pf;
   const int nx = Pf.n[0], ny = Pf.n[1], nz = Pf.n[2], nz4 = nz >> 2;
-  const int xi = st->xi, gi = st->gi;
-  const float* X = d->X32[xi];
-  const float* Pd = d->Sb + (long long)st->pbuf * d->hstride;
-  const float t = (float)ctl->t;
+  const float* X = io.X;
+  const float* Pd = io.P;
+  const float t = io.t;
   LineCoef K;
   K.V = (float)Pf.vol_of_type[1];
   K.fb = (float)Pf.kappa[0] / 16 * K.V;
@@ -554,16 +575,7 @@ k_lines(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, double* pa
   const int zq = threadIdx.x, nl = nx * ny;
   const int z0 = 4 * zq;
   const int izm = z0 == 0 ? nz - 1 : z0 - 1, izp = z0 + 4 == nz ? 0 : z0 + 4;
-  float* Xa = d->X32[1 - xi];
-  float* Ga = d->G[1 - gi];
-  float* Ya = d->Yb + (long long)st->ybuf * d->hstride;
-  // two-trial pass, or (gmode) the gradient at t alone
-  const bool two = DUAL && ctl->gmode == 0;
-  float* Xb = DUAL ? d->X32s : nullptr;
-  float* Gb = DUAL ? d->Gs : nullptr;
-  float* Yb2 = DUAL ? d->Yb + (long long)st->ybuf2 * d->hstride : nullptr;
-  const float* Go = d->G[gi];
-  Acc e, gg, py, yy, e2, gg2, py2, yy2, gpa;
+  const bool two = DUAL && io.two;
   if (zq < nz4) {
     for (int l = blockIdx.x * blockDim.y + threadIdx.y; l < nl; l += gridDim.x * blockDim.y) {
 
@@ -572,67 +584,105 @@ k_lines(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, double* pa
       const int lxm = (x == 0 ? nx - 1 : x - 1) * ny + y, lxp = (x == nx - 1 ? 0 : x + 1) * ny + y;
       const int q = l * nz4 + zq;
       // every load of the quad first
-      auto load_quad = [&](QuadLoads& L) {
-        L.xc = ld4(X, q);
-        L.pc = ld4(Pd, q);
-        L.xzm = X[l * nz + izm];
-        L.pzm = Pd[l * nz + izm];
-        L.xzp = X[l * nz + izp];
-        L.pzp = Pd[l * nz + izp];
-        L.xym = ld4(X, lym * nz4 + zq);
-        L.pym = ld4(Pd, lym * nz4 + zq);
-        L.xyp = ld4(X, lyp * nz4 + zq);
-        L.pyp = ld4(Pd, lyp * nz4 + zq);
-        L.xxm = ld4(X, lxm * nz4 + zq);
-        L.pxm = ld4(Pd, lxm * nz4 + zq);
-        L.xxp = ld4(X, lxp * nz4 + zq);
-        L.pxp = ld4(Pd, lxp * nz4 + zq);
-      };
       QuadLoads L;
-      load_quad(L);
+      L.xc = ld4(X, q);
+      L.pc = ld4(Pd, q);
+      L.xzm = X[l * nz + izm];
+      L.pzm = Pd[l * nz + izm];
+      L.xzp = X[l * nz + izp];
+      L.pzp = Pd[l * nz + izp];
+      L.xym = ld4(X, lym * nz4 + zq);
+      L.pym = ld4(Pd, lym * nz4 + zq);
+      L.xyp = ld4(X, lyp * nz4 + zq);
+      L.pyp = ld4(Pd, lyp * nz4 + zq);
+      L.xxm = ld4(X, lxm * nz4 + zq);
+      L.pxm = ld4(Pd, lxm * nz4 + zq);
+      L.xxp = ld4(X, lxp * nz4 + zq);
+      L.pxp = ld4(Pd, lxp * nz4 + zq);
       float4 go = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (WANT_G) go = ld4(Go, q);
+      if (WANT_G) go = ld4(io.Go, q);
       float4 c4, gv;
-      if (DUAL) gpa.add(dot4(go, L.pc));  // g.P for the first pass of a direction
-      e.add(quad_eval(L, t, K, WANT_G, c4, gv));
+      if (DUAL) a.gpa.add(dot4(go, L.pc));  // g.P for the first pass of a direction
+      a.e.add(quad_eval(L, t, K, WANT_G, c4, gv));
       if (WANT_G) {
-        st4(Xa, q, c4);
-        st4(Ga, q, gv);
-        gg.add(dot4(gv, gv));
+        st4(io.Xa, q, c4);
+        st4(io.Ga, q, gv);
+        a.gg.add(dot4(gv, gv));
         const float4 yv = make_float4(gv.x - go.x, gv.y - go.y, gv.z - go.z, gv.w - go.w);
-        st4(Ya, q, yv);
-        py.add(dot4(L.pc, yv));
-        yy.add(dot4(yv, yv));
+        st4(io.Ya, q, yv);
+        a.py.add(dot4(L.pc, yv));
+        a.yy.add(dot4(yv, yv));
       }
       if (DUAL && two) {
-        e2.add(quad_eval(L, 0.5f * t, K, true, c4, gv));
-        st4(Xb, q, c4);
-        st4(Gb, q, gv);
-        gg2.add(dot4(gv, gv));
+        a.e2.add(quad_eval(L, 0.5f * t, K, true, c4, gv));
+        st4(io.Xb, q, c4);
+        st4(io.Gb, q, gv);
+        a.gg2.add(dot4(gv, gv));
         const float4 yv = make_float4(gv.x - go.x, gv.y - go.y, gv.z - go.z, gv.w - go.w);
-        st4(Yb2, q, yv);
-        py2.add(dot4(L.pc, yv));
-        yy2.add(dot4(yv, yv));
+        st4(io.Yb, q, yv);
+        a.py2.add(dot4(L.pc, yv));
+        a.yy2.add(dot4(yv, yv));
       }
     }
   }
-  if (DUAL) {
-    double v[9] = {e.total(),   gg.total(),  py.total(),  yy.total(), e2.total(),
-                   gg2.total(), py2.total(), yy2.total(), gpa.total()};
-    block_row<9>(v, part + (size_t)blockIdx.x * MINIM_WIDE);
-  } else if (WANT_G) {
-    double v[4] = {e.total(), gg.total(), py.total(), yy.total()};
-    block_row<4>(v, part + (size_t)blockIdx.x * MINIM_WIDE);
+}
+
+// the block's row of partial sums of a line-stencil pass
+template <int MODE>
+__device__ __forceinline__ void lines_row(const LinesAcc& a, double* row) {
+  if (MODE == 3) {
+    double v[9] = {a.e.total(),   a.gg.total(),  a.py.total(),  a.yy.total(), a.e2.total(),
+                   a.gg2.total(), a.py2.total(), a.yy2.total(), a.gpa.total()};
+    block_row<9>(v, row);
+  } else if (MODE != 0) {
+    double v[4] = {a.e.total(), a.gg.total(), a.py.total(), a.yy.total()};
+    block_row<4>(v, row);
   } else {
-    double v[1] = {e.total()};
-    block_row<1>(v, part + (size_t)blockIdx.x * MINIM_WIDE);
+    double v[1] = {a.e.total()};
+    block_row<1>(v, row);
   }
+}
+
+template <int MODE, int MINB = lines_min_blocks(MODE)>
+__global__ void __launch_bounds__(kThreads, MINB)
+k_lines(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, double* part, cudaGraphConditionalHandle ls,
+        cudaGraphConditionalHandle grad, cudaGraphConditionalHandle outer) {
+  constexpr bool DUAL = MODE == 3;
+  span_begin(ctl);
+  const int xi = st->xi, gi = st->gi;
+  LinesIO io;
+  io.X = d->X32[xi];
+  io.P = d->Sb + (long long)st->pbuf * d->hstride;
+  io.Go = d->G[gi];
+  io.t = (float)ctl->t;
+  io.Xa = d->X32[1 - xi];
+  io.Ga = d->G[1 - gi];
+  io.Ya = d->Yb + (long long)st->ybuf * d->hstride;
+  // two-trial pass, or (gmode) the gradient at t alone
+  io.two = DUAL && ctl->gmode == 0;
+  io.Xb = DUAL ? d->X32s : nullptr;
+  io.Gb = DUAL ? d->Gs : nullptr;
+  io.Yb = DUAL ? d->Yb + (long long)st->ybuf2 * d->hstride : nullptr;
+  LinesAcc a;
+  lines_sweep<MODE>(d->pf, io, a);
+  lines_row<MODE>(a, part + (size_t)blockIdx.x * MINIM_WIDE);
   if (last_block(ctl)) {
     if (MODE == 0) ctl_ls(d, st, ctl, part, gridDim.x, ls);
     else if (MODE == 1) ctl_g(d, st, ctl, part, gridDim.x, outer);
     else if (MODE == 2) ctl_lsg(d, st, ctl, part, gridDim.x, ls, grad, outer);
     else ctl_lsg2(d, st, ctl, part, gridDim.x, outer);
   }
+}
+
+// One line-stencil pass outside the graph, with no controller: the same
+// sweep as k_lines<MODE> on the given buffers, each block's partial row to
+// part.  For checking the stencil against an FP64 evaluation.
+template <int MODE>
+__global__ void __launch_bounds__(kThreads, lines_min_blocks(MODE))
+k_lines_probe(const InstDesc* __restrict__ d, LinesIO io, double* part) {
+  LinesAcc a;
+  lines_sweep<MODE>(d->pf, io, a);
+  lines_row<MODE>(a, part + (size_t)blockIdx.x * MINIM_WIDE);
 }
 
 // ---- controllers (one block) ----------------------------------------------------
@@ -1367,4 +1417,34 @@ extern "C" void mg_stepped_free_all() {
   std::lock_guard<std::mutex> lk(g_graphs_mu);
   for (SteppedGraph* sg : g_graphs) free_graph(sg);
   g_graphs.clear();
+}
+
+// One line-stencil pass outside the graph (no controller), for checking the
+// stencil against an FP64 evaluation: mode 0 the trial energy at X + t P;
+// mode 3 the points, gradients and y = g - Go at t (Xa, Ga, Ya) and at t/2
+// (Xb, Gb, Yb).  Each block's partial row goes to part (at most max_rows
+// rows of MINIM_WIDE doubles); *rows receives the block count.  The grid
+// must take the line stencil (nz % 4 == 0, nz / 4 <= 256).  Returns a
+// cudaError_t.
+extern "C" int mg_stepped_lines_probe(const InstDesc* d, const int* grid, int mode, const float* X,
+                                      const float* P, const float* Go, float t, float* Xa, float* Ga, float* Ya,
+                                      float* Xb, float* Gb, float* Yb, double* part, int max_rows, int nsm,
+                                      int* rows, void* stream) {
+  const int nz4 = grid[2] / 4;
+  if (grid[2] % 4 != 0 || nz4 > 256 || nz4 < 1) return (int)cudaErrorInvalidValue;
+  int by = kThreads / nz4;
+  while (by > 1 && (nz4 * by) % 32) by--;
+  if ((nz4 * by) % 32) return (int)cudaErrorInvalidValue;
+  const dim3 blk(nz4, by);
+  const void* f = mode == 3 ? (const void*)k_lines_probe<3> : (const void*)k_lines_probe<0>;
+  if (mode != 0 && mode != 3) return (int)cudaErrorInvalidValue;
+  const int occ = occupancy(f, (int)(blk.x * blk.y));
+  if (occ < 1) return (int)cudaErrorInvalidConfiguration;
+  const int nb = std::min(nsm * occ, max_rows);
+  LinesIO io{X, P, Go, Xa, Ga, Ya, Xb, Gb, Yb, t, mode == 3};
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (mode == 3) k_lines_probe<3><<<nb, blk, 0, s>>>(d, io, part);
+  else k_lines_probe<0><<<nb, blk, 0, s>>>(d, io, part);
+  *rows = nb;
+  return (int)cudaGetLastError();
 }

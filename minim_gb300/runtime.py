@@ -32,6 +32,7 @@ EXPORTS = [
     "minim_gpu_server_poll", "minim_gpu_server_take", "minim_gpu_server_cancel",
     "minim_gpu_server_destroy", "minim_gpu_bah_elements", "minim_gpu_bah_colouring",
     "minim_gpu_pf_setup", "minim_gpu_lj_minimise_noalloc", "minim_gpu_instance_bah_arrays",
+    "minim_gpu_eval_kernel",
 ]
 
 
@@ -84,6 +85,7 @@ def load(path=LIB_PATH):
         "minim_gpu_pf_setup": ([C.c_int, P, _dp, C.c_size_t, _dp, _dp, _ip, _dp, _dp, _ip], C.c_int),
         "minim_gpu_instance_bah_arrays": ([P, C.c_int, _ip, _ip, _dp, _ip, _ip, _ip, _ip, _dp, _ip, _ip, _ip],
                                           C.c_int),
+        "minim_gpu_eval_kernel": ([P, C.c_int, _dp, _dp, C.c_double, _dp, _dp, _dp], C.c_int),
         "minim_gpu_lj_minimise_noalloc": ([P, C.c_void_p, C.c_size_t, C.POINTER(abi.MinimiserParams),
                                            C.POINTER(abi.Result), C.c_void_p], C.c_int),
     }
@@ -187,6 +189,27 @@ class Instance:
 
     def gradient(self, x=None):
         return self.energy_gradient(x, energy=False)[1]
+
+    def eval_kernel(self, path, x, p=None, t=0.0, gradient=True, points=False):
+        """One evaluation by a minimiser stage's own kernels at x + t p
+        (minim_gpu_eval_kernel; path is one of abi.EVAL_*).  Returns (e, g)
+        -- for abi.EVAL_LINES each holds the two trials (t, t/2) -- and, with
+        points (line stencil only), the two points the stencil formed."""
+        xv = _vec(x)
+        pv = None if p is None else _vec(p)
+        two = path == abi.EVAL_LINES
+        e = np.zeros(2 if two else 1)
+        g = np.zeros((2 if two else 1) * self.ndof) if gradient else None
+        xt = np.zeros(2 * self.ndof) if points else None
+        _check(_lib.minim_gpu_eval_kernel(self.h, path, xv.ctypes.data_as(_dp),
+                                          None if pv is None else pv.ctypes.data_as(_dp), float(t),
+                                          e.ctypes.data_as(_dp), None if g is None else g.ctypes.data_as(_dp),
+                                          None if xt is None else xt.ctypes.data_as(_dp)))
+        if two:
+            out = (e, None if g is None else g.reshape(2, self.ndof))
+        else:
+            out = (e[0], g)
+        return out + ((xt.reshape(2, self.ndof),) if points else ())
 
     def apply_constraints(self, v):
         a = _vec(v).copy()
