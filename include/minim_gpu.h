@@ -36,7 +36,7 @@
 extern "C" {
 #endif
 
-#define MINIM_GPU_ABI_VERSION 1
+#define MINIM_GPU_ABI_VERSION 2
 
 /* ---- call status ------------------------------------------------------ */
 enum {
@@ -188,6 +188,9 @@ typedef struct {
    * L-BFGS direction passes (single-instance calls; summed over instances
    * for batches) */
   double phase_ms[3];
+  /* batch and server calls: device time the autotuner spent timing
+   * candidate launch shapes before the run (not in kernel_ms) */
+  double tune_ms;
 } minim_gpu_run_stats;
 
 typedef struct minim_gpu_instance_s* minim_gpu_handle;
@@ -233,8 +236,21 @@ int minim_gpu_minimise(minim_gpu_handle h, const minim_gpu_minimiser_params* mp,
 int minim_gpu_batch_create(minim_gpu_batch* out);
 int minim_gpu_batch_add(minim_gpu_batch b, minim_gpu_handle h,
                         const minim_gpu_minimiser_params* mp);
-/* threads_per_cta 0 = autotuned; results has one entry per added instance. */
+/* threads_per_cta > 0 runs every instance with that many threads per CTA;
+ * 0 = autotuned: each instance's shape depends only on its own potential
+ * kind, size bucket, method and precision (never on the rest of the batch),
+ * chosen the first time that key is seen in the process by timing every
+ * candidate on a short slice of copies of the batch's instances of that key
+ * (MINIM_GPU_TUNE=0: a fixed size rule instead; MINIM_GPU_TUNE_CACHE=file
+ * keeps the choices across processes).  results has one entry per added
+ * instance. */
 int minim_gpu_batch_run(minim_gpu_batch b, int threads_per_cta, minim_gpu_result* results);
+/* The autotuner's choices so far (no counterpart in the reference): up to
+ * cap rows of 7 ints {potential kind (MINIM_GPU_*), size bucket, method,
+ * precision, threads per CTA, measured (1) or read from the cache file (0),
+ * candidates timed}, and per row up to 4 measured slice times in ms
+ * (ms may be NULL).  *n receives the number of rows. */
+int minim_gpu_tune_table(int cap, int* rows, double* ms, int* n);
 int minim_gpu_batch_destroy(minim_gpu_batch b);
 
 /* ---- serving: continuous batching ------------------------------------------ */
@@ -317,6 +333,15 @@ enum { MINIM_EVAL_FP32_GRID = 0, MINIM_EVAL_FP32_CTA = 1, MINIM_EVAL_FP64S_GRID 
        MINIM_EVAL_FP64S_CTA = 3, MINIM_EVAL_LINES = 4 };
 int minim_gpu_eval_kernel(minim_gpu_handle h, int path, const double* x, const double* p, double t,
                           double* e, double* g, double* xt);
+
+/* Failure detection check (no counterpart in the reference): one block
+ * runs the device barrier's bounded wait on an arrival count that nothing
+ * reaches, with its limit set to limit_ms (1 .. 60000).  The wait gives up,
+ * records the error the host reads, and the kernel returns: *timed_out = 1,
+ * *elapsed_ms = the kernel's device time.  The same bound (5 s) protects
+ * every wait of the single-instance kernels, whose minimisations then end
+ * with status MINIM_RES_TIMEOUT. */
+int minim_gpu_wait_probe(int limit_ms, int* timed_out, double* elapsed_ms);
 
 /* ---- allocation-free minimisation (no counterpart in the reference) ------
  * Minimises one Lennard-Jones cluster (LjNd energy, the given minimiser) in

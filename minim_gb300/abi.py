@@ -91,7 +91,7 @@ class RunStats(C.Structure):
     _fields_ = [("kernel_ms", C.c_double), ("wall_ms", C.c_double), ("launches", C.c_int64),
                 ("abytes", C.c_double), ("pairs32", C.c_double), ("pairs64", C.c_double),
                 ("iterations", C.c_int64), ("fp64_iterations", C.c_int64),
-                ("switches", C.c_int64 * 4), ("phase_ms", C.c_double * 3)]
+                ("switches", C.c_int64 * 4), ("phase_ms", C.c_double * 3), ("tune_ms", C.c_double)]
 
 
 class ServerConfig(C.Structure):

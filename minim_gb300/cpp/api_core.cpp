@@ -326,6 +326,9 @@ bool Minimiser::deviceMinimise(State& state) {
   throw_gpu(minim_gpu_instance_get_coords(state.device(), state._coords.data()));
   iter = lastResult.iter;
   deviceDone(lastResult);
+  // a device failure (non-finite values, a device wait that gave up) is the
+  // reference's failure flag, State::failed() (src/State.cpp:326-328)
+  if (lastResult.status == MINIM_RES_NAN || lastResult.status == MINIM_RES_TIMEOUT) state.failed();
   return true;
 }
 

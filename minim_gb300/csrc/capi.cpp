@@ -57,7 +57,7 @@ struct Dev {
   int nsm = 0;
   std::string why;
   cudaStream_t s = nullptr;             // runtime stream (allocations, copies)
-  cudaStream_t ks[4] = {nullptr, nullptr, nullptr, nullptr};  // one per kernel kind
+  cudaStream_t ks[8] = {};              // batch launch streams (one per launch group)
 };
 
 Dev& dev() {
@@ -545,7 +545,7 @@ void do_eval(minim_gpu_instance_s* h, const double* x, double* e, double* g) {
   if (e) *e = ev;
 }
 
-int default_threads(int kk, const std::vector<InstDesc>& ds);
+int rule_threads(int kk, const InstDesc& d);
 
 // One evaluation by a minimiser stage's own potential kernels (the checks of
 // minim_gpu_eval_kernel).  Temporary buffers come from the caching pool.
@@ -646,7 +646,7 @@ void do_eval_kernel(minim_gpu_instance_s* h, int path, const double* x, const do
     if (path == MINIM_EVAL_FP32_GRID || path == MINIM_EVAL_FP64S_GRID) {
       launch_grid(h, OP_EVAL_STAGE, 0);
     } else {
-      const int thr = default_threads(h->kk, std::vector<InstDesc>{h->d});
+      const int thr = rule_threads(h->kk, h->d);
       CK((cudaError_t)kern(h->kk).cta_eval(h->d_desc, h->d_io, thr, pot_smem(h->kk), D.s));
       g_launches++;
     }
@@ -801,79 +801,286 @@ struct minim_gpu_batch_s {
 
 namespace {
 
-// The grid-sized kinds run 512 threads per CTA (one CTA per SM at 128
-// registers a thread): sixteen warps to hide the stencil's and the element
-// gathers' memory and FP64 latency.  The choice depends on the kind alone,
-// so an instance's result does not depend on the rest of the batch.
-int default_threads(int kk, const std::vector<InstDesc>& ds) {
-  if (kk == K_LJ) {
-    int nmax = 0;
-    for (auto& d : ds) nmax = std::max(nmax, d.lj.np);
-    return nmax <= 96 ? 64 : (nmax <= 192 ? 128 : 256);
-  }
-  return 512;
-}
-
 double cost_of(const InstDesc& d, int kk) {
   if (kk == K_LJ) return (double)d.lj.np * d.lj.np;
   if (kk == K_BAH) return (double)d.bah.nbar + 4.0 * d.bah.nhinge + d.ndof;
   return (double)d.ndof;
 }
 
-// Runs the given instances with the batch kernels (one launch per kernel
-// kind, the kinds concurrently on their own streams).  descs[i].st must
-// point into d_st.  Returns when all launches are done.
+// ---- launch shapes and the autotuner ----------------------------------------------
+// An instance's batch launch shape (threads per CTA) is a function of its
+// own kernel kind, size bucket, method and precision only -- never of the
+// rest of the batch -- so that its result is the same alone and in any mix.
+// The shape of a (kind, bucket, method, precision) key is chosen the first
+// time the key is seen in the process: every candidate runs a short slice
+// of the same instances (copies of their coordinates and state; the
+// workspace is not yet in use) and the fastest is kept.  MINIM_GPU_TUNE=0
+// takes the size rule instead; MINIM_GPU_TUNE_CACHE names a file that keeps
+// the choices across processes (keyed by the device name and the driver).
+int size_bucket(int kk, const InstDesc& d) {
+  if (kk == K_LJ) {
+    static const int edges[] = {32, 64, 96, 128, 192, 256, 384, 512, 768, 1024, 1536};
+    int b = 0;
+    while (b < 11 && d.lj.np > edges[b]) b++;
+    return b;
+  }
+  static const double edges[] = {4096, 16384, 65536, 262144, 1048576};
+  const double sz = kk == K_BAH ? (double)d.bah.nvert * 3 : (double)d.ndof;
+  int b = 0;
+  while (b < 5 && sz > edges[b]) b++;
+  return b;
+}
+
+// The size rule: Lennard-Jones 64 / 128 / 256 threads by cluster size; the
+// grid-sized kinds 512 (one CTA per SM at 128 registers a thread: sixteen
+// warps to hide the stencil's and the element gathers' latency).
+int rule_threads(int kk, const InstDesc& d) {
+  if (kk == K_LJ) return d.lj.np <= 96 ? 64 : (d.lj.np <= 192 ? 128 : 256);
+  return 512;
+}
+
+std::vector<int> thread_candidates(int kk) {
+  if (kk == K_LJ) return {64, 128, 256};
+  return {256, 512};
+}
+
+struct TuneKey {
+  int kk, bucket, method, prec;
+  bool operator==(const TuneKey& o) const {
+    return kk == o.kk && bucket == o.bucket && method == o.method && prec == o.prec;
+  }
+};
+struct TuneEntry {
+  TuneKey key;
+  int threads;
+  double ms[4];  // measured time per candidate (0: not measured)
+  int from_file;
+};
+std::vector<TuneEntry> g_tune;
+bool g_tune_loaded = false;
+double g_tune_ms = 0;  // device time spent tuning in the last batch call
+
+TuneKey tune_key(int kk, const InstDesc& d) {
+  return {kk, size_bucket(kk, d), d.mp.method, d.mp.precision};
+}
+
+std::string tune_device_tag() {
+  cudaDeviceProp p;
+  int drv = 0;
+  cudaGetDeviceProperties(&p, dev().id);
+  cudaDriverGetVersion(&drv);
+  std::string tag = std::string(p.name) + "/" + std::to_string(drv);
+  for (auto& c : tag)
+    if (c == ' ') c = '_';
+  return tag;
+}
+
+void tune_load() {
+  if (g_tune_loaded) return;
+  g_tune_loaded = true;
+  const char* fn = std::getenv("MINIM_GPU_TUNE_CACHE");
+  if (!fn || !*fn) return;
+  FILE* f = std::fopen(fn, "r");
+  if (!f) return;
+  const std::string tag = tune_device_tag();
+  char dev_tag[256];
+  TuneEntry e{};
+  while (std::fscanf(f, "%255s %d %d %d %d %d", dev_tag, &e.key.kk, &e.key.bucket, &e.key.method, &e.key.prec,
+                     &e.threads) == 6) {
+    if (tag != dev_tag) continue;
+    bool ok = false;
+    for (int c : thread_candidates(e.key.kk)) ok |= c == e.threads;
+    if (!ok) continue;
+    e.from_file = 1;
+    g_tune.push_back(e);
+  }
+  std::fclose(f);
+}
+
+void tune_save(const TuneEntry& e) {
+  const char* fn = std::getenv("MINIM_GPU_TUNE_CACHE");
+  if (!fn || !*fn) return;
+  FILE* f = std::fopen(fn, "a");
+  if (!f) return;
+  std::fprintf(f, "%s %d %d %d %d %d\n", tune_device_tag().c_str(), e.key.kk, e.key.bucket, e.key.method,
+               e.key.prec, e.threads);
+  std::fclose(f);
+}
+
+bool tune_enabled() {
+  const char* e = std::getenv("MINIM_GPU_TUNE");
+  return !(e && e[0] == '0');
+}
+
+const TuneEntry* tune_find(const TuneKey& k) {
+  for (auto& e : g_tune)
+    if (e.key == k) return &e;
+  return nullptr;
+}
+
+// Times every candidate shape on a short slice of the given fresh
+// instances (at most two per SM of them, largest first) and records the
+// fastest for the key.
+void tune_measure(const TuneKey& key, const std::vector<InstDesc>& sample) {
+  Dev& D = need_dev();
+  const int ns = (int)sample.size();
+  const char* it_env = std::getenv("MINIM_GPU_TUNE_ITERS");
+  const int iters = it_env ? std::max(1, std::atoi(it_env)) : 12;
+  // trial copies: the coordinates (written back by an instance that stops
+  // within the slice) and fresh state records
+  size_t xbytes = 0;
+  std::vector<size_t> xo(ns);
+  for (int i = 0; i < ns; i++) {
+    xo[i] = xbytes;
+    xbytes += align256((size_t)sample[i].ndof * sizeof(double));
+  }
+  char* xcopy = (char*)dalloc(xbytes);
+  MinScalars* st = (MinScalars*)dalloc(ns * sizeof(MinScalars));
+  InstDesc* dd = (InstDesc*)dalloc(ns * sizeof(InstDesc));
+  int* counter = (int*)dalloc(sizeof(int));
+  std::vector<InstDesc> trial(sample);
+  for (int i = 0; i < ns; i++) {
+    trial[i].xres = (double*)(xcopy + xo[i]);
+    trial[i].st = st + i;
+    CK(cudaMemcpyAsync(trial[i].xres, sample[i].xres, sample[i].ndof * sizeof(double), cudaMemcpyDeviceToDevice,
+                       D.s));
+  }
+  CK(cudaMemcpyAsync(dd, trial.data(), ns * sizeof(InstDesc), cudaMemcpyHostToDevice, D.s));
+  std::vector<MinScalars> fresh(ns, fresh_scalars());
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  TuneEntry ent{};
+  ent.key = key;
+  double best = 1e300;
+  const std::vector<int> cand = thread_candidates(key.kk);
+  for (size_t c = 0; c < cand.size(); c++) {
+    int per_sm = 0;
+    CK((cudaError_t)kern(key.kk).occ(0, cand[c], pot_smem(key.kk), &per_sm));
+    if (per_sm < 1) continue;
+    const int blocks = std::min(ns, D.nsm * per_sm);
+    // two runs of the slice, the second timed (the first loads the kernel)
+    float ms = 0;
+    for (int rep = 0; rep < 2; rep++) {
+      CK(cudaMemcpyAsync(st, fresh.data(), ns * sizeof(MinScalars), cudaMemcpyHostToDevice, D.s));
+      CK(cudaMemsetAsync(counter, 0, sizeof(int), D.s));
+      CK(cudaEventRecord(e0, D.s));
+      CK((cudaError_t)kern(key.kk).batch(dd, ns, counter, iters, cand[c], blocks, pot_smem(key.kk), D.s));
+      g_launches++;
+      CK(cudaEventRecord(e1, D.s));
+      CK(cudaEventSynchronize(e1));
+      CK(cudaEventElapsedTime(&ms, e0, e1));
+      g_tune_ms += ms;
+    }
+    ent.ms[c] = ms;
+    if (ms < best) {
+      best = ms;
+      ent.threads = cand[c];
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  dfree(xcopy);
+  dfree(st);
+  dfree(dd);
+  dfree(counter);
+  if (ent.threads == 0) throw ApiError{MINIM_GPU_ERR_CUDA, "batch kernel does not fit on an SM"};
+  g_tune.push_back(ent);
+  tune_save(ent);
+}
+
+// Threads per CTA of every instance: the caller's override, else the tuned
+// (or, with tuning off, the rule's) shape of its key.  Keys not yet tuned
+// are measured on their fresh instances.
+std::vector<int> batch_threads(const std::vector<InstDesc>& descs, const std::vector<int>& kks,
+                               const std::vector<char>& fresh, int threads) {
+  const int n = (int)descs.size();
+  std::vector<int> thr(n, threads);
+  if (threads > 0) return thr;
+  const bool tune = tune_enabled();
+  if (tune) tune_load();
+  std::vector<TuneKey> keys(n);
+  for (int i = 0; i < n; i++) keys[i] = tune_key(kks[i], descs[i]);
+  if (tune) {
+    for (int i = 0; i < n; i++) {
+      if (tune_find(keys[i]) || !fresh[i]) continue;
+      // every fresh instance of this key, largest first, at most two per SM
+      std::vector<int> idx;
+      for (int j = i; j < n; j++)
+        if (fresh[j] && keys[j] == keys[i]) idx.push_back(j);
+      std::stable_sort(idx.begin(), idx.end(),
+                       [&](int a, int b) { return cost_of(descs[a], kks[a]) > cost_of(descs[b], kks[b]); });
+      if ((int)idx.size() > 2 * need_dev().nsm) idx.resize(2 * need_dev().nsm);
+      std::vector<InstDesc> sample;
+      for (int j : idx) sample.push_back(descs[j]);
+      tune_measure(keys[i], sample);
+    }
+  }
+  for (int i = 0; i < n; i++) {
+    const TuneEntry* e = tune ? tune_find(keys[i]) : nullptr;
+    thr[i] = e ? e->threads : rule_threads(kks[i], descs[i]);
+  }
+  return thr;
+}
+
+// Runs the given instances with the batch kernels: one launch per (kernel
+// kind, threads per CTA) group, the groups concurrently on their own
+// streams.  descs[i].st must point into d_st; fresh[i] marks instances not
+// yet started (the autotuner may run trial slices on copies of those).
+// Returns when all launches are done.
 void run_batch(std::vector<InstDesc>& descs, const std::vector<int>& kks, MinScalars* d_st,
-               const std::vector<MinScalars>& st_init, int slice, int threads) {
+               const std::vector<MinScalars>& st_init, int slice, int threads, const std::vector<char>& fresh) {
   Dev& D = need_dev();
   const int n = (int)descs.size();
   if (n == 0) return;
+  g_tune_ms = 0;
+  const std::vector<int> thr = batch_threads(descs, kks, fresh, threads);
   if (!st_init.empty())
     CK(cudaMemcpyAsync(d_st, st_init.data(), n * sizeof(MinScalars), cudaMemcpyHostToDevice, D.s));
-  // group by kernel kind, largest first within a group
+  // group by kernel kind and threads, largest first within a group (LPT)
   std::vector<int> order(n);
   for (int i = 0; i < n; i++) order[i] = i;
   std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
     if (kks[a] != kks[b]) return kks[a] < kks[b];
+    if (thr[a] != thr[b]) return thr[a] < thr[b];
     return cost_of(descs[a], kks[a]) > cost_of(descs[b], kks[b]);
   });
   std::vector<InstDesc> sorted(n);
   for (int i = 0; i < n; i++) sorted[i] = descs[order[i]];
-  InstDesc* d_descs = (InstDesc*)dalloc(n * sizeof(InstDesc));
-  int* d_counters = (int*)dalloc(4 * sizeof(int));
-  CK(cudaMemcpyAsync(d_descs, sorted.data(), n * sizeof(InstDesc), cudaMemcpyHostToDevice, D.s));
-  CK(cudaMemsetAsync(d_counters, 0, 4 * sizeof(int), D.s));
-  cudaEvent_t ready, t_end;
-  CK(cudaEventCreate(&ready));
-  CK(cudaEventCreate(&t_end));
-  CK(cudaEventRecord(ready, D.s));
   // Every group's launch configuration first: the occupancy query loads a
   // kernel that has not run yet in this process, and loading one while
   // another kernel runs waits for it (lazy module loading), which would
-  // serialise the kinds' launches.
+  // serialise the groups' launches.
   struct Launch {
     int kk, i0, i1, thr, blocks;
     size_t smem;
   };
   std::vector<Launch> launches;
   for (int i0 = 0; i0 < n;) {
-    const int kk = kks[order[i0]];
+    const int kk = kks[order[i0]], t = thr[order[i0]];
     int i1 = i0;
-    while (i1 < n && kks[order[i1]] == kk) i1++;
-    std::vector<InstDesc> grp(sorted.begin() + i0, sorted.begin() + i1);
-    const int thr = threads > 0 ? threads : default_threads(kk, grp);
+    while (i1 < n && kks[order[i1]] == kk && thr[order[i1]] == t) i1++;
     const size_t smem = pot_smem(kk);
     int per_sm = 0;
-    CK((cudaError_t)kern(kk).occ(0, thr, smem, &per_sm));
+    CK((cudaError_t)kern(kk).occ(0, t, smem, &per_sm));
     if (per_sm < 1) throw ApiError{MINIM_GPU_ERR_CUDA, "batch kernel does not fit on an SM"};
-    launches.push_back({kk, i0, i1, thr, std::min(i1 - i0, D.nsm * per_sm), smem});
+    launches.push_back({kk, i0, i1, t, std::min(i1 - i0, D.nsm * per_sm), smem});
     i0 = i1;
   }
+  InstDesc* d_descs = (InstDesc*)dalloc(n * sizeof(InstDesc));
+  int* d_counters = (int*)dalloc(launches.size() * sizeof(int));
+  CK(cudaMemcpyAsync(d_descs, sorted.data(), n * sizeof(InstDesc), cudaMemcpyHostToDevice, D.s));
+  CK(cudaMemsetAsync(d_counters, 0, launches.size() * sizeof(int), D.s));
+  cudaEvent_t ready, t_end;
+  CK(cudaEventCreate(&ready));
+  CK(cudaEventCreate(&t_end));
+  CK(cudaEventRecord(ready, D.s));
   std::vector<cudaEvent_t> done;
-  for (const Launch& L : launches) {
-    cudaStream_t ks = D.ks[L.kk];
+  for (size_t g = 0; g < launches.size(); g++) {
+    const Launch& L = launches[g];
+    cudaStream_t ks = D.ks[g % 8];
     CK(cudaStreamWaitEvent(ks, ready, 0));
-    CK((cudaError_t)kern(L.kk).batch(d_descs + L.i0, L.i1 - L.i0, d_counters + L.kk, slice, L.thr, L.blocks,
+    CK((cudaError_t)kern(L.kk).batch(d_descs + L.i0, L.i1 - L.i0, d_counters + g, slice, L.thr, L.blocks,
                                      L.smem, ks));
     g_launches++;
     cudaEvent_t ev;
@@ -891,6 +1098,7 @@ void run_batch(std::vector<InstDesc>& descs, const std::vector<int>& kks, MinSca
   CK(cudaEventElapsedTime(&ms, ready, t_end));
   g_stats.kernel_ms = ms;
   g_stats.launches = (int64_t)done.size();
+  g_stats.tune_ms = g_tune_ms;
   cudaEventDestroy(ready);
   cudaEventDestroy(t_end);
   dfree(d_descs);
@@ -1124,7 +1332,7 @@ int minim_gpu_batch_run(minim_gpu_batch b, int threads, minim_gpu_result* result
     }
     std::vector<MinScalars> st(n, fresh_scalars());
     const double t0 = now_ms();
-    run_batch(descs, kks, d_st, st, 0x7fffffff, threads);
+    run_batch(descs, kks, d_st, st, 0x7fffffff, threads, std::vector<char>(n, 1));
     CK(cudaMemcpyAsync(st.data(), d_st, n * sizeof(MinScalars), cudaMemcpyDeviceToHost, D.s));
     CK(cudaStreamSynchronize(D.s));
     g_stats.wall_ms = now_ms() - t0;
@@ -1146,6 +1354,50 @@ int minim_gpu_batch_run(minim_gpu_batch b, int threads, minim_gpu_result* result
     dfree(d_st);
     if (results)
       for (int i = 0; i < n; i++) fill_result(&results[i], st[i], b->inst[i]->n);
+  });
+}
+
+int minim_gpu_wait_probe(int limit_ms, int* timed_out, double* elapsed_ms) {
+  return guarded([&] {
+    Dev& D = need_dev();
+    if (limit_ms < 1 || limit_ms > 60000) throw ApiError{MINIM_GPU_ERR_INVALID, "limit_ms must be 1 .. 60000"};
+    GridSyncState* bar = (GridSyncState*)dalloc(sizeof(GridSyncState));
+    GridSyncState h{};
+    h.limit_ms = (unsigned)limit_ms;
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    CK(cudaMemcpyAsync(bar, &h, sizeof h, cudaMemcpyHostToDevice, D.s));
+    CK(cudaEventRecord(e0, D.s));
+    CK((cudaError_t)mg_wait_probe(bar, D.s));
+    g_launches++;
+    CK(cudaEventRecord(e1, D.s));
+    CK(cudaMemcpyAsync(&h, bar, sizeof h, cudaMemcpyDeviceToHost, D.s));
+    CK(cudaStreamSynchronize(D.s));
+    float ms = 0;
+    CK(cudaEventElapsedTime(&ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    dfree(bar);
+    if (timed_out) *timed_out = h.err != 0;
+    if (elapsed_ms) *elapsed_ms = ms;
+  });
+}
+
+int minim_gpu_tune_table(int cap, int* rows, double* ms, int* n) {
+  return guarded([&] {
+    const int k = (int)g_tune.size();
+    if (n) *n = k;
+    for (int i = 0; i < k && i < cap; i++) {
+      const TuneEntry& e = g_tune[i];
+      const int kind = e.key.kk == K_LJ ? MINIM_GPU_LJ : (e.key.kk == K_BAH ? MINIM_GPU_BAH : MINIM_GPU_PF);
+      const int cand = (int)thread_candidates(e.key.kk).size();
+      const int row[7] = {kind, e.key.bucket, e.key.method, e.key.prec, e.threads, e.from_file ? 0 : 1,
+                          e.from_file ? 0 : cand};
+      if (rows) std::memcpy(rows + 7 * i, row, sizeof row);
+      if (ms)
+        for (int c = 0; c < 4; c++) ms[4 * i + c] = e.ms[c];
+    }
   });
 }
 
@@ -1235,14 +1487,16 @@ int minim_gpu_server_step(minim_gpu_server s, int* n_resident, int* n_queued) {
     // one slice on every resident instance
     std::vector<InstDesc> descs;
     std::vector<int> kks, slot_of;
+    std::vector<char> fresh;
     for (int k = 0; k < s->cfg.max_slots; k++) {
       if (!s->slots[k]) continue;
       descs.push_back(s->descs[k]);
       kks.push_back(s->reqs[s->slots[k]].inst->kk);
       slot_of.push_back(k);
+      fresh.push_back(std::find(admitted.begin(), admitted.end(), k) != admitted.end());
     }
     if (!descs.empty()) {
-      run_batch(descs, kks, s->d_st, {}, s->cfg.slice_iters, s->cfg.threads_per_cta);
+      run_batch(descs, kks, s->d_st, {}, s->cfg.slice_iters, s->cfg.threads_per_cta, fresh);
       std::vector<MinScalars> st(s->cfg.max_slots);
       CK(cudaMemcpyAsync(st.data(), s->d_st, s->cfg.max_slots * sizeof(MinScalars), cudaMemcpyDeviceToHost, D.s));
       CK(cudaStreamSynchronize(D.s));

@@ -628,6 +628,10 @@ struct GridTeam {
 
   __device__ __forceinline__ bool block0() const { return blockIdx.x == 0; }
   __device__ __forceinline__ bool ok() const { return *s_ok != 0; }
+  __device__ __forceinline__ unsigned long long wait_limit_ns() const {
+    const unsigned int ms = bar->limit_ms;
+    return ms ? (unsigned long long)ms * 1000000ull : kWaitLimitNs;
+  }
   // records a failed wait: this block stops, the others stop at their next
   // barrier (status TIMEOUT)
   __device__ void fail() {
@@ -649,7 +653,7 @@ struct GridTeam {
       const unsigned long long t = globaltimer_ns();
       if (t0 == 0) {
         t0 = t;
-      } else if (t - t0 > kWaitLimitNs) {
+      } else if (t - t0 > wait_limit_ns()) {
         atomicExch(&bar->err, 1);
         return false;
       }

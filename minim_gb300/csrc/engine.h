@@ -180,8 +180,8 @@ struct InstDesc {
 struct GridSyncState {
   unsigned int count;
   unsigned int gen;
-  int err;      // set when a barrier wait gave up
-  int pad;
+  int err;                // set when a barrier wait gave up
+  unsigned int limit_ms;  // bound of every wait (0: 5 s)
 };
 
 // ---- kernel entry points (engine.cu) ---------------------------------------------
@@ -224,6 +224,10 @@ MG_DECLARE_LAUNCHERS(bah)
 MG_DECLARE_LAUNCHERS(pf1)
 // engine_misc.cu: FP64 <-> FP32 vector conversion on a stream
 int mg_convert(const void* src, void* dst, size_t n, int to_float, void* stream);
+// engine_misc.cu: one block waits, with the grid barrier's bounded wait, for
+// an arrival count that nothing reaches; *bar must be zeroed with its
+// limit_ms set.  The kernel returns when the wait gives up (bar->err = 1).
+int mg_wait_probe(mg::GridSyncState* bar, void* stream);
 // stepped.cu: up to `slice` FP32 L-BFGS iterations (history m) of a binary
 // PhaseField instance as one launch of the graph of its shape (cached per
 // process); dual: the workspace has the spare buffers for two trials per

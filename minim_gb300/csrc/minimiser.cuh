@@ -154,9 +154,15 @@ struct Runner {
   }
 
   // ---- potential dispatch -------------------------------------------------------
-  // kFast: the FP64-coordinate evaluations of the minimiser may use
-  // double-float arithmetic (general PhaseField, BarAndHinge); the API
-  // evaluation and Anneal's Metropolis energies use FP64 throughout.
+  // kFast: the FP64-coordinate evaluations of a MIXED-precision minimiser
+  // use double-float arithmetic (general PhaseField, BarAndHinge; about 47
+  // bits); the API evaluation, FP64-precision minimisations, Anneal's
+  // Metropolis energies and a start already near convergence (switch
+  // reason 5) use FP64 throughout.  At such a start the gradient may be
+  // exactly zero in FP64 but not in double-float, and the first L-BFGS step
+  // is a unit step along -g/|g| whenever |g| > 0 (src/minimisers/
+  // Lbfgs.cpp:93-97): double-float rounding noise would set its direction.
+  __device__ bool df_stage() const { return in.mp.method != 3 && in.mp.precision == 0 && switch_reason != 5; }
   template <typename T, bool kFast = true, class Emit>
   __device__ double pot_eval(CView<T> cv, T* xw, Emit& em, bool want_e, bool want_g) {
     if constexpr (KIND == K_LJ) {
@@ -172,7 +178,7 @@ struct Runner {
     } else if constexpr (KIND == K_PF) {
       if constexpr (kFast && std::is_same_v<T, double>) {
         // the FP32 coordinate buffers are free while the coordinates are FP64
-        if (in.mp.method != 3) return pf_eval_df(tm, in.pf, cv, xw, &em, want_e, want_g, in.X32[0], in.X32[1]);
+        if (df_stage()) return pf_eval_df(tm, in.pf, cv, xw, &em, want_e, want_g, in.X32[0], in.X32[1]);
       }
       return pf_eval<T>(tm, in.pf, cv, xw, &em, want_e, want_g);
     } else if constexpr (KIND == K_PF1) {
@@ -180,7 +186,7 @@ struct Runner {
       return pf1_eval<T>(tm, in.pf, cv, xw, &em, want_e, want_g);
     } else {
       if constexpr (kFast && std::is_same_v<T, double>) {
-        if (in.mp.method != 3)
+        if (df_stage())
           return bah_eval_df(tm, in.bah, cv, xw, in.GA, &em, want_e, want_g, in.X32[0], in.X32[1]);
       }
       return bah_eval<T>(tm, in.bah, cv, xw, in.GA, &em, want_e, want_g);
@@ -1105,6 +1111,20 @@ struct Runner {
         gi = 0;
       }
       if (mp.precision == 1) stage = 1;
+      if (mixed && mp.method != 3) {
+        // A start already near convergence stays in FP64: rounding it to
+        // FP32 would only add noise that the FP64 stage must then relax
+        // (a sheet started at its rest shape).  The FP64 gradient at the
+        // exact start decides.
+        stage = 1;
+        switch_reason = 5;  // the decision's evaluation in FP64 arithmetic
+        double py, yyv;
+        grad_eval(0.0, nullptr, false, false, py, yyv);
+        if (!(rms() < 100.0 * mp.tol)) {
+          stage = 0;
+          switch_reason = 0;
+        }
+      }
       if (mp.method == 0) {
         ii = 0;
         if (threadIdx.x == 0)

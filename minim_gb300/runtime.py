@@ -32,7 +32,7 @@ EXPORTS = [
     "minim_gpu_server_poll", "minim_gpu_server_take", "minim_gpu_server_cancel",
     "minim_gpu_server_destroy", "minim_gpu_bah_elements", "minim_gpu_bah_colouring",
     "minim_gpu_pf_setup", "minim_gpu_lj_minimise_noalloc", "minim_gpu_instance_bah_arrays",
-    "minim_gpu_eval_kernel",
+    "minim_gpu_eval_kernel", "minim_gpu_tune_table", "minim_gpu_wait_probe",
 ]
 
 
@@ -85,6 +85,8 @@ def load(path=LIB_PATH):
         "minim_gpu_pf_setup": ([C.c_int, P, _dp, C.c_size_t, _dp, _dp, _ip, _dp, _dp, _ip], C.c_int),
         "minim_gpu_instance_bah_arrays": ([P, C.c_int, _ip, _ip, _dp, _ip, _ip, _ip, _ip, _dp, _ip, _ip, _ip],
                                           C.c_int),
+        "minim_gpu_tune_table": ([C.c_int, _ip, _dp, _ip], C.c_int),
+        "minim_gpu_wait_probe": ([C.c_int, _ip, _dp], C.c_int),
         "minim_gpu_eval_kernel": ([P, C.c_int, _dp, _dp, C.c_double, _dp, _dp, _dp], C.c_int),
         "minim_gpu_lj_minimise_noalloc": ([P, C.c_void_p, C.c_size_t, C.POINTER(abi.MinimiserParams),
                                            C.POINTER(abi.Result), C.c_void_p], C.c_int),
@@ -119,6 +121,36 @@ def last_run_stats():
     d["switches"] = list(s.switches)
     d["phase_ms"] = list(s.phase_ms)
     return d
+
+
+def wait_probe(limit_ms):
+    """Runs the device barrier's bounded wait on a count nothing reaches
+    with the given limit: (timed_out, elapsed device ms)."""
+    lib = load()
+    t, ms = C.c_int(), C.c_double()
+    _check(lib.minim_gpu_wait_probe(int(limit_ms), C.byref(t), C.byref(ms)))
+    return bool(t.value), ms.value
+
+
+def tune_table():
+    """The autotuner's choices so far: one dict per (kind, size bucket,
+    method, precision) key with the chosen threads per CTA and the measured
+    slice time of each candidate (ms)."""
+    lib = load()
+    n = C.c_int()
+    _check(lib.minim_gpu_tune_table(0, None, None, C.byref(n)))
+    k = n.value
+    rows = np.zeros(7 * max(k, 1), np.int32)
+    ms = np.zeros(4 * max(k, 1))
+    _check(lib.minim_gpu_tune_table(k, rows.ctypes.data_as(_ip), ms.ctypes.data_as(_dp), C.byref(n)))
+    kinds = {abi.LJ: "lj", abi.PF: "pf", abi.BAH: "bah"}
+    out = []
+    for i in range(k):
+        r = rows[7 * i:7 * i + 7]
+        out.append({"kind": kinds.get(int(r[0]), int(r[0])), "bucket": int(r[1]), "method": int(r[2]),
+                    "precision": int(r[3]), "threads": int(r[4]), "measured": bool(r[5]),
+                    "candidate_ms": [float(v) for v in ms[4 * i:4 * i + int(r[6])]]})
+    return out
 
 
 class Instance:

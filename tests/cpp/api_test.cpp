@@ -116,9 +116,33 @@ static void host_tests() {
     Lbfgs lbfgs = Lbfgs().setMaxIter(10);
     CHECK(lbfgs.maxIter == 10);
   }
+  {  // State::failed() from the adjustState callback ends the loop before
+     // that iteration (src/Minimiser.cpp:33, src/State.cpp:326-328)
+    Toy2d pot;
+    State state = pot.newState({1, 4});
+    GradDescent gd = GradDescent().setMaxIter(100);
+    gd.minimise(state, [](int i, State& s) {
+      if (i == 3) s.failed();
+    });
+    CHECK(state.isFailed && gd.iter == 3);
+    State ref = pot.newState({1, 4});
+    GradDescent gd3 = GradDescent().setMaxIter(2);
+    gd3.minimise(ref);
+    CHECK(state.coords() == ref.coords());
+  }
 }
 
 static void device_tests() {
+  {  // a device minimisation that produces non-finite values reports the
+     // reference's failure flag; a clean one does not
+    Lj3d pot;
+    State bad = pot.newState({0, 0, 0, 1.1, 0, 0, 0, NAN, 0.3});
+    Lbfgs().minimise(bad);
+    CHECK(bad.isFailed);
+    State good = pot.newState({0, 0, 0, 1.1, 0, 0, 0, 1.2, 0.3});
+    Lbfgs().minimise(good);
+    CHECK(!good.isFailed);
+  }
   {  // State_test TestEnergyGradient / TestClone
     Lj3d pot;
     State s = pot.newState({0, 0, 0, 2, 0, 0});

@@ -354,3 +354,35 @@ def test_server_roundtrip():
         assert r.latency_ms > 0
         x = srv.take(rid)
         check_minimum(p, ids[rid], x, r, 1e-6)
+
+
+@pytest.mark.parametrize("amp", [1e-4, 0.0])
+def test_mixed_start_near_convergence_runs_fp64(amp):
+    """A start within 100x of the tolerance (a sheet at its rest shape, or
+    barely perturbed from it) is minimised in FP64 from the exact start:
+    rounding it to FP32 would add noise that the FP64 stage must then relax
+    through the soft hinge modes.  Mixed precision then takes about as many
+    iterations as FP64."""
+    from tests.workloads import Rng
+    flat, tris, _ = sheet(48, seed=6100)
+    x0 = flat.copy()
+    x0[2::3] += Rng(6101).normal(48 * 48) * amp
+    p = abi.bar_and_hinge(triangulation=tris, rigidity=(1, 0.01))
+    out = {}
+    for prec in ("fp64", "mixed"):
+        inst = runtime.Instance(p, flat)
+        inst.coords = x0
+        b = runtime.Batch()
+        b.add(inst, abi.minimiser("lbfgs", tol=1e-7, precision=prec, max_iter=50000))
+        r = b.run()[0]
+        assert r.status == abi.RES_CONVERGED, (prec, r.as_dict())
+        ora = Oracle(p, flat)
+        e, g = ora.energy_gradient(inst.coords)
+        assert np.sqrt(np.mean(g ** 2)) < 1e-7
+        out[prec] = r
+    # the whole run in FP64 coordinates (double-float arithmetic in mixed
+    # mode, so the iteration counts differ by rounding, not by the FP32
+    # noise relaxation that took thousands of iterations)
+    info = {k: v.as_dict() for k, v in out.items()}
+    assert out["mixed"].fp64_iters >= out["mixed"].iter, info
+    assert out["mixed"].iter <= 1.5 * out["fp64"].iter + 10, info

@@ -28,7 +28,7 @@ def test_exports_every_declared_symbol(engine):
 
 
 def test_abi_version(engine):
-    assert engine.minim_gpu_abi_version() == 1
+    assert engine.minim_gpu_abi_version() == 2
 
 
 def test_struct_layout_matches_header(tmp_path):
