@@ -317,7 +317,8 @@ def run_batched(args):
     out = {
         "batched": {"value": batched, "unit": "converged minimisations/s", "instances": len(items),
                     "converged": int(conv), "kernel_ms": st["kernel_ms"], "tune_ms": st["tune_ms"],
-                    "by_method": by_method,
+                    "by_method": by_method, "iterations": st["iterations"],
+                    "fp64_iteration_share": st["fp64_iterations"] / max(st["iterations"], 1),
                     "fp32_tflops": flops32 / (st["kernel_ms"] / 1e3) / 1e12,
                     "launch_shapes": [t for t in runtime.tune_table() if t["kind"] == "lj"],
                     "workload": f"{len(items)} LJ clusters N~U{{13..400}}, half Fire(0.1) half Lbfgs(m=5), "

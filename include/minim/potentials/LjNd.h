@@ -8,7 +8,8 @@
 namespace minim {
 using std::vector;
 
-// Lennard-Jones over all particle pairs (no cutoff), evaluated on the GPU.
+// Lennard-Jones over all particle pairs, evaluated on the GPU.  setCutoff
+// (not in the reference) keeps only the pairs closer than the cutoff.
 class LjNd : public NewPotential<LjNd> {
  public:
   int potentialType() const override { return Potential::UNSTRUCTURED; }
@@ -17,6 +18,7 @@ class LjNd : public NewPotential<LjNd> {
   int nParticle = 0;
   double sigma = 1;
   double epsilon = 1;
+  double cutoff = 0;  // 0: every pair
 
   LjNd(int nDim) : nDim(nDim) {}
   LjNd(int nDim, double sigma, double epsilon) : nDim(nDim), sigma(sigma), epsilon(epsilon) {}
@@ -28,6 +30,9 @@ class LjNd : public NewPotential<LjNd> {
 
   LjNd& setSigma(double sigma);
   LjNd& setEpsilon(double epsilon);
+  // Pairs with r >= rc contribute nothing (plain truncation; 0 = every
+  // pair).  No counterpart in the reference; found by a device cell list.
+  LjNd& setCutoff(double rc);
 };
 
 class Lj2d : public LjNd {

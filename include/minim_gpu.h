@@ -67,11 +67,16 @@ enum {
  * penalty, DENSITY_FIXED as the Nth fluid computed from the others). */
 enum { MINIM_GPU_LJ = 0, MINIM_GPU_PF = 1, MINIM_GPU_BAH = 2, MINIM_GPU_PFU = 3 };
 
-/* LjNd(nDim, sigma, epsilon): include/potentials/LjNd.h:22-24 */
+/* LjNd(nDim, sigma, epsilon): include/potentials/LjNd.h:22-24.  cutoff has
+ * no counterpart in the reference, which sums every pair: 0 (the default)
+ * keeps every pair; rc > 0 keeps the pairs with r^2 < rc^2, r^2 evaluated
+ * in FP64 ((dx^2 + dy^2) + dz^2, one rounding per operation) of the
+ * coordinates the evaluation sees, found through a device cell list. */
 typedef struct {
   int ndim;         /* 2 or 3 */
   double sigma;     /* default 1 */
   double epsilon;   /* default 1 */
+  double cutoff;    /* 0 = every pair (the reference) */
 } minim_gpu_lj_params;
 
 /* PhaseField (MODEL_BASIC): include/potentials/PhaseField.h:13-69.
@@ -333,6 +338,13 @@ enum { MINIM_EVAL_FP32_GRID = 0, MINIM_EVAL_FP32_CTA = 1, MINIM_EVAL_FP64S_GRID 
        MINIM_EVAL_FP64S_CTA = 3, MINIM_EVAL_LINES = 4 };
 int minim_gpu_eval_kernel(minim_gpu_handle h, int path, const double* x, const double* p, double t,
                           double* e, double* g, double* xt);
+
+/* The pairs i < j that the FP32 stage of a Lennard-Jones instance with a
+ * cutoff evaluates at x (rounded to FP32), from the device cell list (no
+ * counterpart in the reference): up to cap pairs (2 ints each) sorted by
+ * (i, j) into pairs, the total into *npairs.  For checking the pair set
+ * against a CPU enumeration with the same FP64 r^2 of the same FP32 values. */
+int minim_gpu_lj_cutoff_pairs(minim_gpu_handle h, const double* x, int cap, int* pairs, int* npairs);
 
 /* Failure detection check (no counterpart in the reference): one block
  * runs the device barrier's bounded wait on an arrival count that nothing

@@ -31,7 +31,7 @@ _cp = C.c_char_p
 
 
 class LjParams(C.Structure):
-    _fields_ = [("ndim", C.c_int), ("sigma", C.c_double), ("epsilon", C.c_double)]
+    _fields_ = [("ndim", C.c_int), ("sigma", C.c_double), ("epsilon", C.c_double), ("cutoff", C.c_double)]
 
 
 class PfParams(C.Structure):
@@ -125,9 +125,10 @@ class Params:
         return C.cast(C.pointer(self.struct), C.c_void_p)
 
 
-def lj(ndim=3, sigma=1.0, epsilon=1.0):
-    """LjNd(nDim, sigma, epsilon)."""
-    return Params(LJ, LjParams(ndim, sigma, epsilon), [])
+def lj(ndim=3, sigma=1.0, epsilon=1.0, cutoff=0.0):
+    """LjNd(nDim, sigma, epsilon); cutoff > 0 keeps only the pairs closer
+    than it (LjNd::setCutoff, no counterpart in the reference)."""
+    return Params(LJ, LjParams(ndim, sigma, epsilon, cutoff), [])
 
 
 def phase_field(grid, nfluid=1, resolution=1.0, interface_size=None, surface_tension=None,

@@ -21,7 +21,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU = ["engine_lj.cu", "engine_pf.cu", "engine_pf1.cu", "engine_bah.cu", "engine_misc.cu", "noalloc.cu", "stepped.cu", "topology.cu"]
 CPP = ["setup.cpp", "capi.cpp"]
 API = ["api_core.cpp", "api_minimisers.cpp", "api_potentials.cpp"]  # source-compatible C++ API
-HEADERS = ["common.cuh", "potentials.cuh", "minimiser.cuh", "kernels.cuh", "engine.h", "setup.h"]
+HEADERS = ["common.cuh", "potentials.cuh", "ljcells.cuh", "minimiser.cuh", "kernels.cuh", "engine.h", "setup.h"]
 API_HEADERS = ["minim.h", "State.h", "Potential.h", "Minimiser.h", "Communicator.h", "minimisers/Lbfgs.h",
                "minimisers/Fire.h", "minimisers/GradDescent.h", "potentials/LjNd.h", "potentials/PhaseField.h",
                "potentials/BarAndHinge.h", "utils/vec.h", "utils/mpi.h", "utils/print.h"]

@@ -27,6 +27,7 @@ void LjNd::elementEnergyGradient(const vector<double>& x, const Element& el, dou
     dx[d] = x[el.idof[d]] - x[el.idof[nDim + d]];
     r2 += dx[d] * dx[d];
   }
+  if (cutoff > 0 && r2 >= cutoff * cutoff) return;
   const double lj6 = std::pow(sigma, 6) / std::pow(r2, 3);
   const double lj12 = lj6 * lj6;
   if (e) *e += 4 * epsilon * (lj12 - lj6);
@@ -40,7 +41,7 @@ void LjNd::elementEnergyGradient(const vector<double>& x, const Element& el, dou
 }
 
 minim_gpu_handle LjNd::createDevice(const vector<double>& coords) const {
-  minim_gpu_lj_params p{nDim, sigma, epsilon};
+  minim_gpu_lj_params p{nDim, sigma, epsilon, cutoff};
   minim_gpu_handle h = nullptr;
   throw_gpu(minim_gpu_instance_create(MINIM_GPU_LJ, &p, coords.data(), coords.size(), &h));
   return h;
@@ -52,6 +53,11 @@ LjNd& LjNd::setSigma(double s) {
 }
 LjNd& LjNd::setEpsilon(double e) {
   epsilon = e;
+  return *this;
+}
+LjNd& LjNd::setCutoff(double rc) {
+  if (!(rc >= 0)) throw std::invalid_argument("LjNd: the cutoff must be >= 0.");
+  cutoff = rc;
   return *this;
 }
 

@@ -439,6 +439,17 @@ minim_gpu_instance_s* create_instance(int kind, const void* params, const double
       h->d.lj.np = (int)(ndof / q->ndim);
       h->d.lj.s6 = std::pow(q->sigma, 6);
       h->d.lj.eps = q->epsilon;
+      if (!(q->cutoff >= 0) || std::isinf(q->cutoff))
+        throw ApiError{MINIM_GPU_ERR_INVALID, "LjNd: the cutoff must be a finite value >= 0."};
+      if (q->cutoff > 0) {
+        // cell-list scratch: a hash table of at least 2N buckets
+        int hb = 6;
+        while (((size_t)1 << hb) < 2 * (size_t)h->d.lj.np) hb++;
+        h->d.lj.rc2 = q->cutoff * q->cutoff;
+        h->d.lj.inv_cs = 1.0 / (q->cutoff * (1.0 + 1e-3));
+        h->d.lj.hbits = hb;
+        h->d.lj.cells = (int*)h->own(dalloc(lj_cell_ints(h->d.lj.np, hb) * sizeof(int)));
+      }
     } else if (kind == MINIM_GPU_PF || kind == MINIM_GPU_PFU) {
       PfHost H = setup_pf(*(const minim_gpu_pf_params*)params, x0, ndof, kind == MINIM_GPU_PFU);
       h->kk = H.kernel_kind;
@@ -1354,6 +1365,56 @@ int minim_gpu_batch_run(minim_gpu_batch b, int threads, minim_gpu_result* result
     dfree(d_st);
     if (results)
       for (int i = 0; i < n; i++) fill_result(&results[i], st[i], b->inst[i]->n);
+  });
+}
+
+int minim_gpu_lj_cutoff_pairs(minim_gpu_handle h, const double* x, int cap, int* pairs, int* npairs) {
+  return guarded([&] {
+    if (!h || !x || cap < 0 || (cap > 0 && !pairs) || !npairs)
+      throw ApiError{MINIM_GPU_ERR_INVALID, "minim_gpu_lj_cutoff_pairs: invalid arguments"};
+    if (h->kk != K_LJ || !(h->d.lj.rc2 > 0))
+      throw ApiError{MINIM_GPU_ERR_INVALID, "minim_gpu_lj_cutoff_pairs: not a Lennard-Jones instance with a cutoff"};
+    Dev& D = need_dev();
+    ensure_grid(h);
+    const size_t n = h->n;
+    const size_t xb = align256(n * sizeof(float));
+    char* buf = (char*)dalloc(xb + 256 + (size_t)std::max(cap, 1) * sizeof(int2));
+    float* x32 = (float*)buf;
+    int* cnt = (int*)(buf + xb);
+    int2* out = (int2*)(buf + xb + 256);
+    try {
+      CK(cudaMemcpyAsync(h->d_tmp, x, n * sizeof(double), cudaMemcpyHostToDevice, D.s));
+      CK((cudaError_t)mg_convert(h->d_tmp, x32, n, 1, D.s));
+      CK(cudaMemsetAsync(cnt, 0, sizeof(int), D.s));
+      EvalIO io{};
+      io.x32 = x32;
+      io.pairs = out;
+      io.npairs = cnt;
+      io.cap = cap;
+      CK(cudaMemcpyAsync(h->d_desc, &h->d, sizeof(InstDesc), cudaMemcpyHostToDevice, D.s));
+      CK(cudaMemcpyAsync(h->d_io, &io, sizeof io, cudaMemcpyHostToDevice, D.s));
+      launch_grid(h, OP_LJ_PAIRS, 0);
+      int total = 0;
+      CK(cudaMemcpyAsync(&total, cnt, sizeof(int), cudaMemcpyDeviceToHost, D.s));
+      CK(cudaStreamSynchronize(D.s));
+      if (grid_error(h)) throw ApiError{MINIM_GPU_ERR_RUNTIME, "device barrier timed out"};
+      const int k = std::min(total, cap);
+      std::vector<int2> hp(k);
+      if (k) CK(cudaMemcpyAsync(hp.data(), out, k * sizeof(int2), cudaMemcpyDeviceToHost, D.s));
+      CK(cudaStreamSynchronize(D.s));
+      std::sort(hp.begin(), hp.end(),
+                [](const int2& a, const int2& b) { return a.x != b.x ? a.x < b.x : a.y < b.y; });
+      for (int i = 0; i < k; i++) {
+        pairs[2 * i] = hp[i].x;
+        pairs[2 * i + 1] = hp[i].y;
+      }
+      *npairs = total;
+    } catch (...) {
+      cudaStreamSynchronize(D.s);
+      dfree(buf);
+      throw;
+    }
+    dfree(buf);
   });
 }
 

@@ -22,7 +22,17 @@ struct PotLJ {
   int np;          // particles
   double s6;       // sigma^6
   double eps;      // epsilon
+  // cutoff (no counterpart in the reference, which sums every pair): pairs
+  // with r^2 >= rc2 are left out, found through a hashed cell list
+  double rc2;      // 0: every pair
+  double inv_cs;   // 1 / cell size (the cell size is rc * (1 + 1e-3))
+  int hbits;       // log2 of the hash table's buckets
+  int* cells;      // scratch: lj_cell_ints(np, hbits) ints
 };
+// ints of the cell-list scratch: bucket starts (H + 1), cursors (H), the
+// particles in bucket order (N), each particle's bucket (N), one int of
+// padding, and each particle's 64-bit cell key (2 N)
+inline size_t lj_cell_ints(int np, int hbits) { return 2 * ((size_t)1 << hbits) + 4 * (size_t)np + 2; }
 
 enum PfFlags : unsigned {
   PF_SOLID = 1u << 0,      // aux[] present: node types and solid-neighbour masks
@@ -185,7 +195,7 @@ struct GridSyncState {
 };
 
 // ---- kernel entry points (engine.cu) ---------------------------------------------
-enum Op { OP_MINIMISE = 0, OP_EVAL = 1, OP_CONSTRAIN = 2, OP_EVAL_STAGE = 3 };
+enum Op { OP_MINIMISE = 0, OP_EVAL = 1, OP_CONSTRAIN = 2, OP_EVAL_STAGE = 3, OP_LJ_PAIRS = 4 };
 
 struct EvalIO {      // OP_EVAL / OP_CONSTRAIN on one instance, FP64 in/out
   const double* x;   // coordinates (device), ndof
@@ -202,6 +212,10 @@ struct EvalIO {      // OP_EVAL / OP_CONSTRAIN on one instance, FP64 in/out
   const float* x32;
   const float* p;    // direction (FP32 in both stages), or NULL
   float* g32;
+  // OP_LJ_PAIRS: the pairs i < j within the cutoff at x32 (at most cap)
+  int2* pairs;
+  int* npairs;
+  int cap;
 };
 
 }  // namespace mg

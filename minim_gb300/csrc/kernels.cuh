@@ -195,6 +195,12 @@ grid_kernel(const InstDesc* __restrict__ inst, int op, const EvalIO* io, int sli
     eval_op(R, tm, s_in, *io);
   } else if (op == OP_EVAL_STAGE) {
     eval_stage_op(R, tm, s_in, *io);
+  } else if (op == OP_LJ_PAIRS) {
+    if constexpr (KIND == K_LJ) {
+      CView<float> cv{io->x32, nullptr, 0.f};
+      NoEmit ne;
+      lj_cells_eval<float>(tm, s_in.lj, cv, (float*)nullptr, &ne, false, false, io->pairs, io->npairs, io->cap);
+    }
   } else {
     constrain_op<GridTeam, KIND>(tm, s_in, *io);
   }

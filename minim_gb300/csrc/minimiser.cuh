@@ -146,7 +146,8 @@ struct Runner {
     double b = xbytes() + (trial ? 4.0 : 0.0) + (want_g ? 4.0 : 0.0);
     if constexpr (KIND == K_LJ) {
       const double np = in.lj.np;
-      const double pairs = want_g ? np * (np - 1) : 0.5 * np * (np - 1);
+      // with a cutoff the pairs evaluated are not counted
+      const double pairs = in.lj.rc2 > 0 ? 0.0 : (want_g ? np * (np - 1) : 0.5 * np * (np - 1));
       if (stage) MG_ACCT(pairs64, pairs);
       else MG_ACCT(pairs32, pairs);
     }
@@ -166,6 +167,8 @@ struct Runner {
   template <typename T, bool kFast = true, class Emit>
   __device__ double pot_eval(CView<T> cv, T* xw, Emit& em, bool want_e, bool want_g) {
     if constexpr (KIND == K_LJ) {
+      if (in.lj.rc2 > 0)
+        return lj_cells_eval<T>(tm, in.lj, cv, xw, &em, want_e, want_g, (int2*)nullptr, (int*)nullptr, 0);
       if constexpr (!Team::kGrid) {
         // batched path: each pair once, when positions and forces of all
         // particles fit the tile buffer

@@ -82,6 +82,10 @@ extern "C" int minim_gpu_lj_minimise_noalloc(const minim_gpu_lj_params* p, doubl
     mg_set_last_error("LjNd: Length of coords must be a multiple of the number of dimensions.");
     return MINIM_GPU_ERR_INVALID;
   }
+  if (p->cutoff != 0) {
+    mg_set_last_error("minim_gpu_lj_minimise_noalloc: evaluates every pair (cutoff must be 0)");
+    return MINIM_GPU_ERR_INVALID;
+  }
   if (ndof > (size_t)kMaxDof) {
     mg_set_last_error("minim_gpu_lj_minimise_noalloc: at most 3072 degrees of freedom "
                       "(1024 particles in 3-D) fit the fixed scratch array");

@@ -200,6 +200,10 @@ __device__ __noinline__ double lj_eval(Team& tm, const PotLJ& P, CView<T> cv, T*
   return 4.0 * P.eps * ((e4[0].total() + e4[1].total()) + (e4[2].total() + e4[3].total()));
 }
 
+}  // namespace mg
+#include "ljcells.cuh"
+namespace mg {
+
 // Energy only, for one CTA (the batched path's line-search trials): each
 // unordered pair once, 32x32 tile pairs (I <= J) dealt to the warps in turn
 // -- no forces, so no rounds and no barriers, and every warp gets the same

@@ -32,7 +32,7 @@ EXPORTS = [
     "minim_gpu_server_poll", "minim_gpu_server_take", "minim_gpu_server_cancel",
     "minim_gpu_server_destroy", "minim_gpu_bah_elements", "minim_gpu_bah_colouring",
     "minim_gpu_pf_setup", "minim_gpu_lj_minimise_noalloc", "minim_gpu_instance_bah_arrays",
-    "minim_gpu_eval_kernel", "minim_gpu_tune_table", "minim_gpu_wait_probe",
+    "minim_gpu_eval_kernel", "minim_gpu_tune_table", "minim_gpu_wait_probe", "minim_gpu_lj_cutoff_pairs",
 ]
 
 
@@ -87,6 +87,7 @@ def load(path=LIB_PATH):
                                           C.c_int),
         "minim_gpu_tune_table": ([C.c_int, _ip, _dp, _ip], C.c_int),
         "minim_gpu_wait_probe": ([C.c_int, _ip, _dp], C.c_int),
+        "minim_gpu_lj_cutoff_pairs": ([P, _dp, C.c_int, _ip, _ip], C.c_int),
         "minim_gpu_eval_kernel": ([P, C.c_int, _dp, _dp, C.c_double, _dp, _dp, _dp], C.c_int),
         "minim_gpu_lj_minimise_noalloc": ([P, C.c_void_p, C.c_size_t, C.POINTER(abi.MinimiserParams),
                                            C.POINTER(abi.Result), C.c_void_p], C.c_int),
@@ -242,6 +243,18 @@ class Instance:
         else:
             out = (e[0], g)
         return out + ((xt.reshape(2, self.ndof),) if points else ())
+
+    def cutoff_pairs(self, x):
+        """The pairs (i < j, sorted) that the FP32 stage of this Lennard-Jones
+        instance with a cutoff evaluates at x (rounded to FP32)."""
+        xv = _vec(x)
+        n = C.c_int()
+        _check(_lib.minim_gpu_lj_cutoff_pairs(self.h, xv.ctypes.data_as(_dp), 0, None, C.byref(n)))
+        cap = max(n.value, 1)
+        out = np.zeros(2 * cap, np.int32)
+        _check(_lib.minim_gpu_lj_cutoff_pairs(self.h, xv.ctypes.data_as(_dp), cap, out.ctypes.data_as(_ip),
+                                              C.byref(n)))
+        return out[:2 * n.value].reshape(-1, 2)
 
     def apply_constraints(self, v):
         a = _vec(v).copy()

@@ -89,6 +89,7 @@ struct oracle_inst {
   /* LJ */
   int ndim;
   double sigma, eps;
+  double rc2;  /* cutoff squared (0: every pair) */
   pf_t pf;
   bah_t bah;
   long evals;
@@ -102,7 +103,9 @@ double oracle_default_tol(const oracle_inst* o) { return o->tol_default; }
 /* ------------------------------------------------------------------------ */
 /* LjNd: src/potentials/LjNd.cpp:12-53                                       */
 /* ------------------------------------------------------------------------ */
-/* One element per pair i<j in (i, j) order (LjNd::init, lines 17-25). */
+/* One element per pair i<j in (i, j) order (LjNd::init, lines 17-25).  With
+   a cutoff (an extension: the reference has none) a pair with r2 >= rc2 is
+   left out, r2 summed over the dimensions in order, one rounding each. */
 static void lj_eg(const oracle_inst* o, const double* x, double* e, double* g) {
   int nd = o->ndim;
   int np = (int)(o->ndof / nd);
@@ -113,6 +116,7 @@ static void lj_eg(const oracle_inst* o, const double* x, double* e, double* g) {
       double r2 = 0;
       for (int d = 0; d < nd; d++) dx[d] = x[nd * i + d] - x[nd * j + d];
       for (int d = 0; d < nd; d++) r2 += dx[d] * dx[d];
+      if (o->rc2 > 0 && r2 >= o->rc2) continue;
       double lj6 = s6 / pow(r2, 3);
       double lj12 = lj6 * lj6;
       if (e) *e += 4 * o->eps * (lj12 - lj6);
@@ -1508,6 +1512,7 @@ int oracle_create(int kind, const void* params, const double* x0, size_t ndof,
     o->ndim = q->ndim;
     o->sigma = q->sigma;
     o->eps = q->epsilon;
+    o->rc2 = q->cutoff > 0 ? q->cutoff * q->cutoff : 0.0;
     if (q->ndim < 1 || q->ndim > 3 || ndof % q->ndim)
       rc = set_err(MINIM_GPU_ERR_INVALID, "LjNd: Length of coords must be a multiple of the number of dimensions.");
   } else if (kind == MINIM_GPU_PF || kind == MINIM_GPU_PFU) {

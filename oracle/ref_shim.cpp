@@ -49,6 +49,7 @@ std::unique_ptr<State> build(int kind, const void* params, const double* x0, siz
   vector<int> fix = vec_of(fixed, nfixed);
   if (kind == MINIM_GPU_LJ) {
     auto p = static_cast<const minim_gpu_lj_params*>(params);
+    if (p->cutoff != 0) throw std::invalid_argument("the reference LjNd has no cutoff");
     LjNd pot(p->ndim, p->sigma, p->epsilon);
     if (!fix.empty()) pot.setConstraints(fix);
     return std::make_unique<State>(pot, x);

@@ -133,6 +133,22 @@ static void host_tests() {
 }
 
 static void device_tests() {
+  {  // LjNd::setCutoff (no counterpart in the reference): a pair at r = 2
+     // counts in full, a pair at r = 3 not at all
+    Lj3d pot;
+    pot.setCutoff(2.5);
+    State near_ = pot.newState({0, 0, 0, 2, 0, 0});
+    CHECK(feq(near_.energy(), -63. / 1024));
+    State far_ = pot.newState({0, 0, 0, 3, 0, 0});
+    CHECK(far_.energy() == 0);
+    bool threw = false;
+    try {
+      Lj3d().setCutoff(-1);
+    } catch (const std::invalid_argument&) {
+      threw = true;
+    }
+    CHECK(threw);
+  }
   {  // a device minimisation that produces non-finite values reports the
      // reference's failure flag; a clean one does not
     Lj3d pot;
