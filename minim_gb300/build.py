@@ -48,6 +48,9 @@ def _run(cmd):
 def build(verbose=False, force=False):
     os.makedirs(BUILD, exist_ok=True)
     inc = ["-I" + os.path.join(REPO, "include"), "-I" + CSRC]
+    # MINIM_GPU_LJ_MINB: minimum resident blocks per SM of the Lennard-Jones
+    # batch kernel (its register budget); rebuild with force=True to change it
+    defs = ["-DMG_LJ_MINB=" + os.environ["MINIM_GPU_LJ_MINB"]] if os.environ.get("MINIM_GPU_LJ_MINB") else []
     jobs = []
     objs = []
     for f in CU:
@@ -56,7 +59,7 @@ def build(verbose=False, force=False):
         objs.append(obj)
         if force or _stale(obj, [src] + _deps()):
             jobs.append([NVCC] + ARCH + ["-O3", "-lineinfo", "-std=c++20", "-Xcompiler", "-fPIC",
-                                         "-Xptxas", "-v"] + inc + ["-c", src, "-o", obj])
+                                         "-Xptxas", "-v"] + defs + inc + ["-c", src, "-o", obj])
     for f in CPP:
         src = os.path.join(CSRC, f)
         obj = os.path.join(BUILD, f + ".o")

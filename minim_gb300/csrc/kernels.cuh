@@ -50,9 +50,13 @@ __device__ void setup_runner(Runner<Team, KIND>& R, SS& S, const InstDesc& in) {
 }
 
 // The grid-sized kinds run 512-thread blocks (one per SM at 128 registers a
-// thread); Lennard-Jones keeps up to 256 threads and two or more blocks per SM.
+// thread); Lennard-Jones keeps up to 256 threads and MG_LJ_MINB or more
+// blocks per SM (the register budget of its FP32 pair loops).
+#ifndef MG_LJ_MINB
+#define MG_LJ_MINB 2
+#endif
 template <int KIND>
-__global__ void __launch_bounds__(KIND == K_LJ ? 256 : 512, KIND == K_LJ ? 2 : 1)
+__global__ void __launch_bounds__(KIND == K_LJ ? 256 : 512, KIND == K_LJ ? MG_LJ_MINB : 1)
 batch_kernel(const InstDesc* __restrict__ insts, int ninst, int* counter, int slice, int lj_tile) {
   __shared__ SharedScalars<KIND == K_LJ ? 8 : 16> S;
   __shared__ __align__(16) InstDesc s_in;
