@@ -18,7 +18,10 @@
 //     instead of being recomputed at the start of each line search;
 //   * the L-BFGS direction uses the compact representation (same direction);
 //   * precision MIXED runs FP32 coordinates while FP32 can make progress,
-//     FP64 coordinates near convergence; the final convergence test is FP64.
+//     FP64 coordinates near convergence; the final convergence test is on
+//     FP64 coordinates (the gradient from the FP64 stage's arithmetic:
+//     double-float for Lennard-Jones pairs, general PhaseField and
+//     BarAndHinge; each component stored in FP32).
 // Vector passes move 4 floats per access (float4): every FP32 vector starts
 // on a 16-byte boundary (history buffers are strided by a multiple of 64).
 #pragma once
