@@ -432,12 +432,19 @@ def run_mixed(args):
     conv = sum(r.status == abi.RES_CONVERGED for r in res)
     kinds = {}
     for (kind, p, x0, _), r in zip(items, res):
-        k = kinds.setdefault(kind, {"instances": 0, "converged": 0, "maxiter": 0, "dof": 0, "iterations": 0})
+        k = kinds.setdefault(kind, {"instances": 0, "converged": 0, "maxiter": 0, "dof": 0, "iterations": 0,
+                                    "run_ms": []})
         k["instances"] += 1
         k["converged"] += r.status == abi.RES_CONVERGED
         k["maxiter"] += r.status == abi.RES_MAXITER
         k["dof"] += int(np.size(x0))
         k["iterations"] += r.iter
+        k["run_ms"].append(r.run_ms)
+    for k in kinds.values():
+        # each instance's device time on its SM: the batch's makespan is at
+        # least the longest of them
+        t = np.array(k.pop("run_ms"))
+        k["run_ms_p50_p99_max"] = [float(np.percentile(t, 50)), float(np.percentile(t, 99)), float(t.max())]
     desc = (f"{n_grids} 2-D ternary PhaseField grids (" + ("64^2-512^2" if full else "64^2/128^2") +
             f", fixed volume) + {n_sheets} BarAndHinge sheets (" + ("1k-100k" if full else "1k-4.2k") +
             " vertices), Lbfgs RMS<1e-7")
@@ -745,7 +752,8 @@ def run_profile_lj(iters):
     b.run(threads=256)
     st = runtime.last_run_stats()
     print(json.dumps({"profile_case": "304 LJ clusters N=300 Fire(0.1) fp32", "iterations": st["iterations"],
-                      "kernel_ms": st["kernel_ms"], "launches": st["launches"]}))
+                      "kernel_ms": st["kernel_ms"], "launches": st["launches"],
+                      "phase_ms_summed_over_instances": st["phase_ms"]}))
 
 
 def main():

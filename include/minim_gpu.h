@@ -173,6 +173,8 @@ typedef struct {
   double rms;           /* sqrt(g.g/ndof) at the returned coordinates (Anneal: 0, no gradient) */
   double dt_max;        /* Fire: the dtMax used (estimated when 0 was passed) */
   double latency_ms;    /* serving: submit -> completion wall time */
+  double run_ms;        /* batches and serving: device time from the first slice's start to the
+                           last slice's end of this instance (0 for single-instance calls) */
 } minim_gpu_result;
 
 /* Measurement of the last minimise / batch call, taken by the library on the

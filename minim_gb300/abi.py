@@ -80,7 +80,7 @@ class Result(C.Structure):
     _fields_ = [
         ("status", C.c_int), ("iter", C.c_int), ("fp64_iters", C.c_int), ("evals", C.c_int),
         ("energy", C.c_double), ("rms", C.c_double), ("dt_max", C.c_double),
-        ("latency_ms", C.c_double),
+        ("latency_ms", C.c_double), ("run_ms", C.c_double),
     ]
 
     def as_dict(self):

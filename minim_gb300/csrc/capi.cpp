@@ -298,6 +298,7 @@ void fill_result(minim_gpu_result* r, const MinScalars& s, size_t n) {
   r->energy = s.E;
   r->rms = std::sqrt(s.gg / (double)n);
   r->dt_max = s.dtmax;
+  r->run_ms = (s.t_last > s.t_first && s.t_first) ? (double)(s.t_last - s.t_first) * 1e-6 : 0.0;
 }
 
 }  // namespace

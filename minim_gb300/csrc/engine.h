@@ -154,6 +154,9 @@ struct MinScalars {
   // device time (ns, block 0) in gradient evaluations, line-search trial
   // evaluations and L-BFGS direction passes
   double tphase[3];
+  // batch kernels: %globaltimer when a CTA first took the instance and when
+  // one last stored it (ns)
+  unsigned long long t_first, t_last;
 };
 
 // K_PF1 is the kernel variant for a binary PhaseField with none of the

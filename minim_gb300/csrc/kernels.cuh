@@ -68,12 +68,14 @@ batch_kernel(const InstDesc* __restrict__ insts, int ninst, int* counter, int sl
     if (k >= ninst) break;
     copy_desc(&s_in, &insts[k]);
     __syncthreads();
+    if (threadIdx.x == 0 && s_in.st->t_first == 0) s_in.st->t_first = globaltimer_ns();
     CtaTeam tm{S.red, S.wide};
     Runner<CtaTeam, KIND> R{tm, s_in, dyn, lj_tile};
     setup_runner(R, S, s_in);
     R.load(*s_in.st);
     R.run(slice);
     R.store(*s_in.st);
+    if (threadIdx.x == 0) s_in.st->t_last = globaltimer_ns();
   }
 }
 
