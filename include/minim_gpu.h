@@ -243,20 +243,28 @@ int minim_gpu_minimise(minim_gpu_handle h, const minim_gpu_minimiser_params* mp,
 int minim_gpu_batch_create(minim_gpu_batch* out);
 int minim_gpu_batch_add(minim_gpu_batch b, minim_gpu_handle h,
                         const minim_gpu_minimiser_params* mp);
-/* threads_per_cta > 0 runs every instance with that many threads per CTA;
- * 0 = autotuned: each instance's shape depends only on its own potential
- * kind, size bucket, method and precision (never on the rest of the batch),
- * chosen the first time that key is seen in the process by timing every
- * candidate on a short slice of copies of the batch's instances of that key
+/* threads_per_cta > 0 runs every instance on one CTA of that many threads;
+ * 0 = autotuned: each instance's launch shape -- threads per CTA and CTAs per
+ * instance (one CTA, or a thread-block cluster of 2, 4 or 8 CTAs on as many
+ * SMs for large instances) -- depends only on its own potential kind, size
+ * bucket, method and precision (never on the rest of the batch), chosen the
+ * first time that key is seen in the process by timing every candidate on a
+ * short slice of copies of the batch's instances of that key
  * (MINIM_GPU_TUNE=0: a fixed size rule instead; MINIM_GPU_TUNE_CACHE=file
  * keeps the choices across processes).  results has one entry per added
  * instance. */
 int minim_gpu_batch_run(minim_gpu_batch b, int threads_per_cta, minim_gpu_result* results);
+/* As minim_gpu_batch_run with one launch shape for every instance:
+ * threads_per_cta (32 .. 512, a multiple of 32; Lennard-Jones at most 256)
+ * and ctas CTAs per instance (1 .. 8; more than 1 runs each instance on a
+ * thread-block cluster of that many CTAs). */
+int minim_gpu_batch_run_shape(minim_gpu_batch b, int threads_per_cta, int ctas, minim_gpu_result* results);
 /* The autotuner's choices so far (no counterpart in the reference): up to
- * cap rows of 7 ints {potential kind (MINIM_GPU_*), size bucket, method,
- * precision, threads per CTA, measured (1) or read from the cache file (0),
- * candidates timed}, and per row up to 4 measured slice times in ms
- * (ms may be NULL).  *n receives the number of rows. */
+ * cap rows of 8 ints {potential kind (MINIM_GPU_*), size bucket, method,
+ * precision, threads per CTA, CTAs per instance, measured (1) or read from
+ * the cache file (0), candidates timed}, and per row 8 doubles: the measured
+ * slice time of each candidate in ms (ms may be NULL).  *n receives the
+ * number of rows. */
 int minim_gpu_tune_table(int cap, int* rows, double* ms, int* n);
 int minim_gpu_batch_destroy(minim_gpu_batch b);
 

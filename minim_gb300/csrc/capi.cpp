@@ -119,15 +119,23 @@ struct Kern {
   int (*grid)(const InstDesc*, int, const EvalIO*, int, GridSyncState*, double*, int, int, size_t, void*);
   int (*occ)(int, int, size_t, int*);
   int (*cta_eval)(const InstDesc*, const EvalIO*, int, size_t, void*);
+  int (*cbatch)(const InstDesc*, int, int*, int, int, int, int, size_t, void*);
+  int (*cocc)(int, int, size_t, int*);
 };
+#define MG_KERN(N)                                                                              \
+  Kern {                                                                                        \
+    mg_launch_batch_##N, mg_launch_grid_##N, mg_occupancy_##N, mg_launch_cta_eval_##N,          \
+        mg_launch_cbatch_##N, mg_cluster_occupancy_##N                                          \
+  }
 Kern kern(int kk) {
   switch (kk) {
-    case K_LJ: return {mg_launch_batch_lj, mg_launch_grid_lj, mg_occupancy_lj, mg_launch_cta_eval_lj};
-    case K_PF: return {mg_launch_batch_pf, mg_launch_grid_pf, mg_occupancy_pf, mg_launch_cta_eval_pf};
-    case K_BAH: return {mg_launch_batch_bah, mg_launch_grid_bah, mg_occupancy_bah, mg_launch_cta_eval_bah};
-    default: return {mg_launch_batch_pf1, mg_launch_grid_pf1, mg_occupancy_pf1, mg_launch_cta_eval_pf1};
+    case K_LJ: return MG_KERN(lj);
+    case K_PF: return MG_KERN(pf);
+    case K_BAH: return MG_KERN(bah);
+    default: return MG_KERN(pf1);
   }
 }
+#undef MG_KERN
 const size_t kLjTileBytes = 1024 * 32;  // 1024 particles of 4 doubles
 size_t pot_smem(int kk) { return kk == K_LJ ? kLjTileBytes : 0; }
 // Grid launches of the grid-sized potentials can stream the minimiser's
@@ -843,18 +851,37 @@ int size_bucket(int kk, const InstDesc& d) {
   return b;
 }
 
+// A batch launch shape: threads per CTA and CTAs per instance (a
+// thread-block cluster of that many CTAs, on as many SMs; 1 = one CTA).
+struct Shape {
+  int threads, csize;
+  bool operator==(const Shape& o) const { return threads == o.threads && csize == o.csize; }
+};
+
 // The size rule: Lennard-Jones 64 / 128 / 256 threads by cluster size; the
 // grid-sized kinds 512 (one CTA per SM at 128 registers a thread: sixteen
-// warps to hide the stencil's and the element gathers' latency).
-int rule_threads(int kk, const InstDesc& d) {
-  if (kk == K_LJ) return d.lj.np <= 96 ? 64 : (d.lj.np <= 192 ? 128 : 256);
-  return 512;
+// warps to hide the stencil's and the element gathers' latency); one CTA
+// per instance.
+Shape rule_shape(int kk, const InstDesc& d) {
+  if (kk == K_LJ) return {d.lj.np <= 96 ? 64 : (d.lj.np <= 192 ? 128 : 256), 1};
+  return {512, 1};
 }
+int rule_threads(int kk, const InstDesc& d) { return rule_shape(kk, d).threads; }
 
-std::vector<int> thread_candidates(int kk) {
-  if (kk == K_LJ) return {64, 128, 256};
-  return {256, 512};
+// Candidates of a key: one CTA per instance with each thread count, and for
+// large instances (Lennard-Jones above 512 particles, grid-sized kinds above
+// 16k degrees of freedom) clusters of 2, 4 and 8 CTAs.
+std::vector<Shape> shape_candidates(int kk, int bucket) {
+  if (kk == K_LJ) {
+    std::vector<Shape> c = {{64, 1}, {128, 1}, {256, 1}};
+    if (bucket >= 8) c.insert(c.end(), {{256, 2}, {256, 4}, {256, 8}});
+    return c;
+  }
+  std::vector<Shape> c = {{256, 1}, {512, 1}};
+  if (bucket >= 2) c.insert(c.end(), {{512, 2}, {512, 4}, {512, 8}});
+  return c;
 }
+constexpr int kMaxCand = 8;
 
 struct TuneKey {
   int kk, bucket, method, prec;
@@ -864,8 +891,8 @@ struct TuneKey {
 };
 struct TuneEntry {
   TuneKey key;
-  int threads;
-  double ms[4];  // measured time per candidate (0: not measured)
+  Shape shape;
+  double ms[kMaxCand];  // measured time per candidate (0: not measured)
   int from_file;
 };
 std::vector<TuneEntry> g_tune;
@@ -897,11 +924,11 @@ void tune_load() {
   const std::string tag = tune_device_tag();
   char dev_tag[256];
   TuneEntry e{};
-  while (std::fscanf(f, "%255s %d %d %d %d %d", dev_tag, &e.key.kk, &e.key.bucket, &e.key.method, &e.key.prec,
-                     &e.threads) == 6) {
+  while (std::fscanf(f, "%255s %d %d %d %d %d %d", dev_tag, &e.key.kk, &e.key.bucket, &e.key.method,
+                     &e.key.prec, &e.shape.threads, &e.shape.csize) == 7) {
     if (tag != dev_tag) continue;
     bool ok = false;
-    for (int c : thread_candidates(e.key.kk)) ok |= c == e.threads;
+    for (const Shape& c : shape_candidates(e.key.kk, e.key.bucket)) ok |= c == e.shape;
     if (!ok) continue;
     e.from_file = 1;
     g_tune.push_back(e);
@@ -914,8 +941,8 @@ void tune_save(const TuneEntry& e) {
   if (!fn || !*fn) return;
   FILE* f = std::fopen(fn, "a");
   if (!f) return;
-  std::fprintf(f, "%s %d %d %d %d %d\n", tune_device_tag().c_str(), e.key.kk, e.key.bucket, e.key.method,
-               e.key.prec, e.threads);
+  std::fprintf(f, "%s %d %d %d %d %d %d\n", tune_device_tag().c_str(), e.key.kk, e.key.bucket, e.key.method,
+               e.key.prec, e.shape.threads, e.shape.csize);
   std::fclose(f);
 }
 
@@ -928,6 +955,35 @@ const TuneEntry* tune_find(const TuneKey& k) {
   for (auto& e : g_tune)
     if (e.key == k) return &e;
   return nullptr;
+}
+
+// Resident blocks (csize 1) or clusters (csize > 1) of a shape, 0 when it
+// does not fit.
+int shape_slots(int kk, const Shape& sh) {
+  Dev& D = need_dev();
+  if (sh.csize == 1) {
+    int per_sm = 0;
+    CK((cudaError_t)kern(kk).occ(0, sh.threads, pot_smem(kk), &per_sm));
+    return per_sm * D.nsm;
+  }
+  int clusters = 0;
+  const cudaError_t e = (cudaError_t)kern(kk).cocc(sh.threads, sh.csize, pot_smem(kk), &clusters);
+  if (e != cudaSuccess) {
+    cudaGetLastError();  // a cluster shape the device cannot hold: not a candidate
+    return 0;
+  }
+  return clusters;
+}
+
+// One batch launch of instances [d_insts, +ninst) with a shape on a stream.
+void launch_shape(int kk, const Shape& sh, const InstDesc* d_insts, int ninst, int* counter, int slice, int slots,
+                  cudaStream_t s) {
+  const int n = std::min(ninst, slots);
+  if (sh.csize == 1)
+    CK((cudaError_t)kern(kk).batch(d_insts, ninst, counter, slice, sh.threads, n, pot_smem(kk), s));
+  else
+    CK((cudaError_t)kern(kk).cbatch(d_insts, ninst, counter, slice, sh.threads, sh.csize, n, pot_smem(kk), s));
+  g_launches++;
 }
 
 // Times every candidate shape on a short slice of the given fresh
@@ -965,20 +1021,17 @@ void tune_measure(const TuneKey& key, const std::vector<InstDesc>& sample) {
   TuneEntry ent{};
   ent.key = key;
   double best = 1e300;
-  const std::vector<int> cand = thread_candidates(key.kk);
-  for (size_t c = 0; c < cand.size(); c++) {
-    int per_sm = 0;
-    CK((cudaError_t)kern(key.kk).occ(0, cand[c], pot_smem(key.kk), &per_sm));
-    if (per_sm < 1) continue;
-    const int blocks = std::min(ns, D.nsm * per_sm);
+  const std::vector<Shape> cand = shape_candidates(key.kk, key.bucket);
+  for (size_t c = 0; c < cand.size() && c < (size_t)kMaxCand; c++) {
+    const int slots = shape_slots(key.kk, cand[c]);
+    if (slots < 1) continue;
     // two runs of the slice, the second timed (the first loads the kernel)
     float ms = 0;
     for (int rep = 0; rep < 2; rep++) {
       CK(cudaMemcpyAsync(st, fresh.data(), ns * sizeof(MinScalars), cudaMemcpyHostToDevice, D.s));
       CK(cudaMemsetAsync(counter, 0, sizeof(int), D.s));
       CK(cudaEventRecord(e0, D.s));
-      CK((cudaError_t)kern(key.kk).batch(dd, ns, counter, iters, cand[c], blocks, pot_smem(key.kk), D.s));
-      g_launches++;
+      launch_shape(key.kk, cand[c], dd, ns, counter, iters, slots, D.s);
       CK(cudaEventRecord(e1, D.s));
       CK(cudaEventSynchronize(e1));
       CK(cudaEventElapsedTime(&ms, e0, e1));
@@ -987,7 +1040,7 @@ void tune_measure(const TuneKey& key, const std::vector<InstDesc>& sample) {
     ent.ms[c] = ms;
     if (ms < best) {
       best = ms;
-      ent.threads = cand[c];
+      ent.shape = cand[c];
     }
   }
   cudaEventDestroy(e0);
@@ -996,19 +1049,19 @@ void tune_measure(const TuneKey& key, const std::vector<InstDesc>& sample) {
   dfree(st);
   dfree(dd);
   dfree(counter);
-  if (ent.threads == 0) throw ApiError{MINIM_GPU_ERR_CUDA, "batch kernel does not fit on an SM"};
+  if (ent.shape.threads == 0) throw ApiError{MINIM_GPU_ERR_CUDA, "batch kernel does not fit on an SM"};
   g_tune.push_back(ent);
   tune_save(ent);
 }
 
-// Threads per CTA of every instance: the caller's override, else the tuned
-// (or, with tuning off, the rule's) shape of its key.  Keys not yet tuned
-// are measured on their fresh instances.
-std::vector<int> batch_threads(const std::vector<InstDesc>& descs, const std::vector<int>& kks,
-                               const std::vector<char>& fresh, int threads) {
+// The launch shape of every instance: the caller's thread count (one CTA per
+// instance), else the tuned (or, with tuning off, the rule's) shape of its
+// key.  Keys not yet tuned are measured on their fresh instances.
+std::vector<Shape> batch_shapes(const std::vector<InstDesc>& descs, const std::vector<int>& kks,
+                                const std::vector<char>& fresh, Shape force) {
   const int n = (int)descs.size();
-  std::vector<int> thr(n, threads);
-  if (threads > 0) return thr;
+  std::vector<Shape> sh(n, force);
+  if (force.threads > 0) return sh;
   const bool tune = tune_enabled();
   if (tune) tune_load();
   std::vector<TuneKey> keys(n);
@@ -1030,31 +1083,32 @@ std::vector<int> batch_threads(const std::vector<InstDesc>& descs, const std::ve
   }
   for (int i = 0; i < n; i++) {
     const TuneEntry* e = tune ? tune_find(keys[i]) : nullptr;
-    thr[i] = e ? e->threads : rule_threads(kks[i], descs[i]);
+    sh[i] = e ? e->shape : rule_shape(kks[i], descs[i]);
   }
-  return thr;
+  return sh;
 }
 
 // Runs the given instances with the batch kernels: one launch per (kernel
-// kind, threads per CTA) group, the groups concurrently on their own
-// streams.  descs[i].st must point into d_st; fresh[i] marks instances not
-// yet started (the autotuner may run trial slices on copies of those).
-// Returns when all launches are done.
+// kind, shape) group, the groups concurrently on their own streams.
+// descs[i].st must point into d_st; fresh[i] marks instances not yet started
+// (the autotuner may run trial slices on copies of those).  Returns when all
+// launches are done.
 void run_batch(std::vector<InstDesc>& descs, const std::vector<int>& kks, MinScalars* d_st,
-               const std::vector<MinScalars>& st_init, int slice, int threads, const std::vector<char>& fresh) {
+               const std::vector<MinScalars>& st_init, int slice, Shape force, const std::vector<char>& fresh) {
   Dev& D = need_dev();
   const int n = (int)descs.size();
   if (n == 0) return;
   g_tune_ms = 0;
-  const std::vector<int> thr = batch_threads(descs, kks, fresh, threads);
+  const std::vector<Shape> shp = batch_shapes(descs, kks, fresh, force);
   if (!st_init.empty())
     CK(cudaMemcpyAsync(d_st, st_init.data(), n * sizeof(MinScalars), cudaMemcpyHostToDevice, D.s));
-  // group by kernel kind and threads, largest first within a group (LPT)
+  // group by kernel kind and shape, largest first within a group (LPT)
   std::vector<int> order(n);
   for (int i = 0; i < n; i++) order[i] = i;
   std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
     if (kks[a] != kks[b]) return kks[a] < kks[b];
-    if (thr[a] != thr[b]) return thr[a] < thr[b];
+    if (shp[a].csize != shp[b].csize) return shp[a].csize > shp[b].csize;
+    if (shp[a].threads != shp[b].threads) return shp[a].threads < shp[b].threads;
     return cost_of(descs[a], kks[a]) > cost_of(descs[b], kks[b]);
   });
   std::vector<InstDesc> sorted(n);
@@ -1064,19 +1118,18 @@ void run_batch(std::vector<InstDesc>& descs, const std::vector<int>& kks, MinSca
   // another kernel runs waits for it (lazy module loading), which would
   // serialise the groups' launches.
   struct Launch {
-    int kk, i0, i1, thr, blocks;
-    size_t smem;
+    int kk, i0, i1, slots;
+    Shape sh;
   };
   std::vector<Launch> launches;
   for (int i0 = 0; i0 < n;) {
-    const int kk = kks[order[i0]], t = thr[order[i0]];
+    const int kk = kks[order[i0]];
+    const Shape sh = shp[order[i0]];
     int i1 = i0;
-    while (i1 < n && kks[order[i1]] == kk && thr[order[i1]] == t) i1++;
-    const size_t smem = pot_smem(kk);
-    int per_sm = 0;
-    CK((cudaError_t)kern(kk).occ(0, t, smem, &per_sm));
-    if (per_sm < 1) throw ApiError{MINIM_GPU_ERR_CUDA, "batch kernel does not fit on an SM"};
-    launches.push_back({kk, i0, i1, t, std::min(i1 - i0, D.nsm * per_sm), smem});
+    while (i1 < n && kks[order[i1]] == kk && shp[order[i1]] == sh) i1++;
+    const int slots = shape_slots(kk, sh);
+    if (slots < 1) throw ApiError{MINIM_GPU_ERR_CUDA, "batch kernel does not fit on an SM"};
+    launches.push_back({kk, i0, i1, slots, sh});
     i0 = i1;
   }
   InstDesc* d_descs = (InstDesc*)dalloc(n * sizeof(InstDesc));
@@ -1092,9 +1145,7 @@ void run_batch(std::vector<InstDesc>& descs, const std::vector<int>& kks, MinSca
     const Launch& L = launches[g];
     cudaStream_t ks = D.ks[g % 8];
     CK(cudaStreamWaitEvent(ks, ready, 0));
-    CK((cudaError_t)kern(L.kk).batch(d_descs + L.i0, L.i1 - L.i0, d_counters + g, slice, L.thr, L.blocks,
-                                     L.smem, ks));
-    g_launches++;
+    launch_shape(L.kk, L.sh, d_descs + L.i0, L.i1 - L.i0, d_counters + g, slice, L.slots, ks);
     cudaEvent_t ev;
     CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
     CK(cudaEventRecord(ev, ks));
@@ -1315,8 +1366,9 @@ int minim_gpu_batch_add(minim_gpu_batch b, minim_gpu_handle h, const minim_gpu_m
   });
 }
 
-int minim_gpu_batch_run(minim_gpu_batch b, int threads, minim_gpu_result* results) {
-  return guarded([&] {
+namespace {
+void batch_run_shape(minim_gpu_batch b, Shape force, minim_gpu_result* results) {
+  {
     Dev& D = need_dev();
     const int n = (int)b->inst.size();
     if (n == 0) return;
@@ -1344,7 +1396,7 @@ int minim_gpu_batch_run(minim_gpu_batch b, int threads, minim_gpu_result* result
     }
     std::vector<MinScalars> st(n, fresh_scalars());
     const double t0 = now_ms();
-    run_batch(descs, kks, d_st, st, 0x7fffffff, threads, std::vector<char>(n, 1));
+    run_batch(descs, kks, d_st, st, 0x7fffffff, force, std::vector<char>(n, 1));
     CK(cudaMemcpyAsync(st.data(), d_st, n * sizeof(MinScalars), cudaMemcpyDeviceToHost, D.s));
     CK(cudaStreamSynchronize(D.s));
     g_stats.wall_ms = now_ms() - t0;
@@ -1366,8 +1418,9 @@ int minim_gpu_batch_run(minim_gpu_batch b, int threads, minim_gpu_result* result
     dfree(d_st);
     if (results)
       for (int i = 0; i < n; i++) fill_result(&results[i], st[i], b->inst[i]->n);
-  });
+  }
 }
+}  // namespace
 
 int minim_gpu_lj_cutoff_pairs(minim_gpu_handle h, const double* x, int cap, int* pairs, int* npairs) {
   return guarded([&] {
@@ -1446,6 +1499,21 @@ int minim_gpu_wait_probe(int limit_ms, int* timed_out, double* elapsed_ms) {
   });
 }
 
+int minim_gpu_batch_run(minim_gpu_batch b, int threads, minim_gpu_result* results) {
+  return guarded([&] { batch_run_shape(b, Shape{threads, 1}, results); });
+}
+
+int minim_gpu_batch_run_shape(minim_gpu_batch b, int threads_per_cta, int ctas, minim_gpu_result* results) {
+  return guarded([&] {
+    if (threads_per_cta < 32 || threads_per_cta % 32 || threads_per_cta > 512 || ctas < 1 || ctas > 8)
+      throw ApiError{MINIM_GPU_ERR_INVALID, "minim_gpu_batch_run_shape: threads_per_cta 32..512 (a multiple of 32), ctas 1..8"};
+    for (auto* h : b->inst)
+      if (h->kk == K_LJ && threads_per_cta > 256)
+        throw ApiError{MINIM_GPU_ERR_INVALID, "minim_gpu_batch_run_shape: Lennard-Jones takes at most 256 threads per CTA"};
+    batch_run_shape(b, Shape{threads_per_cta, ctas}, results);
+  });
+}
+
 int minim_gpu_tune_table(int cap, int* rows, double* ms, int* n) {
   return guarded([&] {
     const int k = (int)g_tune.size();
@@ -1453,12 +1521,12 @@ int minim_gpu_tune_table(int cap, int* rows, double* ms, int* n) {
     for (int i = 0; i < k && i < cap; i++) {
       const TuneEntry& e = g_tune[i];
       const int kind = e.key.kk == K_LJ ? MINIM_GPU_LJ : (e.key.kk == K_BAH ? MINIM_GPU_BAH : MINIM_GPU_PF);
-      const int cand = (int)thread_candidates(e.key.kk).size();
-      const int row[7] = {kind, e.key.bucket, e.key.method, e.key.prec, e.threads, e.from_file ? 0 : 1,
-                          e.from_file ? 0 : cand};
-      if (rows) std::memcpy(rows + 7 * i, row, sizeof row);
+      const int cand = (int)shape_candidates(e.key.kk, e.key.bucket).size();
+      const int row[8] = {kind, e.key.bucket, e.key.method, e.key.prec, e.shape.threads, e.shape.csize,
+                          e.from_file ? 0 : 1, e.from_file ? 0 : cand};
+      if (rows) std::memcpy(rows + 8 * i, row, sizeof row);
       if (ms)
-        for (int c = 0; c < 4; c++) ms[4 * i + c] = e.ms[c];
+        for (int c = 0; c < kMaxCand; c++) ms[kMaxCand * i + c] = e.ms[c];
     }
   });
 }
@@ -1558,7 +1626,7 @@ int minim_gpu_server_step(minim_gpu_server s, int* n_resident, int* n_queued) {
       fresh.push_back(std::find(admitted.begin(), admitted.end(), k) != admitted.end());
     }
     if (!descs.empty()) {
-      run_batch(descs, kks, s->d_st, {}, s->cfg.slice_iters, s->cfg.threads_per_cta, fresh);
+      run_batch(descs, kks, s->d_st, {}, s->cfg.slice_iters, Shape{s->cfg.threads_per_cta, 1}, fresh);
       std::vector<MinScalars> st(s->cfg.max_slots);
       CK(cudaMemcpyAsync(st.data(), s->d_st, s->cfg.max_slots * sizeof(MinScalars), cudaMemcpyDeviceToHost, D.s));
       CK(cudaStreamSynchronize(D.s));

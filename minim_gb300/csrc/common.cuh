@@ -8,6 +8,7 @@
 // then a fixed-order sum over warps / blocks, all in FP64, and every thread
 // of the team receives bitwise the same result (uniform control flow).
 #pragma once
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -466,6 +467,7 @@ struct CtaTeam {
   double* red;  // shared scratch, >= (32 + 1) * MINIM_MAXRED doubles
   double* wide; // shared scratch, one row of MINIM_WIDE doubles per warp
   static constexpr bool kGrid = false;
+  static constexpr bool kCluster = false;
   __device__ __forceinline__ void sync() { __syncthreads(); }
   __device__ __forceinline__ bool ok() const { return true; }
   __device__ __forceinline__ bool block0() const { return true; }
@@ -624,6 +626,7 @@ struct GridTeam {
   int* s_ok;              // shared flag
   unsigned int epoch;     // barriers passed in this launch (uniform)
   static constexpr bool kGrid = true;
+  static constexpr bool kCluster = false;
   static constexpr unsigned long long kWaitLimitNs = 5000000000ull;  // 5 s
 
   __device__ __forceinline__ bool block0() const { return blockIdx.x == 0; }
@@ -760,6 +763,116 @@ struct GridTeam {
       P[blockIdx.x * MINIM_WIDE + k] = s;
     }
     arrive_release(K, out);
+  }
+};
+
+// ---------------------------------------------------------------------------
+// Team = a thread-block cluster (one instance on several SMs of the batch
+// path).  Barriers are the cluster's hardware barrier (every thread of every
+// CTA, release / acquire at cluster scope); a reduction writes each CTA's
+// totals to its own shared-memory row and every CTA then reads all rows
+// through distributed shared memory in rank order, so every CTA holds
+// bitwise the same totals and takes the same branches.  Rows are
+// double-buffered: a CTA writes a row again only after the next barrier,
+// which every reader of the previous use has passed.
+// ---------------------------------------------------------------------------
+struct ClusterTeam {
+  double* red;   // per-CTA shared scratch as in CtaTeam
+  double* wide;  // per-CTA shared scratch as in CtaTeam
+  double* xch;   // per-CTA shared exchange rows: 2 x MINIM_WIDE doubles
+  int buf;       // exchange row in use
+  static constexpr bool kGrid = true;      // a multi-CTA team: team-generic kernels
+  static constexpr bool kCluster = true;
+  __device__ __forceinline__ int rank() const { return (int)cooperative_groups::this_cluster().block_rank(); }
+  __device__ __forceinline__ int csize() const { return (int)cooperative_groups::this_cluster().num_blocks(); }
+  __device__ __forceinline__ int tid() const { return rank() * blockDim.x + threadIdx.x; }
+  __device__ __forceinline__ int nthr() const { return csize() * blockDim.x; }
+  __device__ __forceinline__ void sync() { cooperative_groups::this_cluster().sync(); }
+  __device__ __forceinline__ bool ok() const { return true; }
+  __device__ __forceinline__ bool block0() const { return rank() == 0; }
+  __device__ __forceinline__ void fail() {}
+
+  // this CTA's K totals are in xch row `buf`: the cluster's totals (rank
+  // order) into out (this CTA's shared memory)
+  __device__ void exchange(int K, double* out) {
+    auto cl = cooperative_groups::this_cluster();
+    cl.sync();
+    const int nc = (int)cl.num_blocks();
+    double* row = xch + buf * MINIM_WIDE;
+    for (int k = threadIdx.x; k < K; k += blockDim.x) {
+      double s = 0.0;
+      for (int r = 0; r < nc; r++) s += cl.map_shared_rank(row, r)[k];
+      out[k] = s;
+    }
+    buf ^= 1;
+    __syncthreads();
+  }
+
+  template <int K>
+  __device__ void reduce(double (&v)[K]) {
+    static_assert(K <= MINIM_MAXRED, "too many values");
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+    for (int k = 0; k < K; k++) v[k] = warp_sum(v[k]);
+    if (lane == 0) {
+#pragma unroll
+      for (int k = 0; k < K; k++) red[w * MINIM_MAXRED + k] = v[k];
+    }
+    __syncthreads();
+    if (threadIdx.x < K) {
+      double s = 0.0;
+      for (int i = 0; i < nw; i++) s += red[i * MINIM_MAXRED + threadIdx.x];
+      xch[buf * MINIM_WIDE + threadIdx.x] = s;
+    }
+    exchange(K, red + 32 * MINIM_MAXRED);
+#pragma unroll
+    for (int k = 0; k < K; k++) v[k] = red[32 * MINIM_MAXRED + k];
+    __syncthreads();
+  }
+
+  // As CtaTeam::reduce_pairs within each CTA, then the CTAs' FP64 totals
+  // summed in rank order; post in thread 0 of every CTA.
+  template <int K, int D = 0, class Post = NoPost>
+  __device__ void reduce_pairs(float (&s)[K], float (&c)[K], double (&out)[K + D], Post post = Post{}) {
+    static_assert(K + D <= MINIM_MAXRED, "too many values");
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    float* rf = reinterpret_cast<float*>(red);
+    double* tot = red + 32 * MINIM_MAXRED;
+#pragma unroll
+    for (int k = 0; k < K; k++) warp_pair_sum(s[k], c[k]);
+    if (lane == 0) {
+#pragma unroll
+      for (int k = 0; k < K; k++) {
+        rf[w * 2 * MINIM_MAXRED + 2 * k] = s[k];
+        rf[w * 2 * MINIM_MAXRED + 2 * k + 1] = c[k];
+      }
+    }
+    __syncthreads();
+    if (threadIdx.x < K) {
+      double t = 0.0;
+      for (int i = 0; i < nw; i++)
+        t += (double)rf[i * 2 * MINIM_MAXRED + 2 * threadIdx.x] + (double)rf[i * 2 * MINIM_MAXRED + 2 * threadIdx.x + 1];
+      xch[buf * MINIM_WIDE + threadIdx.x] = t;
+    }
+    exchange(K, tot);
+    if (threadIdx.x == 0) post(tot);
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < K + D; k++) out[k] = tot[k];
+    __syncthreads();
+  }
+
+  __device__ __forceinline__ void wide_clear() { wide_clear_row(wide); }
+  __device__ __forceinline__ void wide_store32(float (&v)[32], int k0) { wide_store_row(v, k0, wide); }
+  __device__ void wide_combine(int K, double* out) {
+    const int nw = (blockDim.x + 31) >> 5;
+    __syncthreads();
+    for (int k = threadIdx.x; k < K; k += blockDim.x) {
+      double s = 0.0;
+      for (int i = 0; i < nw; i++) s += wide[i * MINIM_WIDE + k];
+      xch[buf * MINIM_WIDE + k] = s;
+    }
+    exchange(K, out);
   }
 };
 

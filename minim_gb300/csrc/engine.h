@@ -234,7 +234,10 @@ extern "C" {
                             int threads, int blocks, size_t smem, void* stream);                 \
   int mg_occupancy_##NAME(int grid, int threads, size_t smem, int* blocks_per_sm);              \
   int mg_launch_cta_eval_##NAME(const mg::InstDesc* d_inst, const mg::EvalIO* d_io, int threads,  \
-                                size_t smem, void* stream);
+                                size_t smem, void* stream);                                    \
+  int mg_launch_cbatch_##NAME(const mg::InstDesc* d_insts, int ninst, int* d_counter, int slice_iters, \
+                              int threads, int csize, int clusters, size_t smem, void* stream);   \
+  int mg_cluster_occupancy_##NAME(int threads, int csize, size_t smem, int* clusters);
 MG_DECLARE_LAUNCHERS(lj)
 MG_DECLARE_LAUNCHERS(pf)
 MG_DECLARE_LAUNCHERS(bah)

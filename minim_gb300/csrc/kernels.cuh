@@ -79,6 +79,42 @@ batch_kernel(const InstDesc* __restrict__ insts, int ninst, int* counter, int sl
   }
 }
 
+// The batch path with one instance per thread-block cluster: the cluster's
+// CTAs (on as many SMs) share the instance's every phase through the cluster
+// team.  Rank 0 pulls instance indices from the counter and the others read
+// the index from its shared memory; every CTA leaves the loop after the same
+// cluster barrier, so no CTA exits while another may still read its shared
+// memory.
+template <int KIND>
+__global__ void __launch_bounds__(KIND == K_LJ ? 256 : 512, 1)
+cluster_batch_kernel(const InstDesc* __restrict__ insts, int ninst, int* counter, int slice, int lj_tile) {
+  __shared__ SharedScalars<KIND == K_LJ ? 8 : 16> S;
+  __shared__ __align__(16) InstDesc s_in;
+  __shared__ double xch[2 * MINIM_WIDE];
+  __shared__ int next;
+  extern __shared__ __align__(16) unsigned char dyn[];
+  auto cl = cooperative_groups::this_cluster();
+  const bool lead = cl.block_rank() == 0;
+  for (;;) {
+    if (lead && threadIdx.x == 0) next = atomicAdd(counter, 1);
+    cl.sync();
+    const int k = *cl.map_shared_rank(&next, 0);
+    // every CTA has read the index before the leader draws the next one
+    cl.sync();
+    if (k >= ninst) break;
+    copy_desc(&s_in, &insts[k]);
+    __syncthreads();
+    if (lead && threadIdx.x == 0 && s_in.st->t_first == 0) s_in.st->t_first = globaltimer_ns();
+    ClusterTeam tm{S.red, S.wide, xch, 0};
+    Runner<ClusterTeam, KIND> R{tm, s_in, dyn, lj_tile};
+    setup_runner(R, S, s_in);
+    R.load(*s_in.st);
+    R.run(slice);
+    R.store(*s_in.st);
+    if (lead && threadIdx.x == 0) s_in.st->t_last = globaltimer_ns();
+  }
+}
+
 template <class Team, int KIND>
 __device__ void eval_op(Runner<Team, KIND>& R, Team& tm, const InstDesc& in, const EvalIO& io) {
   CView<double> cv{io.x, nullptr, 0.0};
@@ -262,6 +298,47 @@ grid_kernel(const InstDesc* __restrict__ inst, int op, const EvalIO* io, int sli
     if (a != cudaSuccess) return (int)a;                                                          \
     mg::cta_eval_kernel<KIND><<<1, threads, smem, (cudaStream_t)stream>>>(d_inst, d_io, tile);    \
     return (int)cudaGetLastError();                                                               \
+  }                                                                                               \
+  /* one instance per cluster of csize CTAs; blocks = clusters * csize */                          \
+  extern "C" int mg_launch_cbatch_##NAME(const mg::InstDesc* d_insts, int ninst, int* d_counter,  \
+                                         int slice_iters, int threads, int csize, int clusters,    \
+                                         size_t smem, void* stream) {                              \
+    const cudaError_t a = cudaFuncSetAttribute((const void*)mg::cluster_batch_kernel<KIND>,       \
+                                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
+    if (a != cudaSuccess) return (int)a;                                                          \
+    cudaLaunchConfig_t cfg = {};                                                                  \
+    cfg.gridDim = dim3(clusters * csize);                                                         \
+    cfg.blockDim = dim3(threads);                                                                 \
+    cfg.dynamicSmemBytes = smem;                                                                  \
+    cfg.stream = (cudaStream_t)stream;                                                            \
+    cudaLaunchAttribute at[1];                                                                    \
+    at[0].id = cudaLaunchAttributeClusterDimension;                                               \
+    at[0].val.clusterDim.x = csize;                                                               \
+    at[0].val.clusterDim.y = 1;                                                                   \
+    at[0].val.clusterDim.z = 1;                                                                   \
+    cfg.attrs = at;                                                                               \
+    cfg.numAttrs = 1;                                                                             \
+    const int tile = (int)(smem / sizeof(mg::D4));                                                \
+    return (int)cudaLaunchKernelEx(&cfg, mg::cluster_batch_kernel<KIND>, d_insts, ninst, d_counter, \
+                                   slice_iters, tile);                                            \
+  }                                                                                               \
+  /* clusters of csize CTAs that can be resident at once */                                      \
+  extern "C" int mg_cluster_occupancy_##NAME(int threads, int csize, size_t smem, int* clusters) { \
+    const cudaError_t a = cudaFuncSetAttribute((const void*)mg::cluster_batch_kernel<KIND>,       \
+                                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
+    if (a != cudaSuccess) return (int)a;                                                          \
+    cudaLaunchConfig_t cfg = {};                                                                  \
+    cfg.gridDim = dim3(csize);                                                                    \
+    cfg.blockDim = dim3(threads);                                                                 \
+    cfg.dynamicSmemBytes = smem;                                                                  \
+    cudaLaunchAttribute at[1];                                                                    \
+    at[0].id = cudaLaunchAttributeClusterDimension;                                               \
+    at[0].val.clusterDim.x = csize;                                                               \
+    at[0].val.clusterDim.y = 1;                                                                   \
+    at[0].val.clusterDim.z = 1;                                                                   \
+    cfg.attrs = at;                                                                               \
+    cfg.numAttrs = 1;                                                                             \
+    return (int)cudaOccupancyMaxActiveClusters(clusters, (const void*)mg::cluster_batch_kernel<KIND>, &cfg); \
   }                                                                                               \
   extern "C" int mg_occupancy_##NAME(int grid, int threads, size_t smem, int* blocks_per_sm) {    \
     if (grid) mg_grid_smem_##NAME(smem);                                                          \

@@ -431,7 +431,7 @@ struct Runner {
   // Chunk length for nv vectors: the largest multiple of 64 floats whose nv
   // rows fit one stage (0 = the passes read global memory directly).
   __device__ int stage_chunk(int nv) const {
-    if constexpr (!Team::kGrid) {
+    if constexpr (!Team::kGrid || Team::kCluster) {
       return 0;
     } else {
       if (in.stage_bytes <= 0) return 0;

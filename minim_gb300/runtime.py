@@ -32,7 +32,7 @@ EXPORTS = [
     "minim_gpu_server_poll", "minim_gpu_server_take", "minim_gpu_server_cancel",
     "minim_gpu_server_destroy", "minim_gpu_bah_elements", "minim_gpu_bah_colouring",
     "minim_gpu_pf_setup", "minim_gpu_lj_minimise_noalloc", "minim_gpu_instance_bah_arrays",
-    "minim_gpu_eval_kernel", "minim_gpu_tune_table", "minim_gpu_wait_probe", "minim_gpu_lj_cutoff_pairs",
+    "minim_gpu_eval_kernel", "minim_gpu_tune_table", "minim_gpu_batch_run_shape", "minim_gpu_wait_probe", "minim_gpu_lj_cutoff_pairs",
 ]
 
 
@@ -69,6 +69,7 @@ def load(path=LIB_PATH):
         "minim_gpu_batch_create": ([C.POINTER(P)], C.c_int),
         "minim_gpu_batch_add": ([P, P, C.POINTER(abi.MinimiserParams)], C.c_int),
         "minim_gpu_batch_run": ([P, C.c_int, C.POINTER(abi.Result)], C.c_int),
+        "minim_gpu_batch_run_shape": ([P, C.c_int, C.c_int, C.POINTER(abi.Result)], C.c_int),
         "minim_gpu_batch_destroy": ([P], C.c_int),
         "minim_gpu_server_create": ([C.POINTER(abi.ServerConfig), C.POINTER(P)], C.c_int),
         "minim_gpu_server_submit": ([P, C.c_int, P, _dp, C.c_size_t, C.POINTER(abi.MinimiserParams),
@@ -135,22 +136,22 @@ def wait_probe(limit_ms):
 
 def tune_table():
     """The autotuner's choices so far: one dict per (kind, size bucket,
-    method, precision) key with the chosen threads per CTA and the measured
-    slice time of each candidate (ms)."""
+    method, precision) key with the chosen threads per CTA and CTAs per
+    instance and the measured slice time of each candidate (ms)."""
     lib = load()
     n = C.c_int()
     _check(lib.minim_gpu_tune_table(0, None, None, C.byref(n)))
     k = n.value
-    rows = np.zeros(7 * max(k, 1), np.int32)
-    ms = np.zeros(4 * max(k, 1))
+    rows = np.zeros(8 * max(k, 1), np.int32)
+    ms = np.zeros(8 * max(k, 1))
     _check(lib.minim_gpu_tune_table(k, rows.ctypes.data_as(_ip), ms.ctypes.data_as(_dp), C.byref(n)))
     kinds = {abi.LJ: "lj", abi.PF: "pf", abi.BAH: "bah"}
     out = []
     for i in range(k):
-        r = rows[7 * i:7 * i + 7]
+        r = rows[8 * i:8 * i + 8]
         out.append({"kind": kinds.get(int(r[0]), int(r[0])), "bucket": int(r[1]), "method": int(r[2]),
-                    "precision": int(r[3]), "threads": int(r[4]), "measured": bool(r[5]),
-                    "candidate_ms": [float(v) for v in ms[4 * i:4 * i + int(r[6])]]})
+                    "precision": int(r[3]), "threads": int(r[4]), "ctas": int(r[5]), "measured": bool(r[6]),
+                    "candidate_ms": [float(v) for v in ms[8 * i:8 * i + int(r[7])]]})
     return out
 
 
@@ -305,9 +306,14 @@ class Batch:
         _check(_lib.minim_gpu_batch_add(self.h, inst.h, C.byref(mp)))
         self.items.append((inst, mp))
 
-    def run(self, threads=0):
+    def run(self, threads=0, ctas=0):
+        """Runs the batch: autotuned shapes, or `threads` per CTA (and, with
+        ctas > 0, that many CTAs per instance) for every instance."""
         res = (abi.Result * len(self.items))()
-        _check(_lib.minim_gpu_batch_run(self.h, threads, res))
+        if ctas > 0:
+            _check(_lib.minim_gpu_batch_run_shape(self.h, threads, ctas, res))
+        else:
+            _check(_lib.minim_gpu_batch_run(self.h, threads, res))
         return list(res)
 
     def close(self):
