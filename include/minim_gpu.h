@@ -262,9 +262,12 @@ int minim_gpu_batch_run_shape(minim_gpu_batch b, int threads_per_cta, int ctas, 
 /* The autotuner's choices so far (no counterpart in the reference): up to
  * cap rows of 8 ints {potential kind (MINIM_GPU_*), size bucket, method,
  * precision, threads per CTA, CTAs per instance, measured (1) or read from
- * the cache file (0), candidates timed}, and per row 8 doubles: the measured
- * slice time of each candidate in ms (ms may be NULL).  *n receives the
- * number of rows. */
+ * the cache file (0), times recorded}, and per row 8 doubles: the measured
+ * slice time of each candidate in ms -- one-CTA candidates on the batch's
+ * sample of the key, cluster candidates on its largest instance alone,
+ * followed (when there are cluster candidates) by the chosen one-CTA
+ * shape's time on that instance (ms may be NULL).  *n receives the number
+ * of rows. */
 int minim_gpu_tune_table(int cap, int* rows, double* ms, int* n);
 int minim_gpu_batch_destroy(minim_gpu_batch b);
 

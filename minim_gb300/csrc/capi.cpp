@@ -1020,27 +1020,55 @@ void tune_measure(const TuneKey& key, const std::vector<InstDesc>& sample) {
   CK(cudaEventCreate(&e1));
   TuneEntry ent{};
   ent.key = key;
-  double best = 1e300;
-  const std::vector<Shape> cand = shape_candidates(key.kk, key.bucket);
-  for (size_t c = 0; c < cand.size() && c < (size_t)kMaxCand; c++) {
-    const int slots = shape_slots(key.kk, cand[c]);
-    if (slots < 1) continue;
-    // two runs of the slice, the second timed (the first loads the kernel)
+  // the slice on the first `count` instances of the sample with a shape:
+  // two runs, the second timed (the first loads the kernel)
+  auto time_shape = [&](const Shape& sh, int count) -> float {
+    const int slots = shape_slots(key.kk, sh);
+    if (slots < 1) return -1.f;
     float ms = 0;
     for (int rep = 0; rep < 2; rep++) {
       CK(cudaMemcpyAsync(st, fresh.data(), ns * sizeof(MinScalars), cudaMemcpyHostToDevice, D.s));
       CK(cudaMemsetAsync(counter, 0, sizeof(int), D.s));
       CK(cudaEventRecord(e0, D.s));
-      launch_shape(key.kk, cand[c], dd, ns, counter, iters, slots, D.s);
+      launch_shape(key.kk, sh, dd, count, counter, iters, slots, D.s);
       CK(cudaEventRecord(e1, D.s));
       CK(cudaEventSynchronize(e1));
       CK(cudaEventElapsedTime(&ms, e0, e1));
       g_tune_ms += ms;
     }
+    return ms;
+  };
+  // one CTA per instance: the shape that runs the sample fastest
+  double best = 1e300;
+  const std::vector<Shape> cand = shape_candidates(key.kk, key.bucket);
+  bool clusters = false;
+  for (size_t c = 0; c < cand.size() && c < (size_t)kMaxCand; c++) {
+    if (cand[c].csize > 1) {
+      clusters = true;
+      continue;
+    }
+    const float ms = time_shape(cand[c], ns);
+    if (ms < 0) continue;
     ent.ms[c] = ms;
     if (ms < best) {
       best = ms;
       ent.shape = cand[c];
+    }
+  }
+  // Large instances: a batch's makespan is at least its largest instance's
+  // time on its CTAs, so the cluster shapes are judged by the slice time of
+  // the sample's largest instance alone; the largest cluster whose parallel
+  // efficiency t(1) / (C t(C)) is at least 1/2 is taken.  (The one-CTA
+  // shape's time of that instance is kept after the candidates' times.)
+  if (clusters && ent.shape.threads > 0) {
+    const float t1 = time_shape(ent.shape, 1);
+    if (cand.size() < (size_t)kMaxCand) ent.ms[cand.size()] = t1;
+    for (size_t c = 0; c < cand.size() && c < (size_t)kMaxCand; c++) {
+      if (cand[c].csize == 1) continue;
+      const float tc = time_shape(cand[c], 1);
+      if (tc <= 0) continue;
+      ent.ms[c] = tc;
+      if (t1 > 0 && t1 >= 0.5 * cand[c].csize * tc && cand[c].csize > ent.shape.csize) ent.shape = cand[c];
     }
   }
   cudaEventDestroy(e0);
@@ -1521,7 +1549,12 @@ int minim_gpu_tune_table(int cap, int* rows, double* ms, int* n) {
     for (int i = 0; i < k && i < cap; i++) {
       const TuneEntry& e = g_tune[i];
       const int kind = e.key.kk == K_LJ ? MINIM_GPU_LJ : (e.key.kk == K_BAH ? MINIM_GPU_BAH : MINIM_GPU_PF);
-      const int cand = (int)shape_candidates(e.key.kk, e.key.bucket).size();
+      const std::vector<Shape> cs = shape_candidates(e.key.kk, e.key.bucket);
+      bool cl = false;
+      for (const Shape& c : cs) cl |= c.csize > 1;
+      // with cluster candidates, the one-CTA shape's time of the largest
+      // instance follows the candidates' times
+      const int cand = (int)cs.size() + (cl ? 1 : 0);
       const int row[8] = {kind, e.key.bucket, e.key.method, e.key.prec, e.shape.threads, e.shape.csize,
                           e.from_file ? 0 : 1, e.from_file ? 0 : cand};
       if (rows) std::memcpy(rows + 8 * i, row, sizeof row);

@@ -118,5 +118,11 @@ def test_tuner_times_cluster_candidates():
     rows = [t for t in runtime.tune_table() if t["kind"] == "pf" and t["bucket"] >= 2 and t["measured"]]
     assert rows
     for t in rows:
-        assert len(t["candidate_ms"]) == 5
+        # 256 / 512 threads on one CTA (the sample), clusters of 2 / 4 / 8
+        # (the largest instance alone), and the one-CTA time of that instance
+        ms = t["candidate_ms"]
+        assert len(ms) == 6 and all(v > 0 for v in ms)
         assert t["ctas"] in (1, 2, 4, 8)
+        if t["ctas"] > 1:
+            c = {2: 2, 4: 3, 8: 4}[t["ctas"]]
+            assert ms[5] >= 0.5 * t["ctas"] * ms[c]
