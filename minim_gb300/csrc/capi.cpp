@@ -136,7 +136,10 @@ Kern kern(int kk) {
   }
 }
 #undef MG_KERN
-const size_t kLjTileBytes = 1024 * 32;  // 1024 particles of 4 doubles
+// Lennard-Jones shared memory: 1536 particles of 4 doubles (the tiles of the
+// generic pair loop), or positions and eight warps' force accumulators of
+// up to 416 particles (the dealt FP32 evaluation)
+const size_t kLjTileBytes = 1536 * 32;
 size_t pot_smem(int kk) { return kk == K_LJ ? kLjTileBytes : 0; }
 // Grid launches of the grid-sized potentials can stream the minimiser's
 // vector passes through a ring of kStages shared-memory stages of

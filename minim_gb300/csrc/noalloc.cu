@@ -109,7 +109,7 @@ extern "C" int minim_gpu_lj_minimise_noalloc(const minim_gpu_lj_params* p, doubl
     mg_set_last_error("minim_gpu_lj_minimise_noalloc: the kernels are built for sm_103a");
     return MINIM_GPU_ERR_NO_DEVICE;
   }
-  const int lj_tile = 1024;
+  const int lj_tile = 1536;  // the batch kernels' shared memory (48 KB)
   const size_t smem = (size_t)lj_tile * sizeof(D4);
   unsigned char* base = nullptr;
   {

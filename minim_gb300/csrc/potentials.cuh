@@ -276,6 +276,121 @@ __device__ __noinline__ double lj_energy_sym(CtaTeam& tm, const PotLJ& P, CView<
   return 4.0 * P.eps * e.total();
 }
 
+// FP32 energy and gradient for one CTA without rounds: each unordered pair
+// once, the tile pairs (I <= J) dealt to the warps in turn as in
+// lj_energy_sym, every warp adding its pairs' forces to its own
+// shared-memory accumulators (no two warps write one accumulator, so no
+// barrier between tile pairs and no warp idles while others finish a round),
+// then one fixed-order sum over the warps per particle.  Within a tile pair
+// the j tile's positions and forces rotate through the lanes with shuffles,
+// as in lj_eval_sym.  Shared memory: 32 nt positions (3 floats) and nw x 3 x
+// 32 nt accumulators (lj_dealt_bytes).
+__host__ __device__ __forceinline__ size_t lj_dealt_bytes(int np, int nwarps) {
+  const size_t nt = (size_t)(np + 31) >> 5;
+  return 32 * nt * (3 * sizeof(float)) * (1 + (size_t)nwarps);
+}
+template <class Emit>
+__device__ __noinline__ double lj_eval_dealt(CtaTeam& tm, const PotLJ& P, CView<float> cv, float* xw, Emit* emp,
+                                             bool want_e, void* smem) {
+  Emit emit = *emp;
+  const int N = P.np, nd = P.ndim;
+  const int nt = (N + 31) >> 5, npad = 32 * nt;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  CV3<float>* sx = reinterpret_cast<CV3<float>*>(smem);
+  float* acc = reinterpret_cast<float*>(sx + npad);  // [warp][dim][particle]
+  const float s6 = (float)P.s6;
+  for (int j = threadIdx.x; j < npad; j += blockDim.x) {
+    CV3<float> v;
+    if (j < N) {
+      v.x = cv(nd * j);
+      v.y = cv(nd * j + 1);
+      v.z = (nd == 3) ? cv(nd * j + 2) : 0.f;
+      if (xw) {
+        xw[nd * j] = v.x;
+        xw[nd * j + 1] = v.y;
+        if (nd == 3) xw[nd * j + 2] = v.z;
+      }
+    } else {
+      v.x = (float)(1e6 * (double)(j + 1));
+      v.y = 0.f;
+      v.z = 0.f;
+    }
+    sx[j] = v;
+  }
+  for (int k = threadIdx.x; k < 3 * nw * npad; k += blockDim.x) acc[k] = 0.f;
+  __syncthreads();
+  float* mine = acc + (size_t)w * 3 * npad;
+  LjAcc<float> e;
+  const int npairs = nt * (nt + 1) / 2;
+  for (int p = w; p < npairs; p += nw) {
+    int I = 0, rem = p;
+    while (rem >= nt - I) {
+      rem -= nt - I;
+      I++;
+    }
+    const int J = I + rem;
+    const int i = 32 * I + lane;
+    const CV3<float> a = sx[i];
+    float fx = 0.f, fy = 0.f, fz = 0.f, ee = 0.f;
+    if (I == J) {
+      // each lane with the 31 others of its tile (every pair twice, half the
+      // energy each), force on the own particle only
+#pragma unroll 4
+      for (int s = 1; s < 32; s++) {
+        const CV3<float> b = sx[32 * I + ((lane + s) & 31)];
+        const float dx = a.x - b.x, dy = a.y - b.y, dz = a.z - b.z;
+        float lj6, lj12, f;
+        lj_pair(dx, dy, dz, s6, lj6, lj12, f);
+        fx += dx * f; fy += dy * f; fz += dz * f;
+        ee += lj12 - lj6;
+      }
+      mine[i] += fx; mine[npad + i] += fy; mine[2 * npad + i] += fz;
+      if (want_e && i < N) e.add(0.5f * ee);
+    } else {
+      CV3<float> b = sx[32 * J + lane];
+      float gx = 0.f, gy = 0.f, gz = 0.f;
+      const int src = (lane + 1) & 31;
+#pragma unroll 4
+      for (int s = 0; s < 32; s++) {
+        const CV3<float> bc = b;
+        b.x = __shfl_sync(0xffffffffu, b.x, src);
+        b.y = __shfl_sync(0xffffffffu, b.y, src);
+        b.z = __shfl_sync(0xffffffffu, b.z, src);
+        const float dx = a.x - bc.x, dy = a.y - bc.y, dz = a.z - bc.z;
+        float lj6, lj12, f;
+        lj_pair(dx, dy, dz, s6, lj6, lj12, f);
+        const float ex = dx * f, ey = dy * f, ez = dz * f;
+        fx += ex; fy += ey; fz += ez;
+        gx = __shfl_sync(0xffffffffu, gx - ex, src);
+        gy = __shfl_sync(0xffffffffu, gy - ey, src);
+        gz = __shfl_sync(0xffffffffu, gz - ez, src);
+        ee += lj12 - lj6;
+      }
+      const int j = 32 * J + lane;
+      mine[i] += fx; mine[npad + i] += fy; mine[2 * npad + i] += fz;
+      mine[j] += gx; mine[npad + j] += gy; mine[2 * npad + j] += gz;
+      if (want_e) e.add(ee);
+    }
+  }
+  __syncthreads();
+  const double c = -24.0 * P.eps;
+  for (int i = threadIdx.x; i < N; i += blockDim.x) {
+    float f[3];
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+      float t = 0.f;
+      for (int k = 0; k < nw; k++) t += acc[((size_t)k * 3 + d) * npad + i];
+      f[d] = t;
+    }
+    emit(nd * i, (float)c * f[0]);
+    emit(nd * i + 1, (float)c * f[1]);
+    if (nd == 3) emit(nd * i + 2, (float)c * f[2]);
+  }
+  __syncthreads();
+  *emp = emit;
+  return 4.0 * P.eps * e.total();
+}
+
 // Symmetric all-pairs evaluation for one CTA (the batched path): each
 // unordered pair is computed once.  Particles are grouped in tiles of 32;
 // tile pairs are scheduled round-robin (circle method) so that within a
