@@ -756,6 +756,22 @@ def run_profile_lj(iters):
                       "phase_ms_summed_over_instances": st["phase_ms"]}))
 
 
+def run_profile_cluster(iters):
+    """One 512^2 three-fluid PhaseField grid (hard density, fixed volumes)
+    on a thread-block cluster of 8 CTAs for `iters` L-BFGS iterations in FP32
+    (profiler capture of the cluster batch kernel)."""
+    from minim_gb300 import abi, runtime
+    from tests.workloads import pf_simplex
+    g = (512, 512, 1)
+    inst = runtime.Instance(abi.phase_field(g, nfluid=3, volume_fixed=True), pf_simplex(g, 3, seed=5007))
+    b = runtime.Batch()
+    b.add(inst, abi.minimiser("lbfgs", tol=1e-7, max_iter=iters, precision="fp32"))
+    r = b.run(threads=512, ctas=8)[0]
+    st = runtime.last_run_stats()
+    print(json.dumps({"profile_case": "PhaseField 512^2 three-fluid on a cluster of 8 CTAs", "iter": r.iter,
+                      "kernel_ms": st["kernel_ms"], "abytes": st["abytes"]}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -791,9 +807,14 @@ def main():
     ap.add_argument("--profile-pf", type=int, default=0,
                     help="run one 128^2 three-fluid PhaseField grid for N iterations (profiler capture) and exit")
     ap.add_argument("--profile-prec", default="fp64", help="coordinate precision of --profile-pf")
+    ap.add_argument("--profile-cluster", type=int, default=0,
+                    help="run one 512^2 three-fluid grid on a cluster of 8 CTAs for N iterations and exit")
     args = ap.parse_args()
     if args.profile_pf:
         run_profile_pf(args.profile_pf, args.profile_prec)
+        return
+    if args.profile_cluster:
+        run_profile_cluster(args.profile_cluster)
         return
     if args.profile:
         run_profile_case(args.profile)
