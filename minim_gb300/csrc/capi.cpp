@@ -141,6 +141,14 @@ Kern kern(int kk) {
 // up to 416 particles (the dealt FP32 evaluation)
 const size_t kLjTileBytes = 1536 * 32;
 size_t pot_smem(int kk) { return kk == K_LJ ? kLjTileBytes : 0; }
+// dynamic shared memory of a one-CTA (or cluster) batch launch of these
+// instances with this many threads: the largest need among them
+size_t group_smem(int kk, const InstDesc* d, int n, int threads) {
+  if (kk != K_LJ) return 0;
+  size_t s = 0;
+  for (int i = 0; i < n; i++) s = std::max(s, lj_smem_bytes(d[i].lj.np, threads));
+  return s;
+}
 // Grid launches of the grid-sized potentials can stream the minimiser's
 // vector passes through a ring of kStages shared-memory stages of
 // MINIM_GPU_STAGE_KB kilobytes each (at most 50; 4 x 22.5 KB keeps two
@@ -670,7 +678,7 @@ void do_eval_kernel(minim_gpu_instance_s* h, int path, const double* x, const do
       launch_grid(h, OP_EVAL_STAGE, 0);
     } else {
       const int thr = rule_threads(h->kk, h->d);
-      CK((cudaError_t)kern(h->kk).cta_eval(h->d_desc, h->d_io, thr, pot_smem(h->kk), D.s));
+      CK((cudaError_t)kern(h->kk).cta_eval(h->d_desc, h->d_io, thr, group_smem(h->kk, &h->d, 1, thr), D.s));
       g_launches++;
     }
     CK(cudaMemcpyAsync(&ev[0], h->d_e, sizeof(double), cudaMemcpyDeviceToHost, D.s));
@@ -962,15 +970,15 @@ const TuneEntry* tune_find(const TuneKey& k) {
 
 // Resident blocks (csize 1) or clusters (csize > 1) of a shape, 0 when it
 // does not fit.
-int shape_slots(int kk, const Shape& sh) {
+int shape_slots(int kk, const Shape& sh, size_t smem) {
   Dev& D = need_dev();
   if (sh.csize == 1) {
     int per_sm = 0;
-    CK((cudaError_t)kern(kk).occ(0, sh.threads, pot_smem(kk), &per_sm));
+    CK((cudaError_t)kern(kk).occ(0, sh.threads, smem, &per_sm));
     return per_sm * D.nsm;
   }
   int clusters = 0;
-  const cudaError_t e = (cudaError_t)kern(kk).cocc(sh.threads, sh.csize, pot_smem(kk), &clusters);
+  const cudaError_t e = (cudaError_t)kern(kk).cocc(sh.threads, sh.csize, smem, &clusters);
   if (e != cudaSuccess) {
     cudaGetLastError();  // a cluster shape the device cannot hold: not a candidate
     return 0;
@@ -980,12 +988,12 @@ int shape_slots(int kk, const Shape& sh) {
 
 // One batch launch of instances [d_insts, +ninst) with a shape on a stream.
 void launch_shape(int kk, const Shape& sh, const InstDesc* d_insts, int ninst, int* counter, int slice, int slots,
-                  cudaStream_t s) {
+                  size_t smem, cudaStream_t s) {
   const int n = std::min(ninst, slots);
   if (sh.csize == 1)
-    CK((cudaError_t)kern(kk).batch(d_insts, ninst, counter, slice, sh.threads, n, pot_smem(kk), s));
+    CK((cudaError_t)kern(kk).batch(d_insts, ninst, counter, slice, sh.threads, n, smem, s));
   else
-    CK((cudaError_t)kern(kk).cbatch(d_insts, ninst, counter, slice, sh.threads, sh.csize, n, pot_smem(kk), s));
+    CK((cudaError_t)kern(kk).cbatch(d_insts, ninst, counter, slice, sh.threads, sh.csize, n, smem, s));
   g_launches++;
 }
 
@@ -1026,14 +1034,15 @@ void tune_measure(const TuneKey& key, const std::vector<InstDesc>& sample) {
   // the slice on the first `count` instances of the sample with a shape:
   // two runs, the second timed (the first loads the kernel)
   auto time_shape = [&](const Shape& sh, int count) -> float {
-    const int slots = shape_slots(key.kk, sh);
+    const size_t smem = group_smem(key.kk, sample.data(), count, sh.threads);
+    const int slots = shape_slots(key.kk, sh, smem);
     if (slots < 1) return -1.f;
     float ms = 0;
     for (int rep = 0; rep < 2; rep++) {
       CK(cudaMemcpyAsync(st, fresh.data(), ns * sizeof(MinScalars), cudaMemcpyHostToDevice, D.s));
       CK(cudaMemsetAsync(counter, 0, sizeof(int), D.s));
       CK(cudaEventRecord(e0, D.s));
-      launch_shape(key.kk, sh, dd, count, counter, iters, slots, D.s);
+      launch_shape(key.kk, sh, dd, count, counter, iters, slots, smem, D.s);
       CK(cudaEventRecord(e1, D.s));
       CK(cudaEventSynchronize(e1));
       CK(cudaEventElapsedTime(&ms, e0, e1));
@@ -1151,6 +1160,7 @@ void run_batch(std::vector<InstDesc>& descs, const std::vector<int>& kks, MinSca
   struct Launch {
     int kk, i0, i1, slots;
     Shape sh;
+    size_t smem;
   };
   std::vector<Launch> launches;
   for (int i0 = 0; i0 < n;) {
@@ -1158,9 +1168,10 @@ void run_batch(std::vector<InstDesc>& descs, const std::vector<int>& kks, MinSca
     const Shape sh = shp[order[i0]];
     int i1 = i0;
     while (i1 < n && kks[order[i1]] == kk && shp[order[i1]] == sh) i1++;
-    const int slots = shape_slots(kk, sh);
+    const size_t smem = group_smem(kk, sorted.data() + i0, i1 - i0, sh.threads);
+    const int slots = shape_slots(kk, sh, smem);
     if (slots < 1) throw ApiError{MINIM_GPU_ERR_CUDA, "batch kernel does not fit on an SM"};
-    launches.push_back({kk, i0, i1, slots, sh});
+    launches.push_back({kk, i0, i1, slots, sh, smem});
     i0 = i1;
   }
   InstDesc* d_descs = (InstDesc*)dalloc(n * sizeof(InstDesc));
@@ -1176,7 +1187,7 @@ void run_batch(std::vector<InstDesc>& descs, const std::vector<int>& kks, MinSca
     const Launch& L = launches[g];
     cudaStream_t ks = D.ks[g % 8];
     CK(cudaStreamWaitEvent(ks, ready, 0));
-    launch_shape(L.kk, L.sh, d_descs + L.i0, L.i1 - L.i0, d_counters + g, slice, L.slots, ks);
+    launch_shape(L.kk, L.sh, d_descs + L.i0, L.i1 - L.i0, d_counters + g, slice, L.slots, L.smem, ks);
     cudaEvent_t ev;
     CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
     CK(cudaEventRecord(ev, ks));

@@ -176,11 +176,11 @@ struct Runner {
         // batched path: each pair once, when positions and forces of all
         // particles fit the tile buffer
         const int ntp = ((in.lj.np + 31) >> 5) + (((in.lj.np + 31) >> 5) & 1);
-        const bool fits = (size_t)32 * ntp * 7 * sizeof(T) <= (size_t)lj_tile * sizeof(D4) && (blockDim.x & 31) == 0;
+        const bool fits = (size_t)32 * ntp * 7 * sizeof(T) <= kLjSmemBudget && (blockDim.x & 31) == 0;
         if constexpr (std::is_same_v<T, float>) {
           // FP32: tile pairs dealt to the warps, per-warp force accumulators
           if (want_g && (blockDim.x & 31) == 0 &&
-              lj_dealt_bytes(in.lj.np, blockDim.x >> 5) <= (size_t)lj_tile * sizeof(D4))
+              lj_dealt_bytes(in.lj.np, blockDim.x >> 5) <= kLjSmemBudget)
             return lj_eval_dealt(tm, in.lj, cv, xw, &em, want_e, smem_pot);
         }
         if (fits && want_g) return lj_eval_sym<T>(tm, in.lj, cv, xw, &em, want_e, smem_pot);
