@@ -29,6 +29,46 @@ struct PotLJ {
   int hbits;       // log2 of the hash table's buckets
   int* cells;      // scratch: lj_cell_ints(np, hbits) ints
 };
+#ifdef __CUDACC__
+#define MG_HD __host__ __device__
+#else
+#define MG_HD
+#endif
+// Lennard-Jones shared memory of the one-CTA paths (positions and eight
+// warps' force accumulators of the dealt FP32 evaluation, the symmetric
+// tiles of the double-float and FP32 evaluations)
+MG_HD inline size_t lj_dealt_bytes(int np, int nwarps) {
+  const size_t nt = (size_t)(np + 31) >> 5;
+  return 32 * nt * (3 * sizeof(float)) * (1 + (size_t)nwarps);
+}
+// The one-CTA Lennard-Jones paths are chosen against this fixed shared-
+// memory budget (not the memory a launch gives), so that an instance's path
+// -- and its result -- does not depend on the other instances of its launch;
+// each launch then gives the bytes its instances' paths use
+// (lj_smem_bytes).
+constexpr size_t kLjSmemBudget = 48 * 1024;
+MG_HD inline size_t lj_sym_bytes(int np, size_t elem) {
+  const size_t nt = (size_t)(np + 31) >> 5, ntp = nt + (nt & 1);
+  return 32 * ntp * 7 * elem;
+}
+// shared memory of a one-CTA launch for a cluster of np particles with the
+// given threads: the dealt FP32 gradient, the FP64-stage (double-float) and
+// FP32 symmetric tiles when they fit the budget, and at least 128 tile
+// entries for the generic pair loop (whose result does not depend on its
+// tile length, a multiple of 4)
+MG_HD inline size_t lj_smem_bytes(int np, int threads) {
+  size_t need = 128 * 32;
+  const size_t dealt = lj_dealt_bytes(np, threads >> 5);
+  if (dealt <= kLjSmemBudget && need < dealt) need = dealt;
+  const size_t sd = lj_sym_bytes(np, 8), sf = lj_sym_bytes(np, 4);
+  if (sd <= kLjSmemBudget) {
+    if (need < sd) need = sd;
+  } else if (sf <= kLjSmemBudget && need < sf) {
+    need = sf;
+  }
+  return (need + 127) & ~(size_t)127;
+}
+
 // ints of the cell-list scratch: bucket starts (H + 1), cursors (H), the
 // particles in bucket order (N), each particle's bucket (N), one int of
 // padding, and each particle's 64-bit cell key (2 N)

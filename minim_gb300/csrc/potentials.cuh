@@ -285,37 +285,6 @@ __device__ __noinline__ double lj_energy_sym(CtaTeam& tm, const PotLJ& P, CView<
 // the j tile's positions and forces rotate through the lanes with shuffles,
 // as in lj_eval_sym.  Shared memory: 32 nt positions (3 floats) and nw x 3 x
 // 32 nt accumulators (lj_dealt_bytes).
-__host__ __device__ __forceinline__ size_t lj_dealt_bytes(int np, int nwarps) {
-  const size_t nt = (size_t)(np + 31) >> 5;
-  return 32 * nt * (3 * sizeof(float)) * (1 + (size_t)nwarps);
-}
-// The one-CTA Lennard-Jones paths are chosen against this fixed shared-
-// memory budget (not the memory a launch gives), so that an instance's path
-// -- and its result -- does not depend on the other instances of its launch;
-// each launch then gives the bytes its instances' paths use
-// (lj_smem_bytes).
-constexpr size_t kLjSmemBudget = 48 * 1024;
-__host__ __device__ __forceinline__ size_t lj_sym_bytes(int np, size_t elem) {
-  const size_t nt = (size_t)(np + 31) >> 5, ntp = nt + (nt & 1);
-  return 32 * ntp * 7 * elem;
-}
-// shared memory of a one-CTA launch for a cluster of np particles with the
-// given threads: the dealt FP32 gradient, the FP64-stage (double-float) and
-// FP32 symmetric tiles when they fit the budget, and at least 128 tile
-// entries for the generic pair loop (whose result does not depend on its
-// tile length, a multiple of 4)
-__host__ __device__ __forceinline__ size_t lj_smem_bytes(int np, int threads) {
-  size_t need = 128 * 32;
-  const size_t dealt = lj_dealt_bytes(np, threads >> 5);
-  if (dealt <= kLjSmemBudget && need < dealt) need = dealt;
-  const size_t sd = lj_sym_bytes(np, 8), sf = lj_sym_bytes(np, 4);
-  if (sd <= kLjSmemBudget) {
-    if (need < sd) need = sd;
-  } else if (sf <= kLjSmemBudget && need < sf) {
-    need = sf;
-  }
-  return (need + 127) & ~(size_t)127;
-}
 template <class Emit>
 __device__ __noinline__ double lj_eval_dealt(CtaTeam& tm, const PotLJ& P, CView<float> cv, float* xw, Emit* emp,
                                              bool want_e, void* smem) {
