@@ -39,7 +39,7 @@ struct PotLJ {
 // tiles of the double-float and FP32 evaluations)
 MG_HD inline size_t lj_dealt_bytes(int np, int nwarps) {
   const size_t nt = (size_t)(np + 31) >> 5;
-  return 32 * nt * (3 * sizeof(float)) * (1 + (size_t)nwarps);
+  return 32 * nt * (4 * sizeof(float)) + 32 * nt * (3 * sizeof(float)) * (size_t)nwarps;
 }
 // The one-CTA Lennard-Jones paths are chosen against this fixed shared-
 // memory budget (not the memory a launch gives), so that an instance's path

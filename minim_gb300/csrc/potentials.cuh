@@ -283,7 +283,7 @@ __device__ __noinline__ double lj_energy_sym(CtaTeam& tm, const PotLJ& P, CView<
 // barrier between tile pairs and no warp idles while others finish a round),
 // then one fixed-order sum over the warps per particle.  Within a tile pair
 // the j tile's positions and forces rotate through the lanes with shuffles,
-// as in lj_eval_sym.  Shared memory: 32 nt positions (3 floats) and nw x 3 x
+// as in lj_eval_sym.  Shared memory: 32 nt positions (4 floats) and nw x 3 x
 // 32 nt accumulators (lj_dealt_bytes).
 template <class Emit>
 __device__ __noinline__ double lj_eval_dealt(CtaTeam& tm, const PotLJ& P, CView<float> cv, float* xw, Emit* emp,
@@ -292,11 +292,13 @@ __device__ __noinline__ double lj_eval_dealt(CtaTeam& tm, const PotLJ& P, CView<
   const int N = P.np, nd = P.ndim;
   const int nt = (N + 31) >> 5, npad = 32 * nt;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  CV3<float>* sx = reinterpret_cast<CV3<float>*>(smem);
+  // positions as 16-byte records (one conflict-free vector load per lane)
+  float4* sx = reinterpret_cast<float4*>(smem);
   float* acc = reinterpret_cast<float*>(sx + npad);  // [warp][dim][particle]
   const float s6 = (float)P.s6;
   for (int j = threadIdx.x; j < npad; j += blockDim.x) {
-    CV3<float> v;
+    float4 v;
+    v.w = 0.f;
     if (j < N) {
       v.x = cv(nd * j);
       v.y = cv(nd * j + 1);
@@ -326,14 +328,14 @@ __device__ __noinline__ double lj_eval_dealt(CtaTeam& tm, const PotLJ& P, CView<
     }
     const int J = I + rem;
     const int i = 32 * I + lane;
-    const CV3<float> a = sx[i];
+    const float4 a = sx[i];
     float fx = 0.f, fy = 0.f, fz = 0.f, ee = 0.f;
     if (I == J) {
       // each lane with the 31 others of its tile (every pair twice, half the
       // energy each), force on the own particle only
 #pragma unroll 4
       for (int s = 1; s < 32; s++) {
-        const CV3<float> b = sx[32 * I + ((lane + s) & 31)];
+        const float4 b = sx[32 * I + ((lane + s) & 31)];
         const float dx = a.x - b.x, dy = a.y - b.y, dz = a.z - b.z;
         float lj6, lj12, f;
         lj_pair(dx, dy, dz, s6, lj6, lj12, f);
@@ -343,12 +345,12 @@ __device__ __noinline__ double lj_eval_dealt(CtaTeam& tm, const PotLJ& P, CView<
       mine[i] += fx; mine[npad + i] += fy; mine[2 * npad + i] += fz;
       if (want_e && i < N) e.add(0.5f * ee);
     } else {
-      CV3<float> b = sx[32 * J + lane];
+      float4 b = sx[32 * J + lane];
       float gx = 0.f, gy = 0.f, gz = 0.f;
       const int src = (lane + 1) & 31;
 #pragma unroll 4
       for (int s = 0; s < 32; s++) {
-        const CV3<float> bc = b;
+        const float4 bc = b;
         b.x = __shfl_sync(0xffffffffu, b.x, src);
         b.y = __shfl_sync(0xffffffffu, b.y, src);
         b.z = __shfl_sync(0xffffffffu, b.z, src);
