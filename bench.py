@@ -243,6 +243,21 @@ def run_gpu(args):
     return out
 
 
+def _fp32_peak():
+    """Nominal FP32 rate of this GPU in TFLOP/s: 128 FP32 lanes per SM x 2
+    flops per fused multiply-add x SMs x the maximum SM clock (the measured
+    peaks file's `sm_max_mhz`, else 2070 MHz)."""
+    import torch
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    mhz = 2070.0
+    try:
+        with open(os.path.join(HERE, "MEASURED_PEAKS.json")) as f:
+            mhz = float(json.load(f).get("sm_max_mhz", mhz))
+    except Exception:
+        pass
+    return 128 * 2 * sms * mhz * 1e6 / 1e12
+
+
 def _oracle_lj_job(job):
     """One CPU oracle minimisation of a batched Lennard-Jones instance (run in
     a worker process): (index, status, iterations, energy, seconds)."""
@@ -320,6 +335,8 @@ def run_batched(args):
                     "by_method": by_method, "iterations": st["iterations"],
                     "fp64_iteration_share": st["fp64_iterations"] / max(st["iterations"], 1),
                     "fp32_tflops": flops32 / (st["kernel_ms"] / 1e3) / 1e12,
+                    "fp32_peak_tflops": _fp32_peak(),
+                    "fp32_frac": flops32 / (st["kernel_ms"] / 1e3) / 1e12 / _fp32_peak(),
                     "launch_shapes": [t for t in runtime.tune_table() if t["kind"] == "lj"],
                     "workload": f"{len(items)} LJ clusters N~U{{13..400}}, half Fire(0.1) half Lbfgs(m=5), "
                                 f"RMS<1e-6"},
