@@ -1116,17 +1116,23 @@ __device__ void pf_volume_project_f32(Team& tm, const PotPF& P, float* v) {
     }
   }
   float ps[MINIM_MAXF], pc[MINIM_MAXF];
-  double tot[MINIM_MAXF];
+  double tot[2 * MINIM_MAXF];
 #pragma unroll
   for (int f = 0; f < MINIM_MAXF; f++) {
     ps[f] = part[f].s;
     pc[f] = part[f].c;
   }
-  tm.template reduce_pairs<MINIM_MAXF>(ps, pc, tot);
+  // the components tot / totalVolume2, divided once per team (the FP64
+  // divisions of a uniform value in every thread kept the FP64 pipe busy)
+  const double tv2 = P.total_volume2;
+  tm.template reduce_pairs<MINIM_MAXF, MINIM_MAXF>(ps, pc, tot, [tv2](double* o) {
+#pragma unroll
+    for (int f = 0; f < MINIM_MAXF; f++) o[MINIM_MAXF + f] = o[f] / tv2;
+  });
   float comp[MINIM_MAXF], csum = 0.f;
 #pragma unroll
   for (int f = 0; f < MINIM_MAXF; f++) {
-    comp[f] = (f < nf && !((P.fix_mask >> f) & 1u)) ? (float)(tot[f] / P.total_volume2) : 0.f;
+    comp[f] = (f < nf && !((P.fix_mask >> f) & 1u)) ? (float)tot[MINIM_MAXF + f] : 0.f;
     csum += comp[f];
   }
   for (int iG = tm.tid(); iG < P.ngrid; iG += tm.nthr()) {
