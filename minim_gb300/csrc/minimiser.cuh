@@ -149,8 +149,9 @@ struct Runner {
     double b = xbytes() + (trial ? 4.0 : 0.0) + (want_g ? 4.0 : 0.0);
     if constexpr (KIND == K_LJ) {
       const double np = in.lj.np;
-      // with a cutoff the pairs evaluated are not counted
-      const double pairs = in.lj.rc2 > 0 ? 0.0 : (want_g ? np * (np - 1) : 0.5 * np * (np - 1));
+      // N (N - 1) / 2 pairs per evaluation (with a cutoff the pairs evaluated
+      // are not counted)
+      const double pairs = in.lj.rc2 > 0 ? 0.0 : 0.5 * np * (np - 1);
       if (stage) MG_ACCT(pairs64, pairs);
       else MG_ACCT(pairs32, pairs);
     }
