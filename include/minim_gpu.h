@@ -338,17 +338,20 @@ int minim_gpu_pf_setup(int kind, const minim_gpu_pf_params* q, const double* x0,
  *   MINIM_EVAL_LINES       the line stencil of the stepped L-BFGS graph (binary
  *                          PhaseField without optional terms, nz % 4 == 0): two
  *                          trials in one pass, at t and at t/2
+ *   MINIM_EVAL_LINES_TMA   the same pass with its lines brought into shared
+ *                          memory as tensor-map tiles (nz % 32 == 0, nz <= 256,
+ *                          ny % 4 == 0, ny >= 8); g is required
  * x (ndof) is rounded to FP32 on the FP32 paths; p (ndof, or NULL for the
  * point x itself) is rounded to FP32, as the minimiser's directions are.
  * The FP32 paths form the point as x32 + fl(t32 * p32) (the line stencil as
  * one fused multiply-add), the FP64 paths as x + t * p.  g receives the
  * gradient as the minimiser stores it (FP32 values, constraints applied);
  * g == NULL runs the energy-only evaluation (the line-search trial kernels).
- * For MINIM_EVAL_LINES, e and g (if given) hold two evaluations, at t then at
+ * For the two line-stencil paths, e and g (if given) hold two evaluations, at t then at
  * t/2 (2 and 2 * ndof entries), and xt (optional, 2 * ndof) receives the two
  * points as the stencil formed them; on the other paths xt must be NULL. */
 enum { MINIM_EVAL_FP32_GRID = 0, MINIM_EVAL_FP32_CTA = 1, MINIM_EVAL_FP64S_GRID = 2,
-       MINIM_EVAL_FP64S_CTA = 3, MINIM_EVAL_LINES = 4 };
+       MINIM_EVAL_FP64S_CTA = 3, MINIM_EVAL_LINES = 4, MINIM_EVAL_LINES_TMA = 5 };
 int minim_gpu_eval_kernel(minim_gpu_handle h, int path, const double* x, const double* p, double t,
                           double* e, double* g, double* xt);
 

@@ -23,7 +23,7 @@ LBFGS, FIRE, GD, ANNEAL = 0, 1, 2, 3
 LS_BACKTRACKING, LS_NONE = 0, 1
 PREC_MIXED, PREC_FP64, PREC_FP32 = 0, 1, 2
 # minim_gpu_eval_kernel paths: the kernels of a minimiser stage
-EVAL_FP32_GRID, EVAL_FP32_CTA, EVAL_FP64S_GRID, EVAL_FP64S_CTA, EVAL_LINES = range(5)
+EVAL_FP32_GRID, EVAL_FP32_CTA, EVAL_FP64S_GRID, EVAL_FP64S_CTA, EVAL_LINES, EVAL_LINES_TMA = range(6)
 
 _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int)

@@ -583,14 +583,21 @@ int rule_threads(int kk, const InstDesc& d);
 void do_eval_kernel(minim_gpu_instance_s* h, int path, const double* x, const double* p, double t, double* e,
                     double* g, double* xt) {
   Dev& D = need_dev();
-  if (path < MINIM_EVAL_FP32_GRID || path > MINIM_EVAL_LINES || !x)
+  if (path < MINIM_EVAL_FP32_GRID || path > MINIM_EVAL_LINES_TMA || !x)
     throw ApiError{MINIM_GPU_ERR_INVALID, "minim_gpu_eval_kernel: invalid path or null coordinates"};
-  if (xt && path != MINIM_EVAL_LINES)
+  const bool tma = path == MINIM_EVAL_LINES_TMA;
+  const bool lines = path == MINIM_EVAL_LINES || tma;
+  if (xt && !lines)
     throw ApiError{MINIM_GPU_ERR_INVALID, "minim_gpu_eval_kernel: xt is only returned by the line stencil"};
-  const bool lines = path == MINIM_EVAL_LINES;
   if (lines && h->kk != K_PF1)
     throw ApiError{MINIM_GPU_ERR_INVALID, "minim_gpu_eval_kernel: the line stencil runs binary PhaseField "
                                           "instances without optional terms only"};
+  if (tma && !g) throw ApiError{MINIM_GPU_ERR_INVALID, "minim_gpu_eval_kernel: the TMA line stencil needs g"};
+  if (tma) {
+    const int* n = h->d.pf.n;
+    if (n[2] % 32 || n[2] > 256 || n[1] % 4 || n[1] < 8 || n[0] < 3)
+      throw ApiError{MINIM_GPU_ERR_INVALID, "minim_gpu_eval_kernel: the grid does not take the TMA line stencil"};
+  }
   ensure_grid(h);
   const size_t n = h->n, vb = align256(n * sizeof(float));
   // x32, p32, g32, two scratch vectors, and the line stencil's Xa Ga Ya Xb Gb Yb Go
@@ -625,8 +632,14 @@ void do_eval_kernel(minim_gpu_instance_s* h, int path, const double* x, const do
       double* part = (double*)(buf + nvec * vb);
       int rows = 0;
       const int mode = g ? 3 : 0;
-      CK((cudaError_t)mg_stepped_lines_probe(h->d_desc, h->d.pf.n, mode, x32, p32, Go, (float)t, vec(5), vec(6),
-                                             vec(7), vec(8), vec(9), vec(10), part, max_rows, D.nsm, &rows, D.s));
+      if (tma)
+        CK((cudaError_t)mg_stepped_lines_tma_probe(h->d_desc, h->d.pf.n, x32, p32, Go, (float)t, vec(5), vec(6),
+                                                   vec(7), vec(8), vec(9), vec(10), part, max_rows, D.nsm, &rows,
+                                                   D.s));
+      else
+        CK((cudaError_t)mg_stepped_lines_probe(h->d_desc, h->d.pf.n, mode, x32, p32, Go, (float)t, vec(5),
+                                               vec(6), vec(7), vec(8), vec(9), vec(10), part, max_rows, D.nsm,
+                                               &rows, D.s));
       g_launches++;
       std::vector<double> hp((size_t)rows * MINIM_WIDE);
       CK(cudaMemcpyAsync(hp.data(), part, hp.size() * sizeof(double), cudaMemcpyDeviceToHost, D.s));
@@ -756,7 +769,7 @@ void do_minimise(minim_gpu_instance_s* h, const minim_gpu_minimiser_params& mp, 
       const int it0 = s.iter;
       double kernels = 0;
       CK(cudaEventRecord(ev0, D.s));
-      CK((cudaError_t)mg_stepped_pf1_run(h->d_desc, h->d_st, mp.m, h->d.pf.n, D.nsm, 4096, dual ? 1 : 0, D.s, &kernels));
+      CK((cudaError_t)mg_stepped_pf1_run(h->d_desc, &h->d, h->d_st, mp.m, h->d.pf.n, D.nsm, 4096, dual ? 1 : 0, D.s, &kernels));
       CK(cudaEventRecord(ev1, D.s));
       CK(cudaMemcpyAsync(&s, h->d_st, sizeof s, cudaMemcpyDeviceToHost, D.s));
       CK(cudaStreamSynchronize(D.s));

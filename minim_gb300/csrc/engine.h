@@ -291,12 +291,17 @@ int mg_wait_probe(mg::GridSyncState* bar, void* stream);
 // stepped.cu: up to `slice` FP32 L-BFGS iterations (history m) of a binary
 // PhaseField instance as one launch of the graph of its shape (cached per
 // process); dual: the workspace has the spare buffers for two trials per
-// pass.  Returns a cudaError_t.
-int mg_stepped_pf1_run(mg::InstDesc* d, mg::MinScalars* st, int m, const int* grid, int nsm, int slice,
-                       int dual, void* stream, double* kernels);
+// pass; hd: the host's copy of the descriptor (buffer addresses for the
+// trial pass's tensor maps).  Returns a cudaError_t.
+int mg_stepped_pf1_run(mg::InstDesc* d, const mg::InstDesc* hd, mg::MinScalars* st, int m, const int* grid,
+                       int nsm, int slice, int dual, void* stream, double* kernels);
 void mg_stepped_free_all();
 // stepped.cu: one line-stencil pass outside the graph (kernel checks)
 int mg_stepped_lines_probe(const mg::InstDesc* d, const int* grid, int mode, const float* X, const float* P,
                            const float* Go, float t, float* Xa, float* Ga, float* Ya, float* Xb, float* Gb,
                            float* Yb, double* part, int max_rows, int nsm, int* rows, void* stream);
+// stepped.cu: the same two-trial pass through tensor-map tiles
+int mg_stepped_lines_tma_probe(const mg::InstDesc* d, const int* grid, const float* X, const float* P,
+                               const float* Go, float t, float* Xa, float* Ga, float* Ya, float* Xb, float* Gb,
+                               float* Yb, double* part, int max_rows, int nsm, int* rows, void* stream);
 }

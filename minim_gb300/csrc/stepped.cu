@@ -31,6 +31,7 @@
 // the policy counters whether the minimisation simply continues; if not, it
 // leaves the end-of-iteration bookkeeping to the persistent kernel (state
 // `resume`), which redoes it from the same state.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -80,6 +81,7 @@ struct StepCtl {
   unsigned long long tw;  // start of the current controller's scalar work
   int cur;                // its span slot
   unsigned acc_hist[11];  // iterations by the trial accepted (10: none)
+  int tma_err;            // TMA trial pass: a copy wait gave up (1) or no tensor map fits a buffer (2)
 };
 
 // adds the last phase kernel's span to slot j of the span records
@@ -555,23 +557,61 @@ struct LinesAcc {
 
 constexpr int lines_min_blocks(int mode) { return mode == 3 ? 2 : (mode ? 3 : 4); }
 
-// The sweep of a line-stencil pass over every line of the grid (blocks of
-// (nz/4) x lines threads, lines dealt round-robin to the blocks).
+// One quad of a line-stencil pass from its loads: the trial point(s), energy
+// and gradient, the writes of the point, g and y, and the pass's sums.
 template <int MODE>
-__device__ __forceinline__ void lines_sweep(const PotPF& Pf, const LinesIO& io, LinesAcc& a) {
+__device__ __forceinline__ void lines_quad(const LinesIO& io, const LineCoef& K, const QuadLoads& L, int q, float t,
+                                           bool two, LinesAcc& a) {
   constexpr bool WANT_G = MODE != 0;
   constexpr bool DUAL = MODE == 3;
-  const int nx = Pf.n[0], ny = Pf.n[1], nz = Pf.n[2], nz4 = nz >> 2;
-  const float* X = io.X;
-  const float* Pd = io.P;
-  const float t = io.t;
+  float4 go = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (WANT_G) go = ld4(io.Go, q);
+  float4 c4, gv;
+  if (DUAL) a.gpa.add(dot4(go, L.pc));  // g.P for the first pass of a direction
+  a.e.add(quad_eval(L, t, K, WANT_G, c4, gv));
+  if (WANT_G) {
+    st4(io.Xa, q, c4);
+    st4(io.Ga, q, gv);
+    a.gg.add(dot4(gv, gv));
+    const float4 yv = make_float4(gv.x - go.x, gv.y - go.y, gv.z - go.z, gv.w - go.w);
+    st4(io.Ya, q, yv);
+    a.py.add(dot4(L.pc, yv));
+    a.yy.add(dot4(yv, yv));
+  }
+  if (DUAL && two) {
+    a.e2.add(quad_eval(L, 0.5f * t, K, true, c4, gv));
+    st4(io.Xb, q, c4);
+    st4(io.Gb, q, gv);
+    a.gg2.add(dot4(gv, gv));
+    const float4 yv = make_float4(gv.x - go.x, gv.y - go.y, gv.z - go.z, gv.w - go.w);
+    st4(io.Yb, q, yv);
+    a.py2.add(dot4(L.pc, yv));
+    a.yy2.add(dot4(yv, yv));
+  }
+}
+
+// The stencil's constants of a binary PhaseField
+__device__ __forceinline__ LineCoef line_coef(const PotPF& Pf) {
   LineCoef K;
   K.V = (float)Pf.vol_of_type[1];
   K.fb = (float)Pf.kappa[0] / 16 * K.V;
   K.Fi = 0.25f / (float)Pf.res2 * (float)Pf.kappaP[0] * K.V;
   K.pr = (Pf.flags & PF_PRESSURE) ? (float)Pf.pressure[0] : 0.f;
-  K.dx_on = nx > 1;
-  K.dy_on = ny > 1;
+  K.dx_on = Pf.n[0] > 1;
+  K.dy_on = Pf.n[1] > 1;
+  return K;
+}
+
+// The sweep of a line-stencil pass over every line of the grid (blocks of
+// (nz/4) x lines threads, lines dealt round-robin to the blocks).
+template <int MODE>
+__device__ __forceinline__ void lines_sweep(const PotPF& Pf, const LinesIO& io, LinesAcc& a) {
+  constexpr bool DUAL = MODE == 3;
+  const int nx = Pf.n[0], ny = Pf.n[1], nz = Pf.n[2], nz4 = nz >> 2;
+  const float* X = io.X;
+  const float* Pd = io.P;
+  const float t = io.t;
+  const LineCoef K = line_coef(Pf);
   const int zq = threadIdx.x, nl = nx * ny;
   const int z0 = 4 * zq;
   const int izm = z0 == 0 ? nz - 1 : z0 - 1, izp = z0 + 4 == nz ? 0 : z0 + 4;
@@ -599,31 +639,194 @@ __device__ __forceinline__ void lines_sweep(const PotPF& Pf, const LinesIO& io, 
       L.pxm = ld4(Pd, lxm * nz4 + zq);
       L.xxp = ld4(X, lxp * nz4 + zq);
       L.pxp = ld4(Pd, lxp * nz4 + zq);
-      float4 go = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (WANT_G) go = ld4(io.Go, q);
-      float4 c4, gv;
-      if (DUAL) a.gpa.add(dot4(go, L.pc));  // g.P for the first pass of a direction
-      a.e.add(quad_eval(L, t, K, WANT_G, c4, gv));
-      if (WANT_G) {
-        st4(io.Xa, q, c4);
-        st4(io.Ga, q, gv);
-        a.gg.add(dot4(gv, gv));
-        const float4 yv = make_float4(gv.x - go.x, gv.y - go.y, gv.z - go.z, gv.w - go.w);
-        st4(io.Ya, q, yv);
-        a.py.add(dot4(L.pc, yv));
-        a.yy.add(dot4(yv, yv));
-      }
-      if (DUAL && two) {
-        a.e2.add(quad_eval(L, 0.5f * t, K, true, c4, gv));
-        st4(io.Xb, q, c4);
-        st4(io.Gb, q, gv);
-        a.gg2.add(dot4(gv, gv));
-        const float4 yv = make_float4(gv.x - go.x, gv.y - go.y, gv.z - go.z, gv.w - go.w);
-        st4(io.Yb, q, yv);
-        a.py2.add(dot4(L.pc, yv));
-        a.yy2.add(dot4(yv, yv));
+      lines_quad<MODE>(io, K, L, q, t, two, a);
+    }
+  }
+}
+
+// ---- line stencil through TMA plane tiles (two trials per pass) -----------------
+// The same pass as lines_sweep<3>, with the field and the direction brought
+// into shared memory by the tensor memory accelerator.  A block owns a strip
+// of kTmaY lines (y0 .. y0 + kTmaY - 1) over a run of planes x = xa .. xb - 1
+// and walks it along x.  One plane tile is, per array (x and P), the strip's
+// lines with their y neighbours -- one 3-D box of {nz, kTmaY + 2, 1} --
+// and a ring of kTmaStages tiles holds planes x - 1, x and x + 1 while the
+// next planes land: every value is brought on chip once per block, the x
+// neighbours come from the ring and the y neighbours from the tile.
+//
+// A tile holds kTmaY + 2 lines per array: line y0 - 1 + j in slot j.
+// Inside the grid one box brings all of them; a strip at the periodic
+// boundary in y (y0 = 0 or y0 + kTmaY = ny) brings them as kTmaY + 2
+// one-line boxes with the line index wrapped.  Plane wrap in x is the box's
+// own coordinate.  Every box starts at z = 0.
+//
+// Thread 0 issues the copies; each tile has an mbarrier that completes when
+// its bytes have landed.  Waits are bounded: a wait that gives up sets *err
+// (the pass's results are then unusable), the block issues no further copy,
+// and before it exits it waits (bounded again) for every copy it issued.
+constexpr int kTmaY = 4;
+constexpr int kTmaBoxY = kTmaY + 2;
+constexpr int kTmaSlots = kTmaY + 2;
+constexpr int kTmaStages = 4;
+// whether the stepped graph's trial pass uses the tiles unless
+// MINIM_GPU_LINES_TMA says otherwise
+constexpr int kTmaLinesDefault = 0;
+// tensor maps of one instance's buffers: for each of the three coordinate
+// buffers and the MINIM_MAXM + 1 direction slots, the strip box and the
+// one-line box
+constexpr int kTmaBufs = 3 + MINIM_MAXM + 1;
+struct alignas(128) TmaMaps {
+  CUtensorMap box[kTmaBufs];
+  CUtensorMap line[kTmaBufs];
+  const float* xbase[3];
+};
+
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, int c0, int c1, int c2,
+                                            unsigned long long* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];" ::
+          "r"(smem_u32(dst)),
+      "l"(map), "r"(c0), "r"(c1), "r"(c2), "r"(smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ void tma_map_acquire(const CUtensorMap* map) {
+  asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(map) : "memory");
+}
+
+// bytes of dynamic shared memory of the TMA line stencil for lines of nz
+// (the stages plus room to align the first to 128 bytes)
+__host__ __device__ constexpr size_t tma_lines_smem(int nz) {
+  return (size_t)kTmaStages * 2 * kTmaSlots * nz * sizeof(float) + 128;
+}
+// whether a grid takes the TMA line stencil: whole warps of quads, tile
+// slots on 128-byte boundaries, at least two strips
+__host__ __device__ constexpr bool tma_lines_fits(int nx, int ny, int nz) {
+  return nz % 32 == 0 && nz <= 256 && ny % kTmaY == 0 && ny >= 2 * kTmaY && nx >= 3;
+}
+// the strip and plane run of block b of a grid of (ny / kTmaY) * nch blocks
+struct TmaRun {
+  int y0, xa, xb;
+};
+__host__ __device__ inline TmaRun tma_run(int b, int nch, int nx) {
+  const int strip = b / nch, c = b - strip * nch;
+  return {strip * kTmaY, (int)((long long)c * nx / nch), (int)((long long)(c + 1) * nx / nch)};
+}
+
+// Launch shape of the TMA line stencil: blocks of (nz / 4) x kTmaY threads,
+// (ny / kTmaY) strips times nch plane runs, about `target` blocks.
+inline int tma_shape(const int* grid, int target, int* nch) {
+  const int nstrip = grid[1] / kTmaY;
+  *nch = std::max(1, std::min(grid[0], target / nstrip));
+  return nstrip * *nch;
+}
+
+__device__ __forceinline__ void lines_sweep_tma(const PotPF& Pf, const LinesIO& io, LinesAcc& a,
+                                                const CUtensorMap* mbx, const CUtensorMap* mlx,
+                                                const CUtensorMap* mbp, const CUtensorMap* mlp, int nch, int* err) {
+  extern __shared__ unsigned char tma_raw[];
+  __shared__ __align__(8) unsigned long long full[kTmaStages];
+  float* sm = reinterpret_cast<float*>(tma_raw + ((128u - (smem_u32(tma_raw) & 127u)) & 127u));
+  const int nx = Pf.n[0], ny = Pf.n[1], nz = Pf.n[2], nz4 = nz >> 2;
+  const TmaRun run = tma_run(blockIdx.x, nch, nx);
+  const int y0 = run.y0;
+  const bool wrap = y0 == 0 || y0 + kTmaY == ny;
+  const int sfl = kTmaSlots * nz;  // floats of one array's tile
+  const unsigned bytes = 2u * (unsigned)sfl * (unsigned)sizeof(float);
+  const int nplanes = run.xb - run.xa + 2;  // planes xa - 1 .. xb
+  const bool lead = threadIdx.x == 0 && threadIdx.y == 0;
+  auto issue = [&](int k) {
+    const int s = k % kTmaStages;
+    int px = run.xa - 1 + k;
+    px = px < 0 ? px + nx : (px >= nx ? px - nx : px);
+    float* dx = sm + (size_t)s * 2 * sfl;
+    float* dp = dx + sfl;
+    mbar_expect_tx(&full[s], bytes);
+    if (!wrap) {
+      tma_load_3d(dx, mbx, 0, y0 - 1, px, &full[s]);
+      tma_load_3d(dp, mbp, 0, y0 - 1, px, &full[s]);
+    } else {
+      for (int j = 0; j < kTmaSlots; j++) {
+        int yl = y0 - 1 + j;
+        yl = yl < 0 ? yl + ny : (yl >= ny ? yl - ny : yl);
+        tma_load_3d(dx + j * nz, mlx, 0, yl, px, &full[s]);
+        tma_load_3d(dp + j * nz, mlp, 0, yl, px, &full[s]);
       }
     }
+  };
+  if (lead) {
+    for (int s = 0; s < kTmaStages; s++) mbar_init(&full[s], 1);
+    mbar_init_fence();
+    tma_map_acquire(wrap ? mlx : mbx);
+    tma_map_acquire(wrap ? mlp : mbp);
+  }
+  __syncthreads();
+  // issued / waited: planes issued and planes whose wait has run (the same
+  // in every thread)
+  int issued = nplanes < kTmaStages ? nplanes : kTmaStages, waited = 0;
+  if (lead)
+    for (int k = 0; k < issued; k++) issue(k);
+  const LineCoef K = line_coef(Pf);
+  const float t = io.t;
+  const int zq = threadIdx.x, ly = threadIdx.y;
+  const int z0 = 4 * zq;
+  const int izm = z0 == 0 ? nz - 1 : z0 - 1, izp = z0 + 4 == nz ? 0 : z0 + 4;
+  const int y = y0 + ly;
+  bool failed = false;
+  unsigned long long limit = 1000000000ull;
+  for (int x = run.xa; x < run.xb; x++) {
+    // planes x - 1, x, x + 1 are planes i, i + 1, i + 2 of the run
+    const int i = x - run.xa;
+    bool bad = false;
+    while (waited <= i + 2) {
+      const int s = waited % kTmaStages;
+      if (!failed && !mbar_wait(&full[s], (unsigned)(waited / kTmaStages) & 1u, limit)) bad = true;
+      waited++;
+    }
+    if (__syncthreads_or(bad)) {
+      if (!failed && lead) atomicExch(err, 1);
+      failed = true;
+      limit = 1000000ull;
+    }
+    if (failed) break;
+    if (zq < nz4) {
+      const float* bm = sm + (size_t)(i % kTmaStages) * 2 * sfl;
+      const float* bc = sm + (size_t)((i + 1) % kTmaStages) * 2 * sfl;
+      const float* bq = sm + (size_t)((i + 2) % kTmaStages) * 2 * sfl;
+      auto q4 = [&](const float* b, int slot) { return reinterpret_cast<const float4*>(b + slot * nz)[zq]; };
+      const int sc = ly + 1;
+      const float* xc = bc + sc * nz;
+      const float* pc = bc + sfl + sc * nz;
+      QuadLoads L;
+      L.xc = q4(bc, sc);
+      L.pc = q4(bc + sfl, sc);
+      L.xzm = xc[izm];
+      L.pzm = pc[izm];
+      L.xzp = xc[izp];
+      L.pzp = pc[izp];
+      L.xym = q4(bc, sc - 1);
+      L.pym = q4(bc + sfl, sc - 1);
+      L.xyp = q4(bc, sc + 1);
+      L.pyp = q4(bc + sfl, sc + 1);
+      L.xxm = q4(bm, sc);
+      L.pxm = q4(bm + sfl, sc);
+      L.xxp = q4(bq, sc);
+      L.pxp = q4(bq + sfl, sc);
+      lines_quad<3>(io, K, L, (x * ny + y) * nz4 + zq, t, io.two, a);
+    }
+    // plane i is done in every thread: its stage takes plane i + kTmaStages
+    __syncthreads();
+    if (issued < nplanes && issued == i + kTmaStages) {
+      if (lead) issue(issued);
+      issued++;
+    }
+  }
+  // After a failed wait, copies issued earlier may still be in flight.  A
+  // stage has at most one fill outstanding, so they are among the last
+  // kTmaStages planes issued: wait for each (bounded) before leaving.
+  if (failed) {
+    for (int k = issued > kTmaStages ? issued - kTmaStages : 0; k < issued; k++)
+      mbar_wait(&full[k % kTmaStages], (unsigned)(k / kTmaStages) & 1u, 1000000ull);
+    __syncthreads();
   }
 }
 
@@ -685,6 +888,65 @@ k_lines_probe(const InstDesc* __restrict__ d, LinesIO io, double* part) {
   lines_row<MODE>(a, part + (size_t)blockIdx.x * MINIM_WIDE);
 }
 
+// The graph's two-trial pass with its lines staged through tensor-map tiles
+// (k_lines<3> with lines_sweep_tma).  maps holds the tensor maps of the
+// instance's buffers: the point's map is found by the buffer's address (the
+// controllers exchange the three coordinate buffers), the direction's by
+// its ring slot.  A copy wait that gave up, or a buffer with no map, sets
+// ctl->tma_err; later passes of the launch then skip their sweeps and the
+// controller ends the graph's loop instead of taking a step.
+template <int MAXT, int MINB>
+__global__ void __launch_bounds__(MAXT, MINB)
+k_lines_tma(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, double* part,
+            cudaGraphConditionalHandle ls, cudaGraphConditionalHandle grad, cudaGraphConditionalHandle outer,
+            const TmaMaps* __restrict__ maps, int nch) {
+  span_begin(ctl);
+  const int xi = st->xi, gi = st->gi;
+  LinesIO io;
+  io.X = d->X32[xi];
+  io.P = d->Sb + (long long)st->pbuf * d->hstride;
+  io.Go = d->G[gi];
+  io.t = (float)ctl->t;
+  io.Xa = d->X32[1 - xi];
+  io.Ga = d->G[1 - gi];
+  io.Ya = d->Yb + (long long)st->ybuf * d->hstride;
+  io.two = ctl->gmode == 0;
+  io.Xb = d->X32s;
+  io.Gb = d->Gs;
+  io.Yb = d->Yb + (long long)st->ybuf2 * d->hstride;
+  int ix = -1;
+  for (int i = 0; i < 3; i++)
+    if (maps->xbase[i] == io.X) ix = i;
+  const int ip = 3 + st->pbuf;
+  const bool lead = threadIdx.x == 0 && threadIdx.y == 0;
+  const bool nomap = ix < 0 || ip >= kTmaBufs;
+  if (nomap && lead) atomicExch(&ctl->tma_err, 2);
+  const bool skip = __syncthreads_or(nomap || (lead && *(volatile int*)&ctl->tma_err != 0));
+  LinesAcc a;
+  if (!skip)
+    lines_sweep_tma(d->pf, io, a, &maps->box[ix], &maps->line[ix], &maps->box[ip], &maps->line[ip], nch,
+                    &ctl->tma_err);
+  lines_row<3>(a, part + (size_t)blockIdx.x * MINIM_WIDE);
+  if (last_block(ctl)) {
+    if (*(volatile int*)&ctl->tma_err) {
+      if (lead) cudaGraphSetConditional(outer, 0u);
+    } else {
+      ctl_lsg2(d, st, ctl, part, gridDim.x, outer);
+    }
+  }
+}
+
+// One TMA line-stencil pass outside the graph (two trials, no controller):
+// the sweep of lines_sweep_tma on the buffers of io, whose tensor maps are
+// maps->box[0] / line[0] (x) and box[1] / line[1] (P).
+__global__ void __launch_bounds__(kThreads, 3)
+k_lines_tma_probe(const InstDesc* __restrict__ d, LinesIO io, const TmaMaps* __restrict__ maps, int nch,
+                  double* part, int* err) {
+  LinesAcc a;
+  lines_sweep_tma(d->pf, io, a, &maps->box[0], &maps->line[0], &maps->box[1], &maps->line[1], nch, err);
+  lines_row<3>(a, part + (size_t)blockIdx.x * MINIM_WIDE);
+}
+
 // ---- controllers (one block) ----------------------------------------------------
 
 __global__ void k_begin(const InstDesc* __restrict__ d, const MinScalars* __restrict__ st, StepCtl* ctl,
@@ -692,6 +954,7 @@ __global__ void k_begin(const InstDesc* __restrict__ d, const MinScalars* __rest
   if (threadIdx.x == 0) {
     ctl->timing = timing;
     ctl->retry = 0;
+    ctl->tma_err = 0;
     ctl->iters = 0;
     ctl->slice = slice;
     ctl->kernels = 1;
@@ -1155,6 +1418,38 @@ int occupancy(const void* f, int threads) {
 
 }  // namespace
 
+using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+// the driver's tensor-map encoder, looked up through the runtime (the
+// library does not link the driver library itself)
+EncodeTiledFn encode_tiled() {
+  static EncodeTiledFn fn = [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q{};
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) !=
+            cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      return (EncodeTiledFn) nullptr;
+    return (EncodeTiledFn)f;
+  }();
+  return fn;
+}
+// A tensor map of an FP32 field of grid n at base (dimensions z, y, x
+// innermost first) whose box is `lines` lines of one plane.
+int encode_lines_map(CUtensorMap* m, const float* base, const int* n, int lines) {
+  const EncodeTiledFn f = encode_tiled();
+  if (!f) return (int)cudaErrorNotSupported;
+  const cuuint64_t dim[3] = {(cuuint64_t)n[2], (cuuint64_t)n[1], (cuuint64_t)n[0]};
+  const cuuint64_t stride[2] = {(cuuint64_t)n[2] * sizeof(float), (cuuint64_t)n[2] * n[1] * sizeof(float)};
+  const cuuint32_t box[3] = {(cuuint32_t)n[2], (cuuint32_t)lines, 1u};
+  const cuuint32_t es[3] = {1u, 1u, 1u};
+  const CUresult r = f(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float*>(base), dim, stride, box, es,
+                       CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                       CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS ? 0 : (int)cudaErrorInvalidValue;
+}
+
 // A stepped graph and the records its kernels run on.  Graphs are kept per
 // process, one per shape (grid, history length, SM count, iterations per
 // launch, trials per pass): a launch copies the instance's descriptor and
@@ -1170,7 +1465,12 @@ struct SteppedGraph {
   InstDesc* d = nullptr;     // the graph's copy of the descriptor
   MinScalars* st = nullptr;  // the graph's copy of the state record
   int n[3] = {0, 0, 0};
-  int m = 0, nsm = 0, slice = 0, dual = 0, spec = 0;
+  int m = 0, nsm = 0, slice = 0, dual = 0, spec = 0, tma = 0;
+  // TMA trial pass: the tensor maps of the instance's buffers, and the
+  // buffer addresses they were encoded for
+  TmaMaps* maps = nullptr;
+  const void* enc[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+  int enc_hstride = 0;
 };
 
 }  // namespace mg
@@ -1186,12 +1486,12 @@ using namespace mg;
 namespace {
 
 int add_kernel(cudaGraphNode_t* node, cudaGraph_t g, const cudaGraphNode_t* deps, int ndeps, const void* f,
-               int blocks, dim3 threads, void** args) {
+               int blocks, dim3 threads, void** args, unsigned smem = 0) {
   cudaKernelNodeParams p{};
   p.func = const_cast<void*>(f);
   p.gridDim = dim3(blocks);
   p.blockDim = threads;
-  p.sharedMemBytes = 0;
+  p.sharedMemBytes = smem;
   p.kernelParams = args;
   return (int)cudaGraphAddKernelNode(node, g, deps, ndeps, &p);
 }
@@ -1233,7 +1533,8 @@ bool dir_kernels(int m, const void** a, const void** b) {
   }
 }
 
-int build(SteppedGraph* sg, int m, const int* grid, int nsm, int slice, int dual, int spec, cudaStream_t s) {
+int build(SteppedGraph* sg, int m, const int* grid, int nsm, int slice, int dual, int spec, int tma,
+          cudaStream_t s) {
   const void* fa = nullptr;
   const void* fb = nullptr;
   if (!dir_kernels(m, &fa, &fb)) return (int)cudaErrorInvalidValue;
@@ -1258,7 +1559,28 @@ int build(SteppedGraph* sg, int m, const int* grid, int nsm, int slice, int dual
   const int occ_a = occupancy(fa, kThreads), occ_b = occupancy(fb, kThreads);
   const int occ_e = occupancy(fe, (int)(sblock.x * sblock.y)), occ_g = occupancy(fg, (int)(sblock.x * sblock.y));
   if (!occ_a || !occ_b || !occ_e || !occ_g) return (int)cudaErrorInvalidConfiguration;
-  const int nb_a = nsm * occ_a, nb_b = nsm * occ_b, nb_e = nsm * occ_e, nb_g = nsm * occ_g;
+  const int nb_a = nsm * occ_a, nb_b = nsm * occ_b, nb_g = nsm * occ_g;
+  int nb_e = nsm * occ_e;
+  // the two-trial pass through tensor-map tiles (on request, where the grid
+  // takes it): blocks of (nz / 4) x kTmaY threads over strips x plane runs
+  const bool use_tma = tma && two && tma_lines_fits(grid[0], grid[1], grid[2]);
+  // tma: 1, the kernel compiled for blocks of up to 256 threads, three per
+  // SM (four of 192 threads fit); 2, for blocks of up to 192 threads, three
+  // per SM (more registers)
+  dim3 eblock = sblock;
+  unsigned esmem = 0;
+  int nch = 1;
+  if (use_tma) {
+    fe = tma == 2 && nz4 * kTmaY <= 192 ? (const void*)k_lines_tma<192, 3> : (const void*)k_lines_tma<kThreads, 3>;
+    eblock = dim3(nz4, kTmaY);
+    esmem = (unsigned)tma_lines_smem(grid[2]);
+    SCK(cudaFuncSetAttribute(fe, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)esmem));
+    int occ = 0;
+    SCK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fe, (int)(eblock.x * eblock.y), (int)esmem));
+    if (!occ) return (int)cudaErrorInvalidConfiguration;
+    nb_e = tma_shape(grid, nsm * occ, &nch);
+    SCK(cudaMallocAsync((void**)&sg->maps, sizeof(TmaMaps), s));
+  }
   const int nb_max = std::max(std::max(nb_a, nb_b), std::max(nb_e, nb_g));
   SCK(cudaMallocAsync((void**)&sg->d, sizeof(InstDesc), s));
   SCK(cudaMallocAsync((void**)&sg->st, sizeof(MinScalars), s));
@@ -1273,6 +1595,7 @@ int build(SteppedGraph* sg, int m, const int* grid, int nsm, int slice, int dual
   sg->slice = slice;
   sg->dual = dual;
   sg->spec = spec;
+  sg->tma = tma;
   const InstDesc* d = sg->d;
   MinScalars* st = sg->st;
   int timing = std::getenv("MINIM_GPU_STEPPED_TIMING") != nullptr;
@@ -1309,7 +1632,14 @@ int build(SteppedGraph* sg, int m, const int* grid, int nsm, int slice, int dual
     // gradient-only pass) ends the iteration; one that does not sets
     // `retry`, and the next pass of the outer loop skips the direction
     cudaGraphNode_t nt;
-    SCK(add_kernel(&nt, body, &nb, 1, fe, nb_e, sblock, args_s));
+    if (use_tma) {
+      TmaMaps* maps = sg->maps;
+      void* args_t[] = {(void*)&d,     (void*)&st,      (void*)&ctl,  (void*)&part, (void*)&h_ls,
+                        (void*)&h_grad, (void*)&h_outer, (void*)&maps, (void*)&nch};
+      SCK(add_kernel(&nt, body, &nb, 1, fe, nb_e, eblock, args_t, esmem));
+    } else {
+      SCK(add_kernel(&nt, body, &nb, 1, fe, nb_e, sblock, args_s));
+    }
     SCK(cudaGraphInstantiate(&sg->exec, g, 0));
     return 0;
   }
@@ -1345,25 +1675,31 @@ void free_graph(SteppedGraph* sg) {
   if (sg->part) cudaFree(sg->part);
   if (sg->d) cudaFree(sg->d);
   if (sg->st) cudaFree(sg->st);
+  if (sg->maps) cudaFree(sg->maps);
   delete sg;
 }
 }  // namespace
 
 // Runs up to `slice` FP32 L-BFGS iterations (history m) of the binary
-// PhaseField instance (device descriptor d, state st) as one graph launch on
-// stream s, with the graph of this shape (built on first use).  Adds the
-// kernels executed to *kernels.  Returns a cudaError_t.
-extern "C" int mg_stepped_pf1_run(InstDesc* d, MinScalars* st, int m, const int* grid, int nsm, int slice,
-                                  int dual, void* stream, double* kernels) {
+// PhaseField instance (device descriptor d, host copy hd, state st) as one
+// graph launch on stream s, with the graph of this shape (built on first
+// use).  The trial pass stages its lines through tensor-map tiles when
+// MINIM_GPU_LINES_TMA=1 (default kTmaLinesDefault) and the grid takes them.
+// Adds the kernels executed to *kernels.  Returns a cudaError_t
+// (cudaErrorLaunchTimeout when a tile's copy wait gave up).
+extern "C" int mg_stepped_pf1_run(InstDesc* d, const InstDesc* hd, MinScalars* st, int m, const int* grid,
+                                  int nsm, int slice, int dual, void* stream, double* kernels) {
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   const char* env = std::getenv("MINIM_GPU_SPECULATIVE");
   const int spec = !(env && env[0] == '0');
+  const char* tenv = std::getenv("MINIM_GPU_LINES_TMA");
+  const int tma = tenv ? std::atoi(tenv) : kTmaLinesDefault;
   std::lock_guard<std::mutex> lk(g_graphs_mu);
   SteppedGraph* sg = nullptr;
   for (size_t i = 0; i < g_graphs.size(); i++) {
     SteppedGraph* c = g_graphs[i];
     if (c->n[0] == grid[0] && c->n[1] == grid[1] && c->n[2] == grid[2] && c->m == m && c->nsm == nsm &&
-        c->slice == slice && c->dual == dual && c->spec == spec) {
+        c->slice == slice && c->dual == dual && c->spec == spec && c->tma == tma) {
       sg = c;
       g_graphs.erase(g_graphs.begin() + (long)i);
       g_graphs.push_back(sg);
@@ -1377,7 +1713,7 @@ extern "C" int mg_stepped_pf1_run(InstDesc* d, MinScalars* st, int m, const int*
       g_graphs.erase(g_graphs.begin());
     }
     sg = new SteppedGraph;
-    const int rc = build(sg, m, grid, nsm, slice, dual, spec, s);
+    const int rc = build(sg, m, grid, nsm, slice, dual, spec, tma, s);
     if (rc) {
       cudaStreamSynchronize(s);
       free_graph(sg);
@@ -1390,6 +1726,30 @@ extern "C" int mg_stepped_pf1_run(InstDesc* d, MinScalars* st, int m, const int*
     const size_t o = offsetof(StepCtl, gap_pre);
     SCK(cudaMemsetAsync(reinterpret_cast<char*>(sg->ctl) + o, 0, sizeof(StepCtl) - o, s));
   }
+  if (sg->maps) {
+    // tensor maps of this instance's three coordinate buffers (the set is
+    // the same whichever the controllers have exchanged) and m + 1
+    // direction slots, encoded again when the buffers differ from the last
+    const void* enc[5] = {hd->X32[0], hd->X32[1], hd->X32s, hd->Sb, nullptr};
+    bool same = hd->hstride == sg->enc_hstride;
+    for (int k = 0; k < 4; k++) same = same && enc[k] == sg->enc[k];
+    if (!same) {
+      if (!hd->X32s || m + 1 > MINIM_MAXM + 1) return (int)cudaErrorInvalidValue;
+      TmaMaps hm{};
+      const float* xb[3] = {hd->X32[0], hd->X32[1], hd->X32s};
+      for (int k = 0; k < kTmaBufs; k++) {
+        const float* base = k < 3 ? xb[k] : (k - 3 <= m ? hd->Sb + (long long)(k - 3) * hd->hstride : nullptr);
+        if (!base) continue;
+        SCK(encode_lines_map(&hm.box[k], base, grid, kTmaSlots));
+        SCK(encode_lines_map(&hm.line[k], base, grid, 1));
+      }
+      for (int k = 0; k < 3; k++) hm.xbase[k] = xb[k];
+      SCK(cudaMemcpyAsync(sg->maps, &hm, sizeof hm, cudaMemcpyHostToDevice, s));
+      SCK(cudaStreamSynchronize(s));
+      for (int k = 0; k < 4; k++) sg->enc[k] = enc[k];
+      sg->enc_hstride = hd->hstride;
+    }
+  }
   SCK(cudaMemcpyAsync(sg->d, d, sizeof(InstDesc), cudaMemcpyDeviceToDevice, s));
   SCK(cudaMemcpyAsync(sg->st, st, sizeof(MinScalars), cudaMemcpyDeviceToDevice, s));
   SCK(cudaGraphLaunch(sg->exec, s));
@@ -1400,6 +1760,7 @@ extern "C" int mg_stepped_pf1_run(InstDesc* d, MinScalars* st, int m, const int*
   SCK(cudaMemcpyAsync(&c, sg->ctl, sizeof c, cudaMemcpyDeviceToHost, s));
   SCK(cudaStreamSynchronize(s));
   if (kernels) *kernels += c.kernels;
+  if (c.tma_err) return (int)cudaErrorLaunchTimeout;
   if (timing) {
     static const char* name[4] = {"trials", "gradient", "dirA", "dirB"};
     for (int j = 0; j < 4; j++)
@@ -1447,4 +1808,52 @@ extern "C" int mg_stepped_lines_probe(const InstDesc* d, const int* grid, int mo
   else k_lines_probe<0><<<nb, blk, 0, s>>>(d, io, part);
   *rows = nb;
   return (int)cudaGetLastError();
+}
+
+
+// The TMA line stencil's two-trial pass outside the graph: the points,
+// gradients and y = g - Go at t (Xa, Ga, Ya) and t/2 (Xb, Gb, Yb) of
+// lines_sweep_tma, for checking it against the direct line stencil and an
+// FP64 evaluation.  Arguments as mg_stepped_lines_probe's; the grid must
+// satisfy tma_lines_fits.  Synchronises the stream; a copy wait that gave up
+// returns cudaErrorLaunchTimeout.
+extern "C" int mg_stepped_lines_tma_probe(const InstDesc* d, const int* grid, const float* X, const float* P,
+                                          const float* Go, float t, float* Xa, float* Ga, float* Ya, float* Xb,
+                                          float* Gb, float* Yb, double* part, int max_rows, int nsm, int* rows,
+                                          void* stream) {
+  if (!tma_lines_fits(grid[0], grid[1], grid[2])) return (int)cudaErrorInvalidValue;
+  const dim3 blk(grid[2] / 4, kTmaY);
+  const void* f = (const void*)k_lines_tma_probe;
+  const int smem = (int)tma_lines_smem(grid[2]);
+  SCK(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  int occ = 0;
+  SCK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, f, (int)(blk.x * blk.y), smem));
+  if (occ < 1) return (int)cudaErrorInvalidConfiguration;
+  int nch = 1;
+  const int nb = tma_shape(grid, nsm * occ, &nch);
+  if (nb > max_rows) return (int)cudaErrorInvalidConfiguration;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  TmaMaps hm{};
+  SCK(encode_lines_map(&hm.box[0], X, grid, kTmaBoxY));
+  SCK(encode_lines_map(&hm.line[0], X, grid, 1));
+  SCK(encode_lines_map(&hm.box[1], P, grid, kTmaBoxY));
+  SCK(encode_lines_map(&hm.line[1], P, grid, 1));
+  char* dm = nullptr;
+  SCK(cudaMallocAsync((void**)&dm, sizeof(TmaMaps) + 128, s));
+  TmaMaps* maps = reinterpret_cast<TmaMaps*>(dm);
+  int* err = reinterpret_cast<int*>(dm + sizeof(TmaMaps));
+  int herr = 0;
+  int rc = (int)cudaMemcpyAsync(maps, &hm, sizeof hm, cudaMemcpyHostToDevice, s);
+  if (!rc) rc = (int)cudaMemsetAsync(err, 0, sizeof(int), s);
+  if (!rc) {
+    LinesIO io{X, P, Go, Xa, Ga, Ya, Xb, Gb, Yb, t, true};
+    k_lines_tma_probe<<<nb, blk, smem, s>>>(d, io, maps, nch, part, err);
+    rc = (int)cudaGetLastError();
+  }
+  if (!rc) rc = (int)cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, s);
+  cudaFreeAsync(dm, s);
+  if (!rc) rc = (int)cudaStreamSynchronize(s);
+  if (!rc && herr) rc = (int)cudaErrorLaunchTimeout;
+  *rows = nb;
+  return rc;
 }

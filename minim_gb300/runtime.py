@@ -227,11 +227,12 @@ class Instance:
     def eval_kernel(self, path, x, p=None, t=0.0, gradient=True, points=False):
         """One evaluation by a minimiser stage's own kernels at x + t p
         (minim_gpu_eval_kernel; path is one of abi.EVAL_*).  Returns (e, g)
-        -- for abi.EVAL_LINES each holds the two trials (t, t/2) -- and, with
+        -- for the line stencils (abi.EVAL_LINES, abi.EVAL_LINES_TMA) each
+        holds the two trials (t, t/2) -- and, with
         points (line stencil only), the two points the stencil formed."""
         xv = _vec(x)
         pv = None if p is None else _vec(p)
-        two = path == abi.EVAL_LINES
+        two = path in (abi.EVAL_LINES, abi.EVAL_LINES_TMA)
         e = np.zeros(2 if two else 1)
         g = np.zeros((2 if two else 1) * self.ndof) if gradient else None
         xt = np.zeros(2 * self.ndof) if points else None

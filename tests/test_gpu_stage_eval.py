@@ -244,3 +244,42 @@ def test_stage_eval_rejects_bad_arguments():
     with pytest.raises(runtime.MinimGpuError) as e:
         inst.eval_kernel(abi.EVAL_FP32_GRID, x, points=True)
     assert e.value.code == abi.ERR_INVALID
+
+
+@pytest.mark.parametrize("grid", [(192, 192, 192), (5, 12, 64), (16, 8, 32), (6, 16, 256)])
+def test_pf_line_stencil_tma(grid):
+    """The two-trial line stencil with its lines staged through tensor-map
+    tiles: points and gradients bitwise those of the direct stencil (same
+    arithmetic per quad), energies those of the direct stencil up to the
+    order of the sums, and both trials within the FP32 tolerances of the
+    oracle.  The small grids put every strip at the periodic boundary in y
+    (one-line wrap copies) and give plane runs of one to three planes."""
+    p = abi.phase_field(grid, interface_size=1.0, surface_tension=1.0)
+    x = pf_noise(grid, seed=3, amp=0.05)
+    inst = runtime.Instance(p, x)
+    ora = Oracle(p, x)
+    _, g0 = ora.energy_gradient(x)
+    d = -g0 * 0.1
+    for t in (1.0, 0.25):
+        e, g, pts = inst.eval_kernel(abi.EVAL_LINES_TMA, x, d, t, points=True)
+        ed, gd, ptd = inst.eval_kernel(abi.EVAL_LINES, x, d, t, points=True)
+        assert np.array_equal(pts, ptd)
+        assert np.array_equal(g, gd)
+        for k in range(2):
+            assert abs(e[k] - ed[k]) <= 1e-12 * abs(ed[k]), (k, e[k], ed[k])
+            eo, go = ora.energy_gradient(pts[k])
+            de, dg = _errs(e[k], g[k], eo, go)
+            _log("pf_lines_tma", abi.EVAL_LINES_TMA, grid=list(grid), trial=k, t=t, energy_rel_err=de,
+                 grad_rel_err=dg)
+            assert dg <= GRAD32, (k, dg)
+            assert de <= E32, (k, de)
+
+
+def test_pf_line_stencil_tma_rejects_grids():
+    for grid in [(8, 8, 36), (8, 6, 32), (8, 4, 32), (2, 8, 32)]:
+        p = abi.phase_field(grid, interface_size=1.0, surface_tension=1.0)
+        x = pf_noise(grid, seed=1, amp=0.05)
+        inst = runtime.Instance(p, x)
+        with pytest.raises(runtime.MinimGpuError) as e:
+            inst.eval_kernel(abi.EVAL_LINES_TMA, x, np.zeros_like(x), 1.0)
+        assert e.value.code == abi.ERR_INVALID
