@@ -769,7 +769,7 @@ void do_minimise(minim_gpu_instance_s* h, const minim_gpu_minimiser_params& mp, 
       const int it0 = s.iter;
       double kernels = 0;
       CK(cudaEventRecord(ev0, D.s));
-      CK((cudaError_t)mg_stepped_pf1_run(h->d_desc, &h->d, h->d_st, mp.m, h->d.pf.n, D.nsm, 4096, dual ? 1 : 0, D.s, &kernels));
+      CK((cudaError_t)mg_stepped_pf1_run(h->d_desc, &d, h->d_st, mp.m, h->d.pf.n, D.nsm, 4096, dual ? 1 : 0, D.s, &kernels));
       CK(cudaEventRecord(ev1, D.s));
       CK(cudaMemcpyAsync(&s, h->d_st, sizeof s, cudaMemcpyDeviceToHost, D.s));
       CK(cudaStreamSynchronize(D.s));
