@@ -693,10 +693,10 @@ __device__ __forceinline__ void tma_map_acquire(const CUtensorMap* map) {
   asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(map) : "memory");
 }
 
-// bytes of dynamic shared memory of the TMA line stencil for lines of nz
-// (the stages plus room to align the first to 128 bytes)
-__host__ __device__ constexpr size_t tma_lines_smem(int nz) {
-  return (size_t)kTmaStages * 2 * kTmaSlots * nz * sizeof(float) + 128;
+// bytes of dynamic shared memory of the TMA line stencil with ns stages for
+// lines of nz (the stages plus room to align the first to 128 bytes)
+__host__ __device__ constexpr size_t tma_lines_smem(int nz, int ns = kTmaStages) {
+  return (size_t)ns * 2 * kTmaSlots * nz * sizeof(float) + 128;
 }
 // whether a grid takes the TMA line stencil: whole warps of quads, tile
 // slots on 128-byte boundaries, at least two strips
@@ -720,11 +720,12 @@ inline int tma_shape(const int* grid, int target, int* nch) {
   return nstrip * *nch;
 }
 
+template <int NS>
 __device__ __forceinline__ void lines_sweep_tma(const PotPF& Pf, const LinesIO& io, LinesAcc& a,
                                                 const CUtensorMap* mbx, const CUtensorMap* mlx,
                                                 const CUtensorMap* mbp, const CUtensorMap* mlp, int nch, int* err) {
   extern __shared__ unsigned char tma_raw[];
-  __shared__ __align__(8) unsigned long long full[kTmaStages];
+  __shared__ __align__(8) unsigned long long full[NS];
   float* sm = reinterpret_cast<float*>(tma_raw + ((128u - (smem_u32(tma_raw) & 127u)) & 127u));
   const int nx = Pf.n[0], ny = Pf.n[1], nz = Pf.n[2], nz4 = nz >> 2;
   const TmaRun run = tma_run(blockIdx.x, nch, nx);
@@ -735,7 +736,7 @@ __device__ __forceinline__ void lines_sweep_tma(const PotPF& Pf, const LinesIO& 
   const int nplanes = run.xb - run.xa + 2;  // planes xa - 1 .. xb
   const bool lead = threadIdx.x == 0 && threadIdx.y == 0;
   auto issue = [&](int k) {
-    const int s = k % kTmaStages;
+    const int s = k % NS;
     int px = run.xa - 1 + k;
     px = px < 0 ? px + nx : (px >= nx ? px - nx : px);
     float* dx = sm + (size_t)s * 2 * sfl;
@@ -754,7 +755,7 @@ __device__ __forceinline__ void lines_sweep_tma(const PotPF& Pf, const LinesIO& 
     }
   };
   if (lead) {
-    for (int s = 0; s < kTmaStages; s++) mbar_init(&full[s], 1);
+    for (int s = 0; s < NS; s++) mbar_init(&full[s], 1);
     mbar_init_fence();
     tma_map_acquire(wrap ? mlx : mbx);
     tma_map_acquire(wrap ? mlp : mbp);
@@ -762,7 +763,7 @@ __device__ __forceinline__ void lines_sweep_tma(const PotPF& Pf, const LinesIO& 
   __syncthreads();
   // issued / waited: planes issued and planes whose wait has run (the same
   // in every thread)
-  int issued = nplanes < kTmaStages ? nplanes : kTmaStages, waited = 0;
+  int issued = nplanes < NS ? nplanes : NS, waited = 0;
   if (lead)
     for (int k = 0; k < issued; k++) issue(k);
   const LineCoef K = line_coef(Pf);
@@ -778,8 +779,8 @@ __device__ __forceinline__ void lines_sweep_tma(const PotPF& Pf, const LinesIO& 
     const int i = x - run.xa;
     bool bad = false;
     while (waited <= i + 2) {
-      const int s = waited % kTmaStages;
-      if (!failed && !mbar_wait(&full[s], (unsigned)(waited / kTmaStages) & 1u, limit)) bad = true;
+      const int s = waited % NS;
+      if (!failed && !mbar_wait(&full[s], (unsigned)(waited / NS) & 1u, limit)) bad = true;
       waited++;
     }
     if (__syncthreads_or(bad)) {
@@ -789,9 +790,9 @@ __device__ __forceinline__ void lines_sweep_tma(const PotPF& Pf, const LinesIO& 
     }
     if (failed) break;
     if (zq < nz4) {
-      const float* bm = sm + (size_t)(i % kTmaStages) * 2 * sfl;
-      const float* bc = sm + (size_t)((i + 1) % kTmaStages) * 2 * sfl;
-      const float* bq = sm + (size_t)((i + 2) % kTmaStages) * 2 * sfl;
+      const float* bm = sm + (size_t)(i % NS) * 2 * sfl;
+      const float* bc = sm + (size_t)((i + 1) % NS) * 2 * sfl;
+      const float* bq = sm + (size_t)((i + 2) % NS) * 2 * sfl;
       auto q4 = [&](const float* b, int slot) { return reinterpret_cast<const float4*>(b + slot * nz)[zq]; };
       const int sc = ly + 1;
       const float* xc = bc + sc * nz;
@@ -813,19 +814,19 @@ __device__ __forceinline__ void lines_sweep_tma(const PotPF& Pf, const LinesIO& 
       L.pxp = q4(bq + sfl, sc);
       lines_quad<3>(io, K, L, (x * ny + y) * nz4 + zq, t, io.two, a);
     }
-    // plane i is done in every thread: its stage takes plane i + kTmaStages
+    // plane i is done in every thread: its stage takes plane i + NS
     __syncthreads();
-    if (issued < nplanes && issued == i + kTmaStages) {
+    if (issued < nplanes && issued == i + NS) {
       if (lead) issue(issued);
       issued++;
     }
   }
   // After a failed wait, copies issued earlier may still be in flight.  A
   // stage has at most one fill outstanding, so they are among the last
-  // kTmaStages planes issued: wait for each (bounded) before leaving.
+  // NS planes issued: wait for each (bounded) before leaving.
   if (failed) {
-    for (int k = issued > kTmaStages ? issued - kTmaStages : 0; k < issued; k++)
-      mbar_wait(&full[k % kTmaStages], (unsigned)(k / kTmaStages) & 1u, 1000000ull);
+    for (int k = issued > NS ? issued - NS : 0; k < issued; k++)
+      mbar_wait(&full[k % NS], (unsigned)(k / NS) & 1u, 1000000ull);
     __syncthreads();
   }
 }
@@ -895,7 +896,7 @@ k_lines_probe(const InstDesc* __restrict__ d, LinesIO io, double* part) {
 // its ring slot.  A copy wait that gave up, or a buffer with no map, sets
 // ctl->tma_err; later passes of the launch then skip their sweeps and the
 // controller ends the graph's loop instead of taking a step.
-template <int MAXT, int MINB>
+template <int MAXT, int MINB, int NS>
 __global__ void __launch_bounds__(MAXT, MINB)
 k_lines_tma(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, double* part,
             cudaGraphConditionalHandle ls, cudaGraphConditionalHandle grad, cudaGraphConditionalHandle outer,
@@ -924,8 +925,8 @@ k_lines_tma(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, double
   const bool skip = __syncthreads_or(nomap || (lead && *(volatile int*)&ctl->tma_err != 0));
   LinesAcc a;
   if (!skip)
-    lines_sweep_tma(d->pf, io, a, &maps->box[ix], &maps->line[ix], &maps->box[ip], &maps->line[ip], nch,
-                    &ctl->tma_err);
+    lines_sweep_tma<NS>(d->pf, io, a, &maps->box[ix], &maps->line[ix], &maps->box[ip], &maps->line[ip], nch,
+                        &ctl->tma_err);
   lines_row<3>(a, part + (size_t)blockIdx.x * MINIM_WIDE);
   if (last_block(ctl)) {
     if (*(volatile int*)&ctl->tma_err) {
@@ -943,7 +944,7 @@ __global__ void __launch_bounds__(kThreads, 3)
 k_lines_tma_probe(const InstDesc* __restrict__ d, LinesIO io, const TmaMaps* __restrict__ maps, int nch,
                   double* part, int* err) {
   LinesAcc a;
-  lines_sweep_tma(d->pf, io, a, &maps->box[0], &maps->line[0], &maps->box[1], &maps->line[1], nch, err);
+  lines_sweep_tma<kTmaStages>(d->pf, io, a, &maps->box[0], &maps->line[0], &maps->box[1], &maps->line[1], nch, err);
   lines_row<3>(a, part + (size_t)blockIdx.x * MINIM_WIDE);
 }
 
@@ -1564,16 +1565,16 @@ int build(SteppedGraph* sg, int m, const int* grid, int nsm, int slice, int dual
   // the two-trial pass through tensor-map tiles (on request, where the grid
   // takes it): blocks of (nz / 4) x kTmaY threads over strips x plane runs
   const bool use_tma = tma && two && tma_lines_fits(grid[0], grid[1], grid[2]);
-  // tma: 1, the kernel compiled for blocks of up to 256 threads, three per
-  // SM (four of 192 threads fit); 2, for blocks of up to 192 threads, three
-  // per SM (more registers)
+  // tma: 1, 2, 3: rings of 4, 6, 8 plane stages
   dim3 eblock = sblock;
   unsigned esmem = 0;
   int nch = 1;
   if (use_tma) {
-    fe = tma == 2 && nz4 * kTmaY <= 192 ? (const void*)k_lines_tma<192, 3> : (const void*)k_lines_tma<kThreads, 3>;
+    const int ns = tma == 3 ? 8 : (tma == 2 ? 6 : 4);
+    fe = ns == 8 ? (const void*)k_lines_tma<kThreads, 2, 8>
+                 : (ns == 6 ? (const void*)k_lines_tma<kThreads, 2, 6> : (const void*)k_lines_tma<kThreads, 3, 4>);
     eblock = dim3(nz4, kTmaY);
-    esmem = (unsigned)tma_lines_smem(grid[2]);
+    esmem = (unsigned)tma_lines_smem(grid[2], ns);
     SCK(cudaFuncSetAttribute(fe, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)esmem));
     int occ = 0;
     SCK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fe, (int)(eblock.x * eblock.y), (int)esmem));
