@@ -847,8 +847,8 @@ __device__ __forceinline__ void lines_row(const LinesAcc& a, double* row) {
   }
 }
 
-template <int MODE, int MINB = lines_min_blocks(MODE)>
-__global__ void __launch_bounds__(kThreads, MINB)
+template <int MODE, int MINB = lines_min_blocks(MODE), int MAXT = kThreads>
+__global__ void __launch_bounds__(MAXT, MINB)
 k_lines(const InstDesc* __restrict__ d, MinScalars* st, StepCtl* ctl, double* part, cudaGraphConditionalHandle ls,
         cudaGraphConditionalHandle grad, cudaGraphConditionalHandle outer) {
   constexpr bool DUAL = MODE == 3;
@@ -1553,8 +1553,12 @@ int build(SteppedGraph* sg, int m, const int* grid, int nsm, int slice, int dual
   // workspace has the spare buffers
   const bool two = spec && use_lines && dual;
   const int bmode = two ? 2 : spec;  // direction pass B's set-up of the trials
-  const void* fe = spec ? (use_lines ? (dual ? (const void*)k_lines<3> : (const void*)k_lines<2>)
-                                     : (const void*)k_grad<true>)
+  // blocks of at most 192 threads take the two-trial pass compiled for
+  // three blocks per SM (96 registers) unless MINIM_GPU_LINES_B3=0
+  const char* b3env = std::getenv("MINIM_GPU_LINES_B3");
+  const bool b3 = sblock.x * sblock.y <= 192 && !(b3env && b3env[0] == '0');
+  const void* f3 = b3 ? (const void*)k_lines<3, 3, 192> : (const void*)k_lines<3>;
+  const void* fe = spec ? (use_lines ? (dual ? f3 : (const void*)k_lines<2>) : (const void*)k_grad<true>)
                         : (use_lines ? (const void*)k_lines<0> : (const void*)k_eonly);
   const void* fg = use_lines ? (const void*)k_lines<1> : (const void*)k_grad<false>;
   const int occ_a = occupancy(fa, kThreads), occ_b = occupancy(fb, kThreads);
