@@ -382,8 +382,8 @@ int minim_gpu_wait_probe(int limit_ms, int* timed_out, double* elapsed_ms);
  * 3-D; larger calls return MINIM_GPU_ERR_INVALID).  Work is queued on
  * `stream` (a cudaStream_t, NULL = legacy default stream) and the call
  * returns after synchronising that stream.  The first call on a device (with
- * that device current) looks up the array's device address; make it before
- * any stream capture.  All calls share the one array: calls that overlap on
+ * that device current) looks up the array's device address.  All calls
+ * share the one array: calls that overlap on
  * the GPU race and must be serialised by the caller.  The tolerance
  * mp->tol < 0 means 1e-6.  Results equal minim_gpu_batch_run with 256
  * threads per CTA. */

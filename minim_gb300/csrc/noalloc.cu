@@ -19,8 +19,7 @@
 //   * the host does not know the array's device address; it is looked up
 //     with cudaGetSymbolAddress on the first call on each device (with that
 //     device current), together with the kernel's per-device opt-in to its
-//     shared-memory size, so that first call is the one to make before any
-//     stream capture;
+//     shared-memory size;
 //   * the state record at the start of the array is reset on every call; the
 //     kernel writes every vector before reading it.
 #include <cuda_runtime.h>
