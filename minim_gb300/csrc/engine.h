@@ -185,6 +185,8 @@ struct MinScalars {
   double SY[MINIM_MAXM][MINIM_MAXM], YY[MINIM_MAXM][MINIM_MAXM];
   int pend;
   int cool;          // iterations before a stalled run may re-enter FP64
+  int fp64_fails;    // FP64 stages left on a stall (each doubles the next wait, up to 16x)
+  int spare_;
   // set by the stepped FP32 path when it hands an iteration's end-of-
   // iteration bookkeeping (precision switch, convergence) to the kernel
   int resume, resume_exhausted;

@@ -112,7 +112,7 @@ struct Runner {
   int lj_tile;
   // uniform scalars (every thread holds identical copies)
   int n, status, initd, iter, ii, stage, xi, gi, evals, fp64_iters, stall, nsteps, pbuf, ybuf;
-  int exhausted_run, switch_reason, pend, cool, resume, resume_exhausted;
+  int exhausted_run, switch_reason, pend, cool, fp64_fails, resume, resume_exhausted;
   double E, gg, best_rms, dt, a, dtmax, gnorm;
   double rms_v, gnorm_v;  // sqrt(gg / n) and sqrt(gg) of the current gradient
   double abytes, pairs32, pairs64;
@@ -991,6 +991,7 @@ struct Runner {
     xi = s.xi; gi = s.gi; evals = s.evals; fp64_iters = s.fp64_iters; stall = s.stall;
     nsteps = s.nsteps; pbuf = s.pbuf; ybuf = s.ybuf; E = s.E; gg = s.gg; best_rms = s.best_rms;
     exhausted_run = s.exhausted_run; switch_reason = s.switch_reason; pend = s.pend; cool = s.cool;
+    fp64_fails = s.fp64_fails;
     resume = s.resume; resume_exhausted = s.resume_exhausted;
     dt = s.dt; a = s.a; dtmax = s.dtmax; gnorm = s.gnorm;
     rms_v = sqrt(gg / n);
@@ -1015,6 +1016,7 @@ struct Runner {
       s.evals = evals; s.fp64_iters = fp64_iters; s.stall = stall; s.nsteps = nsteps;
       s.pbuf = pbuf; s.ybuf = ybuf; s.E = E; s.gg = gg; s.best_rms = best_rms;
       s.exhausted_run = exhausted_run; s.switch_reason = switch_reason; s.pend = pend; s.cool = cool;
+      s.fp64_fails = fp64_fails;
       s.resume = resume; s.resume_exhausted = resume_exhausted;
       s.dt = dt; s.a = a; s.dtmax = dtmax; s.gnorm = gnorm; s.initialised = 1;
       s.abytes = abytes; s.pairs32 = pairs32; s.pairs64 = pairs64;
@@ -1082,12 +1084,18 @@ struct Runner {
           // a basin change), or that has not improved its RMS gradient by 1%
           // in 2000 iterations (an orbit that will not converge), continues
           // in FP32; a stalled run may re-enter FP64 on a stall only after
-          // 5000 more iterations.
+          // 5000 more iterations, twice as many after each FP64 stage that
+          // ended on a stall (up to 80000): an orbit that FP64 does not
+          // settle either (FIRE with a large time step) spends a shrinking
+          // share of its iterations in the costlier FP64 arithmetic.
           if (r < 0.99 * best_rms) { best_rms = r; stall = 0; }
           else stall++;
           const bool far = r > 1e4 * mp.tol && r > 100.0 * best_rms;
           if (far || stall >= 2000) {
-            if (!far) cool = 5000;
+            if (!far) {
+              cool = 5000 << (fp64_fails < 4 ? fp64_fails : 4);
+              fp64_fails++;
+            }
             to_fp32();
             reeval();
             best_rms = rms();
@@ -1168,6 +1176,7 @@ struct Runner {
       stall = 0;
       exhausted_run = 0;
       cool = 0;
+      fp64_fails = 0;
     }
     // an iteration run outside this kernel (the stepped FP32 path) may hand
     // its end-of-iteration bookkeeping over to here
