@@ -59,7 +59,36 @@ struct NoEmit {
 struct alignas(16) F4 { float x, y, z, w; };
 struct alignas(16) D4 { double x, y, z, w; };
 
-// Pair arithmetic type: FP32 in the FP32 stage; double-float (DF, about 48
+// Double-float for the Lennard-Jones pair terms: the DF representation with
+// the cheaper operations that suffice there.  A sum is TwoSum of the high
+// parts with the low parts added to its error (11 FP32 instructions instead
+// of the cancellation-safe form's 20); its error is bounded by a few units
+// of 2^-46 of the operands' magnitudes, as an FP64 sum's is by 2^-53 of
+// theirs, and every force and energy the pair code sums is compared with
+// operands of its own size.  The reciprocal takes its Newton residual
+// 1 - b y from one fused multiply-add (b.hi y is within 2^-22 of 1, so the
+// residual is formed to FP32 relative accuracy) and the low part's product.
+struct DFl {
+  float hi, lo;
+};
+__device__ __forceinline__ DFl dfl(DF a) { return DFl{a.hi, a.lo}; }
+__device__ __forceinline__ DFl operator+(DFl a, DFl b) {
+  const DF s = df_2sum(a.hi, b.hi);
+  const DF r = df_fast2sum(s.hi, __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo)));
+  return DFl{r.hi, r.lo};
+}
+__device__ __forceinline__ DFl operator-(DFl a) { return DFl{-a.hi, -a.lo}; }
+__device__ __forceinline__ DFl operator-(DFl a, DFl b) { return a + (-b); }
+__device__ __forceinline__ DFl operator*(DFl a, DFl b) { return dfl(DF{a.hi, a.lo} * DF{b.hi, b.lo}); }
+__device__ __forceinline__ DFl dfl_rcp(DFl b) {
+  const float y = rcp_nr(b.hi);
+  const float r = __fmaf_rn(-b.lo, y, __fmaf_rn(-b.hi, y, 1.f));  // 1 - b y
+  const DF q = df_fast2sum(y, __fmul_rn(y, r));
+  return DFl{q.hi, q.lo};
+}
+__device__ __forceinline__ double dfl_to(DFl a) { return (double)a.hi + (double)a.lo; }
+
+// Pair arithmetic type: FP32 in the FP32 stage; double-float (DFl, about 46
 // bits) in the FP64 stage and the FP64 API evaluation -- the O(N^2) pair
 // terms stay off the FP64 pipe.  A pair closer than r^2 = 1e-5 sigma^2 (where
 // FP32's exponent range could overflow lj12) is computed in double.
@@ -71,15 +100,15 @@ template <> struct LjC<float> {
   __device__ static float scaled(double c, C x) { return (float)c * x; }  // no FP64 per DOF
 };
 template <> struct LjC<double> {
-  using C = DF;
-  __device__ static C from(double x) { return df_from(x); }
-  __device__ static double to(C x) { return df_to(x); }
-  __device__ static double scaled(double c, C x) { return c * df_to(x); }
+  using C = DFl;
+  __device__ static C from(double x) { return dfl(df_from(x)); }
+  __device__ static double to(C x) { return dfl_to(x); }
+  __device__ static double scaled(double c, C x) { return c * dfl_to(x); }
 };
 template <typename C> struct CV3 { C x, y, z; };
 
 __device__ __forceinline__ float lj_shfl(float a, int src) { return __shfl_sync(0xffffffffu, a, src); }
-__device__ __forceinline__ DF lj_shfl(DF a, int src) { return df_shfl(a, src); }
+__device__ __forceinline__ DFl lj_shfl(DFl a, int src) { return dfl(df_shfl(DF{a.hi, a.lo}, src)); }
 
 // lj6 = s6 / r^6, lj12 = lj6^2 and the force factor f = (2 lj12 - lj6) / r^2
 // of one pair separated by (dx, dy, dz)
@@ -90,21 +119,22 @@ __device__ __forceinline__ void lj_pair(float dx, float dy, float dz, float s6, 
   lj12 = lj6 * lj6;
   f = (lj12 + lj12 - lj6) * inv;
 }
-__device__ __forceinline__ void lj_pair(DF dx, DF dy, DF dz, DF s6, DF& lj6, DF& lj12, DF& f) {
-  const DF r2 = dx * dx + dy * dy + dz * dz;
+__device__ __forceinline__ void lj_pair(DFl dx, DFl dy, DFl dz, DFl s6, DFl& lj6, DFl& lj12, DFl& f) {
+  const DFl r2 = dx * dx + dy * dy + dz * dz;
   if (r2.hi >= 1e-5f) {
-    const DF inv = df_rcp(r2);
-    const DF inv3 = inv * inv * inv;
+    const DFl inv = dfl_rcp(r2);
+    const DFl inv3 = inv * inv * inv;
     lj6 = s6 * inv3;
     lj12 = lj6 * lj6;
-    f = (lj12 + lj12 - lj6) * inv;
+    // 2 lj12 exactly (both parts doubled)
+    f = (DFl{2.f * lj12.hi, 2.f * lj12.lo} - lj6) * inv;
   } else {
-    const double ddx = df_to(dx), ddy = df_to(dy), ddz = df_to(dz);
+    const double ddx = dfl_to(dx), ddy = dfl_to(dy), ddz = dfl_to(dz);
     const double inv = 1.0 / (ddx * ddx + ddy * ddy + ddz * ddz);
-    const double l6 = df_to(s6) * inv * inv * inv, l12 = l6 * l6;
-    lj6 = df_from(l6);
-    lj12 = df_from(l12);
-    f = df_from((2 * l12 - l6) * inv);
+    const double l6 = dfl_to(s6) * inv * inv * inv, l12 = l6 * l6;
+    lj6 = dfl(df_from(l6));
+    lj12 = dfl(df_from(l12));
+    f = dfl(df_from((2 * l12 - l6) * inv));
   }
 }
 
@@ -115,10 +145,10 @@ template <> struct LjAcc<float> {
   __device__ __forceinline__ void add(float v) { a.add(v); }
   __device__ __forceinline__ double total() const { return a.total(); }
 };
-template <> struct LjAcc<DF> {
-  DF s{0.f, 0.f};
-  __device__ __forceinline__ void add(DF v) { s = s + v; }
-  __device__ __forceinline__ double total() const { return df_to(s); }
+template <> struct LjAcc<DFl> {
+  DFl s{0.f, 0.f};
+  __device__ __forceinline__ void add(DFl v) { s = s + v; }
+  __device__ __forceinline__ double total() const { return dfl_to(s); }
 };
 
 template <typename T, class Team, class Emit>

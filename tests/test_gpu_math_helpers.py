@@ -11,7 +11,10 @@ CUDA's own correctly rounded operations, over a sweep of inputs
   relative error below 2^-44 against 1.0 / x in FP64;
 * the double-float square root (one Newton step from sqrtf, the BarAndHinge
   FP64 stage): relative error below 2^-44 against sqrt in FP64;
-* the double-float product (Dekker / FMA): relative error below 2^-44.
+* the double-float product (Dekker / FMA): relative error below 2^-44;
+* the Lennard-Jones pair terms' double-float (DFl): the reciprocal with its
+  residual from fused multiply-adds, relative error below 2^-44; the sum,
+  error below 2^-45 of the operands' magnitudes.
 """
 import ctypes as C
 import os
@@ -40,7 +43,7 @@ def probe(tmp_path_factory):
     def run(x, y):
         x = np.ascontiguousarray(x, np.float64)
         y = np.ascontiguousarray(y, np.float64)
-        o = np.zeros((x.size, 8))
+        o = np.zeros((x.size, 12))
         assert lib.math_probe(x.ctypes.data_as(dp), y.ctypes.data_as(dp), o.ctypes.data_as(dp), x.size) == 0
         return o
     return run
@@ -79,3 +82,11 @@ def test_double_float_helpers(probe):
     prod = x * y
     ok = (np.abs(prod) > 2.0 ** -80) & (np.abs(prod) < 2.0 ** 80)
     assert rel(o[ok, 7], prod[ok]).max() < 2.0 ** -44
+
+
+def test_lj_double_float(probe):
+    x = _inputs()
+    y = np.random.default_rng(7).permutation(x)
+    o = probe(x, y)
+    assert (np.abs(o[:, 8] - o[:, 4]) / np.abs(o[:, 4])).max() < 2.0 ** -44
+    assert (np.abs(o[:, 9] - o[:, 10]) / o[:, 11]).max() < 2.0 ** -45

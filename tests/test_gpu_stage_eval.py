@@ -269,7 +269,7 @@ def test_pf_line_stencil_tma(grid):
             assert abs(e[k] - ed[k]) <= 1e-12 * abs(ed[k]), (k, e[k], ed[k])
             eo, go = ora.energy_gradient(pts[k])
             de, dg = _errs(e[k], g[k], eo, go)
-            _log("pf_lines_tma", abi.EVAL_LINES_TMA, grid=list(grid), trial=k, t=t, energy_rel_err=de,
+            _log("pf_lines_tma_%dx%dx%d" % grid, abi.EVAL_LINES_TMA, trial=k, t=t, energy_rel_err=de,
                  grad_rel_err=dg)
             assert dg <= GRAD32, (k, dg)
             assert de <= E32, (k, de)
