@@ -72,11 +72,7 @@ struct DFl {
   float hi, lo;
 };
 __device__ __forceinline__ DFl dfl(DF a) { return DFl{a.hi, a.lo}; }
-__device__ __forceinline__ DFl operator+(DFl a, DFl b) {
-  const DF s = df_2sum(a.hi, b.hi);
-  const DF r = df_fast2sum(s.hi, __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo)));
-  return DFl{r.hi, r.lo};
-}
+__device__ __forceinline__ DFl operator+(DFl a, DFl b) { return dfl(df_add_plain(DF{a.hi, a.lo}, DF{b.hi, b.lo})); }
 __device__ __forceinline__ DFl operator-(DFl a) { return DFl{-a.hi, -a.lo}; }
 __device__ __forceinline__ DFl operator-(DFl a, DFl b) { return a + (-b); }
 __device__ __forceinline__ DFl operator*(DFl a, DFl b) { return dfl(DF{a.hi, a.lo} * DF{b.hi, b.lo}); }
