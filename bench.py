@@ -344,6 +344,11 @@ def run_batched(args):
                   "converged": int(plain_conv), "kernel_ms": plain_ms},
         "batched_vs_plain": batched / plain if plain > 0 else None,
     }
+    # MIXED against FP64 throughout on every 8th cluster of the Lbfgs half
+    # (the FIRE half's 100000-iteration runs take minutes in FP64)
+    sample = [("lj", p, items[i][0], None) for i in range(half, len(items), 8)]
+    out["batched"]["mixed_vs_fp64"] = dict(_precision_compare(sample, items[half][1]),
+                                           sample=f"{len(sample)} Lbfgs clusters (every 8th)")
     if args.cpu_sample > 0 and not args.no_cpu:
         out["batched"]["cpu_baseline"], out["batched"]["fire_vs_oracle"] = \
             _batched_cpu(items, sizes, status, res, args)
@@ -424,9 +429,38 @@ def mixed_items(n_grids, n_sheets, full, seed=11):
     return items
 
 
+def _precision_compare(items, mp):
+    """The same instances (kind, potential, start, displaced start) as one
+    batch run with MIXED precision and one with FP64 throughout: kernel time,
+    iterations and converged count of each, by kind."""
+    from minim_gb300 import abi, runtime
+    out = {}
+    for prec in ("mixed", "fp64"):
+        m = abi.MinimiserParams.from_buffer_copy(mp)
+        m.precision = {"mixed": abi.PREC_MIXED, "fp64": abi.PREC_FP64}[prec]
+        b = runtime.Batch()
+        for kind, p, x0, start in items:
+            inst = runtime.Instance(p, x0)
+            if start is not None:
+                inst.coords = start
+            b.add(inst, m)
+        res = b.run()
+        st = runtime.last_run_stats()
+        kinds = {}
+        for (kind, _, _, _), r in zip(items, res):
+            k = kinds.setdefault(kind, {"converged": 0, "iterations": 0, "fp64_iterations": 0})
+            k["converged"] += r.status == abi.RES_CONVERGED
+            k["iterations"] += r.iter
+            k["fp64_iterations"] += r.fp64_iters
+        out[prec] = {"kernel_ms": st["kernel_ms"], "by_kind": kinds}
+    out["mixed_over_fp64_time"] = out["mixed"]["kernel_ms"] / out["fp64"]["kernel_ms"]
+    return out
+
+
 def run_mixed(args):
     """One batch run of mixed phase-field and mesh instances (mixed_items),
-    all kinds at once on their own streams."""
+    all kinds at once on their own streams; then the same instances with
+    MIXED and with FP64 precision on their own (_precision_compare)."""
     from minim_gb300 import abi, runtime
     full = args.mixed_full
     n_grids = args.mixed_grids if args.mixed_grids >= 0 else (2 * args.mixed) // 3
@@ -462,6 +496,7 @@ def run_mixed(args):
         # least the longest of them
         t = np.array(k.pop("run_ms"))
         k["run_ms_p50_p99_max"] = [float(np.percentile(t, 50)), float(np.percentile(t, 99)), float(t.max())]
+    prec = _precision_compare(items, mp) if not full else None
     desc = (f"{n_grids} 2-D ternary PhaseField grids (" + ("64^2-512^2" if full else "64^2/128^2") +
             f", fixed volume) + {n_sheets} BarAndHinge sheets (" + ("1k-100k" if full else "1k-4.2k") +
             " vertices), Lbfgs RMS<1e-7")
@@ -469,7 +504,7 @@ def run_mixed(args):
                             "instances": len(items), "converged": int(conv), "kernel_ms": st["kernel_ms"],
                             "tune_ms": st["tune_ms"], "setup_s": t_set, "by_kind": kinds,
                             "fp64_iteration_share": st["fp64_iterations"] / max(st["iterations"], 1),
-                            "stated_sizes": bool(full), "workload": desc}}
+                            "stated_sizes": bool(full), "workload": desc, "mixed_vs_fp64": prec}}
 
 
 def run_rows(args):
