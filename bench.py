@@ -344,6 +344,7 @@ def run_batched(args):
                   "converged": int(plain_conv), "kernel_ms": plain_ms},
         "batched_vs_plain": batched / plain if plain > 0 else None,
     }
+    out["batched"]["iteration_cost_fit"] = _iteration_cost_fit(sizes[:half], res[:half])
     # MIXED against FP64 throughout on every 8th cluster of the Lbfgs half
     # (the FIRE half's 100000-iteration runs take minutes in FP64)
     sample = [("lj", p, items[i][0], None) for i in range(half, len(items), 8)]
@@ -353,6 +354,29 @@ def run_batched(args):
         out["batched"]["cpu_baseline"], out["batched"]["fire_vs_oracle"] = \
             _batched_cpu(items, sizes, status, res, args)
     return out
+
+
+def _iteration_cost_fit(sizes, res):
+    """Device time of one FIRE iteration in each precision stage, from the
+    per-instance results of the runs that reached the iteration limit (every
+    one runs the same number of iterations, split between the stages):
+    run_ms = a32 N^2 n32 + b32 n32 + a64 N^2 n64 + b64 n64 by least squares,
+    with n64 the FP64-stage iterations.  Times are per instance while it
+    shares its SM with the batch's other resident instances."""
+    from minim_gb300 import abi
+    rows = [(n, r.iter - r.fp64_iters, r.fp64_iters, r.run_ms) for n, r in zip(sizes, res)
+            if r.status == abi.RES_MAXITER]
+    if len(rows) < 8:
+        return None
+    a = np.array(rows, dtype=float)
+    n2 = a[:, 0] ** 2
+    X = np.stack([n2 * a[:, 1], a[:, 1], n2 * a[:, 2], a[:, 2]], 1)
+    c, *_ = np.linalg.lstsq(X, a[:, 3] * 1e3, rcond=None)  # microseconds
+    at = lambda n, k: float(c[k] * n * n + c[k + 1])
+    return {"instances": len(rows), "us_per_n2_fp32": float(c[0]), "us_fixed_fp32": float(c[1]),
+            "us_per_n2_fp64": float(c[2]), "us_fixed_fp64": float(c[3]),
+            "us_per_iteration_n390": {"fp32": at(390, 0), "fp64": at(390, 2)},
+            "fp64_share_of_instance_time": float((X[:, 2:] @ c[2:]).sum() / (X @ c).sum())}
 
 
 def _batched_cpu(items, sizes, status, res, args):
