@@ -815,19 +815,21 @@ def run_profile_pf(iters, precision):
     print(json.dumps({"iter": r.iter, "evals": r.evals, "kernel_ms": st["kernel_ms"], "precision": precision}))
 
 
-def run_profile_lj(iters):
-    """One batch launch of 304 Lennard-Jones clusters (N=300, Fire(0.1), FP32
-    coordinates, `iters` iterations each) for profiler captures of the batched
-    kernel."""
+def run_profile_lj(iters, precision="fp32"):
+    """One batch launch of 304 Lennard-Jones clusters (N=300, Fire(0.1),
+    `iters` iterations each; FP32 coordinates, or with "fp64" FP64
+    coordinates and the double-float pair code of the FP64 stage) for
+    profiler captures of the batched kernel."""
     from minim_gb300 import abi, runtime
     from tests.workloads import lj_cluster
     insts = [runtime.Instance(abi.lj(), lj_cluster(300, seed=i)) for i in range(304)]
     b = runtime.Batch()
     for a in insts:
-        b.add(a, abi.minimiser("fire", dt_max=0.1, tol=1e-12, max_iter=iters, precision="fp32"))
+        b.add(a, abi.minimiser("fire", dt_max=0.1, tol=1e-12, max_iter=iters, precision=precision))
     b.run(threads=256)
     st = runtime.last_run_stats()
-    print(json.dumps({"profile_case": "304 LJ clusters N=300 Fire(0.1) fp32", "iterations": st["iterations"],
+    print(json.dumps({"profile_case": f"304 LJ clusters N=300 Fire(0.1) {precision}", "iterations": st["iterations"],
+                      "pairs32": st["pairs32"], "pairs64": st["pairs64"],
                       "kernel_ms": st["kernel_ms"], "launches": st["launches"],
                       "phase_ms_summed_over_instances": st["phase_ms"]}))
 
@@ -883,6 +885,7 @@ def main():
     ap.add_argument("--profile-pf", type=int, default=0,
                     help="run one 128^2 three-fluid PhaseField grid for N iterations (profiler capture) and exit")
     ap.add_argument("--profile-prec", default="fp64", help="coordinate precision of --profile-pf")
+    ap.add_argument("--profile-lj-prec", default="fp32", help="coordinate precision of --profile-lj")
     ap.add_argument("--profile-cluster", type=int, default=0,
                     help="run one 512^2 three-fluid grid on a cluster of 8 CTAs for N iterations and exit")
     args = ap.parse_args()
@@ -896,7 +899,7 @@ def main():
         run_profile_case(args.profile)
         return
     if args.profile_lj:
-        run_profile_lj(args.profile_lj)
+        run_profile_lj(args.profile_lj, args.profile_lj_prec)
         return
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
