@@ -650,8 +650,9 @@ __device__ __forceinline__ void lines_sweep(const PotPF& Pf, const LinesIO& io, 
 // of kTmaY lines (y0 .. y0 + kTmaY - 1) over a run of planes x = xa .. xb - 1
 // and walks it along x.  One plane tile is, per array (x and P), the strip's
 // lines with their y neighbours -- one 3-D box of {nz, kTmaY + 2, 1} --
-// and a ring of kTmaStages tiles holds planes x - 1, x and x + 1 while the
-// next planes land: every value is brought on chip once per block, the x
+// and a ring of NS tiles (kTmaStages = 4 by default; 6 or 8 through
+// MINIM_GPU_LINES_TMA) holds planes x - 1, x and x + 1 while the next
+// planes land: every value is brought on chip once per block, the x
 // neighbours come from the ring and the y neighbours from the tile.
 //
 // A tile holds kTmaY + 2 lines per array: line y0 - 1 + j in slot j.
@@ -665,7 +666,6 @@ __device__ __forceinline__ void lines_sweep(const PotPF& Pf, const LinesIO& io, 
 // (the pass's results are then unusable), the block issues no further copy,
 // and before it exits it waits (bounded again) for every copy it issued.
 constexpr int kTmaY = 4;
-constexpr int kTmaBoxY = kTmaY + 2;
 constexpr int kTmaSlots = kTmaY + 2;
 constexpr int kTmaStages = 4;
 // whether the stepped graph's trial pass uses the tiles unless
@@ -1839,9 +1839,9 @@ extern "C" int mg_stepped_lines_tma_probe(const InstDesc* d, const int* grid, co
   if (nb > max_rows) return (int)cudaErrorInvalidConfiguration;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   TmaMaps hm{};
-  SCK(encode_lines_map(&hm.box[0], X, grid, kTmaBoxY));
+  SCK(encode_lines_map(&hm.box[0], X, grid, kTmaSlots));
   SCK(encode_lines_map(&hm.line[0], X, grid, 1));
-  SCK(encode_lines_map(&hm.box[1], P, grid, kTmaBoxY));
+  SCK(encode_lines_map(&hm.box[1], P, grid, kTmaSlots));
   SCK(encode_lines_map(&hm.line[1], P, grid, 1));
   char* dm = nullptr;
   SCK(cudaMallocAsync((void**)&dm, sizeof(TmaMaps) + 128, s));
