@@ -140,7 +140,6 @@ Kern kern(int kk) {
 // generic pair loop), or positions and eight warps' force accumulators of
 // up to 416 particles (the dealt FP32 evaluation)
 const size_t kLjTileBytes = 1536 * 32;
-size_t pot_smem(int kk) { return kk == K_LJ ? kLjTileBytes : 0; }
 // dynamic shared memory of a one-CTA (or cluster) batch launch of these
 // instances with this many threads: the largest need among them
 size_t group_smem(int kk, const InstDesc* d, int n, int threads) {
@@ -562,7 +561,10 @@ void do_eval(minim_gpu_instance_s* h, const double* x, double* e, double* g) {
     CK(cudaMemcpyAsync(h->d_tmp, x, h->n * sizeof(double), cudaMemcpyHostToDevice, D.s));
     xd = h->d_tmp;
   }
-  EvalIO io{xd, g ? h->d_g : nullptr, h->d_e, nullptr};
+  EvalIO io{};
+  io.x = xd;
+  io.g = g ? h->d_g : nullptr;
+  io.e = h->d_e;
   InstDesc d = h->d;
   d.fixed = h->d.fixed;
   CK(cudaMemcpyAsync(h->d_desc, &d, sizeof d, cudaMemcpyHostToDevice, D.s));
@@ -1391,7 +1393,8 @@ int minim_gpu_apply_constraints(minim_gpu_handle h, double* v) {
     Dev& D = need_dev();
     ensure_grid(h);
     CK(cudaMemcpyAsync(h->d_tmp, v, h->n * sizeof(double), cudaMemcpyHostToDevice, D.s));
-    EvalIO io{nullptr, nullptr, nullptr, h->d_tmp};
+    EvalIO io{};
+    io.v = h->d_tmp;
     CK(cudaMemcpyAsync(h->d_desc, &h->d, sizeof(InstDesc), cudaMemcpyHostToDevice, D.s));
     CK(cudaMemcpyAsync(h->d_io, &io, sizeof io, cudaMemcpyHostToDevice, D.s));
     launch_grid(h, OP_CONSTRAIN, 0);
