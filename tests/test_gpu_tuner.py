@@ -13,7 +13,7 @@ import pytest
 
 from minim_gb300 import abi, runtime
 from oracle.oracle import Oracle
-from tests.workloads import lj_cluster, pf_simplex, sheet
+from tests.workloads import lj_cluster, pf_simplex
 
 pytestmark = pytest.mark.gpu
 

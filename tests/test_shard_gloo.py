@@ -4,7 +4,6 @@ The per-rank worker is the FP64 oracle (no GPU here)."""
 import os
 
 import numpy as np
-import pytest
 import torch.multiprocessing as mp
 
 from minim_gb300 import shard
