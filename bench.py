@@ -453,6 +453,91 @@ def mixed_items(n_grids, n_sheets, full, seed=11):
     return items
 
 
+def _oracle_rate(jobs, strata):
+    """CPU oracle baseline of a set of minimisations: `jobs` maps a stratum
+    to its sampled (potential, start coordinates, minimiser parameters);
+    `strata` maps each stratum to the number of instances it stands for.
+    The sampled minimisations run on one host thread each, all host threads
+    at once (the oracle's C calls release the interpreter lock), each timed
+    from its first iteration (set-up excluded, as on the GPU side); the mean
+    time and converged fraction of each stratum's sample are extrapolated to
+    its instances.  Returns (converged minimisations/s on all threads,
+    threads, sample description)."""
+    import concurrent.futures as cf
+    from minim_gb300 import abi
+    from oracle.oracle import Oracle
+
+    def one(job):
+        p, x0, start, mp = job
+        o = Oracle(p, x0)
+        if start is not None:
+            o.coords = start
+        t = time.perf_counter()
+        r = o.minimise(mp)
+        return int(r.status), time.perf_counter() - t
+
+    cores = os.cpu_count() or 1
+    flat = [(k, j) for k, js in jobs.items() for j in js]
+    t0 = time.perf_counter()
+    with cf.ThreadPoolExecutor(max_workers=cores) as ex:
+        outs = list(ex.map(lambda kj: (kj[0],) + one(kj[1]), flat))
+    wall = time.perf_counter() - t0
+    total_s, total_conv = 0.0, 0.0
+    for k, count in strata.items():
+        samp = [o for o in outs if o[0] == k]
+        if not samp or not count:
+            continue
+        total_s += count * float(np.mean([o[2] for o in samp]))
+        total_conv += count * float(np.mean([o[1] == abi.RES_CONVERGED for o in samp]))
+    rate = total_conv / (total_s / cores) if total_s > 0 else None
+    desc = (f"{len(flat)} instances in {len(jobs)} strata, one host thread each, {cores} threads, "
+            f"{wall:.1f} s wall; per-instance times extrapolated to {sum(strata.values())} instances")
+    return rate, cores, desc
+
+
+def _mixed_cpu(items, mp, per):
+    """The oracle baseline of the mixed batch: `per` instances of each
+    stratum (PhaseField grid side; BarAndHinge sheet size, split at the
+    median vertex count)."""
+    rng = np.random.default_rng(2)
+    key = {}
+    sheets = sorted(np.size(x0) for kind, _, x0, _ in items if kind == "bah")
+    split = sheets[len(sheets) // 2] if sheets else 0
+    for j, (kind, p, x0, start) in enumerate(items):
+        k = f"pf{int(round(np.sqrt(np.size(x0) / 3)))}" if kind == "pf" else \
+            ("bah_small" if np.size(x0) < split else "bah_large")
+        key.setdefault(k, []).append(j)
+    strata = {k: len(v) for k, v in key.items()}
+    jobs = {}
+    for k, v in key.items():
+        pick = rng.choice(v, size=min(per, len(v)), replace=False)
+        jobs[k] = [(items[j][1], items[j][2], items[j][3], mp) for j in sorted(int(i) for i in pick)]
+    return _oracle_rate(jobs, strata)
+
+
+def _serving_cpu(reqs, per):
+    """The oracle baseline of a serving stream's requests (their throughput
+    with every host thread busy, arrivals ignored): `per` requests of each
+    stratum (LJ below / above 100 particles, 2-D and 3-D PhaseField,
+    BarAndHinge)."""
+    rng = np.random.default_rng(3)
+    key = {}
+    for j, (_, kind, p, x0, mp) in enumerate(reqs):
+        if kind == "lj":
+            k = "lj_small" if np.size(x0) < 300 else "lj_large"
+        elif kind == "pf":
+            k = "pf3d" if p.struct.grid[2] > 1 else "pf2d"
+        else:
+            k = "bah"
+        key.setdefault(k, []).append(j)
+    strata = {k: len(v) for k, v in key.items()}
+    jobs = {}
+    for k, v in key.items():
+        pick = rng.choice(v, size=min(per, len(v)), replace=False)
+        jobs[k] = [(reqs[j][2], reqs[j][3], None, reqs[j][4]) for j in sorted(int(i) for i in pick)]
+    return _oracle_rate(jobs, strata)
+
+
 def _precision_compare(items, mp):
     """The same instances (kind, potential, start, displaced start) as one
     batch run with MIXED precision and one with FP64 throughout: kernel time,
@@ -521,6 +606,11 @@ def run_mixed(args):
         t = np.array(k.pop("run_ms"))
         k["run_ms_p50_p99_max"] = [float(np.percentile(t, 50)), float(np.percentile(t, 99)), float(t.max())]
     prec = _precision_compare(items, mp) if not full else None
+    cpu = None
+    if args.cpu_sample > 0 and not args.no_cpu and not full:
+        rate, cores, sample = _mixed_cpu(items, mp, max(1, args.cpu_sample // 32))
+        cpu = {"value": rate, "unit": "converged minimisations/s", "cores": cores, "kind": "port",
+               "sample": sample}
     desc = (f"{n_grids} 2-D ternary PhaseField grids (" + ("64^2-512^2" if full else "64^2/128^2") +
             f", fixed volume) + {n_sheets} BarAndHinge sheets (" + ("1k-100k" if full else "1k-4.2k") +
             " vertices), Lbfgs RMS<1e-7")
@@ -528,7 +618,8 @@ def run_mixed(args):
                             "instances": len(items), "converged": int(conv), "kernel_ms": st["kernel_ms"],
                             "tune_ms": st["tune_ms"], "setup_s": t_set, "by_kind": kinds,
                             "fp64_iteration_share": st["fp64_iterations"] / max(st["iterations"], 1),
-                            "stated_sizes": bool(full), "workload": desc, "mixed_vs_fp64": prec}}
+                            "stated_sizes": bool(full), "workload": desc, "mixed_vs_fp64": prec,
+                            "cpu_baseline": cpu}}
 
 
 def run_rows(args):
@@ -718,6 +809,10 @@ def run_serving(args):
            "arrival_rate": args.serve_rate, "stated_sizes": bool(full),
            "workload": "Poisson stream of " + kinds + ", Lbfgs"}
     cap = conv / wall
+    if args.cpu_sample > 0 and not args.no_cpu and not full:
+        rate, cores, sample = _serving_cpu(reqs, max(1, args.cpu_sample // 32))
+        out["cpu_baseline"] = {"value": rate, "unit": "converged minimisations/s", "cores": cores,
+                               "kind": "port", "sample": sample + " (the request mix; arrivals ignored)"}
     if args.serve_carried and cap > 0:
         rate2 = 0.5 * cap
         reqs2 = serving_requests(args.serve_carried, rate2, full, seed=8)

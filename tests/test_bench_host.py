@@ -41,3 +41,19 @@ def test_iteration_cost_fit_needs_enough_runs():
     rng = np.random.default_rng(4)
     sizes, res = _results(2e-4, 14.0, 1.5e-3, 70.0, rng, n=5)
     assert bench._iteration_cost_fit(sizes, res) is None
+
+
+def test_oracle_rate_extrapolates_by_stratum():
+    """Two strata of small Lennard-Jones clusters, each sampled once and
+    standing for 3 and 5 instances: every sampled run converges, so the rate
+    is the 8 instances over their extrapolated CPU seconds per thread."""
+    from tests.workloads import lj_cluster
+    mp = abi.minimiser("lbfgs", m=5, tol=1e-6)
+    jobs = {"a": [(abi.lj(), lj_cluster(13, seed=1), None, mp)],
+            "b": [(abi.lj(), lj_cluster(20, seed=2), None, mp)]}
+    rate, cores, desc = bench._oracle_rate(jobs, {"a": 3, "b": 5})
+    assert rate is not None and rate > 0
+    assert cores >= 1
+    assert "2 instances in 2 strata" in desc and "8 instances" in desc
+    # a stratum with no instances contributes nothing; none at all gives no rate
+    assert bench._oracle_rate(jobs, {"a": 0, "b": 0})[0] is None
